@@ -1,0 +1,154 @@
+/*
+ * kb2pi.h -- C ABI of libkb2pi, a GB300 (sm_103a) implementation of the 2PI
+ * Kadanoff-Baym time step of magdalenaeriksson/QFTdynamicsM.jl
+ * src/TwoPIScalar (O(N) lambda phi^4 on an Ns^3 periodic lattice; LambdaLO,
+ * LambdaNLO quantum = 3-loop sunset, LambdaNLO classical truncations).
+ *
+ * The entry points are what a Julia `TwoPIScalarGPU <: TwoPIScalarNumerics`
+ * backend binds with `ccall`; each cites the reference function it replaces.
+ * Plain C types only. Every call returns 0 on success or a negative KB_ERR_*
+ * code; kb_last_error() gives the message. Calls on one handle must be
+ * serialised (one CUDA stream per handle); distinct handles are independent.
+ *
+ * Time indices follow the reference: t counts from 1, the window after a step
+ * t is [tmin, t] with tmin = max(1, t - M + 1) (expandSimData!,
+ * src/TwoPIScalar/TwoPIScalar_SimDataStruct.jl:262-278).
+ *
+ * Momenta are stored per cubic orbit: the orbit of a lattice site is the set
+ * reached by permuting and reflecting its coordinates. Orbits are numbered by
+ * their sorted folded coordinates a <= b <= c (a_i = min(n_i, Ns - n_i)) as
+ * c(c+1)(c+2)/6 + b(b+1)/2 + a. kb_get_orbits() returns the table.
+ */
+#ifndef KB2PI_H
+#define KB2PI_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct kb_handle kb_handle;
+
+enum {
+  KB_OK = 0,
+  KB_ERR_PARAM = -1,   /* invalid parameter or call order */
+  KB_ERR_OOM = -2,     /* device allocation failed */
+  KB_ERR_CUDA = -3,    /* CUDA runtime error */
+  KB_ERR_NAN = -4,     /* non-finite value detected in a measurement */
+  KB_ERR_TIMEOUT = -5, /* a bounded device wait expired (kernel returned early) */
+  KB_ERR_RANGE = -6,   /* time index outside the memory window (BoundsError) */
+  KB_ERR_NODEV = -7    /* no CUDA device / library built without a device */
+};
+
+/* Perturbative expansion (src/TwoPIScalar/TwoPIScalar_Problemdefinition.jl:115-118) */
+enum { KB_PEXP_LO = 0, KB_PEXP_NLO_QUANTUM = 1, KB_PEXP_NLO_CLASSICAL = 2 };
+/* Precision: plain FP64 everywhere, or FP32 history/transforms/sunset with
+ * FP64 leapfrog state, accumulation of the memory integrals, tadpole and
+ * diagnostics. */
+enum { KB_PREC_FP64 = 0, KB_PREC_MIXED = 1 };
+
+/* One simulation; mirrors the fields of TwoPIScalarDiscretizationLattice
+ * (TwoPIScalar_Discretization.jl:4-17) and Phi4 (…_ModelExpansionRenormalization.jl:5-9). */
+typedef struct kb_params {
+  int32_t Ns;        /* disc.Nx (even, 2..64) */
+  int32_t sdim;      /* disc.sdim (3) */
+  int32_t M;         /* NstepsinMemory (3 <= M <= 1024) */
+  int32_t N;         /* model.ONgroup */
+  int32_t pexp;      /* KB_PEXP_* */
+  int32_t precision; /* KB_PREC_*; must be equal for all runs of one handle */
+  int32_t device;    /* CUDA device ordinal */
+  int32_t flags;     /* reserved, 0 */
+  double dt;         /* disc.dt */
+  double lambda;     /* model.Lambda */
+  double mass2;      /* model.Mass2: m^2 used in the evolution (after Renormalize) */
+  double mass;       /* disc.Mass: time unit of measurements */
+} kb_params;
+
+/* Scalars of MeasurementTwoPIScalar (TwoPIScalar_Measurement.jl:2-23) */
+typedef struct kb_meas_scalars {
+  double time, E, E_pot, E_kin, E_mem, M2;
+} kb_meas_scalars;
+
+/* Replaces getTwoPISimData + getTwoPIScalarTmpData
+ * (TwoPIScalar_SimDataStruct.jl:669-721): allocates the device-resident
+ * two-time history ring, self-energy ring and scratch for one run. */
+int kb_create(const kb_params *p, kb_handle **out);
+/* Batched form: nruns independent simulations that advance in lock-step
+ * (same t) in one launch per kernel. Runs may differ in Ns, M, N, lambda,
+ * mass2, pexp; dt and precision are per run too but precision must agree. */
+int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out);
+/* Replaces the finalizer of the simulation data. */
+void kb_destroy(kb_handle *h);
+/* Message of the last failed call on this handle (or of kb_create). */
+const char *kb_last_error(const kb_handle *h);
+
+/* Number of cubic orbits S of run `run`, and their table: rep = sorted folded
+ * coordinates (3 per orbit), k2 = lev2 = sum_i 4 sin^2(pi n_i / Ns), deg =
+ * number of lattice sites (replaces FFTWhelper's getfftwhelper, used at
+ * TwoPIScalar_Modelfile.jl:64). Any output pointer may be NULL. */
+int kb_num_orbits(const kb_handle *h, int32_t run, int32_t *S);
+int kb_get_orbits(const kb_handle *h, int32_t run, int32_t *rep, double *k2, int64_t *deg);
+/* orbit index of every lattice site (column-major site order, Ns^3 entries) */
+int kb_site_orbits(const kb_handle *h, int32_t run, int32_t *orbit_of_site);
+
+/* Replaces initSimData! (TwoPIScalar_Initialization.jl:8-47): F(1,1), F(2,1),
+ * F(2,2), rho(2,1) = dt from the occupation n (per orbit, without the 1/2)
+ * and the initialisation mass; sets the window to [1,2]. */
+int kb_init(kb_handle *h, int32_t run, const double *n_of_orbit, double init_mass);
+/* Generic form: caller-computed F(1,1), F(2,1), F(2,2) per orbit, rho(2,1) =
+ * dt (e.g. initSimData! for TwoPIScalarGauss, TwoPIScalar_Initialization.jl:95-112). */
+int kb_init_rows(kb_handle *h, int32_t run, const double *F11, const double *F21, const double *F22);
+
+/* Replaces evolve!(thesolution, tmpdata, t) (TwoPIScalar_Evolution.jl:924-981)
+ * for every run of the handle; t must be the last evolved step + 1. Also
+ * prepares the measurement of step t. */
+int kb_step(kb_handle *h, int32_t t);
+/* `count` steps t0, t0+1, ... from one captured CUDA graph; when
+ * measure_every > 0 the scalars of steps with (t - 2) % measure_every == 0 are
+ * stored run-major in out (nruns x ceil(count / measure_every) entries). */
+int kb_steps(kb_handle *h, int32_t t0, int32_t count, int32_t measure_every, kb_meas_scalars *out,
+             int32_t out_capacity);
+/* Replaces expandSimData! alone (window advance without computing), as the
+ * reference benchmark fills the window (TwoPIScalar_Bechmark.jl:64-69). */
+int kb_expand(kb_handle *h);
+
+/* Replaces measure!/createMeasurement (TwoPIScalar_Measurement.jl:31-99,223-228)
+ * for the last evolved step t. Per-orbit arrays (S entries, NULL to skip):
+ * F = F(t-1,t-1), ddF, n, omega, c. */
+int kb_measure(kb_handle *h, int32_t run, int32_t t, kb_meas_scalars *s, double *F, double *ddF,
+               double *n, double *omega, double *c);
+/* Traces of createMeasurement at lattice site 1 (TwoPIScalar_Measurement.jl:89-96):
+ * SigF/Sigr at (t-1, tp) for tp = t-1 down to tmin; Fonet/ronet = F/rho(tmin, tp)
+ * for tp = tmin .. t-1. Each has t - tmin entries. */
+int kb_get_traces(kb_handle *h, int32_t run, double *Fonet, double *ronet, double *SigF, double *Sigr);
+
+/* Host view of the history (SymMatrix getindex, DefSimDataElements.jl:185-208):
+ * which = 0 for F, 1 for rho (true antisymmetric value), a and b in the window. */
+int kb_get(kb_handle *h, int32_t run, int32_t which, int32_t a, int32_t b, double *out);
+/* Test hook: overwrite F/rho(a,b) for all orbits (SymMatrix setindex!). */
+int kb_set(kb_handle *h, int32_t run, int32_t which, int32_t a, int32_t b, const double *in);
+/* Replaces calcSelfEnergies! alone (TwoPIScalar_Evolution.jl:16-31):
+ * Sigma(tmone, tp) for every tp in [tmin, tmone] of the current window. */
+int kb_self_energies(kb_handle *h, int32_t tmone);
+/* Sigma_F (which = 0) or Sigma_rho (which = 1) at (t-1, z) from the last step
+ * or kb_self_energies (CyclVector getindex, DefSimDataElements.jl:129-132). */
+int kb_get_sigma(kb_handle *h, int32_t run, int32_t which, int32_t z, double *out);
+/* simdata.indices after the last step: [tmin, tmax] */
+int kb_window(const kb_handle *h, int32_t run, int32_t *tmin, int32_t *tmax);
+
+/* Snapshot of the full state (history, self-energies, window) into a host
+ * buffer and back; replaces the serialisation the reference could not do
+ * ("Serialization broke because of pointers in simdata", G_SimulationArgs.jl:117). */
+int kb_checkpoint_size(const kb_handle *h, size_t *bytes);
+int kb_checkpoint_save(kb_handle *h, void *host_buf, size_t bytes);
+int kb_checkpoint_restore(kb_handle *h, const void *host_buf, size_t bytes);
+
+/* Wait for all work of the handle and report device-side errors (timeouts,
+ * non-finite measurements). */
+int kb_sync(kb_handle *h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,858 @@
+// kb_oracle.cpp -- CPU FP64 restatement of the TwoPIScalar Kadanoff-Baym step.
+//
+// TEST INFRASTRUCTURE ONLY: the parity checker for libkb2pi. See kb_oracle.h
+// for the parity status ("parity unpinned" against outputs of the Julia
+// reference, which cannot run here) and for what pins it instead.
+//
+// Each function names the reference lines it restates (paths relative to the
+// root of magdalenaeriksson/QFTdynamicsM.jl). Per-site operation order follows
+// the Julia broadcasts so that the engines agree with the reference's
+// arithmetic as closely as a different FFT allows.
+#include "kb_oracle.h"
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdint>
+#include <cstring>
+#include <functional>
+#include <stdexcept>
+#include <thread>
+#include <vector>
+
+namespace {
+
+typedef std::complex<double> cplx;
+
+// ---------------------------------------------------------------------------
+// Mixed-radix complex FFT (unnormalised, sign -1 forward / +1 backward), the
+// convention of FFTW's rfft/brfft used at TwoPIScalar_SimDataStruct.jl:381-382.
+// ---------------------------------------------------------------------------
+struct FFTPlan {
+  int n = 0;
+  std::vector<int> factors;
+  std::vector<cplx> tw;  // exp(-2 pi i j / n), j < n
+  explicit FFTPlan(int n_ = 1) : n(n_) {
+    int m = n;
+    for (int p = 2; m > 1;) {
+      if (m % p == 0) {
+        factors.push_back(p);
+        m /= p;
+      } else {
+        ++p;
+      }
+    }
+    tw.resize(std::max(n, 1));
+    for (int j = 0; j < n; ++j) {
+      double a = -2.0 * M_PI * (double)j / (double)n;
+      tw[j] = cplx(std::cos(a), std::sin(a));
+    }
+  }
+  // w_len^(e) for the given sign, expressed through the length-n table
+  inline cplx w(int len, long e, int sign) const {
+    long j = ((e % len) + len) % len;
+    cplx v = tw[(size_t)(j * (n / len))];
+    return sign < 0 ? v : std::conj(v);
+  }
+  void rec(cplx *out, const cplx *in, int len, int stride, int sign, int fi,
+           std::vector<cplx> &tmp) const {
+    if (len == 1) {
+      out[0] = in[0];
+      return;
+    }
+    const int p = factors[fi];
+    const int m = len / p;
+    for (int r = 0; r < p; ++r) rec(out + r * m, in + r * stride, m, stride * p, sign, fi + 1, tmp);
+    cplx *t = tmp.data() + (size_t)fi * 64;  // radix <= 64 per level scratch
+    cplx small[64];
+    for (int k = 0; k < m; ++k) {
+      for (int r = 0; r < p; ++r) t[r] = out[r * m + k] * w(len, (long)r * k, sign);
+      for (int q = 0; q < p; ++q) {
+        cplx s = 0;
+        for (int r = 0; r < p; ++r) s += t[r] * w(p, (long)r * q, sign);
+        small[q] = s;
+      }
+      for (int q = 0; q < p; ++q) out[k + q * m] = small[q];
+    }
+  }
+  // in-place transform of a strided line
+  void run(cplx *data, int stride, int sign, std::vector<cplx> &buf_in,
+           std::vector<cplx> &buf_out, std::vector<cplx> &tmp) const {
+    if (n == 1) return;
+    for (int i = 0; i < n; ++i) buf_in[i] = data[(size_t)i * stride];
+    rec(buf_out.data(), buf_in.data(), n, 1, sign, 0, tmp);
+    for (int i = 0; i < n; ++i) data[(size_t)i * stride] = buf_out[i];
+  }
+};
+
+struct FFTScratch {
+  std::vector<cplx> a, b, tmp, lat, lat2;
+};
+
+// ---------------------------------------------------------------------------
+// Lattice and cubic orbits. Sites use Julia's column-major order
+// (first coordinate fastest); momenta p_i = 2 pi n_i / Ns;
+// lev2 = sum_i 4 sin^2(p_i / 2). An orbit is the set of sites reached by
+// permutations and reflections of the coordinates; its label is the sorted
+// folded coordinate triple (a <= b <= c, a_i = min(n_i, Ns - n_i)).
+// FFTWhelper (Manifest.toml:352-358, not vendored) groups sites by lev2 value;
+// the orbit is the exact symmetry class, and every CPUfull quantity the
+// reference computes is independent of the grouping.
+// ---------------------------------------------------------------------------
+struct Orbits {
+  int Ns = 1, sdim = 3, H = 1, S = 0;
+  long V = 1;
+  std::vector<int32_t> rep;      // 3 per orbit
+  std::vector<double> k2;        // lev2 of the orbit
+  std::vector<int64_t> deg;      // number of sites
+  std::vector<int32_t> orbit_of_site;
+  std::vector<long> rep_site;    // first site (column-major) of each orbit
+  std::vector<long> site_start, site_list;  // sites of each orbit (CSR)
+
+  static long tri_index(int sdim, int a, int b, int c) {
+    if (sdim == 1) return c;
+    if (sdim == 2) return (long)c * (c + 1) / 2 + b;
+    return (long)c * (c + 1) * (c + 2) / 6 + (long)b * (b + 1) / 2 + a;
+  }
+  void build(int Ns_, int sdim_) {
+    Ns = Ns_;
+    sdim = sdim_;
+    H = Ns / 2 + 1;
+    V = 1;
+    for (int d = 0; d < sdim; ++d) V *= Ns;
+    long Smax = sdim == 1 ? H : (sdim == 2 ? (long)H * (H + 1) / 2 : (long)H * (H + 1) * (H + 2) / 6);
+    S = (int)Smax;
+    rep.assign((size_t)3 * S, 0);
+    k2.assign(S, 0.0);
+    deg.assign(S, 0);
+    rep_site.assign(S, -1);
+    orbit_of_site.assign(V, 0);
+    for (long s = 0; s < V; ++s) {
+      int n[3] = {0, 0, 0};
+      long r = s;
+      for (int d = 0; d < sdim; ++d) {
+        n[d] = (int)(r % Ns);
+        r /= Ns;
+      }
+      int f[3] = {0, 0, 0};
+      for (int d = 0; d < sdim; ++d) f[d] = std::min(n[d], Ns - n[d]);
+      // sort the active coordinates ascending; place them in the last slots
+      int g[3] = {0, 0, 0};
+      for (int d = 0; d < sdim; ++d) g[3 - sdim + d] = f[d];
+      std::sort(g + 3 - sdim, g + 3);
+      long o = tri_index(sdim, g[0], g[1], g[2]);
+      orbit_of_site[s] = (int32_t)o;
+      if (rep_site[o] < 0) {
+        rep_site[o] = s;
+        rep[3 * o + 0] = g[0];
+        rep[3 * o + 1] = g[1];
+        rep[3 * o + 2] = g[2];
+        double kk = 0.0;
+        for (int d = 0; d < sdim; ++d) {
+          double sn = std::sin(M_PI * (double)g[3 - sdim + d] / (double)Ns);
+          kk += 4.0 * sn * sn;
+        }
+        k2[o] = kk;
+      }
+      deg[o] += 1;
+    }
+    site_start.assign(S + 1, 0);
+    for (int o = 0; o < S; ++o) site_start[o + 1] = site_start[o] + deg[o];
+    site_list.assign(V, 0);
+    std::vector<long> fill(site_start.begin(), site_start.end() - 1);
+    for (long s = 0; s < V; ++s) site_list[fill[orbit_of_site[s]]++] = s;
+  }
+};
+
+// Cosine matrix of the even octant: C[X][x] = m(x) cos(2 pi x X / Ns), with
+// m(x) = 1 at x = 0 and at the Nyquist point, 2 elsewhere. For data that is
+// even along an axis, the length-Ns DFT along it equals this H x H product.
+static std::vector<double> octant_matrix(int Ns) {
+  int H = Ns / 2 + 1;
+  std::vector<double> C((size_t)H * H);
+  for (int X = 0; X < H; ++X)
+    for (int x = 0; x < H; ++x) {
+      double m = (x == 0 || (Ns % 2 == 0 && 2 * x == Ns)) ? 1.0 : 2.0;
+      C[(size_t)X * H + x] = m * std::cos(2.0 * M_PI * (double)((long)x * X % Ns) / (double)Ns);
+    }
+  return C;
+}
+
+// splitter (src/DefAbstractSimSetup.jl:7-10): xz = ceil.(range(0, n, length=k+1))
+static std::vector<std::pair<int, int>> splitter(int idxmin, int n, int k) {
+  std::vector<std::pair<int, int>> r;
+  std::vector<long> xz(k + 1);
+  for (int i = 0; i <= k; ++i) {
+    double v = (k == 0) ? 0.0 : (double)n * (double)i / (double)k;
+    xz[i] = (long)std::ceil(v - 1e-12 * std::max(1.0, std::fabs(v)));
+  }
+  for (int i = 0; i < k; ++i) r.push_back({(int)(xz[i] + idxmin), (int)(xz[i + 1] + idxmin - 1)});
+  return r;
+}
+
+static void parallel_chunks(const std::vector<std::pair<int, int>> &ranges,
+                            const std::function<void(int, int, int)> &body) {
+  if (ranges.size() <= 1) {
+    for (size_t c = 0; c < ranges.size(); ++c) body((int)c, ranges[c].first, ranges[c].second);
+    return;
+  }
+  std::vector<std::thread> th;
+  for (size_t c = 0; c < ranges.size(); ++c)
+    th.emplace_back([&, c]() { body((int)c, ranges[c].first, ranges[c].second); });
+  for (auto &t : th) t.join();
+}
+
+// ---------------------------------------------------------------------------
+// The simulation state: SymMatrix F, r and CyclVector SigF, Sigr
+// (src/DefSimDataElements.jl:88-230, TwoPIScalar_SimDataStruct.jl:63-89,204-247).
+// ---------------------------------------------------------------------------
+struct Oracle {
+  orc_params p{};
+  Orbits orb;
+  int nv = 0;       // values per stored lattice (V or S)
+  int M = 0;
+  int tmin = 0, tmax = 0;  // simdata.indices
+  std::vector<double> Fst, rst;      // M(M+1)/2 slots of nv values
+  std::vector<double> SigF, Sigr;    // M slots of nv values
+  std::vector<double> kL2, omega2;   // per stored value
+  double hartreemass2 = 0.0;
+  std::vector<double> Coct;          // octant cosine matrix
+  std::vector<FFTPlan> plans;
+  std::vector<FFTScratch> scratch;
+  std::vector<std::vector<double>> rhs;  // per chunk
+
+  int mod1(int i) const { return ((i - 1) % M + M) % M + 1; }
+  double thesign(int i, int j) const { return mod1(i) >= mod1(j) ? 1.0 : -1.0; }
+  size_t pair_slot(int i, int j) const {
+    int a = mod1(i) - 1, b = mod1(j) - 1;
+    if (a < b) std::swap(a, b);
+    return (size_t)a * (a + 1) / 2 + b;
+  }
+  void check(int i, int j) const {
+    if (!(tmin <= i && i <= tmax) || !(tmin <= j && j <= tmax))
+      throw std::out_of_range("Indices not in range!");
+  }
+  // raw slot values as stored (r carries the thesign of the slot order)
+  double *Fp(int i, int j) {
+    check(i, j);
+    return Fst.data() + pair_slot(i, j) * nv;
+  }
+  double *rp(int i, int j) {
+    check(i, j);
+    return rst.data() + pair_slot(i, j) * nv;
+  }
+  double *sigFp(int z) {
+    if (!(tmin <= z && z <= tmax)) throw std::out_of_range("Indices not in range!");
+    return SigF.data() + (size_t)(mod1(z) - 1) * nv;
+  }
+  double *sigrp(int z) {
+    if (!(tmin <= z && z <= tmax)) throw std::out_of_range("Indices not in range!");
+    return Sigr.data() + (size_t)(mod1(z) - 1) * nv;
+  }
+
+  void setup(const orc_params &pp) {
+    p = pp;
+    if (p.sdim < 1 || p.sdim > 3 || p.Ns < 1 || p.M < 3 || p.N < 1)
+      throw std::invalid_argument("bad parameters");
+    if (p.nthreads < 1) p.nthreads = 1;
+    orb.build(p.Ns, p.sdim);
+    M = p.M;
+    nv = (p.engine == ORC_ENGINE_FULL) ? (int)orb.V : orb.S;
+    size_t npairs = (size_t)M * (M + 1) / 2;
+    // createlattice returns ones (DefSimDataElements.jl:24-28)
+    Fst.assign(npairs * nv, 1.0);
+    rst.assign(npairs * nv, 1.0);
+    SigF.assign((size_t)M * nv, 0.0);
+    Sigr.assign((size_t)M * nv, 0.0);
+    kL2.assign(nv, 0.0);
+    omega2.assign(nv, 0.0);
+    // getTwoPISimData (TwoPIScalar_SimDataStruct.jl:669-687)
+    for (int v = 0; v < nv; ++v) {
+      int o = (p.engine == ORC_ENGINE_FULL) ? orb.orbit_of_site[v] : v;
+      kL2[v] = orb.k2[o];
+      omega2[v] = (orb.k2[o] + p.mass * p.mass) * (p.dt * p.dt);
+    }
+    Coct = octant_matrix(p.Ns);
+    plans.clear();
+    plans.emplace_back(p.Ns);
+    scratch.resize(p.nthreads);
+    for (auto &s : scratch) {
+      s.a.resize(p.Ns);
+      s.b.resize(p.Ns);
+      s.tmp.resize(64 * 64);
+      s.lat.resize(orb.V);
+      s.lat2.resize(orb.V);
+    }
+    rhs.assign(p.nthreads, std::vector<double>(nv));
+  }
+
+  // expandSimData! (TwoPIScalar_SimDataStruct.jl:262-278, DefSimDataElements.jl:141-165)
+  void expand() {
+    if (tmax + 1 > M) {
+      tmin += 1;
+      tmax += 1;
+    } else {
+      tmin = 1;
+      tmax += 1;
+    }
+  }
+
+  double hartree_prefactor() const {
+    // Hartreeprefactor for the lambda expansion (TwoPIScalar_Initialization.jl:245)
+    return p.lambda * (double)(p.N + 2) / (double)(6 * p.N);
+  }
+  double ivol() const { return 1.0 / (double)orb.V; }
+
+  // getHartreeMass2 (TwoPIScalar_Initialization.jl:207-229)
+  double hartree(int a, int b) {
+    double h = 0.0;
+    const double *F = Fp(a, b);
+    if (p.engine == ORC_ENGINE_FULL) {
+      // loop over shells and their sites: every site once
+      for (int o = 0; o < orb.S; ++o)
+        for (long q = orb.site_start[o]; q < orb.site_start[o + 1]; ++q) h += F[orb.site_list[q]];
+    } else {
+      for (int o = 0; o < orb.S; ++o) h += F[o] * (double)orb.deg[o];
+    }
+    h *= hartree_prefactor() * ivol();
+    h += p.mass2;
+    return h;
+  }
+
+  // --- 3D FFT on the full lattice, column-major --------------------------
+  void fft_lattice(cplx *x, int sign, FFTScratch &sc) {
+    const int Ns = p.Ns;
+    const FFTPlan &pl = plans[0];
+    long stride = 1;
+    for (int d = 0; d < p.sdim; ++d) {
+      long nlines = orb.V / Ns;
+      for (long l = 0; l < nlines; ++l) {
+        long lo = l % stride, hi = l / stride;
+        long base = lo + hi * stride * Ns;
+        pl.run(x + base, (int)stride, sign, sc.a, sc.b, sc.tmp);
+      }
+      stride *= Ns;
+    }
+  }
+  // real(rfft(x)) followed by the Hermitian extension brfft applies to the
+  // half spectrum: the values with first index above Ns/2 are those of -k.
+  void real_half_spectrum(std::vector<cplx> &X) {
+    const int Ns = p.Ns;
+    for (long s = 0; s < orb.V; ++s) X[s] = cplx(X[s].real(), 0.0);
+    for (long s = 0; s < orb.V; ++s) {
+      int n[3] = {0, 0, 0};
+      long r = s;
+      for (int d = 0; d < p.sdim; ++d) {
+        n[d] = (int)(r % Ns);
+        r /= Ns;
+      }
+      if (n[0] <= Ns / 2) continue;
+      long m = 0, mul = 1;
+      for (int d = 0; d < p.sdim; ++d) {
+        m += (long)((Ns - n[d]) % Ns) * mul;
+        mul *= Ns;
+      }
+      X[s] = X[m];
+    }
+  }
+
+  // One sunset on full lattices: Fin, rin (rin already times thesign).
+  // calcSelfEnergyattp! CPUfull (TwoPIScalar_Evolution.jl:25-31)
+  void sunset_lattice(const double *Fin, const double *rin, double *sF, double *sr, FFTScratch &sc) {
+    std::vector<cplx> &X = sc.lat, &Y = sc.lat2;
+    for (long s = 0; s < orb.V; ++s) X[s] = cplx(rin[s], 0.0);
+    fft_lattice(X.data(), -1, sc);
+    real_half_spectrum(X);  // rx
+    for (long s = 0; s < orb.V; ++s) Y[s] = cplx(Fin[s], 0.0);
+    fft_lattice(Y.data(), -1, sc);
+    real_half_spectrum(Y);  // Fx
+    const double iv = ivol();
+    const double lam2 = p.lambda * p.lambda;
+    const double N = (double)p.N;
+    const double fr = iv * iv * iv * (-lam2 * (N + 2.0) / (6.0 * N * N));
+    const double fF = iv * iv * iv * (-lam2 * (N + 2.0) / (18.0 * N * N));
+    const bool classical = (p.pexp == ORC_PEXP_NLO_CLASSICAL);
+    // pointwise products, then brfft
+    std::vector<cplx> Z(orb.V);
+    for (long s = 0; s < orb.V; ++s) {
+      double rx = X[s].real(), Fx = Y[s].real();
+      double gr = classical ? rx * (Fx * Fx) : rx * (Fx * Fx - (1 / 12.) * (rx * rx));
+      double gF = classical ? Fx * (Fx * Fx) : Fx * (Fx * Fx - 0.75 * (rx * rx));
+      X[s] = cplx(gr, 0.0);
+      Z[s] = cplx(gF, 0.0);
+    }
+    fft_lattice(X.data(), +1, sc);
+    fft_lattice(Z.data(), +1, sc);
+    for (long s = 0; s < orb.V; ++s) {
+      sr[s] = fr * X[s].real();
+      sF[s] = fF * Z[s].real();
+    }
+  }
+
+  // Octant form of the same sunset on orbit rows (ENGINE_OCTANT).
+  void octant_transform(std::vector<double> &a, std::vector<double> &tmp) {
+    const int H = orb.H;
+    long npt = 1;
+    for (int d = 0; d < p.sdim; ++d) npt *= H;
+    long stride = 1;
+    for (int d = 0; d < p.sdim; ++d) {
+      for (long q = 0; q < npt; ++q) {
+        long xi = (q / stride) % H;
+        long base = q - xi * stride;
+        double s = 0.0;
+        for (int x = 0; x < H; ++x) s += Coct[(size_t)xi * H + x] * a[base + (long)x * stride];
+        tmp[q] = s;
+      }
+      std::swap(a, tmp);
+      stride *= H;
+    }
+  }
+  void sunset_octant(const double *Fin, const double *rin, double *sF, double *sr) {
+    const int H = orb.H;
+    long npt = 1;
+    for (int d = 0; d < p.sdim; ++d) npt *= H;
+    std::vector<double> fa(npt), ra(npt), tmp(npt);
+    for (long q = 0; q < npt; ++q) {
+      int g[3] = {0, 0, 0};
+      long r = q;
+      for (int d = 0; d < p.sdim; ++d) {
+        g[3 - p.sdim + d] = (int)(r % H);
+        r /= H;
+      }
+      std::sort(g + 3 - p.sdim, g + 3);
+      long o = Orbits::tri_index(p.sdim, g[0], g[1], g[2]);
+      fa[q] = Fin[o];
+      ra[q] = rin[o];
+    }
+    octant_transform(fa, tmp);
+    octant_transform(ra, tmp);
+    const double iv = ivol();
+    const double lam2 = p.lambda * p.lambda;
+    const double N = (double)p.N;
+    const double fr = iv * iv * iv * (-lam2 * (N + 2.0) / (6.0 * N * N));
+    const double fF = iv * iv * iv * (-lam2 * (N + 2.0) / (18.0 * N * N));
+    const bool classical = (p.pexp == ORC_PEXP_NLO_CLASSICAL);
+    for (long q = 0; q < npt; ++q) {
+      double rx = ra[q], Fx = fa[q];
+      ra[q] = classical ? rx * (Fx * Fx) : rx * (Fx * Fx - (1 / 12.) * (rx * rx));
+      fa[q] = classical ? Fx * (Fx * Fx) : Fx * (Fx * Fx - 0.75 * (rx * rx));
+    }
+    octant_transform(fa, tmp);
+    octant_transform(ra, tmp);
+    for (int o = 0; o < orb.S; ++o) {
+      long q = 0, mul = 1;
+      for (int d = 0; d < p.sdim; ++d) {
+        q += (long)orb.rep[3 * o + 3 - p.sdim + d] * mul;
+        mul *= H;
+      }
+      sr[o] = fr * ra[q];
+      sF[o] = fF * fa[q];
+    }
+  }
+
+  void sunset_rows(const double *F, const double *r, double *sF, double *sr, FFTScratch &sc) {
+    if (p.engine == ORC_ENGINE_FULL) {
+      sunset_lattice(F, r, sF, sr, sc);
+    } else if (p.engine == ORC_ENGINE_ORBIT) {
+      // copytolattice! -> FFT sunset -> copytoreducedlattice!
+      // (TwoPIScalar_Evolution.jl:91-105, DefSimDataElements.jl:71-83)
+      std::vector<double> Fl(orb.V), rl(orb.V), sFl(orb.V), srl(orb.V);
+      for (long s = 0; s < orb.V; ++s) {
+        Fl[s] = F[orb.orbit_of_site[s]];
+        rl[s] = r[orb.orbit_of_site[s]];
+      }
+      sunset_lattice(Fl.data(), rl.data(), sFl.data(), srl.data(), sc);
+      for (int o = 0; o < orb.S; ++o) {
+        sF[o] = sFl[orb.rep_site[o]];
+        sr[o] = srl[orb.rep_site[o]];
+      }
+    } else {
+      sunset_octant(F, r, sF, sr);
+    }
+  }
+
+  // calcSelfEnergyattp! (TwoPIScalar_Evolution.jl:25-31 / 91-105)
+  void self_energy_at(int tmone, int tp, int ichunk) {
+    std::vector<double> rs(nv);
+    const double s = thesign(tmone, tp);
+    const double *r = rp(tmone, tp);
+    for (int v = 0; v < nv; ++v) rs[v] = r[v] * s;
+    sunset_rows(Fp(tmone, tp), rs.data(), sigFp(tp), sigrp(tp), scratch[ichunk]);
+  }
+
+  // calcSelfEnergies! (TwoPIScalar_Evolution.jl:8-23)
+  void self_energies(int tmone) {
+    if (p.pexp == ORC_PEXP_LO) return;  // LO: no self-energy (:8-9)
+    int n = (tmax - 1) - tmin + 1;
+    auto ranges = splitter(tmin, n, p.nthreads);
+    parallel_chunks(ranges, [&](int c, int lo, int hi) {
+      for (int tp = lo; tp <= hi; ++tp) self_energy_at(tmone, tp, c);
+    });
+  }
+
+  // getRHS_r! (TwoPIScalar_Evolution.jl:846-865); LO: zero (:842-844)
+  void rhs_r(double *Mem, int t, int tp) {
+    for (int v = 0; v < nv; ++v) Mem[v] = 0.0;
+    if (p.pexp == ORC_PEXP_LO) return;
+    for (int z = tp + 1; z <= t - 2; ++z) {
+      const double *S = sigrp(z), *r = rp(z, tp);
+      const double s = thesign(z, tp);
+      for (int v = 0; v < nv; ++v) Mem[v] -= S[v] * r[v] * s;
+    }
+  }
+  // getRHS_F! (TwoPIScalar_Evolution.jl:766-801); LO: zero (:763-765)
+  void rhs_F(double *Mem, int t, int tp) {
+    if (p.pexp == ORC_PEXP_LO) {
+      for (int v = 0; v < nv; ++v) Mem[v] = 0.0;
+      return;
+    }
+    const int tpmin = tmin;
+    {
+      const double *S = sigrp(tpmin), *F = Fp(tpmin, tp);
+      for (int v = 0; v < nv; ++v) Mem[v] = S[v] * F[v];
+      for (int v = 0; v < nv; ++v) Mem[v] *= -0.5;
+    }
+    for (int z = tpmin + 1; z <= t - 2; ++z) {
+      const double *S = sigrp(z), *F = Fp(z, tp);
+      for (int v = 0; v < nv; ++v) Mem[v] -= S[v] * F[v];
+    }
+    {
+      const double *S = sigFp(tpmin), *r = rp(tpmin, tp);
+      const double s = thesign(tpmin, tp);
+      for (int v = 0; v < nv; ++v) Mem[v] += 0.5 * S[v] * r[v] * s;
+    }
+    for (int z = tpmin + 1; z <= tp - 1; ++z) {
+      const double *S = sigFp(z), *r = rp(z, tp);
+      const double s = thesign(z, tp);
+      for (int v = 0; v < nv; ++v) Mem[v] += S[v] * r[v] * s;
+    }
+  }
+  // evolve_r! (TwoPIScalar_Evolution.jl:890-905)
+  void evolve_r(double *RHS, int t, int tp) {
+    double *out = rp(t, tp);
+    const double st = thesign(t, tp);
+    if (tp == t - 1) {
+      for (int v = 0; v < nv; ++v) out[v] = st * p.dt;
+    } else if (tp == t) {
+      for (int v = 0; v < nv; ++v) out[v] = 0.0;
+    } else {
+      const double dt3 = p.dt * p.dt * p.dt;
+      for (int v = 0; v < nv; ++v) RHS[v] *= dt3;
+      const double *r1 = rp(t - 1, tp), *r2 = rp(t - 2, tp);
+      const double s1 = thesign(t - 1, tp), s2 = thesign(t - 2, tp);
+      for (int v = 0; v < nv; ++v) out[v] = (2 - omega2[v]) * r1[v] * s1 - r2[v] * s2 + RHS[v];
+      for (int v = 0; v < nv; ++v) out[v] *= st;
+    }
+  }
+  // evolve_F! (TwoPIScalar_Evolution.jl:908-915)
+  void evolve_F(double *RHS, int t, int tp) {
+    const double dt3 = p.dt * p.dt * p.dt;
+    for (int v = 0; v < nv; ++v) RHS[v] *= dt3;
+    double *out = Fp(t, tp);
+    const double *F1 = Fp(t - 1, tp), *F2 = Fp(t - 2, tp);
+    for (int v = 0; v < nv; ++v) out[v] = (2 - omega2[v]) * F1[v] - F2[v] + RHS[v];
+  }
+  // setomega2values! (TwoPIScalar_Evolution.jl:918-921)
+  void set_omega2() {
+    for (int v = 0; v < nv; ++v) omega2[v] = kL2[v] + hartreemass2;
+    for (int v = 0; v < nv; ++v) omega2[v] *= p.dt * p.dt;
+  }
+
+  // evolve! (TwoPIScalar_Evolution.jl:924-981)
+  void evolve(int t) {
+    expand();
+    if (tmax != t) throw std::invalid_argument("evolve! must be called with t = lastEvolStep + 1");
+    self_energies(t - 1);
+    hartreemass2 = hartree(t - 1, t - 1);
+    set_omega2();
+    int n = (tmax - 1) - tmin + 1;
+    auto ranges = splitter(tmin, n, p.nthreads);
+    parallel_chunks(ranges, [&](int c, int lo, int hi) {
+      double *R = rhs[c].data();
+      for (int tp = lo; tp <= hi; ++tp) {
+        rhs_r(R, t, tp);
+        evolve_r(R, t, tp);
+        rhs_F(R, t, tp);
+        evolve_F(R, t, tp);
+      }
+    });
+    double *R = rhs[0].data();
+    evolve_r(R, t, t);
+    rhs_F(R, t, t);
+    evolve_F(R, t, t);
+  }
+
+  // initSimData! (TwoPIScalar_Initialization.jl:8-47)
+  void init_occupation(const double *n, double initmass) {
+    expand();
+    expand();
+    for (int v = 0; v < nv; ++v) {
+      int o = (p.engine == ORC_ENGINE_FULL) ? orb.orbit_of_site[v] : v;
+      double omega = std::sqrt(orb.k2[o] + initmass * initmass);
+      Fp(1, 1)[v] = (1 / omega) * (n[o] + 0.5);
+      Fp(2, 1)[v] = (1 / omega) * (n[o] + 0.5);
+      Fp(2, 2)[v] = (omega * (n[o] + 0.5) * (p.dt * p.dt) + (1 / omega) * (n[o] + 0.5));
+      rp(1, 1)[v] = 0.0;
+      rp(2, 1)[v] = p.dt * thesign(2, 1);
+      rp(2, 2)[v] = 0.0;
+    }
+    hartreemass2 = hartree(2, 2);
+  }
+  // initSimData! for the Gauss state (TwoPIScalar_Initialization.jl:95-112)
+  void init_gauss(double xi, double eta, double sig) {
+    expand();
+    expand();
+    for (int v = 0; v < nv; ++v) {
+      Fp(1, 1)[v] = xi * xi;
+      Fp(2, 1)[v] = xi * eta * p.dt + Fp(1, 1)[v];
+      Fp(2, 2)[v] = (eta * eta + sig * sig / (4 * xi * xi)) * (p.dt * p.dt) - Fp(1, 1)[v] + 2 * Fp(2, 1)[v];
+      rp(1, 1)[v] = 0.0;
+      rp(2, 1)[v] = p.dt * thesign(2, 1);
+      rp(2, 2)[v] = 0.0;
+    }
+    hartreemass2 = hartree(2, 2);
+  }
+
+  int meas_idx(int o) const { return (p.engine == ORC_ENGINE_FULL) ? (int)orb.rep_site[o] : o; }
+
+  // createMeasurement (TwoPIScalar_Measurement.jl:31-99, 135-197)
+  void measure(int t, orc_scalars *sc, double *oF, double *oddF, double *on, double *oomega,
+               double *oc, double *Fonet, double *ronet, double *osigF, double *osigr) {
+    const double dt = p.dt;
+    std::vector<double> ddF(orb.S), Fm(orb.S), om(orb.S), cc(orb.S), nn(orb.S);
+    const double *Ftt = Fp(t, t), *Fmt = Fp(t - 1, t), *Fmm = Fp(t - 1, t - 1);
+    for (int i = 0; i < orb.S; ++i) {
+      int idx = meas_idx(i);
+      ddF[i] = (Ftt[idx] - 2 * Fmt[idx] + Fmm[idx]) / (dt * dt);
+      Fm[i] = Fmm[idx];
+      om[i] = (ddF[i] / Fmm[idx] > 0) ? std::sqrt(ddF[i] / Fmm[idx]) : 0.0;
+      cc[i] = (0.25 * (dt * dt) * (om[i] * om[i]) < 1) ? std::sqrt(1. - 0.25 * (dt * dt) * (om[i] * om[i])) : 1.0;
+      nn[i] = (ddF[i] * Fmm[idx] > 0) ? (cc[i] * std::sqrt(ddF[i] * Fmm[idx])) - 0.5 : 0.0;
+    }
+    double E_kin = 0.0, E_pot = 0.0, E_mem = 0.0, hc = 0.0;
+    for (int i = 0; i < orb.S; ++i) E_kin += 0.5 * ddF[i] * (double)orb.deg[i];
+    for (int i = 0; i < orb.S; ++i) hc += Fm[i] * (double)orb.deg[i];
+    for (int i = 0; i < orb.S; ++i)
+      E_pot += 0.5 * (p.mass2 + orb.k2[i] + 0.5 * ivol() * hartree_prefactor() * hc) * Fm[i] * (double)orb.deg[i];
+    if (t != 2) {
+      const int tp0 = tmin;
+      if (p.engine == ORC_ENGINE_FULL) {
+        const double *S1 = sigrp(tp0), *F = Fp(tp0, t - 1), *S2 = sigFp(tp0), *r = rp(tp0, t - 1);
+        const double s = thesign(tp0, t - 1);
+        double acc = 0.0;
+        for (int v = 0; v < nv; ++v) acc += S1[v] * F[v] - S2[v] * r[v] * s;
+        E_mem = 0.5 * 0.25 * dt * acc;
+        if (t > 3) {
+          double tot = 0.0;
+          for (int tp = tp0 + 1; tp <= t - 2; ++tp) {
+            const double *A = sigrp(tp), *B = Fp(tp, t - 1), *C = sigFp(tp), *D = rp(tp, t - 1);
+            const double st = thesign(tp, t - 1);
+            double a = 0.0;
+            for (int v = 0; v < nv; ++v) a += A[v] * B[v] - C[v] * D[v] * st;
+            tot += a;
+          }
+          E_mem += 0.25 * dt * tot;
+        }
+      } else {
+        const double *S1 = sigrp(tp0), *F = Fp(tp0, t - 1), *S2 = sigFp(tp0), *r = rp(tp0, t - 1);
+        const double s = thesign(tp0, t - 1);
+        for (int i = 0; i < orb.S; ++i)
+          E_mem += 0.5 * 0.25 * dt * (double)orb.deg[i] * (S1[i] * F[i] - S2[i] * r[i] * s);
+        if (t > 3) {
+          for (int i = 0; i < orb.S; ++i)
+            for (int tp = tp0 + 1; tp <= t - 2; ++tp) {
+              const double st = thesign(tp, t - 1);
+              E_mem += 0.25 * dt * (double)orb.deg[i] *
+                       (sigrp(tp)[i] * Fp(tp, t - 1)[i] - sigFp(tp)[i] * rp(tp, t - 1)[i] * st);
+            }
+        }
+      }
+    }
+    sc->time = (t - 1) * dt * p.mass;
+    sc->M2 = hartreemass2;
+    sc->E_kin = E_kin;
+    sc->E_pot = E_pot;
+    sc->E_mem = E_mem;
+    sc->E = E_kin + E_pot + E_mem;
+    for (int i = 0; i < orb.S; ++i) {
+      if (oF) oF[i] = Fm[i];
+      if (oddF) oddF[i] = ddF[i];
+      if (on) on[i] = nn[i];
+      if (oomega) oomega[i] = om[i];
+      if (oc) oc[i] = cc[i];
+    }
+    // traces at site 1 (Measurement.jl:89-96)
+    int k = 0;
+    if (osigF || osigr)
+      for (int tp = tmax - 1; tp >= tmin; --tp, ++k) {
+        if (osigF) osigF[k] = sigFp(tp)[0];
+        if (osigr) osigr[k] = sigrp(tp)[0];
+      }
+    k = 0;
+    if (Fonet || ronet)
+      for (int tp = tmin; tp <= tmax - 1; ++tp, ++k) {
+        if (Fonet) Fonet[k] = Fp(tmin, tp)[0];
+        if (ronet) ronet[k] = rp(tmin, tp)[0] * thesign(tmin, tp);
+      }
+  }
+
+  // getGapMass (TwoPIScalar_Initialization.jl:250-266); Newton's method on
+  // the gap equation with its analytic derivative.
+  double gap_mass(const double *n, double x0) {
+    auto g = [&](double x, double *dg) {
+      double res = 0.0, dres = 0.0;
+      for (int i = 0; i < orb.S; ++i) {
+        double w2 = orb.k2[i] + x * x;
+        res += (1 / std::sqrt(w2)) * (n[i] + 0.5) * (double)orb.deg[i];
+        dres += -x / (w2 * std::sqrt(w2)) * (n[i] + 0.5) * (double)orb.deg[i];
+      }
+      *dg = dres * ivol() * hartree_prefactor() - 2 * x;
+      return res * ivol() * hartree_prefactor() + p.mass2 - x * x;
+    };
+    double x = x0;
+    for (int it = 0; it < 200; ++it) {
+      double d;
+      double f = g(x, &d);
+      if (f == 0.0) break;
+      double xn = x - f / d;
+      if (std::fabs(xn - x) <= 4 * 2.220446049250313e-16 * std::fabs(xn)) {
+        x = xn;
+        break;
+      }
+      x = xn;
+    }
+    return x;
+  }
+};
+
+template <class Fn>
+int guarded(Fn f) {
+  try {
+    f();
+    return 0;
+  } catch (const std::out_of_range &) {
+    return -6;
+  } catch (const std::invalid_argument &) {
+    return -1;
+  } catch (...) {
+    return -99;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+void *orc_create(const orc_params *p) {
+  try {
+    Oracle *o = new Oracle();
+    o->setup(*p);
+    return o;
+  } catch (...) {
+    return nullptr;
+  }
+}
+void orc_destroy(void *h) { delete (Oracle *)h; }
+int orc_num_orbits(void *h) { return ((Oracle *)h)->orb.S; }
+int64_t orc_num_sites(void *h) { return ((Oracle *)h)->orb.V; }
+void orc_orbits(void *h, int32_t *rep, double *k2, int64_t *deg) {
+  Oracle *o = (Oracle *)h;
+  for (int i = 0; i < o->orb.S; ++i) {
+    if (rep)
+      for (int d = 0; d < 3; ++d) rep[3 * i + d] = o->orb.rep[3 * i + d];
+    if (k2) k2[i] = o->orb.k2[i];
+    if (deg) deg[i] = o->orb.deg[i];
+  }
+}
+void orc_site_orbit(void *h, int32_t *out) {
+  Oracle *o = (Oracle *)h;
+  std::memcpy(out, o->orb.orbit_of_site.data(), sizeof(int32_t) * o->orb.V);
+}
+int orc_init_occupation(void *h, const double *n, double m) {
+  return guarded([&] { ((Oracle *)h)->init_occupation(n, m); });
+}
+int orc_init_gauss(void *h, double xi, double eta, double sig) {
+  return guarded([&] { ((Oracle *)h)->init_gauss(xi, eta, sig); });
+}
+int orc_step(void *h, int32_t t) {
+  return guarded([&] { ((Oracle *)h)->evolve(t); });
+}
+int orc_expand(void *h) {
+  return guarded([&] { ((Oracle *)h)->expand(); });
+}
+int orc_self_energies(void *h, int32_t tmone) {
+  return guarded([&] { ((Oracle *)h)->self_energies(tmone); });
+}
+int orc_measure(void *h, int32_t t, orc_scalars *s, double *F, double *ddF, double *n,
+                double *omega, double *c, double *Fonet, double *ronet, double *sigF, double *sigr) {
+  return guarded([&] { ((Oracle *)h)->measure(t, s, F, ddF, n, omega, c, Fonet, ronet, sigF, sigr); });
+}
+int orc_get(void *h, int32_t which, int32_t a, int32_t b, double *out) {
+  Oracle *o = (Oracle *)h;
+  return guarded([&] {
+    const double *src = which == 0 ? o->Fp(a, b) : o->rp(a, b);
+    double s = which == 0 ? 1.0 : o->thesign(a, b);
+    for (int i = 0; i < o->orb.S; ++i) out[i] = src[o->meas_idx(i)] * s;
+  });
+}
+int orc_set(void *h, int32_t which, int32_t a, int32_t b, const double *in) {
+  Oracle *o = (Oracle *)h;
+  return guarded([&] {
+    double *dst = which == 0 ? o->Fp(a, b) : o->rp(a, b);
+    double s = which == 0 ? 1.0 : o->thesign(a, b);
+    for (int v = 0; v < o->nv; ++v) {
+      int orb = (o->p.engine == ORC_ENGINE_FULL) ? o->orb.orbit_of_site[v] : v;
+      dst[v] = in[orb] * s;
+    }
+  });
+}
+int orc_get_sigma(void *h, int32_t which, int32_t z, double *out) {
+  Oracle *o = (Oracle *)h;
+  return guarded([&] {
+    const double *src = which == 0 ? o->sigFp(z) : o->sigrp(z);
+    for (int i = 0; i < o->orb.S; ++i) out[i] = src[o->meas_idx(i)];
+  });
+}
+int orc_get_lattice(void *h, int32_t which, int32_t a, int32_t b, double *out) {
+  Oracle *o = (Oracle *)h;
+  if (o->p.engine != ORC_ENGINE_FULL) return -1;
+  return guarded([&] {
+    const double *src = which == 0 ? o->Fp(a, b) : o->rp(a, b);
+    double s = which == 0 ? 1.0 : o->thesign(a, b);
+    for (long v = 0; v < o->orb.V; ++v) out[v] = src[v] * s;
+  });
+}
+int orc_window(void *h, int32_t *tmin, int32_t *tmax) {
+  Oracle *o = (Oracle *)h;
+  *tmin = o->tmin;
+  *tmax = o->tmax;
+  return 0;
+}
+double orc_hartree_mass2(void *h, int32_t a, int32_t b) {
+  double v = 0.0;
+  guarded([&] { v = ((Oracle *)h)->hartree(a, b); });
+  return v;
+}
+double orc_hartree_prefactor(void *h) { return ((Oracle *)h)->hartree_prefactor(); }
+double orc_gap_mass(void *h, const double *n, double x0) { return ((Oracle *)h)->gap_mass(n, x0); }
+int orc_sunset_rows(void *h, const double *F, const double *rho, double *sig_F, double *sig_r) {
+  Oracle *o = (Oracle *)h;
+  return guarded([&] {
+    if (o->p.engine == ORC_ENGINE_FULL) {
+      std::vector<double> Fl(o->orb.V), rl(o->orb.V), a(o->orb.V), b(o->orb.V);
+      for (long s = 0; s < o->orb.V; ++s) {
+        Fl[s] = F[o->orb.orbit_of_site[s]];
+        rl[s] = rho[o->orb.orbit_of_site[s]];
+      }
+      o->sunset_lattice(Fl.data(), rl.data(), a.data(), b.data(), o->scratch[0]);
+      for (int i = 0; i < o->orb.S; ++i) {
+        sig_F[i] = a[o->orb.rep_site[i]];
+        sig_r[i] = b[o->orb.rep_site[i]];
+      }
+    } else {
+      o->sunset_rows(F, rho, sig_F, sig_r, o->scratch[0]);
+    }
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,747 @@
+// kb_api.cu -- host side of libkb2pi: the C ABI declared in include/kb2pi.h.
+//
+// Owns the device memory of one or more runs, orchestrates one KB step as
+// two kernel launches (sunset, memory integral + leapfrog), captures multi-step
+// sequences in a CUDA graph, and exposes host views of the history for the
+// reference's measure!/getindex. No computation of the step happens on the
+// host; without a CUDA device every entry point fails with KB_ERR_NODEV.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/kb2pi.h"
+#include "kb_internal.cuh"
+
+using kb::KC;
+using kb::RunDev;
+
+namespace {
+
+struct Run {
+  kb_params p{};
+  int H = 0, S = 0, Spad = 0, nchunks = 0, Malloc = 0, T = 0;
+  long V = 0;
+  std::vector<int32_t> rep;   // 3 per orbit
+  std::vector<double> k2, degd;
+  std::vector<int64_t> deg;
+  std::vector<double> Cm;
+  size_t esz = 8;  // bytes per stored history element
+  // device allocations
+  void *hist_F = nullptr, *hist_r = nullptr, *sig_F = nullptr, *sig_r = nullptr;
+  double *st_F = nullptr, *st_r = nullptr, *k2_d = nullptr, *deg_d = nullptr, *Cm_d = nullptr;
+  double *tad = nullptr, *meas = nullptr, *epart = nullptr;
+  size_t hist_elems = 0, st_elems = 0, sig_elems = 0;
+  RunDev dev{};
+};
+
+}  // namespace
+
+struct kb_handle {
+  std::string err;
+  int device = 0;
+  cudaStream_t st = nullptr;
+  bool fp64 = true;
+  std::vector<Run> runs;
+  RunDev *d_runs = nullptr;
+  int *d_base_sun = nullptr, *d_base_mi = nullptr;
+  int total_sun = 0, total_mi = 0;
+  int *d_t = nullptr, *d_err = nullptr;
+  size_t smem_sun = 0, smem_mi = 0;
+  int t_cur = 0;      // last evolved (or initialised) step; window is [tmin(t_cur), t_cur]
+  int inited_runs = 0;
+  bool any_nlo = false;
+  bool sigma_valid = false;
+  cudaGraphExec_t graph = nullptr;
+  int graph_measure = -1;
+};
+
+namespace {
+
+thread_local std::string g_create_err;
+
+int fail(kb_handle *h, int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (h) h->err = buf;
+  else g_create_err = buf;
+  return code;
+}
+
+#define KB_CUDA(h, call)                                                                 \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess)                                                               \
+      return fail((h), KB_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));     \
+  } while (0)
+
+long tet3h(int c) { return (long)c * (c + 1) * (c + 2) / 6; }
+
+// cubic orbits of the Ns^3 lattice (same numbering as the kernels)
+void build_orbits(Run &R) {
+  const int Ns = R.p.Ns, H = Ns / 2 + 1;
+  R.H = H;
+  R.S = (int)tet3h(H);
+  R.V = (long)Ns * Ns * Ns;
+  R.rep.assign((size_t)3 * R.S, 0);
+  R.k2.assign(R.S, 0.0);
+  R.deg.assign(R.S, 0);
+  auto mult = [&](int x) { return (x == 0 || 2 * x == Ns) ? 1 : 2; };
+  for (int c = 0; c < H; ++c)
+    for (int b = 0; b <= c; ++b)
+      for (int a = 0; a <= b; ++a) {
+        const int o = kb::orb3(a, b, c);
+        R.rep[3 * o] = a;
+        R.rep[3 * o + 1] = b;
+        R.rep[3 * o + 2] = c;
+        double kk = 0.0;
+        for (int v : {a, b, c}) {
+          const double s = std::sin(M_PI * (double)v / (double)Ns);
+          kk += 4.0 * s * s;
+        }
+        R.k2[o] = kk;
+        const int nperm = (a == b && b == c) ? 1 : ((a == b || b == c) ? 3 : 6);
+        R.deg[o] = (int64_t)nperm * mult(a) * mult(b) * mult(c);
+      }
+  R.nchunks = (R.S + KC - 1) / KC;
+  R.Spad = R.nchunks * KC;
+  R.degd.assign(R.Spad, 0.0);
+  for (int o = 0; o < R.S; ++o) R.degd[o] = (double)R.deg[o];
+  R.Cm.assign((size_t)H * H, 0.0);
+  for (int X = 0; X < H; ++X)
+    for (int x = 0; x < H; ++x)
+      R.Cm[(size_t)X * H + x] = mult(x) * std::cos(2.0 * M_PI * (double)((long)x * X % Ns) / (double)Ns);
+}
+
+int validate(const kb_params &p, std::string &why) {
+  char b[256];
+  if (p.sdim != 3) { snprintf(b, sizeof b, "sdim=%d: only sdim=3 lattices are supported", p.sdim); why = b; return -1; }
+  if ((p.Ns < 2 || p.Ns > 64 || (p.Ns % 2) != 0) && p.Ns != 1) { snprintf(b, sizeof b, "Ns=%d must be 1 or even in [2,64]", p.Ns); why = b; return -1; }
+  if (p.M < 3 || p.M > 1024) { snprintf(b, sizeof b, "NstepsinMemory=%d must be in [3,1024]", p.M); why = b; return -1; }
+  if (p.N < 1) { why = "ONgroup must be >= 1"; return -1; }
+  if (!(p.dt > 0.0) || !std::isfinite(p.dt)) { why = "dt must be positive"; return -1; }
+  if (p.pexp < 0 || p.pexp > 2) { why = "pexp must be KB_PEXP_LO, _NLO_QUANTUM or _NLO_CLASSICAL"; return -1; }
+  if (p.precision != KB_PREC_FP64 && p.precision != KB_PREC_MIXED) { why = "unknown precision"; return -1; }
+  if (!std::isfinite(p.lambda) || !std::isfinite(p.mass2) || !std::isfinite(p.mass)) { why = "non-finite coupling or mass"; return -1; }
+  return 0;
+}
+
+size_t slot_off(const Run &R, int a) { return (size_t)(a % R.Malloc); }
+
+void free_run(Run &R) {
+  void *ptrs[] = {R.hist_F, R.hist_r, R.sig_F, R.sig_r, R.st_F, R.st_r, R.k2_d, R.deg_d, R.Cm_d, R.tad, R.meas, R.epart};
+  for (void *q : ptrs)
+    if (q) cudaFree(q);
+}
+
+int tmin_of(const Run &R, int t) { return std::max(1, t - R.p.M + 1); }
+
+// host <-> device copies of one (a, b) element column: S values spread over
+// chunks (KC contiguous per chunk)
+template <typename TS>
+void gather_host(const std::vector<TS> &chunked, int S, double *out) {
+  for (int o = 0; o < S; ++o) out[o] = (double)chunked[o];
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------
+extern "C" {
+
+const char *kb_last_error(const kb_handle *h) { return h ? h->err.c_str() : g_create_err.c_str(); }
+
+int kb_create(const kb_params *p, kb_handle **out) { return kb_create_batch(p, 1, out); }
+
+int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out) {
+  if (!out || !p || nruns < 1) return fail(nullptr, KB_ERR_PARAM, "kb_create: null argument or nruns < 1");
+  *out = nullptr;
+  for (int r = 0; r < nruns; ++r) {
+    std::string why;
+    if (validate(p[r], why)) return fail(nullptr, KB_ERR_PARAM, "run %d: %s", r, why.c_str());
+    if (p[r].precision != p[0].precision) return fail(nullptr, KB_ERR_PARAM, "all runs of a handle need the same precision");
+    if (p[r].device != p[0].device) return fail(nullptr, KB_ERR_PARAM, "all runs of a handle need the same device");
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return fail(nullptr, KB_ERR_NODEV, "no CUDA device available");
+  }
+  if (p[0].device < 0 || p[0].device >= ndev) return fail(nullptr, KB_ERR_PARAM, "device %d out of range", p[0].device);
+  kb_handle *h = new kb_handle();
+  h->device = p[0].device;
+  h->fp64 = (p[0].precision == KB_PREC_FP64);
+  if (cudaSetDevice(h->device) != cudaSuccess) { delete h; return fail(nullptr, KB_ERR_CUDA, "cudaSetDevice failed"); }
+  if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) {
+    delete h;
+    return fail(nullptr, KB_ERR_CUDA, "cudaStreamCreate failed");
+  }
+  const int T = kb::memint_tile(h->fp64);
+  h->runs.resize(nruns);
+  size_t smem_sun = 0, smem_mi = 0;
+  int base_sun = 0, base_mi = 0;
+  std::vector<int> bsun(nruns), bmi(nruns);
+  for (int r = 0; r < nruns; ++r) {
+    Run &R = h->runs[r];
+    R.p = p[r];
+    build_orbits(R);
+    R.T = T;
+    R.Malloc = ((R.p.M + T - 1) / T) * T;
+    R.esz = h->fp64 ? 8 : 4;
+    smem_sun = std::max(smem_sun, kb::sunset_smem_bytes(h->fp64, R.H));
+    smem_mi = std::max(smem_mi, kb::memint_smem_bytes(h->fp64, R.Malloc));
+    bsun[r] = base_sun;
+    bmi[r] = base_mi;
+    base_sun += R.p.M;
+    base_mi += R.nchunks;
+    if (R.p.pexp != KB_PEXP_LO) h->any_nlo = true;
+  }
+  h->total_sun = base_sun;
+  h->total_mi = base_mi;
+  h->smem_sun = smem_sun;
+  h->smem_mi = smem_mi;
+  int maxsm = 0;
+  cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
+  if ((int)smem_mi > maxsm || (int)smem_sun > maxsm) {
+    fail(nullptr, KB_ERR_PARAM, "shared memory need (%zu / %zu B) exceeds the device limit %d B", smem_sun, smem_mi, maxsm);
+    kb_destroy(h);
+    return KB_ERR_PARAM;
+  }
+  // allocations
+  for (int r = 0; r < nruns; ++r) {
+    Run &R = h->runs[r];
+    R.hist_elems = (size_t)R.nchunks * R.Malloc * R.Malloc * KC;
+    R.st_elems = (size_t)3 * R.nchunks * R.Malloc * KC;
+    R.sig_elems = (size_t)R.nchunks * R.Malloc * KC;
+    struct A { void **p; size_t bytes; } al[] = {
+        {&R.hist_F, R.hist_elems * R.esz}, {&R.hist_r, R.hist_elems * R.esz},
+        {&R.sig_F, R.sig_elems * R.esz},   {&R.sig_r, R.sig_elems * R.esz},
+        {(void **)&R.st_F, R.st_elems * 8}, {(void **)&R.st_r, R.st_elems * 8},
+        {(void **)&R.k2_d, (size_t)R.Spad * 8}, {(void **)&R.deg_d, (size_t)R.Spad * 8},
+        {(void **)&R.Cm_d, (size_t)R.H * R.H * 8}, {(void **)&R.tad, (size_t)2 * R.nchunks * 8},
+        {(void **)&R.meas, (size_t)5 * R.Spad * 8}, {(void **)&R.epart, (size_t)4 * R.nchunks * 8},
+    };
+    for (auto &a : al) {
+      if (cudaMalloc(a.p, a.bytes) != cudaSuccess) {
+        cudaGetLastError();
+        fail(nullptr, KB_ERR_OOM, "cudaMalloc of %zu bytes failed (run %d)", a.bytes, r);
+        kb_destroy(h);
+        return KB_ERR_OOM;
+      }
+      cudaMemsetAsync(*a.p, 0, a.bytes, h->st);
+    }
+    std::vector<double> k2p(R.Spad, 0.0);
+    std::copy(R.k2.begin(), R.k2.end(), k2p.begin());
+    cudaMemcpyAsync(R.k2_d, k2p.data(), R.Spad * 8, cudaMemcpyHostToDevice, h->st);
+    cudaMemcpyAsync(R.deg_d, R.degd.data(), R.Spad * 8, cudaMemcpyHostToDevice, h->st);
+    cudaMemcpyAsync(R.Cm_d, R.Cm.data(), R.Cm.size() * 8, cudaMemcpyHostToDevice, h->st);
+    cudaStreamSynchronize(h->st);  // host vectors above are temporaries
+    RunDev &D = R.dev;
+    D.Ns = R.p.Ns;
+    D.H = R.H;
+    D.S = R.S;
+    D.nchunks = R.nchunks;
+    D.M = R.p.M;
+    D.Malloc = R.Malloc;
+    D.pexp = R.p.pexp;
+    D.T = T;
+    D.dt = R.p.dt;
+    D.dt2 = R.p.dt * R.p.dt;
+    D.dt3 = R.p.dt * R.p.dt * R.p.dt;
+    D.mass2 = R.p.mass2;
+    const double ivol = 1.0 / (double)R.V;
+    const double N = (double)R.p.N, lam = R.p.lambda;
+    D.ivol = ivol;
+    D.pref_ivol = (lam * (N + 2.0) / (6.0 * N)) * ivol;
+    D.fac_r = ivol * ivol * ivol * (-(lam * lam) * (N + 2.0) / (6.0 * N * N));
+    D.fac_F = ivol * ivol * ivol * (-(lam * lam) * (N + 2.0) / (18.0 * N * N));
+    D.mass = R.p.mass;
+    D.hist_F = R.hist_F;
+    D.hist_r = R.hist_r;
+    D.st_F = R.st_F;
+    D.st_r = R.st_r;
+    D.sig_F = R.sig_F;
+    D.sig_r = R.sig_r;
+    D.k2 = R.k2_d;
+    D.deg = R.deg_d;
+    D.Cm = R.Cm_d;
+    D.tad = R.tad;
+    D.meas = R.meas;
+    D.epart = R.epart;
+    D.cta_base_sun = bsun[r];
+    D.cta_base_mi = bmi[r];
+  }
+  std::vector<RunDev> devs(nruns);
+  for (int r = 0; r < nruns; ++r) devs[r] = h->runs[r].dev;
+  bool ok = cudaMalloc(&h->d_runs, sizeof(RunDev) * nruns) == cudaSuccess &&
+            cudaMalloc(&h->d_base_sun, sizeof(int) * nruns) == cudaSuccess &&
+            cudaMalloc(&h->d_base_mi, sizeof(int) * nruns) == cudaSuccess &&
+            cudaMalloc(&h->d_t, sizeof(int)) == cudaSuccess && cudaMalloc(&h->d_err, sizeof(int)) == cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();
+    fail(nullptr, KB_ERR_OOM, "cudaMalloc of the run table failed");
+    kb_destroy(h);
+    return KB_ERR_OOM;
+  }
+  cudaMemcpy(h->d_runs, devs.data(), sizeof(RunDev) * nruns, cudaMemcpyHostToDevice);
+  cudaMemcpy(h->d_base_sun, bsun.data(), sizeof(int) * nruns, cudaMemcpyHostToDevice);
+  cudaMemcpy(h->d_base_mi, bmi.data(), sizeof(int) * nruns, cudaMemcpyHostToDevice);
+  cudaMemset(h->d_t, 0, sizeof(int));
+  cudaMemset(h->d_err, 0, sizeof(int));
+  // the attribute is per kernel, shared by all handles: allow the device maximum
+  cudaError_t e1 = kb::configure_sunset(h->fp64, (size_t)maxsm);
+  cudaError_t e2 = kb::configure_memint(h->fp64, (size_t)maxsm);
+  if (e1 != cudaSuccess || e2 != cudaSuccess) {
+    fail(nullptr, KB_ERR_CUDA, "kernel configuration failed: %s", cudaGetErrorString(e1 != cudaSuccess ? e1 : e2));
+    kb_destroy(h);
+    return KB_ERR_CUDA;
+  }
+  if (cudaDeviceSynchronize() != cudaSuccess) {
+    fail(nullptr, KB_ERR_CUDA, "device error during kb_create: %s", cudaGetErrorString(cudaGetLastError()));
+    kb_destroy(h);
+    return KB_ERR_CUDA;
+  }
+  *out = h;
+  return KB_OK;
+}
+
+void kb_destroy(kb_handle *h) {
+  if (!h) return;
+  cudaSetDevice(h->device);
+  if (h->st) cudaStreamSynchronize(h->st);
+  if (h->graph) cudaGraphExecDestroy(h->graph);
+  for (auto &R : h->runs) free_run(R);
+  void *ptrs[] = {h->d_runs, h->d_base_sun, h->d_base_mi, h->d_t, h->d_err};
+  for (void *q : ptrs)
+    if (q) cudaFree(q);
+  if (h->st) cudaStreamDestroy(h->st);
+  delete h;
+}
+
+int kb_num_orbits(const kb_handle *h, int32_t run, int32_t *S) {
+  if (!h || run < 0 || run >= (int)h->runs.size() || !S) return KB_ERR_PARAM;
+  *S = h->runs[run].S;
+  return KB_OK;
+}
+
+int kb_get_orbits(const kb_handle *h, int32_t run, int32_t *rep, double *k2, int64_t *deg) {
+  if (!h || run < 0 || run >= (int)h->runs.size()) return KB_ERR_PARAM;
+  const Run &R = h->runs[run];
+  if (rep) std::memcpy(rep, R.rep.data(), sizeof(int32_t) * 3 * R.S);
+  if (k2) std::memcpy(k2, R.k2.data(), sizeof(double) * R.S);
+  if (deg) std::memcpy(deg, R.deg.data(), sizeof(int64_t) * R.S);
+  return KB_OK;
+}
+
+int kb_site_orbits(const kb_handle *h, int32_t run, int32_t *out) {
+  if (!h || run < 0 || run >= (int)h->runs.size() || !out) return KB_ERR_PARAM;
+  const Run &R = h->runs[run];
+  const int Ns = R.p.Ns;
+  for (long s = 0; s < R.V; ++s) {
+    int n[3] = {(int)(s % Ns), (int)((s / Ns) % Ns), (int)(s / ((long)Ns * Ns))};
+    int f[3];
+    for (int d = 0; d < 3; ++d) f[d] = std::min(n[d], Ns - n[d]);
+    std::sort(f, f + 3);
+    out[s] = kb::orb3(f[0], f[1], f[2]);
+  }
+  return KB_OK;
+}
+
+// write one (a,b) element column (S values, double on the host) into the
+// history (storage type) and, for the last three rows, into the FP64 state
+static int put_pair(kb_handle *h, Run &R, int which, int a, int b, const double *vals, bool to_state) {
+  // normalise to the later-first pair
+  double sgn = 1.0;
+  if (a < b) {
+    std::swap(a, b);
+    if (which == 1) sgn = -1.0;
+  }
+  const size_t pitch_hist = (size_t)R.Malloc * R.Malloc * KC;
+  const size_t pitch_row = (size_t)R.Malloc * KC;
+  std::vector<double> dv(R.Spad, 0.0);
+  for (int o = 0; o < R.S; ++o) dv[o] = sgn * vals[o];
+  if (a == b && which == 1)
+    for (int o = 0; o < R.S; ++o) dv[o] = 0.0;  // rho(a,a) = 0 is structural
+  std::vector<float> fv;
+  const void *src = dv.data();
+  if (R.esz == 4) {
+    fv.resize(R.Spad);
+    for (int o = 0; o < R.Spad; ++o) fv[o] = (float)dv[o];
+    src = fv.data();
+  }
+  char *hist = (char *)(which == 0 ? R.hist_F : R.hist_r);
+  char *dst = hist + ((size_t)slot_off(R, a) * R.Malloc + slot_off(R, b)) * KC * R.esz;
+  KB_CUDA(h, cudaMemcpy2DAsync(dst, pitch_hist * R.esz, src, KC * R.esz, KC * R.esz, R.nchunks,
+                               cudaMemcpyHostToDevice, h->st));
+  if (to_state) {
+    double *stb = (which == 0 ? R.st_F : R.st_r) + (size_t)(a % 3) * R.nchunks * pitch_row + slot_off(R, b) * KC;
+    KB_CUDA(h, cudaMemcpy2DAsync(stb, pitch_row * 8, dv.data(), KC * 8, KC * 8, R.nchunks,
+                                 cudaMemcpyHostToDevice, h->st));
+  }
+  KB_CUDA(h, cudaStreamSynchronize(h->st));
+  return KB_OK;
+}
+
+int kb_init_rows(kb_handle *h, int32_t run, const double *F11, const double *F21, const double *F22) {
+  if (!h || run < 0 || run >= (int)h->runs.size() || !F11 || !F21 || !F22)
+    return fail(h, KB_ERR_PARAM, "kb_init_rows: bad arguments");
+  if (h->t_cur > 2) return fail(h, KB_ERR_PARAM, "kb_init: the simulation has already been evolved");
+  cudaSetDevice(h->device);
+  Run &R = h->runs[run];
+  std::vector<double> zero(R.S, 0.0), dtv(R.S, R.p.dt);
+  int rc;
+  if ((rc = put_pair(h, R, 0, 1, 1, F11, true))) return rc;
+  if ((rc = put_pair(h, R, 0, 2, 1, F21, true))) return rc;
+  if ((rc = put_pair(h, R, 0, 2, 2, F22, true))) return rc;
+  if ((rc = put_pair(h, R, 1, 1, 1, zero.data(), true))) return rc;
+  if ((rc = put_pair(h, R, 1, 2, 1, dtv.data(), true))) return rc;
+  if ((rc = put_pair(h, R, 1, 2, 2, zero.data(), true))) return rc;
+  h->inited_runs |= 1;  // at least one run initialised
+  h->t_cur = 2;
+  h->sigma_valid = false;
+  // measurement of t = 2 and the tadpole sums of F(2,2) for all runs
+  KB_CUDA(h, kb::launch_measure_init(h->d_runs, (int)h->runs.size(), 2, h->st));
+  KB_CUDA(h, cudaStreamSynchronize(h->st));
+  return KB_OK;
+}
+
+int kb_init(kb_handle *h, int32_t run, const double *n, double init_mass) {
+  if (!h || run < 0 || run >= (int)h->runs.size() || !n) return fail(h, KB_ERR_PARAM, "kb_init: bad arguments");
+  const Run &R = h->runs[run];
+  std::vector<double> F11(R.S), F21(R.S), F22(R.S);
+  const double dt = R.p.dt;
+  // initSimData! (TwoPIScalar_Initialization.jl:38-41)
+  for (int o = 0; o < R.S; ++o) {
+    const double omega = std::sqrt(R.k2[o] + init_mass * init_mass);
+    F11[o] = 1 / omega * (n[o] + 0.5);
+    F21[o] = 1 / omega * (n[o] + 0.5);
+    F22[o] = omega * (n[o] + 0.5) * (dt * dt) + 1 / omega * (n[o] + 0.5);
+  }
+  return kb_init_rows(h, run, F11.data(), F21.data(), F22.data());
+}
+
+static int launch_step(kb_handle *h, int measure) {
+  if (h->any_nlo)
+    KB_CUDA(h, kb::launch_sunset(h->fp64, h->d_runs, h->d_base_sun, (int)h->runs.size(), h->total_sun, h->d_t,
+                                 h->d_err, h->smem_sun, h->st));
+  KB_CUDA(h, kb::launch_memint(h->fp64, h->d_runs, h->d_base_mi, (int)h->runs.size(), h->total_mi, h->d_t,
+                               h->d_err, measure, h->smem_mi, h->st));
+  return KB_OK;
+}
+
+int kb_step(kb_handle *h, int32_t t) {
+  if (!h) return KB_ERR_PARAM;
+  if (h->t_cur < 2) return fail(h, KB_ERR_PARAM, "kb_step before kb_init");
+  if (t != h->t_cur + 1) return fail(h, KB_ERR_PARAM, "kb_step(%d): expected t = %d (lastEvolStep + 1)", t, h->t_cur + 1);
+  cudaSetDevice(h->device);
+  KB_CUDA(h, kb::launch_set_t(h->d_t, t, h->st));
+  int rc = launch_step(h, 1);
+  if (rc) return rc;
+  h->t_cur = t;
+  h->sigma_valid = h->any_nlo;
+  return KB_OK;
+}
+
+int kb_expand(kb_handle *h) {
+  if (!h) return KB_ERR_PARAM;
+  if (h->t_cur < 2) return fail(h, KB_ERR_PARAM, "kb_expand before kb_init");
+  h->t_cur += 1;
+  h->sigma_valid = false;
+  return KB_OK;
+}
+
+static int collect_scalars(kb_handle *h, int run, int t, kb_meas_scalars *s) {
+  Run &R = h->runs[run];
+  std::vector<double> ep((size_t)4 * R.nchunks);
+  KB_CUDA(h, cudaMemcpyAsync(ep.data(), R.epart, ep.size() * 8, cudaMemcpyDeviceToHost, h->st));
+  KB_CUDA(h, cudaStreamSynchronize(h->st));
+  double ek = 0, epo = 0, em = 0;
+  for (int c = 0; c < R.nchunks; ++c) {
+    ek += ep[(size_t)c * 4 + 0];
+    epo += ep[(size_t)c * 4 + 1];
+    em += ep[(size_t)c * 4 + 2];
+  }
+  s->time = (t - 1) * R.p.dt * R.p.mass;
+  s->E_kin = ek;
+  s->E_pot = epo;
+  s->E_mem = (t == 2) ? 0.0 : em;
+  s->E = s->E_kin + s->E_pot + s->E_mem;
+  s->M2 = ep[3];
+  return KB_OK;
+}
+
+int kb_measure(kb_handle *h, int32_t run, int32_t t, kb_meas_scalars *s, double *F, double *ddF, double *n,
+               double *omega, double *c) {
+  if (!h || run < 0 || run >= (int)h->runs.size()) return KB_ERR_PARAM;
+  if (t != h->t_cur || h->t_cur < 2) return fail(h, KB_ERR_PARAM, "kb_measure(%d): only the last evolved step %d can be measured", t, h->t_cur);
+  cudaSetDevice(h->device);
+  Run &R = h->runs[run];
+  int rc = kb_sync(h);
+  if (rc) return rc;
+  double *outs[5] = {F, ddF, n, omega, c};
+  for (int q = 0; q < 5; ++q)
+    if (outs[q]) KB_CUDA(h, cudaMemcpyAsync(outs[q], R.meas + (size_t)q * R.Spad, R.S * 8, cudaMemcpyDeviceToHost, h->st));
+  kb_meas_scalars tmp;
+  rc = collect_scalars(h, run, t, s ? s : &tmp);
+  if (rc) return rc;
+  if (s && !std::isfinite(s->E)) return fail(h, KB_ERR_NAN, "non-finite energy at t=%d", t);
+  return KB_OK;
+}
+
+static int fetch_pair(kb_handle *h, Run &R, int which, int a, int b, double *out) {
+  double sgn = 1.0;
+  if (a < b) {
+    std::swap(a, b);
+    if (which == 1) sgn = -1.0;
+  }
+  const size_t pitch_row = (size_t)R.Malloc * KC;
+  std::vector<double> dv(R.Spad, 0.0);
+  if (a >= h->t_cur - 2 && a <= h->t_cur) {
+    const double *stb = (which == 0 ? R.st_F : R.st_r) + (size_t)(a % 3) * R.nchunks * pitch_row + slot_off(R, b) * KC;
+    KB_CUDA(h, cudaMemcpy2DAsync(dv.data(), KC * 8, stb, pitch_row * 8, KC * 8, R.nchunks, cudaMemcpyDeviceToHost, h->st));
+    KB_CUDA(h, cudaStreamSynchronize(h->st));
+  } else {
+    const size_t pitch_hist = (size_t)R.Malloc * R.Malloc * KC;
+    const char *hist = (const char *)(which == 0 ? R.hist_F : R.hist_r);
+    const char *src = hist + ((size_t)slot_off(R, a) * R.Malloc + slot_off(R, b)) * KC * R.esz;
+    if (R.esz == 8) {
+      KB_CUDA(h, cudaMemcpy2DAsync(dv.data(), KC * 8, src, pitch_hist * 8, KC * 8, R.nchunks, cudaMemcpyDeviceToHost, h->st));
+      KB_CUDA(h, cudaStreamSynchronize(h->st));
+    } else {
+      std::vector<float> fv(R.Spad);
+      KB_CUDA(h, cudaMemcpy2DAsync(fv.data(), KC * 4, src, pitch_hist * 4, KC * 4, R.nchunks, cudaMemcpyDeviceToHost, h->st));
+      KB_CUDA(h, cudaStreamSynchronize(h->st));
+      for (int o = 0; o < R.Spad; ++o) dv[o] = fv[o];
+    }
+  }
+  for (int o = 0; o < R.S; ++o) out[o] = sgn * dv[o];
+  return KB_OK;
+}
+
+int kb_get(kb_handle *h, int32_t run, int32_t which, int32_t a, int32_t b, double *out) {
+  if (!h || run < 0 || run >= (int)h->runs.size() || !out || (which != 0 && which != 1)) return KB_ERR_PARAM;
+  Run &R = h->runs[run];
+  const int tmin = tmin_of(R, h->t_cur);
+  if (h->t_cur < 2 || a < tmin || a > h->t_cur || b < tmin || b > h->t_cur)
+    return fail(h, KB_ERR_RANGE, "Indices not in range! (%d,%d) outside [%d,%d]", a, b, tmin, h->t_cur);
+  cudaSetDevice(h->device);
+  int rc = kb_sync(h);
+  if (rc) return rc;
+  return fetch_pair(h, R, which, a, b, out);
+}
+
+int kb_set(kb_handle *h, int32_t run, int32_t which, int32_t a, int32_t b, const double *in) {
+  if (!h || run < 0 || run >= (int)h->runs.size() || !in || (which != 0 && which != 1)) return KB_ERR_PARAM;
+  Run &R = h->runs[run];
+  const int tmin = tmin_of(R, h->t_cur);
+  if (h->t_cur < 2 || a < tmin || a > h->t_cur || b < tmin || b > h->t_cur)
+    return fail(h, KB_ERR_RANGE, "Indices not in range! (%d,%d) outside [%d,%d]", a, b, tmin, h->t_cur);
+  cudaSetDevice(h->device);
+  int rc = kb_sync(h);
+  if (rc) return rc;
+  const int later = std::max(a, b);
+  return put_pair(h, R, which, a, b, in, later >= h->t_cur - 2);
+}
+
+int kb_self_energies(kb_handle *h, int32_t tmone) {
+  if (!h) return KB_ERR_PARAM;
+  if (tmone != h->t_cur - 1 || h->t_cur < 3)
+    return fail(h, KB_ERR_PARAM, "kb_self_energies(%d): tmone must be the current tmax - 1 = %d", tmone, h->t_cur - 1);
+  cudaSetDevice(h->device);
+  KB_CUDA(h, kb::launch_set_t(h->d_t, h->t_cur, h->st));
+  if (h->any_nlo)
+    KB_CUDA(h, kb::launch_sunset(h->fp64, h->d_runs, h->d_base_sun, (int)h->runs.size(), h->total_sun, h->d_t,
+                                 h->d_err, h->smem_sun, h->st));
+  h->sigma_valid = true;
+  return kb_sync(h);
+}
+
+int kb_get_sigma(kb_handle *h, int32_t run, int32_t which, int32_t z, double *out) {
+  if (!h || run < 0 || run >= (int)h->runs.size() || !out || (which != 0 && which != 1)) return KB_ERR_PARAM;
+  Run &R = h->runs[run];
+  const int tmin = tmin_of(R, h->t_cur);
+  if (!h->sigma_valid) return fail(h, KB_ERR_PARAM, "no self-energies computed for the current window");
+  if (z < tmin || z > h->t_cur - 1) return fail(h, KB_ERR_RANGE, "Indices not in range! z=%d outside [%d,%d]", z, tmin, h->t_cur - 1);
+  cudaSetDevice(h->device);
+  int rc = kb_sync(h);
+  if (rc) return rc;
+  const size_t pitch = (size_t)R.Malloc * KC;
+  const char *base = (const char *)(which == 0 ? R.sig_F : R.sig_r) + slot_off(R, z) * KC * R.esz;
+  std::vector<double> dv(R.Spad);
+  if (R.esz == 8) {
+    KB_CUDA(h, cudaMemcpy2DAsync(dv.data(), KC * 8, base, pitch * 8, KC * 8, R.nchunks, cudaMemcpyDeviceToHost, h->st));
+  } else {
+    std::vector<float> fv(R.Spad);
+    KB_CUDA(h, cudaMemcpy2DAsync(fv.data(), KC * 4, base, pitch * 4, KC * 4, R.nchunks, cudaMemcpyDeviceToHost, h->st));
+    KB_CUDA(h, cudaStreamSynchronize(h->st));
+    for (int o = 0; o < R.Spad; ++o) dv[o] = fv[o];
+  }
+  KB_CUDA(h, cudaStreamSynchronize(h->st));
+  for (int o = 0; o < R.S; ++o) out[o] = dv[o];
+  return KB_OK;
+}
+
+int kb_window(const kb_handle *h, int32_t run, int32_t *tmin, int32_t *tmax) {
+  if (!h || run < 0 || run >= (int)h->runs.size()) return KB_ERR_PARAM;
+  if (tmin) *tmin = h->t_cur >= 1 ? tmin_of(h->runs[run], h->t_cur) : 0;
+  if (tmax) *tmax = h->t_cur;
+  return KB_OK;
+}
+
+int kb_get_traces(kb_handle *h, int32_t run, double *Fonet, double *ronet, double *SigF, double *Sigr) {
+  if (!h || run < 0 || run >= (int)h->runs.size()) return KB_ERR_PARAM;
+  Run &R = h->runs[run];
+  const int t = h->t_cur, tmin = tmin_of(R, t);
+  std::vector<double> v(R.S);
+  for (int tp = tmin, q = 0; tp <= t - 1; ++tp, ++q) {
+    int rc;
+    if (Fonet) {
+      if ((rc = kb_get(h, run, 0, tmin, tp, v.data()))) return rc;
+      Fonet[q] = v[0];
+    }
+    if (ronet) {
+      if ((rc = kb_get(h, run, 1, tmin, tp, v.data()))) return rc;
+      ronet[q] = v[0];
+    }
+  }
+  if (SigF || Sigr) {
+    for (int tp = t - 1, q = 0; tp >= tmin; --tp, ++q) {
+      int rc;
+      if (SigF) {
+        if ((rc = kb_get_sigma(h, run, 0, tp, v.data()))) return rc;
+        SigF[q] = v[0];
+      }
+      if (Sigr) {
+        if ((rc = kb_get_sigma(h, run, 1, tp, v.data()))) return rc;
+        Sigr[q] = v[0];
+      }
+    }
+  }
+  return KB_OK;
+}
+
+int kb_steps(kb_handle *h, int32_t t0, int32_t count, int32_t measure_every, kb_meas_scalars *out,
+             int32_t out_capacity) {
+  if (!h || count < 0) return KB_ERR_PARAM;
+  if (h->t_cur < 2) return fail(h, KB_ERR_PARAM, "kb_steps before kb_init");
+  if (t0 != h->t_cur + 1) return fail(h, KB_ERR_PARAM, "kb_steps(t0=%d): expected t0 = %d", t0, h->t_cur + 1);
+  if (count == 0) return KB_OK;
+  cudaSetDevice(h->device);
+  const int nr = (int)h->runs.size();
+  // steps between measurements run from one captured graph
+  if (!h->graph) {
+    cudaGraph_t g;
+    KB_CUDA(h, cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+    int rc = launch_step(h, 1);
+    cudaError_t ea = (rc == 0) ? (cudaError_t)kb::launch_advance_t(h->d_t, h->st) : cudaSuccess;
+    cudaError_t ec = cudaStreamEndCapture(h->st, &g);
+    if (rc) return rc;
+    if (ea != cudaSuccess || ec != cudaSuccess) return fail(h, KB_ERR_CUDA, "graph capture failed");
+    cudaError_t ei = cudaGraphInstantiate(&h->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) return fail(h, KB_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(ei));
+  }
+  KB_CUDA(h, kb::launch_set_t(h->d_t, t0, h->st));
+  int nm = 0;
+  for (int i = 0; i < count; ++i) {
+    const int t = t0 + i;
+    KB_CUDA(h, cudaGraphLaunch(h->graph, h->st));
+    h->t_cur = t;
+    if (measure_every > 0 && (t - 2) % measure_every == 0 && out) {
+      for (int r = 0; r < nr; ++r) {
+        const int idx = r * ((count + measure_every - 1) / measure_every) + nm;
+        if (idx < out_capacity) {
+          int rc = collect_scalars(h, r, t, &out[idx]);
+          if (rc) return rc;
+        }
+      }
+      ++nm;
+    }
+  }
+  h->sigma_valid = h->any_nlo;
+  return kb_sync(h);
+}
+
+int kb_sync(kb_handle *h) {
+  if (!h) return KB_ERR_PARAM;
+  cudaSetDevice(h->device);
+  KB_CUDA(h, cudaStreamSynchronize(h->st));
+  int e = 0;
+  KB_CUDA(h, cudaMemcpy(&e, h->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e) {
+    cudaMemset(h->d_err, 0, sizeof(int));
+    if (e & kb::DEVERR_TIMEOUT) return fail(h, KB_ERR_TIMEOUT, "a bounded device wait expired (kernel returned early)");
+    return fail(h, KB_ERR_CUDA, "device error flags 0x%x", e);
+  }
+  return KB_OK;
+}
+
+// checkpoint layout: header + per run (hist_F, hist_r, sig_F, sig_r, st_F, st_r, tad, meas, epart)
+struct CkptHeader {
+  uint64_t magic, bytes;
+  int32_t nruns, t_cur, fp64, sigma_valid;
+};
+static const uint64_t kCkptMagic = 0x6b623270692d636bull;
+
+int kb_checkpoint_size(const kb_handle *h, size_t *bytes) {
+  if (!h || !bytes) return KB_ERR_PARAM;
+  size_t b = sizeof(CkptHeader);
+  for (const Run &R : h->runs)
+    b += (2 * R.hist_elems + 2 * R.sig_elems) * R.esz + 2 * R.st_elems * 8 + (2 * R.nchunks + 5 * R.Spad + 4 * R.nchunks) * 8;
+  *bytes = b;
+  return KB_OK;
+}
+
+static int ckpt_copy(kb_handle *h, char *host, size_t bytes, bool save) {
+  size_t need = 0;
+  kb_checkpoint_size(h, &need);
+  if (bytes < need) return fail(h, KB_ERR_PARAM, "checkpoint buffer of %zu bytes, need %zu", bytes, need);
+  cudaSetDevice(h->device);
+  int rc = kb_sync(h);
+  if (rc) return rc;
+  CkptHeader hd{kCkptMagic, need, (int32_t)h->runs.size(), h->t_cur, h->fp64 ? 1 : 0, h->sigma_valid ? 1 : 0};
+  if (save) {
+    std::memcpy(host, &hd, sizeof hd);
+  } else {
+    CkptHeader in;
+    std::memcpy(&in, host, sizeof in);
+    if (in.magic != kCkptMagic || in.bytes != need || in.nruns != hd.nruns || in.fp64 != hd.fp64)
+      return fail(h, KB_ERR_PARAM, "checkpoint does not match this handle");
+    hd = in;
+  }
+  size_t off = sizeof hd;
+  for (Run &R : h->runs) {
+    struct B { void *d; size_t n; } bufs[] = {
+        {R.hist_F, R.hist_elems * R.esz}, {R.hist_r, R.hist_elems * R.esz}, {R.sig_F, R.sig_elems * R.esz},
+        {R.sig_r, R.sig_elems * R.esz},   {R.st_F, R.st_elems * 8},         {R.st_r, R.st_elems * 8},
+        {R.tad, (size_t)2 * R.nchunks * 8}, {R.meas, (size_t)5 * R.Spad * 8}, {R.epart, (size_t)4 * R.nchunks * 8},
+    };
+    for (auto &q : bufs) {
+      if (save) KB_CUDA(h, cudaMemcpyAsync(host + off, q.d, q.n, cudaMemcpyDeviceToHost, h->st));
+      else KB_CUDA(h, cudaMemcpyAsync(q.d, host + off, q.n, cudaMemcpyHostToDevice, h->st));
+      off += q.n;
+    }
+  }
+  KB_CUDA(h, cudaStreamSynchronize(h->st));
+  if (!save) {
+    h->t_cur = hd.t_cur;
+    h->sigma_valid = hd.sigma_valid != 0;
+  }
+  return KB_OK;
+}
+
+int kb_checkpoint_save(kb_handle *h, void *buf, size_t bytes) {
+  if (!h || !buf) return KB_ERR_PARAM;
+  return ckpt_copy(h, (char *)buf, bytes, true);
+}
+int kb_checkpoint_restore(kb_handle *h, const void *buf, size_t bytes) {
+  if (!h || !buf) return KB_ERR_PARAM;
+  return ckpt_copy(h, (char *)const_cast<void *>(buf), bytes, false);
+}
+
+}  // extern "C"

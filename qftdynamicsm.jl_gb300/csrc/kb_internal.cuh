@@ -1,0 +1,74 @@
+// kb_internal.cuh -- device data layout shared by the kernels of libkb2pi.
+//
+// Layout in HBM of one run (S orbits padded to nchunks * KC, KC = 8):
+//   hist_F, hist_r  [nchunks][Malloc][Malloc][KC]  storage type TS
+//       element (a, b) with a >= b (later time first) at row slot(a), column
+//       slot(b); slot(t) = t mod Malloc, Malloc = M rounded up to the tile T.
+//       rho holds the true value rho(a, b) of the later-first pair.
+//   st_F, st_r      [3][nchunks][Malloc][KC]  double: rows t, t-1, t-2 by t mod 3
+//       (the leapfrog state; in KB_PREC_MIXED the only FP64 copy of F, rho)
+//   sig_F, sig_r    [nchunks][Malloc][KC]     TS: Sigma(t-1, z) at slot(z)
+//   tad             [2][nchunks]              double: sum_k deg_k F(t,t,k) per chunk,
+//                                              by t mod 2
+//   meas            [5][Spad]                 double: F(t-1,t-1), ddF, n, omega, c
+//   epart           [nchunks][4]              double: E_kin, E_pot, E_mem partials
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace kb {
+
+constexpr int KC = 8;  // orbits per chunk (innermost dimension)
+
+// device error bits (per handle)
+enum : int { DEVERR_TIMEOUT = 1, DEVERR_SMEM = 2, DEVERR_GEOM = 4 };
+
+struct RunDev {
+  int Ns, H, S, nchunks;
+  int M, Malloc, pexp, T;
+  double dt, dt2, dt3, mass2;
+  double pref_ivol;   // Hartreeprefactor * ivol
+  double ivol;
+  double fac_r, fac_F;  // ivol^3 * coefficient of Sigma_rho, Sigma_F
+  double mass;
+  void *hist_F, *hist_r;
+  double *st_F, *st_r;
+  void *sig_F, *sig_r;
+  const double *k2, *deg;   // [Spad]
+  const double *Cm;         // [H][H] octant cosine matrix
+  double *tad;              // [2][nchunks]
+  double *meas;             // [5][Spad]
+  double *epart;            // [nchunks][4]
+  int cta_base_sun, cta_base_mi;  // first CTA of this run in the batched grids
+  int pad0, pad1;
+};
+
+__host__ __device__ inline long long tet3(int c) { return (long long)c * (c + 1) * (c + 2) / 6; }
+__host__ __device__ inline int tri2(int b) { return b * (b + 1) / 2; }
+// orbit index of the sorted triple a <= b <= c
+__host__ __device__ inline int orb3(int a, int b, int c) { return (int)(tet3(c) + tri2(b) + a); }
+
+__device__ inline int find_run(const int *base, int nruns, int bid) {
+  int lo = 0, hi = nruns - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (base[mid] <= bid) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// host launchers (kb_sunset.cu, kb_memint.cu)
+cudaError_t launch_sunset(bool fp64, const RunDev *d_runs, const int *d_base, int nruns, int total_ctas,
+                          const int *d_t, int *d_err, size_t smem, cudaStream_t st);
+size_t sunset_smem_bytes(bool fp64, int H);
+cudaError_t configure_sunset(bool fp64, size_t smem);
+cudaError_t launch_memint(bool fp64, const RunDev *d_runs, const int *d_base, int nruns, int total_ctas,
+                          const int *d_t, int *d_err, int measure, size_t smem, cudaStream_t st);
+size_t memint_smem_bytes(bool fp64, int Malloc);
+cudaError_t configure_memint(bool fp64, size_t smem);
+int memint_tile(bool fp64);
+cudaError_t launch_measure_init(const RunDev *d_runs, int nruns, int t, cudaStream_t st);
+cudaError_t launch_set_t(int *d_t, int t, cudaStream_t st);
+cudaError_t launch_advance_t(int *d_t, cudaStream_t st);
+
+}  // namespace kb

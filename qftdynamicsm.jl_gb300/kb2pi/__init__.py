@@ -1,0 +1,11 @@
+"""kb2pi -- Python host mirror of the TwoPIScalar GPU numerics (libkb2pi).
+
+``capi`` binds the C ABI of include/kb2pi.h; ``twopiscalar`` mirrors the
+reference's problem/solution/initialize!/evolve!/measure! interface over it.
+"""
+from . import capi  # noqa: F401
+from .capi import Handle, KbError, KbParams, load_library  # noqa: F401
+from .twopiscalar import (  # noqa: F401
+    QFTdynamicsProblem, QFTdynamicsSolution, TwoPIScalarfile, createMeasurement, evolve, getGapMass,
+    getparticlenr, initialize, lattice_orbits, make_problem, measure, run_simulation,
+)

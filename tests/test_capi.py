@@ -1,0 +1,62 @@
+"""The C-ABI library loads and exports every symbol include/kb2pi.h declares."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "kb2pi.h")
+
+
+def declared_symbols():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(kb_[a-z_0-9]+)\s*\(", src)))
+
+
+def test_header_declares_the_binding_list():
+    from kb2pi import capi
+
+    assert sorted(capi.EXPORTS) == declared_symbols()
+
+
+def test_library_exports_all_symbols():
+    from kb2pi import capi
+
+    lib = capi.load_library()
+    for name in declared_symbols():
+        assert hasattr(lib, name), name
+        assert ctypes.cast(getattr(lib, name), ctypes.c_void_p).value
+
+
+def test_create_rejects_bad_parameters_without_touching_a_gpu():
+    from kb2pi import capi
+
+    lib = capi.load_library()
+    h = ctypes.c_void_p()
+    p = capi.KbParams(Ns=7, sdim=3, M=10, N=4, pexp=1, precision=0, device=0, flags=0, dt=0.1, lam=1.0,
+                      mass2=1.0, mass=1.0)
+    assert lib.kb_create(ctypes.byref(p), ctypes.byref(h)) == -1
+    assert b"Ns=7" in lib.kb_last_error(None)
+    p.Ns, p.M = 8, 2
+    assert lib.kb_create(ctypes.byref(p), ctypes.byref(h)) == -1
+    p.M, p.sdim = 10, 2
+    assert lib.kb_create(ctypes.byref(p), ctypes.byref(h)) == -1
+
+
+def test_create_without_device_fails_loudly():
+    try:
+        import torch
+
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except Exception:
+        pass
+    from kb2pi import capi
+
+    p = capi.KbParams(Ns=8, sdim=3, M=10, N=4, pexp=1, precision=0, device=0, flags=0, dt=0.1, lam=1.0,
+                      mass2=1.0, mass=1.0)
+    with pytest.raises(capi.KbError) as ei:
+        capi.Handle([p])
+    assert ei.value.code in (-7, -3)
