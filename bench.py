@@ -1,0 +1,407 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 2PI Kadanoff-Baym step (metric of BASELINE: KB steps/s).
+
+Workload (N=1): the Ns=64 lattice, O(N=4), lambda=2, m=1, dt=0.05, memory
+window M=1000, tsunami initial state (the large configuration of the
+benchmark list). A "step" is one evolve!(t) at a full memory window. The
+window is filled by really evolving the first M steps from the initial
+state, then W warm-up steps and K timed steps run. The history (2 x 1000^2/2
+x 6545 orbits) is far larger than L2, so no flush is needed between steps.
+
+Reported: steps/s of the mixed-precision path (value), the plain FP64 path
+on the same workload, their relative difference in n(p,t) and E, the
+roofline of the dominant kernel (memory integral), an end-to-end number
+through the C ABI with host buffers, GPU clocks during the timed region and
+the CPU baseline (the oracle's CPUred-style port, bounded sample).
+
+--impl reference times the reference's CPU algorithm (the oracle port; the
+Julia reference cannot run here) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "qftdynamicsm.jl_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+CFG = dict(Ns=64, N=4, lam=2.0, mass=1.0, mass2=1.0, dt=0.05, M=1000, init="tsunami")
+# smaller case of the same kernels, used for ncu captures (a few GB on the device)
+SMALL = dict(Ns=40, N=4, lam=2.0, mass=1.0, mass2=1.0, dt=0.05, M=400, init="tsunami")
+METRIC = "KB steps/s at Ns=64 (M=1000 window, mixed precision; plain FP64 GPU alongside)"
+
+
+def tsunami_n(k2):
+    return 5.0 * np.exp(-((np.sqrt(k2) - 1.0) ** 2) / (2 * 0.2 ** 2))
+
+
+def gap_mass(k2, deg, n, lam, N, mass2, vol):
+    from kb2pi.twopiscalar import Discretization, Phi4, getGapMass
+
+    disc = Discretization(1.0, CFG["Ns"], 3, 0, CFG["dt"], vol, 1.0 / vol, CFG["M"], 0)
+    return getGapMass(Phi4(lam, N, mass2), "LambdaNLO", disc, n, k2, deg)
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = str(gpu_index)
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200", "-i", self.gpu], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            time.sleep(0.25)
+            self.p.terminate()
+            self.p.wait()
+
+    def summary(self):
+        self.f.flush()
+        rows = []
+        with open(self.f.name) as fh:
+            for line in fh:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no nvidia-smi samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if os.environ.get("KB_BENCH_GLOO") is None else "gloo")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(ws, v):
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def make_handle(precision, device):
+    from kb2pi import capi
+
+    p = capi.KbParams(Ns=CFG["Ns"], sdim=3, M=CFG["M"], N=CFG["N"], pexp=1, precision=precision, device=device,
+                      flags=0, dt=CFG["dt"], lam=CFG["lam"], mass2=CFG["mass2"], mass=CFG["mass"])
+    return capi.Handle([p])
+
+
+def init_and_fill(h):
+    _, k2, deg = h.orbits(0)
+    n = tsunami_n(k2)
+    m0 = gap_mass(k2, deg, n, CFG["lam"], CFG["N"], CFG["mass2"], CFG["Ns"] ** 3)
+    h.init(0, n, m0)
+    # evolve until the memory window is full (t = M), measuring once at the end
+    h.steps(3, CFG["M"] - 2, 0)
+    return CFG["M"]
+
+
+def timed_steps(h, t0, K, stream_ptr):
+    import torch
+
+    st = torch.cuda.ExternalStream(stream_ptr)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    h.sync()
+    torch.cuda.synchronize()
+    e0.record(st)
+    for i in range(K):
+        h.step(t0 + i)
+    e1.record(st)
+    e1.synchronize()
+    h.sync()
+    return e0.elapsed_time(e1)
+
+
+def timed_graph_steps(h, t0, K, stream_ptr):
+    import torch
+
+    st = torch.cuda.ExternalStream(stream_ptr)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    h.sync()
+    e0.record(st)
+    h.steps(t0, K, 0)
+    e1.record(st)
+    e1.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def read_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def read_traffic(key):
+    """Per-launch DRAM bytes of the memory-integral kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "memint_mixed_ns64_m1000.md")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith(key + ":"):
+                    return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+def algorithmic_bytes(M, S, b_hist, b_sig):
+    """Unique bytes of one memory-integral launch: the two-time triangle of F and rho
+    read once, the new row written, the self-energy row read."""
+    return 2 * (M * (M + 1) // 2) * S * b_hist + 2 * M * S * b_hist + 2 * M * S * b_sig
+
+
+# ---------------------------------------------------------------------------
+def cpu_baseline(steps=1, Msample=128, budget_s=None):
+    """The oracle's CPUred-style port on all host cores, bounded sample: Ns=64 lattice
+    with a window of Msample steps filled by expandSimData! alone (as the reference
+    benchmark does, TwoPIScalar_Bechmark.jl:64-69); the timed step's self-energy time
+    is scaled by the number of t' rows (M-1)/(Msample-1), the rest of evolve! by
+    M^2/Msample^2."""
+    from oracle import ENGINE_ORBIT, Oracle
+
+    threads = os.cpu_count() or 1
+    o = Oracle(CFG["Ns"], 3, M=Msample, N=CFG["N"], dt=CFG["dt"], lam=CFG["lam"], mass2=CFG["mass2"],
+               mass=CFG["mass"], engine=ENGINE_ORBIT, nthreads=threads)
+    _, k2, deg = o.orbits()
+    n = tsunami_n(k2)
+    o.init_occupation(n, 1.0)
+    for _ in range(3, Msample + 1):
+        o.expand()
+    t = Msample
+    ts = []
+    t_start = time.perf_counter()
+    for _ in range(steps):
+        if ts and budget_s is not None and time.perf_counter() - t_start > budget_s:
+            break
+        t += 1
+        o.step(t)
+        s_sun, s_rest = o.step_times()
+        M = CFG["M"]
+        ts.append(s_sun * (M - 1) / (Msample - 1) + s_rest * (M * M) / (Msample * Msample))
+    o.close()
+    sec = statistics.median(ts)
+    return {"value": 1.0 / sec, "unit": "steps/s", "cores": threads, "kind": "port",
+            "sample": f"oracle CPUred port (full-lattice FFT sunset), Ns=64, window {Msample} filled by "
+                      f"expand, {len(ts)} step(s); sunset time x (M-1)/({Msample}-1), memory integrals x "
+                      f"(M/{Msample})^2 to M=1000"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_setup()
+    if rank != 0:
+        return 0
+    # K sample steps, at most ~90 s of CPU time in total (at least one step)
+    cb = cpu_baseline(steps=max(1, args.steps), Msample=args.cpu_window, budget_s=90.0)
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / cb["value"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (tsunami initial state)",
+            "config": {"workload": "KB step at full window, Ns=64, N=4, lambda=2, m=1, dt=0.05, M=1000",
+                       "l2": "history >> L2"},
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+
+    ws, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    dev = local
+    from kb2pi import capi
+
+    cvd = os.environ.get("CUDA_VISIBLE_DEVICES")
+    phys = int(cvd.split(",")[local]) if cvd and cvd.split(",")[local].isdigit() else local
+
+    # --- mixed precision (headline) ------------------------------------------------
+    h = make_handle(capi.KB_PREC_MIXED, dev)
+    S = h.S[0]
+    t = init_and_fill(h)
+    meas_mixed = h.measure(0, t)
+    for i in range(args.warmup):
+        h.step(t + 1 + i)
+    t += args.warmup
+    stream = h.stream()
+    barrier(ws)
+    h.profile(True)
+    with ClockSampler(phys) as clk:
+        ms = timed_steps(h, t + 1, args.steps, stream)
+    t += args.steps
+    prof = h.profile_read()
+    h.profile(False)
+    ms = max_over_ranks(ws, ms)
+    barrier(ws)
+    ms_per_step = ms / args.steps
+    value = ws * args.steps / (ms / 1000.0)
+
+    # graph-captured steps (same work, one graph launch per step)
+    gms = timed_graph_steps(h, t + 1, args.steps, stream)
+    t += args.steps
+
+    # end to end through the C ABI with host buffers: per step kb_step (t by value)
+    # and kb_measure (scalars + n(p) per orbit back to the host)
+    h.sync()
+    n_host = np.zeros(S)
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        h.step(t + 1 + i)
+        m = h.measure(0, t + 1 + i)
+        n_host[:] = m["n"]
+    e2e_s = time.perf_counter() - t0
+    t += args.steps
+    e2e_s = max_over_ranks(ws, e2e_s)
+    e2e_val = ws * args.steps / e2e_s
+    d2h = 5 * S * 8 + (4 * ((S + 7) // 8)) * 8  # per-orbit arrays + energy partials
+    h.close()
+    del h
+
+    # --- plain FP64 path on the same workload ----------------------------------------
+    fp64 = None
+    if not args.no_fp64:
+        h64 = make_handle(capi.KB_PREC_FP64, dev)
+        t64 = init_and_fill(h64)
+        meas64 = h64.measure(0, t64)
+        for i in range(min(args.warmup, 3)):
+            h64.step(t64 + 1 + i)
+        t64 += min(args.warmup, 3)
+        k64 = max(3, min(args.steps, args.fp64_steps))
+        h64.profile(True)
+        ms64 = timed_steps(h64, t64 + 1, k64, h64.stream())
+        prof64 = h64.profile_read()
+        h64.close()
+        ms64 = max_over_ranks(ws, ms64)
+        nn = meas64["n"]
+        fp64 = {"steps_per_s": ws * k64 / (ms64 / 1000.0), "ms_per_step": ms64 / k64, "steps": k64,
+                "memint_ms": prof64["memint"][0] / max(1, prof64["memint"][1]),
+                "sunset_ms": prof64["sunset"][0] / max(1, prof64["sunset"][1]),
+                "mixed_vs_fp64_rel_err": {
+                    "n": float(np.max(np.abs(meas_mixed["n"] - nn)) / np.max(np.abs(nn))),
+                    "E": abs(meas_mixed["E"] - meas64["E"]) / abs(meas64["E"]),
+                    "at_t": t64 - min(args.warmup, 3)}}
+
+    if rank != 0:
+        return 0
+    M = CFG["M"]
+    mi_ms = prof["memint"][0] / max(1, prof["memint"][1])
+    sun_ms = prof["sunset"][0] / max(1, prof["sunset"][1])
+    alg = algorithmic_bytes(M, S, 4, 4)
+    peak, peak_kind = read_peaks()
+    achieved = alg / (mi_ms / 1000.0) / 1e9
+    traffic = read_traffic("traffic_bytes_per_launch")
+    line = {
+        "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 history/sunset, f64 accumulation/leapfrog/diagnostics",
+        "data": "synthetic: tsunami initial state n(p)=5exp(-(|p|-1)^2/0.08), window filled by real evolution",
+        "config": {"workload": "KB step at full memory window: Ns=64, N=4, lambda=2, m=1, dt=0.05, M=1000, "
+                               "LambdaNLO, mixed precision",
+                   "orbits": S, "history_GB": 2 * ((S + 7) // 8) * 8 * ((M + 31) // 32 * 32) ** 2 * 4 / 1e9,
+                   "l2": "no flush: the 55 GB history is >> 129 MB L2",
+                   "parallelism": "replicas" if ws > 1 else "single"},
+        "mode_steps_per_s": value * M * CFG["Ns"] ** 3,
+        "graph_ms_per_step": gms / args.steps,
+        "kernels_ms": {"memint": mi_ms, "sunset": sun_ms},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                     "kernel": "memint_kernel<float,32,2>", "algorithmic_bytes": alg},
+        "clocks": clk.summary(),
+        "e2e": {"value": e2e_val, "unit": "steps/s", "h2d_bytes_per_step": 4, "d2h_bytes_per_step": d2h,
+                "path": "kb_step + kb_measure through the C ABI, host buffers, wall clock"},
+        "gpu_launches": 3 * args.steps,
+        "fp64_plain": fp64,
+        "speedup_mixed_vs_fp64": (value / fp64["steps_per_s"]) if fp64 else None,
+    }
+    if ws == 1 and not args.no_cpu:
+        try:
+            line["cpu_baseline"] = cpu_baseline(steps=1, Msample=args.cpu_window)
+        except Exception as e:  # the baseline is reported, not required
+            line["cpu_baseline"] = {"value": None, "error": str(e)}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--fp64-steps", type=int, default=20)
+    ap.add_argument("--cpu-window", type=int, default=128)
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--config", default="c5", choices=["c5", "small"],
+                    help="c5: the benchmark workload; small: Ns=40, M=400 for profiler captures")
+    args = ap.parse_args()
+    if args.config == "small":
+        CFG.update(SMALL)
+    if args.warmup < 3:
+        ap.error("at least 3 warm-up steps")
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -148,6 +148,19 @@ int kb_checkpoint_restore(kb_handle *h, const void *host_buf, size_t bytes);
  * non-finite measurements). */
 int kb_sync(kb_handle *h);
 
+/* Profiling hooks (the reference times steps with BenchmarkTools,
+ * src/TwoPIScalar/TwoPIScalar_Bechmark.jl:94-116; these time each kernel):
+ * kb_get_stream returns the handle's cudaStream_t (as void*) so that callers
+ * can record their own events on it. While profiling is enabled kb_step and
+ * kb_steps record CUDA events around every kernel launch (kb_steps then
+ * launches step by step instead of replaying its graph); kb_profile_read
+ * synchronises and returns the summed milliseconds and launch counts of
+ * [0] the sunset kernel and [1] the memory-integral kernel since the last
+ * read, then resets them. */
+int kb_get_stream(const kb_handle *h, void **stream);
+int kb_profile(kb_handle *h, int32_t enable);
+int kb_profile_read(kb_handle *h, double *ms, int64_t *launches);
+
 #ifdef __cplusplus
 }
 #endif

@@ -11,6 +11,7 @@
 #include "kb_oracle.h"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <complex>
 #include <cstdint>
@@ -559,10 +560,14 @@ struct Oracle {
   }
 
   // evolve! (TwoPIScalar_Evolution.jl:924-981)
+  double last_t_sunset = 0.0, last_t_rest = 0.0;  // seconds of the last evolve!
+
   void evolve(int t) {
+    auto c0 = std::chrono::steady_clock::now();
     expand();
     if (tmax != t) throw std::invalid_argument("evolve! must be called with t = lastEvolStep + 1");
     self_energies(t - 1);
+    auto c1 = std::chrono::steady_clock::now();
     hartreemass2 = hartree(t - 1, t - 1);
     set_omega2();
     int n = (tmax - 1) - tmin + 1;
@@ -580,6 +585,9 @@ struct Oracle {
     evolve_r(R, t, t);
     rhs_F(R, t, t);
     evolve_F(R, t, t);
+    auto c2 = std::chrono::steady_clock::now();
+    last_t_sunset = std::chrono::duration<double>(c1 - c0).count();
+    last_t_rest = std::chrono::duration<double>(c2 - c1).count();
   }
 
   // initSimData! (TwoPIScalar_Initialization.jl:8-47)
@@ -832,6 +840,10 @@ double orc_hartree_mass2(void *h, int32_t a, int32_t b) {
   double v = 0.0;
   guarded([&] { v = ((Oracle *)h)->hartree(a, b); });
   return v;
+}
+void orc_step_times(void *h, double *t_sunset, double *t_rest) {
+  *t_sunset = ((Oracle *)h)->last_t_sunset;
+  *t_rest = ((Oracle *)h)->last_t_rest;
 }
 double orc_hartree_prefactor(void *h) { return ((Oracle *)h)->hartree_prefactor(); }
 double orc_gap_mass(void *h, const double *n, double x0) { return ((Oracle *)h)->gap_mass(n, x0); }

@@ -98,6 +98,8 @@ int orc_get_lattice(void *h, int32_t which, int32_t a, int32_t b, double *out);
 int orc_window(void *h, int32_t *tmin, int32_t *tmax);
 double orc_hartree_mass2(void *h, int32_t a, int32_t b);
 double orc_hartree_prefactor(void *h);
+/* wall seconds of the last orc_step: self-energies, and the rest of evolve! */
+void orc_step_times(void *h, double *t_sunset, double *t_rest);
 /* getGapMass (TwoPIScalar_Initialization.jl:250-266): Newton from x0 */
 double orc_gap_mass(void *h, const double *n_orbit, double x0);
 

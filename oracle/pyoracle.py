@@ -75,6 +75,7 @@ def _lib():
             lib.orc_gap_mass.argtypes = [C.c_void_p, P(d), d]
             lib.orc_gap_mass.restype = d
             lib.orc_sunset_rows.argtypes = [C.c_void_p, P(d), P(d), P(d), P(d)]
+            lib.orc_step_times.argtypes = [C.c_void_p, P(d), P(d)]
             _LIB = lib
     return _LIB
 
@@ -175,6 +176,11 @@ class Oracle:
         out = np.zeros(self.V)
         _check(self.lib.orc_get_lattice(self.h, which, a, b, _dp(out)), "lattice")
         return out
+
+    def step_times(self):
+        a, b = C.c_double(), C.c_double()
+        self.lib.orc_step_times(self.h, C.byref(a), C.byref(b))
+        return a.value, b.value
 
     def hartree_mass2(self, a, b):
         return self.lib.orc_hartree_mass2(self.h, a, b)

@@ -57,6 +57,13 @@ struct kb_handle {
   bool sigma_valid = false;
   cudaGraphExec_t graph = nullptr;
   int graph_measure = -1;
+  // profiling: event pairs around each kernel launch, summed on read
+  bool profiling = false;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_pending;  // kernel id, (start, stop)
+  size_t ev_next = 0;
+  double prof_ms[2] = {0, 0};
+  int64_t prof_n[2] = {0, 0};
 };
 
 namespace {
@@ -315,6 +322,7 @@ void kb_destroy(kb_handle *h) {
   cudaSetDevice(h->device);
   if (h->st) cudaStreamSynchronize(h->st);
   if (h->graph) cudaGraphExecDestroy(h->graph);
+  for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
   for (auto &R : h->runs) free_run(R);
   void *ptrs[] = {h->d_runs, h->d_base_sun, h->d_base_mi, h->d_t, h->d_err};
   for (void *q : ptrs)
@@ -425,12 +433,37 @@ int kb_init(kb_handle *h, int32_t run, const double *n, double init_mass) {
   return kb_init_rows(h, run, F11.data(), F21.data(), F22.data());
 }
 
+static cudaEvent_t next_event(kb_handle *h) {
+  if (h->ev_next == h->ev_pool.size()) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+    h->ev_pool.push_back(e);
+  }
+  return h->ev_pool[h->ev_next++];
+}
+
 static int launch_step(kb_handle *h, int measure) {
+  cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
+  if (h->profiling) {
+    e0 = next_event(h);
+    e1 = next_event(h);
+    e2 = next_event(h);
+    if (!e0 || !e1 || !e2) return fail(h, KB_ERR_CUDA, "cudaEventCreate failed");
+    KB_CUDA(h, cudaEventRecord(e0, h->st));
+  }
   if (h->any_nlo)
     KB_CUDA(h, kb::launch_sunset(h->fp64, h->d_runs, h->d_base_sun, (int)h->runs.size(), h->total_sun, h->d_t,
                                  h->d_err, h->smem_sun, h->st));
+  if (h->profiling) {
+    KB_CUDA(h, cudaEventRecord(e1, h->st));
+    if (h->any_nlo) h->ev_pending.push_back({0, {e0, e1}});
+  }
   KB_CUDA(h, kb::launch_memint(h->fp64, h->d_runs, h->d_base_mi, (int)h->runs.size(), h->total_mi, h->d_t,
                                h->d_err, measure, h->smem_mi, h->st));
+  if (h->profiling) {
+    KB_CUDA(h, cudaEventRecord(e2, h->st));
+    h->ev_pending.push_back({1, {e1, e2}});
+  }
   return KB_OK;
 }
 
@@ -650,7 +683,13 @@ int kb_steps(kb_handle *h, int32_t t0, int32_t count, int32_t measure_every, kb_
   int nm = 0;
   for (int i = 0; i < count; ++i) {
     const int t = t0 + i;
-    KB_CUDA(h, cudaGraphLaunch(h->graph, h->st));
+    if (h->profiling) {
+      int rc = launch_step(h, 1);
+      if (rc) return rc;
+      KB_CUDA(h, kb::launch_advance_t(h->d_t, h->st));
+    } else {
+      KB_CUDA(h, cudaGraphLaunch(h->graph, h->st));
+    }
     h->t_cur = t;
     if (measure_every > 0 && (t - 2) % measure_every == 0 && out) {
       for (int r = 0; r < nr; ++r) {
@@ -665,6 +704,39 @@ int kb_steps(kb_handle *h, int32_t t0, int32_t count, int32_t measure_every, kb_
   }
   h->sigma_valid = h->any_nlo;
   return kb_sync(h);
+}
+
+int kb_get_stream(const kb_handle *h, void **stream) {
+  if (!h || !stream) return KB_ERR_PARAM;
+  *stream = (void *)h->st;
+  return KB_OK;
+}
+
+int kb_profile(kb_handle *h, int32_t enable) {
+  if (!h) return KB_ERR_PARAM;
+  h->profiling = enable != 0;
+  return KB_OK;
+}
+
+int kb_profile_read(kb_handle *h, double *ms, int64_t *launches) {
+  if (!h) return KB_ERR_PARAM;
+  cudaSetDevice(h->device);
+  KB_CUDA(h, cudaStreamSynchronize(h->st));
+  for (auto &p : h->ev_pending) {
+    float v = 0.f;
+    KB_CUDA(h, cudaEventElapsedTime(&v, p.second.first, p.second.second));
+    h->prof_ms[p.first] += v;
+    h->prof_n[p.first] += 1;
+  }
+  h->ev_pending.clear();
+  h->ev_next = 0;
+  for (int q = 0; q < 2; ++q) {
+    if (ms) ms[q] = h->prof_ms[q];
+    if (launches) launches[q] = h->prof_n[q];
+    h->prof_ms[q] = 0;
+    h->prof_n[q] = 0;
+  }
+  return KB_OK;
 }
 
 int kb_sync(kb_handle *h) {

@@ -28,6 +28,7 @@ EXPORTS = [
     "kb_site_orbits", "kb_init", "kb_init_rows", "kb_step", "kb_steps", "kb_expand", "kb_measure",
     "kb_get_traces", "kb_get", "kb_set", "kb_self_energies", "kb_get_sigma", "kb_window",
     "kb_checkpoint_size", "kb_checkpoint_save", "kb_checkpoint_restore", "kb_sync",
+    "kb_get_stream", "kb_profile", "kb_profile_read",
 ]
 
 
@@ -93,6 +94,9 @@ def load_library(path: str | None = None):
             "kb_checkpoint_save": (C.c_int, [vp, vp, C.c_size_t]),
             "kb_checkpoint_restore": (C.c_int, [vp, vp, C.c_size_t]),
             "kb_sync": (C.c_int, [vp]),
+            "kb_get_stream": (C.c_int, [vp, P(vp)]),
+            "kb_profile": (C.c_int, [vp, i32]),
+            "kb_profile_read": (C.c_int, [vp, dp, P(i64)]),
         }
         for name, (res, args) in sig.items():
             f = getattr(lib, name)
@@ -226,3 +230,17 @@ class Handle:
 
     def sync(self):
         self._check(self.lib.kb_sync(self.h))
+
+    def stream(self):
+        s = C.c_void_p()
+        self._check(self.lib.kb_get_stream(self.h, C.byref(s)))
+        return s.value
+
+    def profile(self, enable=True):
+        self._check(self.lib.kb_profile(self.h, 1 if enable else 0))
+
+    def profile_read(self):
+        ms = np.zeros(2)
+        n = np.zeros(2, np.int64)
+        self._check(self.lib.kb_profile_read(self.h, dptr(ms), n.ctypes.data_as(C.POINTER(C.c_int64))))
+        return {"sunset": (ms[0], int(n[0])), "memint": (ms[1], int(n[1]))}
