@@ -43,6 +43,11 @@ SMALL = dict(Ns=40, N=4, lam=2.0, mass=1.0, mass2=1.0, dt=0.05, M=400, init="tsu
 METRIC = "KB steps/s at Ns=64 (M=1000 window, mixed precision; plain FP64 GPU alongside)"
 
 
+def workload_name():
+    return (f"KB step at full memory window: Ns={CFG['Ns']}, N={CFG['N']}, lambda={CFG['lam']:g}, "
+            f"m={CFG['mass']:g}, dt={CFG['dt']:g}, M={CFG['M']}, tsunami initial state")
+
+
 def tsunami_n(k2):
     return 5.0 * np.exp(-((np.sqrt(k2) - 1.0) ** 2) / (2 * 0.2 ** 2))
 
@@ -255,7 +260,7 @@ def run_reference(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / cb["value"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (tsunami initial state)",
-            "config": {"workload": "KB step at full window, Ns=64, N=4, lambda=2, m=1, dt=0.05, M=1000",
+            "config": {"workload": workload_name(),
                        "l2": "history >> L2"},
             "cpu_baseline": cb,
             "e2e": {"value": cb["value"], "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -354,8 +359,7 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 history/sunset, f64 accumulation/leapfrog/diagnostics",
         "data": "synthetic: tsunami initial state n(p)=5exp(-(|p|-1)^2/0.08), window filled by real evolution",
-        "config": {"workload": "KB step at full memory window: Ns=64, N=4, lambda=2, m=1, dt=0.05, M=1000, "
-                               "LambdaNLO, mixed precision",
+        "config": {"workload": workload_name() + ", LambdaNLO, mixed precision",
                    "orbits": S, "history_GB": 2 * ((S + 7) // 8) * 8 * ((M + 31) // 32 * 32) ** 2 * 4 / 1e9,
                    "l2": "no flush: the 55 GB history is >> 129 MB L2",
                    "parallelism": "replicas" if ws > 1 else "single"},
