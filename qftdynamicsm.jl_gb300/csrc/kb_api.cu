@@ -33,7 +33,7 @@ struct Run {
   // device allocations
   void *hist_F = nullptr, *hist_r = nullptr, *sig_F = nullptr, *sig_r = nullptr;
   double *st_F = nullptr, *st_r = nullptr, *k2_d = nullptr, *deg_d = nullptr, *Cm_d = nullptr;
-  double *tad = nullptr, *meas = nullptr, *epart = nullptr;
+  double *tad = nullptr, *meas = nullptr, *epart = nullptr, *rowacc = nullptr;
   size_t hist_elems = 0, st_elems = 0, sig_elems = 0;
   RunDev dev{};
 };
@@ -51,6 +51,9 @@ struct kb_handle {
   int total_sun = 0, total_mi = 0;
   int *d_t = nullptr, *d_err = nullptr;
   size_t smem_sun = 0, smem_mi = 0;
+  int num_sms = 0, grid_sun = 0;
+  void *sun_scratch = nullptr;    // FP64 cosine-transform intermediates, one slot per CTA
+  size_t sun_scratch_stride = 0;  // elements per slot
   int t_cur = 0;      // last evolved (or initialised) step; window is [tmin(t_cur), t_cur]
   int inited_runs = 0;
   bool any_nlo = false;
@@ -142,7 +145,8 @@ int validate(const kb_params &p, std::string &why) {
 size_t slot_off(const Run &R, int a) { return (size_t)(a % R.Malloc); }
 
 void free_run(Run &R) {
-  void *ptrs[] = {R.hist_F, R.hist_r, R.sig_F, R.sig_r, R.st_F, R.st_r, R.k2_d, R.deg_d, R.Cm_d, R.tad, R.meas, R.epart};
+  void *ptrs[] = {R.hist_F, R.hist_r, R.sig_F, R.sig_r, R.st_F, R.st_r, R.k2_d, R.deg_d, R.Cm_d, R.tad, R.meas, R.epart,
+                  R.rowacc};
   for (void *q : ptrs)
     if (q) cudaFree(q);
 }
@@ -232,6 +236,7 @@ int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out) {
         {(void **)&R.k2_d, (size_t)R.Spad * 8}, {(void **)&R.deg_d, (size_t)R.Spad * 8},
         {(void **)&R.Cm_d, (size_t)R.H * R.H * 8}, {(void **)&R.tad, (size_t)2 * R.nchunks * 8},
         {(void **)&R.meas, (size_t)5 * R.Spad * 8}, {(void **)&R.epart, (size_t)4 * R.nchunks * 8},
+        {(void **)&R.rowacc, (size_t)R.nchunks * R.Malloc * KC * 8},
     };
     for (auto &a : al) {
       if (cudaMalloc(a.p, a.bytes) != cudaSuccess) {
@@ -280,6 +285,7 @@ int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out) {
     D.tad = R.tad;
     D.meas = R.meas;
     D.epart = R.epart;
+    D.rowacc = R.rowacc;
     D.cta_base_sun = bsun[r];
     D.cta_base_mi = bmi[r];
   }
@@ -294,6 +300,20 @@ int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out) {
     fail(nullptr, KB_ERR_OOM, "cudaMalloc of the run table failed");
     kb_destroy(h);
     return KB_ERR_OOM;
+  }
+  cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
+  h->grid_sun = kb::sunset_grid(h->fp64, h->num_sms, h->total_sun);
+  if (h->fp64 && h->any_nlo) {
+    int Hmax = 1;
+    for (auto &R : h->runs) Hmax = std::max(Hmax, R.H);
+    h->sun_scratch_stride = kb::sunset_scratch_elems(Hmax);
+    const size_t bytes = (size_t)h->grid_sun * h->sun_scratch_stride * sizeof(double);
+    if (cudaMalloc(&h->sun_scratch, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      fail(nullptr, KB_ERR_OOM, "cudaMalloc of %zu bytes of sunset scratch failed", bytes);
+      kb_destroy(h);
+      return KB_ERR_OOM;
+    }
   }
   cudaMemcpy(h->d_runs, devs.data(), sizeof(RunDev) * nruns, cudaMemcpyHostToDevice);
   cudaMemcpy(h->d_base_sun, bsun.data(), sizeof(int) * nruns, cudaMemcpyHostToDevice);
@@ -324,7 +344,7 @@ void kb_destroy(kb_handle *h) {
   if (h->graph) cudaGraphExecDestroy(h->graph);
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
   for (auto &R : h->runs) free_run(R);
-  void *ptrs[] = {h->d_runs, h->d_base_sun, h->d_base_mi, h->d_t, h->d_err};
+  void *ptrs[] = {h->d_runs, h->d_base_sun, h->d_base_mi, h->d_t, h->d_err, h->sun_scratch};
   for (void *q : ptrs)
     if (q) cudaFree(q);
   if (h->st) cudaStreamDestroy(h->st);
@@ -452,8 +472,8 @@ static int launch_step(kb_handle *h, int measure) {
     KB_CUDA(h, cudaEventRecord(e0, h->st));
   }
   if (h->any_nlo)
-    KB_CUDA(h, kb::launch_sunset(h->fp64, h->d_runs, h->d_base_sun, (int)h->runs.size(), h->total_sun, h->d_t,
-                                 h->d_err, h->smem_sun, h->st));
+    KB_CUDA(h, kb::launch_sunset(h->fp64, h->d_runs, h->d_base_sun, (int)h->runs.size(), h->total_sun, h->grid_sun,
+                                 h->d_t, h->sun_scratch, h->sun_scratch_stride, h->smem_sun, h->st));
   if (h->profiling) {
     KB_CUDA(h, cudaEventRecord(e1, h->st));
     if (h->any_nlo) h->ev_pending.push_back({0, {e0, e1}});
@@ -588,8 +608,8 @@ int kb_self_energies(kb_handle *h, int32_t tmone) {
   cudaSetDevice(h->device);
   KB_CUDA(h, kb::launch_set_t(h->d_t, h->t_cur, h->st));
   if (h->any_nlo)
-    KB_CUDA(h, kb::launch_sunset(h->fp64, h->d_runs, h->d_base_sun, (int)h->runs.size(), h->total_sun, h->d_t,
-                                 h->d_err, h->smem_sun, h->st));
+    KB_CUDA(h, kb::launch_sunset(h->fp64, h->d_runs, h->d_base_sun, (int)h->runs.size(), h->total_sun, h->grid_sun,
+                                 h->d_t, h->sun_scratch, h->sun_scratch_stride, h->smem_sun, h->st));
   h->sigma_valid = true;
   return kb_sync(h);
 }

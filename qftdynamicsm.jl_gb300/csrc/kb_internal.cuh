@@ -12,6 +12,8 @@
 //                                              by t mod 2
 //   meas            [5][Spad]                 double: F(t-1,t-1), ddF, n, omega, c
 //   epart           [nchunks][4]              double: E_kin, E_pot, E_mem partials
+//   rowacc          [nchunks][Malloc][KC]     double: row sums of the memory integrals
+//   sunset scratch  [grid][R1 + R2]           double: FP64 cosine-transform intermediates
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -39,6 +41,7 @@ struct RunDev {
   double *tad;              // [2][nchunks]
   double *meas;             // [5][Spad]
   double *epart;            // [nchunks][4]
+  double *rowacc;           // [nchunks][Malloc][KC] scratch of the memory-integral kernel
   int cta_base_sun, cta_base_mi;  // first CTA of this run in the batched grids
   int pad0, pad1;
 };
@@ -58,9 +61,11 @@ __device__ inline int find_run(const int *base, int nruns, int bid) {
 }
 
 // host launchers (kb_sunset.cu, kb_memint.cu)
-cudaError_t launch_sunset(bool fp64, const RunDev *d_runs, const int *d_base, int nruns, int total_ctas,
-                          const int *d_t, int *d_err, size_t smem, cudaStream_t st);
+cudaError_t launch_sunset(bool fp64, const RunDev *d_runs, const int *d_base, int nruns, int total_rows, int grid,
+                          const int *d_t, void *scratch, size_t scratch_stride, size_t smem, cudaStream_t st);
 size_t sunset_smem_bytes(bool fp64, int H);
+size_t sunset_scratch_elems(int H);
+int sunset_grid(bool fp64, int num_sms, int total_rows);
 cudaError_t configure_sunset(bool fp64, size_t smem);
 cudaError_t launch_memint(bool fp64, const RunDev *d_runs, const int *d_base, int nruns, int total_ctas,
                           const int *d_t, int *d_err, int measure, size_t smem, cudaStream_t st);

@@ -7,185 +7,351 @@
 //   Sigma_rho(t') = ivol^3 (-lambda^2 (N+2)/(6 N^2))  brfft[rx (Fx^2 - rx^2/12)]
 //   Sigma_F(t')   = ivol^3 (-lambda^2 (N+2)/(18 N^2)) brfft[Fx (Fx^2 - 3/4 rx^2)]
 //
-// F and rho are cubic-symmetric, so both transforms reduce to cosine
-// transforms on the even octant [0, H)^3 (H = Ns/2 + 1) with the matrix
-// C[X][x] = m(x) cos(2 pi x X / Ns) (m = 1 at 0 and Ns/2, else 2), applied
-// along the three axes. The data stay on cubic orbits (S = C(H+2,3) values):
-// for a fixed first output coordinate X the three axis passes need only a
-// slab of H(H+1)/2 + H^2 values, so a whole t' row is transformed in shared
-// memory by one CTA without touching the full lattice:
-//   pass 1  B_X(y,z)  = sum_x C[X][x] f(x,y,z)          y <= z  (symmetric in y,z)
-//   pass 2  C_X(Y,z)  = sum_y C[Y][y] B_X(y,z)          Y >= X
-//   pass 3  P(X,Y,Z)  = sum_z C[Z][z] C_X(Y,z)          X <= Y <= Z  (an orbit)
-// 1.44 M multiply-adds per transform at Ns = 64 instead of 3.6 M on the octant
-// and far fewer than the 4 full-lattice FFTs of the reference.
+// F and rho are cubic-symmetric, so the 3D transforms reduce to cosine
+// transforms on the even octant [0,H)^3 (H = Ns/2 + 1) with the matrix
+// C[X][x] = m(x) cos(2 pi x X / Ns) (m = 1 at 0 and Ns/2, else 2) along each
+// axis. Data stay on cubic orbits (S = C(H+2,3) values); the three axis
+// passes keep the symmetry that survives them:
+//   expand  E[x][p]   = f(x, y_p, z_p)                      p = (y <= z) pair
+//   pass 1  B[X][p]   = sum_x C[X][x] E[x][p]                (symmetric in y,z)
+//   pass 2  D[q][z]   = sum_y C[Y][y] B[X][(y,z)]            q = (X <= Y) pair
+//   pass 3  P(X,Y,Z)  = sum_z C[Z][z] D[(X,Y)][z]            X <= Y <= Z: an orbit
+// Each pass is a small dense GEMM; every thread computes a 4 x 4 register
+// tile, loading four cosine coefficients with one 16-byte load per k. At
+// Ns = 64 a transform costs about 2 M multiply-adds (four per t') instead of
+// the four 262144-point FFTs of the reference.
 //
-// One CTA per t' (grid = sum over runs of M); CTAs with t' outside the window
-// return at once, so the same launch serves every step of a CUDA graph.
+// Intermediates E/D and B live in two regions R1, R2 of H*P values: in shared
+// memory for FP32, in a per-CTA global scratch slot for FP64 (whose regions
+// do not fit next to each other in 227 KB). The grid is persistent: CTA b
+// handles the t' rows b, b + gridDim, ... of all runs of the batch, so the
+// same launch serves every step of a CUDA graph (rows outside the window are
+// skipped).
 #include "kb_internal.cuh"
 
 namespace kb {
 namespace {
 
-constexpr int SUN_THREADS = 256;
+constexpr int SUN_THREADS = 512;
 
-template <typename TC>
-struct SunSmem {
-  TC *Cm, *bufA, *bufB, *bufC, *Bx, *C2;
-  uint16_t *pairs;
+__host__ __device__ inline int rup4(int v) { return (v + 3) & ~3; }
+
+struct SunGeom {
+  int H, H4, P, P4, S;
+  int r1, r2;  // region sizes in elements
+  __host__ __device__ SunGeom(int H_) {
+    H = H_;
+    H4 = rup4(H);
+    P = H * (H + 1) / 2;
+    P4 = rup4(P);
+    S = H * (H + 1) * (H + 2) / 6;
+    const int e = H * P4, d = P * H4;
+    r1 = e > d ? e : d;
+    if (S > r1) r1 = S;
+    r2 = H * P4;
+    if (S > r2) r2 = S;
+    r1 = rup4(r1);
+    r2 = rup4(r2);
+  }
 };
 
+// 4-wide vector load/store for float (float4) and double (2 x double2)
+__device__ __forceinline__ void ld4(const float *p, float v[4]) {
+  const float4 q = *reinterpret_cast<const float4 *>(p);
+  v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+}
+__device__ __forceinline__ void ld4(const double *p, double v[4]) {
+  const double2 a = *reinterpret_cast<const double2 *>(p);
+  const double2 b = *reinterpret_cast<const double2 *>(p + 2);
+  v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+}
+__device__ __forceinline__ void st4(float *p, const float v[4]) {
+  *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+__device__ __forceinline__ void st4(double *p, const double v[4]) {
+  *reinterpret_cast<double2 *>(p) = make_double2(v[0], v[1]);
+  *reinterpret_cast<double2 *>(p + 2) = make_double2(v[2], v[3]);
+}
+
+// orbit index of (x, y, z) given y <= z
+__device__ __forceinline__ int orb_of(int x, int y, int z) {
+  const int lo = min(x, y);
+  const int mid = (x <= y) ? y : min(x, z);
+  const int hi = max(x, z);
+  return orb3(lo, mid, hi);
+}
+
 template <typename TC>
-__device__ inline SunSmem<TC> sun_layout(unsigned char *raw, int H, int S) {
-  SunSmem<TC> s;
-  const int P = H * (H + 1) / 2;
-  TC *p = reinterpret_cast<TC *>(raw);
-  s.Cm = p;
-  p += H * H;
-  s.bufA = p;
-  p += S;
-  s.bufB = p;
-  p += S;
-  s.bufC = p;
-  p += S;
-  s.Bx = p;
-  p += P;
-  s.C2 = p;
-  p += H * H;
-  s.pairs = reinterpret_cast<uint16_t *>(p);
-  return s;
+struct SunCtx {
+  const TC *CT;         // [H][H4]: CT[x][X] = C[X][x]
+  const uint16_t *pr;   // [P]: pair p -> (lo | hi << 8)
+  const int *off2;      // [H+1] item offsets of pass 2
+  const int *off3;      // [P4/4 + 1] item offsets of pass 3
+  TC *R1, *R2, *bufF;
+  SunGeom g;
+};
+
+// expand: E[x][p] = in(orbit of (x, y_p, z_p)) for x < H, p < P
+template <typename TC, typename In>
+__device__ void sun_expand(const SunCtx<TC> &c, TC *E, In in) {
+  const int n = c.g.H * c.g.P;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int x = i / c.g.P, p = i - x * c.g.P;
+    const int y = c.pr[p] & 255, z = c.pr[p] >> 8;
+    E[x * c.g.P4 + p] = in(orb_of(x, y, z));
+  }
 }
 
-// Cosine transform of a cubic-symmetric function given on orbits `in`;
-// out(orbit, value) receives every orbit once. Ends with a barrier.
+// pass 1: B[X][p] = sum_x CT[x][X] E[x][p]
+template <typename TC>
+__device__ void sun_pass1(const SunCtx<TC> &c, const TC *E, TC *B) {
+  const int H = c.g.H, P4 = c.g.P4;
+  const int nxb = c.g.H4 / 4, npb = P4 / 4;
+  for (int it = threadIdx.x; it < nxb * npb; it += blockDim.x) {
+    const int xb = it / npb, pb = it - xb * npb;
+    const int X0 = 4 * xb, p0 = 4 * pb;
+    TC acc[4][4] = {};
+    for (int x = 0; x < H; ++x) {
+      TC cv[4], ev[4];
+      ld4(c.CT + x * c.g.H4 + X0, cv);
+      ld4(E + x * P4 + p0, ev);
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] += cv[i] * ev[j];
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+      if (X0 + i < H) st4(B + (X0 + i) * P4 + p0, acc[i]);
+  }
+}
+
+// pass 2: D[tri2(Y)+X][z] = sum_y CT[y][Y] B[X][(min(y,z), max(y,z))], Y >= X
+template <typename TC>
+__device__ void sun_pass2(const SunCtx<TC> &c, const TC *B, TC *D) {
+  const int H = c.g.H, H4 = c.g.H4, P4 = c.g.P4;
+  const int nzb = H4 / 4;
+  const int total = c.off2[H];
+  for (int it = threadIdx.x; it < total; it += blockDim.x) {
+    int lo = 0, hi = H - 1;  // X with off2[X] <= it < off2[X+1]
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (c.off2[mid] <= it) lo = mid; else hi = mid - 1;
+    }
+    const int X = lo;
+    const int r = it - c.off2[X];
+    const int yb = r / nzb, zb = r - yb * nzb;
+    const int Y0 = 4 * (X / 4) + 4 * yb, z0 = 4 * zb;
+    const TC *Bx = B + X * P4;
+    TC acc[4][4] = {};
+    for (int y = 0; y < H; ++y) {
+      TC cv[4], bv[4];
+      ld4(c.CT + y * H4 + Y0, cv);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int z = min(z0 + j, H - 1);
+        bv[j] = (y <= z) ? Bx[tri2(z) + y] : Bx[tri2(y) + z];
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] += cv[i] * bv[j];
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int Y = Y0 + i;
+      if (Y >= X && Y < H) st4(D + (tri2(Y) + X) * H4 + z0, acc[i]);
+    }
+  }
+}
+
+// pass 3: out(orbit(X,Y,Z), sum_z CT[z][Z] D[q][z]) for q = (X,Y), Z >= Y
 template <typename TC, typename Out>
-__device__ void octant_transform3(const SunSmem<TC> &s, const TC *in, int H, Out out) {
-  const int P = H * (H + 1) / 2;
-  const TC *Cm = s.Cm;
-  for (int X = 0; X < H; ++X) {
-    const TC *cX = Cm + X * H;
-    // pass 1: B_X(y,z) for y <= z; f(x,y,z) looked up on its sorted orbit
-    for (int p = threadIdx.x; p < P; p += blockDim.x) {
-      const int y = s.pairs[p] & 255, z = s.pairs[p] >> 8;
-      const int t3z = (int)tet3(z), t2y = tri2(y), t2z = tri2(z);
-      TC acc = 0;
-      int x = 0;
-      for (; x <= y; ++x) acc += cX[x] * in[t3z + t2y + x];          // (x, y, z)
-      for (; x <= z; ++x) acc += cX[x] * in[t3z + tri2(x) + y];      // (y, x, z)
-      for (; x < H; ++x) acc += cX[x] * in[(int)tet3(x) + t2z + y];  // (y, z, x)
-      s.Bx[p] = acc;
+__device__ void sun_pass3(const SunCtx<TC> &c, const TC *D, Out out) {
+  const int H = c.g.H, H4 = c.g.H4, P = c.g.P;
+  const int nqb = c.g.P4 / 4;
+  const int total = c.off3[nqb];
+  for (int it = threadIdx.x; it < total; it += blockDim.x) {
+    int lo = 0, hi = nqb - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (c.off3[mid] <= it) lo = mid; else hi = mid - 1;
     }
-    __syncthreads();
-    // pass 2: C_X(Y,z) for Y >= X and all z
-    const int n2 = (H - X) * H;
-    for (int q = threadIdx.x; q < n2; q += blockDim.x) {
-      const int Yo = q / H, z = q - Yo * H;
-      const TC *cY = Cm + (X + Yo) * H;
-      const int t2z = tri2(z);
-      TC acc = 0;
-      int y = 0;
-      for (; y <= z; ++y) acc += cY[y] * s.Bx[t2z + y];
-      for (; y < H; ++y) acc += cY[y] * s.Bx[tri2(y) + z];
-      s.C2[Yo * H + z] = acc;
+    const int qb = lo;
+    const int q0 = 4 * qb;
+    const int Ymin = c.pr[min(q0, P - 1)] >> 8;
+    const int Z0 = 4 * (Ymin / 4) + 4 * (it - c.off3[qb]);
+    TC acc[4][4] = {};
+    int qrow[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) qrow[i] = min(q0 + i, P - 1) * H4;
+    for (int z = 0; z < H; ++z) {
+      TC cv[4], dv[4];
+      ld4(c.CT + z * H4 + Z0, cv);
+#pragma unroll
+      for (int i = 0; i < 4; ++i) dv[i] = D[qrow[i] + z];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] += dv[i] * cv[j];
     }
-    __syncthreads();
-    // pass 3: P(X,Y,Z) for X <= Y <= Z
-    const int h = H - X;
-    const int n3 = h * (h + 1) / 2;
-    for (int q = threadIdx.x; q < n3; q += blockDim.x) {
-      const int Yo = s.pairs[q] & 255, Zo = s.pairs[q] >> 8;
-      const TC *cZ = Cm + (X + Zo) * H;
-      const TC *c2 = s.C2 + Yo * H;
-      TC acc = 0;
-      for (int z = 0; z < H; ++z) acc += cZ[z] * c2[z];
-      out(orb3(X, X + Yo, X + Zo), acc);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int q = q0 + i;
+      if (q >= P) continue;
+      const int X = c.pr[q] & 255, Y = c.pr[q] >> 8;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int Z = Z0 + j;
+        if (Z >= Y && Z < H) out(orb3(X, Y, Z), acc[i][j]);
+      }
     }
-    // the next pass 1 writes Bx only, which pass 3 does not read
   }
+}
+
+template <typename TC, typename In, typename Out>
+__device__ void sun_transform(const SunCtx<TC> &c, In in, Out out) {
+  sun_expand<TC>(c, c.R1, in);
+  __syncthreads();
+  sun_pass1<TC>(c, c.R1, c.R2);
+  __syncthreads();
+  sun_pass2<TC>(c, c.R2, c.R1);
+  __syncthreads();
+  sun_pass3<TC>(c, c.R1, out);
   __syncthreads();
 }
 
-template <typename TC, typename TS>
-__global__ void __launch_bounds__(SUN_THREADS)
-sunset_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int nruns,
-              const int *__restrict__ d_t, int *__restrict__ d_err) {
+template <typename TC, typename TS, bool SCRATCH>
+__global__ void __launch_bounds__(SUN_THREADS, 1)
+sunset_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int nruns, int total,
+              const int *__restrict__ d_t, TC *__restrict__ scratch, size_t scratch_stride) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int r = find_run(base, nruns, blockIdx.x);
-  const RunDev &R = runs[r];
   const int t = *d_t;  // Sigma(t-1, t') for t' in [tmin, t-1]
-  const int tmin = max(1, t - R.M + 1);
-  const int tp = tmin + (int)(blockIdx.x - R.cta_base_sun);
-  if (R.pexp == 0 || tp > t - 1 || t < 3) return;
-  const int H = R.H, S = R.S;
-  const int P = H * (H + 1) / 2;
-  SunSmem<TC> s = sun_layout<TC>(smem_raw, H, S);
+  int cur_run = -1;
+  SunCtx<TC> c{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, SunGeom(1)};
+  for (int w = blockIdx.x; w < total; w += gridDim.x) {
+    const int r = find_run(base, nruns, w);
+    const RunDev &R = runs[r];
+    const int tmin = max(1, t - R.M + 1);
+    const int tp = tmin + (w - R.cta_base_sun);
+    if (R.pexp == 0 || tp > t - 1 || t < 3) continue;
+    if (r != cur_run) {
+      // per-run tables: cosine matrix, pair list, pass offsets
+      __syncthreads();
+      cur_run = r;
+      SunGeom g(R.H);
+      TC *p = reinterpret_cast<TC *>(smem_raw);
+      TC *CT = p;
+      p += g.H * g.H4;
+      TC *bufF = p;
+      p += rup4(g.S);
+      TC *R1, *R2;
+      if (SCRATCH) {
+        R1 = scratch + (size_t)blockIdx.x * scratch_stride;
+        R2 = R1 + g.r1;
+      } else {
+        R1 = p;
+        p += g.r1;
+        R2 = p;
+        p += g.r2;
+      }
+      int *off2 = reinterpret_cast<int *>(p);
+      int *off3 = off2 + (g.H + 1);
+      uint16_t *pr = reinterpret_cast<uint16_t *>(off3 + (g.P4 / 4 + 1));
+      for (int i = threadIdx.x; i < g.H * g.H4; i += blockDim.x) {
+        const int x = i / g.H4, X = i - x * g.H4;
+        CT[i] = (X < g.H) ? (TC)R.Cm[X * g.H + x] : (TC)0;
+      }
+      for (int z = threadIdx.x; z < g.H; z += blockDim.x)
+        for (int y = 0; y <= z; ++y) pr[tri2(z) + y] = (uint16_t)(y | (z << 8));
+      if (threadIdx.x == 0) {
+        const int nzb = g.H4 / 4;
+        off2[0] = 0;
+        for (int X = 0; X < g.H; ++X) off2[X + 1] = off2[X] + (g.H4 / 4 - X / 4) * nzb;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        const int nqb = g.P4 / 4;
+        off3[0] = 0;
+        for (int qb = 0; qb < nqb; ++qb) {
+          const int Ymin = pr[min(4 * qb, g.P - 1)] >> 8;
+          off3[qb + 1] = off3[qb] + (g.H4 / 4 - Ymin / 4);
+        }
+      }
+      __syncthreads();
+      c = SunCtx<TC>{CT, pr, off2, off3, R1, R2, bufF, g};
+    }
+    const int S = c.g.S;
+    const int slot = tp % R.Malloc;
+    const size_t rowstride = (size_t)R.Malloc * KC;
+    const int r3 = (t - 1) % 3;
+    const double *stF = R.st_F + (size_t)r3 * R.nchunks * rowstride + (size_t)slot * KC;
+    const double *stR = R.st_r + (size_t)r3 * R.nchunks * rowstride + (size_t)slot * KC;
+    auto gidx = [&](int o) { return (size_t)(o / KC) * rowstride + (o % KC); };
 
-  for (int i = threadIdx.x; i < H * H; i += blockDim.x) s.Cm[i] = (TC)R.Cm[i];
-  for (int z = threadIdx.x; z < H; z += blockDim.x)
-    for (int y = 0; y <= z; ++y) s.pairs[tri2(z) + y] = (uint16_t)(y | (z << 8));
-  (void)P;
+    // forward transforms of F(t-1,t') -> bufF and rho(t-1,t') -> R2 (orbit layout)
+    sun_transform<TC>(c, [&](int o) { return (TC)stF[gidx(o)]; }, [&](int o, TC v) { c.bufF[o] = v; });
+    sun_transform<TC>(c, [&](int o) { return (TC)stR[gidx(o)]; }, [&](int o, TC v) { c.R2[o] = v; });
 
-  // row t-1 of the FP64 leapfrog state: F(t-1, t'), rho(t-1, t')
-  const int r3 = (t - 1) % 3;
-  const int slot = tp % R.Malloc;
-  const size_t rowstride = (size_t)R.Malloc * KC;
-  const double *stF = R.st_F + (size_t)r3 * R.nchunks * rowstride + (size_t)slot * KC;
-  const double *stR = R.st_r + (size_t)r3 * R.nchunks * rowstride + (size_t)slot * KC;
-  for (int k = threadIdx.x; k < S; k += blockDim.x)
-    s.bufA[k] = (TC)stF[(size_t)(k / KC) * rowstride + (k % KC)];
-  __syncthreads();
-  octant_transform3<TC>(s, s.bufA, H, [&](int o, TC v) { s.bufB[o] = v; });  // Fx
-  for (int k = threadIdx.x; k < S; k += blockDim.x)
-    s.bufA[k] = (TC)stR[(size_t)(k / KC) * rowstride + (k % KC)];
-  __syncthreads();
-  octant_transform3<TC>(s, s.bufA, H, [&](int o, TC v) { s.bufC[o] = v; });  // rx
+    // pointwise sunset in position space (Evolution.jl:28-29, classical :114-115)
+    const bool classical = (R.pexp == 2);
+    for (int k = threadIdx.x; k < S; k += blockDim.x) {
+      const TC Fx = c.bufF[k], rx = c.R2[k];
+      const TC F2 = Fx * Fx, r2 = rx * rx;
+      c.R2[k] = classical ? rx * F2 : rx * (F2 - (TC)(1 / 12.) * r2);
+      c.bufF[k] = classical ? Fx * F2 : Fx * (F2 - (TC)0.75 * r2);
+    }
+    __syncthreads();
 
-  // pointwise sunset in position space (Evolution.jl:28-29, classical :114-115)
-  const bool classical = (R.pexp == 2);
-  for (int k = threadIdx.x; k < S; k += blockDim.x) {
-    const TC Fx = s.bufB[k], rx = s.bufC[k];
-    const TC F2 = Fx * Fx, r2 = rx * rx;
-    s.bufC[k] = classical ? rx * F2 : rx * (F2 - (TC)(1 / 12.) * r2);
-    s.bufB[k] = classical ? Fx * F2 : Fx * (F2 - (TC)0.75 * r2);
+    // inverse transforms straight into the Sigma rings (scaled by ivol^3 * coefficient)
+    TS *sigr = reinterpret_cast<TS *>(R.sig_r) + (size_t)slot * KC;
+    TS *sigF = reinterpret_cast<TS *>(R.sig_F) + (size_t)slot * KC;
+    const double fr = R.fac_r, fF = R.fac_F;
+    const TC *gr = c.R2;
+    // expand reads R2 into R1 before pass 1 overwrites R2
+    sun_transform<TC>(c, [&](int o) { return gr[o]; }, [&](int o, TC v) { sigr[gidx(o)] = (TS)(fr * (double)v); });
+    const TC *gF = c.bufF;
+    sun_transform<TC>(c, [&](int o) { return gF[o]; }, [&](int o, TC v) { sigF[gidx(o)] = (TS)(fF * (double)v); });
   }
-  __syncthreads();
-
-  TS *sigr = reinterpret_cast<TS *>(R.sig_r) + (size_t)slot * KC;
-  TS *sigF = reinterpret_cast<TS *>(R.sig_F) + (size_t)slot * KC;
-  const double fr = R.fac_r, fF = R.fac_F;
-  octant_transform3<TC>(s, s.bufC, H, [&](int o, TC v) {
-    sigr[(size_t)(o / KC) * rowstride + (o % KC)] = (TS)(fr * (double)v);
-  });
-  octant_transform3<TC>(s, s.bufB, H, [&](int o, TC v) {
-    sigF[(size_t)(o / KC) * rowstride + (o % KC)] = (TS)(fF * (double)v);
-  });
-  (void)d_err;
 }
 
 }  // namespace
 
 size_t sunset_smem_bytes(bool fp64, int H) {
-  const size_t S = (size_t)H * (H + 1) * (H + 2) / 6;
-  const size_t P = (size_t)H * (H + 1) / 2;
-  const size_t elems = 2 * (size_t)H * H + 3 * S + P;
-  return elems * (fp64 ? sizeof(double) : sizeof(float)) + P * sizeof(uint16_t) + 16;
+  SunGeom g(H);
+  const size_t es = fp64 ? sizeof(double) : sizeof(float);
+  size_t elems = (size_t)g.H * g.H4 + rup4(g.S);
+  if (!fp64) elems += (size_t)g.r1 + g.r2;
+  return elems * es + (size_t)(g.H + 1 + g.P4 / 4 + 1) * sizeof(int) + (size_t)g.P * sizeof(uint16_t) + 64;
+}
+
+size_t sunset_scratch_elems(int H) {
+  SunGeom g(H);
+  return (size_t)g.r1 + g.r2;
+}
+
+int sunset_grid(bool fp64, int num_sms, int total_rows) {
+  (void)fp64;
+  return total_rows < num_sms ? total_rows : num_sms;
 }
 
 cudaError_t configure_sunset(bool fp64, size_t smem) {
   if (fp64)
-    return cudaFuncSetAttribute(sunset_kernel<double, double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    return cudaFuncSetAttribute(sunset_kernel<double, double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem);
-  return cudaFuncSetAttribute(sunset_kernel<float, float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  return cudaFuncSetAttribute(sunset_kernel<float, float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)smem);
 }
 
-cudaError_t launch_sunset(bool fp64, const RunDev *d_runs, const int *d_base, int nruns, int total_ctas,
-                          const int *d_t, int *d_err, size_t smem, cudaStream_t st) {
-  if (total_ctas <= 0) return cudaSuccess;
+cudaError_t launch_sunset(bool fp64, const RunDev *d_runs, const int *d_base, int nruns, int total_rows, int grid,
+                          const int *d_t, void *scratch, size_t scratch_stride, size_t smem, cudaStream_t st) {
+  if (total_rows <= 0 || grid <= 0) return cudaSuccess;
   if (fp64)
-    sunset_kernel<double, double><<<total_ctas, SUN_THREADS, smem, st>>>(d_runs, d_base, nruns, d_t, d_err);
+    sunset_kernel<double, double, true><<<grid, SUN_THREADS, smem, st>>>(
+        d_runs, d_base, nruns, total_rows, d_t, reinterpret_cast<double *>(scratch), scratch_stride);
   else
-    sunset_kernel<float, float><<<total_ctas, SUN_THREADS, smem, st>>>(d_runs, d_base, nruns, d_t, d_err);
+    sunset_kernel<float, float, false><<<grid, SUN_THREADS, smem, st>>>(d_runs, d_base, nruns, total_rows, d_t,
+                                                                         nullptr, 0);
   return cudaGetLastError();
 }
 

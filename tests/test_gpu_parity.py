@@ -216,3 +216,79 @@ def test_errors_are_reported():
     assert ei.value.code == -6
     with pytest.raises(capi.KbError):
         make_gpu(dict(Ns=7, M=9, dt=0.1, lam=1.0))
+
+
+@pytest.mark.parametrize("name", ["small_ns8_m10", "c1_ns16_m202"])
+def test_gpu_matches_golden(name):
+    """Committed oracle trajectories (tests/golden/make_golden.py), config 1 included."""
+    import os
+
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", name + ".npz"))
+    Ns, M, N, lam, dt, T, steps = g["cfg"]
+    cfg = dict(Ns=int(Ns), M=int(M), N=int(N), lam=float(lam), dt=float(dt))
+    h = make_gpu(cfg)
+    h.init(0, g["n0"], 1.0)
+    scal = [[h.measure(0, 2)[k] for k in ("time", "E", "E_pot", "E_kin", "E_mem", "M2")]]
+    snaps = []
+    for t in range(3, 3 + int(steps)):
+        h.step(t)
+        m = h.measure(0, t)
+        scal.append([m[k] for k in ("time", "E", "E_pot", "E_kin", "E_mem", "M2")])
+        if t in set(g["n_t"].tolist()):
+            snaps.append(m["n"])
+    scal = np.array(scal)
+    ref = g["scalars"]
+    for col in range(1, 6):
+        assert rel(scal[:, col], ref[:, col]) <= TOL64, col
+    assert rel(np.array(snaps), g["n"]) <= TOL64
+    t = 2 + int(steps)
+    for i, tp in enumerate(g["tps"]):
+        assert rel(h.get(0, 0, t, int(tp)), g["F_last_row"][i]) <= TOL64
+        if tp < t:
+            assert rel(h.get(0, 1, t, int(tp)), g["rho_last_row"][i]) <= TOL64
+
+
+def test_gauss_zero_plus_one_dimensions():
+    """Nx = 1 Gauss state (Simulationfiles/Anders_NNLOpaper.jl parameters) on the GPU:
+    E(2) is the reference's analytic energy and the run follows the oracle."""
+    from oracle import Oracle
+
+    xi, eta, sig, lam, N, dt = 0.4, 5.0, 1.0, 1.0, 8, 0.01
+    E0 = 0.5 * eta ** 2 + sig ** 2 / (8 * xi ** 2) + 0.5 * xi ** 2 + (1 / 24) * lam * (N + 2) / N * xi ** 4
+    h = make_gpu(dict(Ns=1, M=300, N=N, lam=lam, dt=dt))
+    F11 = np.array([xi ** 2])
+    F21 = xi * eta * dt + F11
+    F22 = (eta ** 2 + sig ** 2 / (4 * xi ** 2)) * dt ** 2 - F11 + 2 * F21
+    h.init_rows(0, F11, F21, F22)
+    o = Oracle(1, 3, M=300, N=N, dt=dt, lam=lam, mass2=1.0, engine=ENGINE_FULL)
+    o.init_gauss(xi, eta, sig)
+    assert abs(h.measure(0, 2)["E"] - E0) <= 1e-12 * E0
+    for t in range(3, 400):
+        h.step(t)
+        o.step(t)
+    mg, mo = h.measure(0, 399), o.measure(399)
+    assert abs(mg["E"] - mo["E"]) <= TOL64 * abs(mo["E"])
+
+
+def test_host_mirror_run_simulation():
+    """The reference's driver loop (G_SimulationArgs.jl:86-106) through kb2pi's mirror
+    of QFTdynamicsProblem / initialize! / evolve! / measure!, against the oracle."""
+    import kb2pi
+    from oracle import Oracle
+
+    parameters = {"Mass": 1.0, "Nx": 8, "sdim": 3, "dt": 0.1, "Nsteps": 20, "NstepsinMemory": 12, "Nmeas": 0,
+                  "Mod": "phi4", "Lambda": 2.0, "ONgroup": 4, "init": "Thermal", "T": 2.0, "Reno": "RMass",
+                  "Pexp": "LambdaNLO", "Num": "GPU", "Nchunks": 0, "tag": "test", "ov": True}
+    sol = kb2pi.run_simulation(dict(parameters))
+    problem = sol.problem
+    o = Oracle(8, 3, M=12, N=4, dt=0.1, lam=2.0, mass2=problem.model.Mass2, mass=1.0)
+    _, k2, _ = o.orbits()
+    o.init_occupation(1.0 / (np.exp(np.sqrt(k2 + 1.0) / 2.0) - 1.0), 1.0)
+    Es = [o.measure(2)["E"]]
+    for t in range(3, 23):
+        o.step(t)
+        Es.append(o.measure(t)["E"])
+    got = [m["E"] for m in sol.measurearray]
+    assert len(got) == 21
+    assert rel(got, Es) <= TOL64
+    assert problem.model.Mass2 < 1.0  # RMass counterterm applied
