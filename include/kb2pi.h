@@ -161,6 +161,26 @@ int kb_get_stream(const kb_handle *h, void **stream);
 int kb_profile(kb_handle *h, int32_t enable);
 int kb_profile_read(kb_handle *h, double *ms, int64_t *launches);
 
+/* Self-energies of caller-owned rows, allocating nothing. No counterpart in
+ * the reference: it is for callers that cannot call cudaMalloc -- a host
+ * whose device memory is owned by its own pool (a CUDA.jl or PyTorch caching
+ * allocator that must stay the only allocator of the process), or a loop that
+ * must not let an allocation synchronise the device. Computes Sigma_F and
+ * Sigma_rho (FP64, the KB_PREC_FP64 sunset of kb_step) for nrows rows given on
+ * the device in orbit order (row i = F(t-1, t'_i) / rho(t-1, t'_i), S values
+ * each, rho sign-corrected), on `stream` (a cudaStream_t, NULL for the legacy
+ * default stream). The transform scratch is one fixed device array of
+ * 160 x 5712 doubles (7.3 MB) compiled into the library, held on every GPU
+ * that loads it until the process exits, so Ns is limited to 1 or an even
+ * value in [2, 32]; larger Ns fails with KB_ERR_PARAM and a message in
+ * kb_last_error(NULL). The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress) with that device current; make that first
+ * call before any stream capture. Every call shares the array, so calls whose
+ * kernels overlap on the GPU (other streams, other host threads) race; issue
+ * them on one stream. Nothing in the array needs to start at zero. */
+int kb_sunset_rows_noalloc(int32_t Ns, int32_t N, double lambda, int32_t pexp, int32_t nrows, const double *F_rows,
+                           const double *rho_rows, double *sigF_rows, double *sigr_rows, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -162,6 +162,8 @@ void gather_host(const std::vector<TS> &chunked, int S, double *out) {
 
 }  // namespace
 
+void kb::kb_set_global_error(const char *msg) { g_create_err = msg; }
+
 // ------------------------------------------------------------------------
 extern "C" {
 

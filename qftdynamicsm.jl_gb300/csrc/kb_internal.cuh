@@ -75,5 +75,7 @@ int memint_tile(bool fp64);
 cudaError_t launch_measure_init(const RunDev *d_runs, int nruns, int t, cudaStream_t st);
 cudaError_t launch_set_t(int *d_t, int t, cudaStream_t st);
 cudaError_t launch_advance_t(int *d_t, cudaStream_t st);
+// message returned by kb_last_error(NULL) (kb_api.cu)
+void kb_set_global_error(const char *msg);
 
 }  // namespace kb

@@ -27,6 +27,12 @@
 // handles the t' rows b, b + gridDim, ... of all runs of the batch, so the
 // same launch serves every step of a CUDA graph (rows outside the window are
 // skipped).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <mutex>
+
+#include "../../include/kb2pi.h"
 #include "kb_internal.cuh"
 
 namespace kb {
@@ -35,6 +41,7 @@ namespace {
 constexpr int SUN_THREADS = 512;
 
 __host__ __device__ inline int rup4(int v) { return (v + 3) & ~3; }
+constexpr int rup4_c(int v) { return (v + 3) & ~3; }
 
 struct SunGeom {
   int H, H4, P, P4, S;
@@ -356,3 +363,167 @@ cudaError_t launch_sunset(bool fp64, const RunDev *d_runs, const int *d_base, in
 }
 
 }  // namespace kb
+
+// ---------------------------------------------------------------------------
+// Allocation-free self-energies (kb_sunset_rows_noalloc)
+//
+// Same FP64 cosine-transform sunset as the persistent kernel above, for rows
+// the caller passes in device memory, with the per-CTA transform scratch in a
+// file-scope device array instead of a cudaMalloc'd buffer. The array holds
+// NOALLOC_MAX_CTAS slots sized for the largest lattice accepted
+// (Ns <= NOALLOC_MAX_NS): 160 x 5712 doubles = 7.3 MB, resident on every GPU
+// that loads the library until the process exits.
+// ---------------------------------------------------------------------------
+namespace kb {
+namespace {
+
+constexpr int NOALLOC_MAX_NS = 32;
+constexpr int NOALLOC_MAX_CTAS = 160;
+
+constexpr size_t na_slot_elems(int H) {
+  // the R1 + R2 regions of SunGeom for octant size H (pass intermediates)
+  return (size_t)rup4_c(std::max(std::max(H * rup4_c(H * (H + 1) / 2), (H * (H + 1) / 2) * rup4_c(H)),
+                                 H * (H + 1) * (H + 2) / 6)) +
+         (size_t)rup4_c(std::max(H * rup4_c(H * (H + 1) / 2), H * (H + 1) * (H + 2) / 6));
+}
+constexpr size_t NOALLOC_SLOT_ELEMS = na_slot_elems(NOALLOC_MAX_NS / 2 + 1);
+
+// Shared by every call on a device; contents persist between calls. Nothing in
+// it needs to start at zero: each transform writes every element it reads.
+__device__ __align__(256) double g_noalloc_scratch[NOALLOC_MAX_CTAS * NOALLOC_SLOT_ELEMS];
+
+__global__ void __launch_bounds__(SUN_THREADS, 1)
+sunset_rows_noalloc_kernel(int Ns, double fac_r, double fac_F, int classical, int nrows,
+                           const double *__restrict__ F_rows, const double *__restrict__ r_rows,
+                           double *__restrict__ sigF_rows, double *__restrict__ sigr_rows, double *scratch,
+                           size_t stride) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int H = Ns / 2 + 1;
+  SunGeom g(H);
+  double *CT = reinterpret_cast<double *>(smem_raw);
+  double *bufF = CT + g.H * g.H4;
+  int *off2 = reinterpret_cast<int *>(bufF + rup4(g.S));
+  int *off3 = off2 + (g.H + 1);
+  uint16_t *pr = reinterpret_cast<uint16_t *>(off3 + (g.P4 / 4 + 1));
+  double *R1 = scratch + (size_t)blockIdx.x * stride;
+  double *R2 = R1 + g.r1;
+  // cosine matrix of the even octant, C[X][x] = m(x) cos(2 pi x X / Ns), stored transposed
+  for (int i = threadIdx.x; i < g.H * g.H4; i += blockDim.x) {
+    const int x = i / g.H4, X = i - x * g.H4;
+    const double m = (x == 0 || 2 * x == Ns) ? 1.0 : 2.0;
+    CT[i] = (X < g.H) ? m * cospi(2.0 * (double)((x * X) % Ns) / (double)Ns) : 0.0;
+  }
+  for (int z = threadIdx.x; z < g.H; z += blockDim.x)
+    for (int y = 0; y <= z; ++y) pr[tri2(z) + y] = (uint16_t)(y | (z << 8));
+  if (threadIdx.x == 0) {
+    const int nzb = g.H4 / 4;
+    off2[0] = 0;
+    for (int X = 0; X < g.H; ++X) off2[X + 1] = off2[X] + (g.H4 / 4 - X / 4) * nzb;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int nqb = g.P4 / 4;
+    off3[0] = 0;
+    for (int qb = 0; qb < nqb; ++qb) {
+      const int Ymin = pr[min(4 * qb, g.P - 1)] >> 8;
+      off3[qb + 1] = off3[qb] + (g.H4 / 4 - Ymin / 4);
+    }
+  }
+  __syncthreads();
+  const SunCtx<double> c{CT, pr, off2, off3, R1, R2, bufF, g};
+  const int S = g.S;
+  for (int row = blockIdx.x; row < nrows; row += gridDim.x) {
+    const double *Fin = F_rows + (size_t)row * S;
+    const double *rin = r_rows + (size_t)row * S;
+    sun_transform<double>(c, [&](int o) { return Fin[o]; }, [&](int o, double v) { c.bufF[o] = v; });
+    sun_transform<double>(c, [&](int o) { return rin[o]; }, [&](int o, double v) { c.R2[o] = v; });
+    for (int k = threadIdx.x; k < S; k += blockDim.x) {
+      const double Fx = c.bufF[k], rx = c.R2[k];
+      const double F2 = Fx * Fx, r2 = rx * rx;
+      c.R2[k] = classical ? rx * F2 : rx * (F2 - (1 / 12.) * r2);
+      c.bufF[k] = classical ? Fx * F2 : Fx * (F2 - 0.75 * r2);
+    }
+    __syncthreads();
+    double *outr = sigr_rows + (size_t)row * S;
+    double *outF = sigF_rows + (size_t)row * S;
+    const double *gr = c.R2;
+    sun_transform<double>(c, [&](int o) { return gr[o]; }, [&](int o, double v) { outr[o] = fac_r * v; });
+    const double *gF = c.bufF;
+    sun_transform<double>(c, [&](int o) { return gF[o]; }, [&](int o, double v) { outF[o] = fac_F * v; });
+  }
+}
+
+std::mutex g_noalloc_mu;
+double *g_noalloc_ptr[64] = {};  // device address of g_noalloc_scratch, per device ordinal
+
+}  // namespace
+}  // namespace kb
+
+extern "C" int kb_sunset_rows_noalloc(int32_t Ns, int32_t N, double lambda, int32_t pexp, int32_t nrows,
+                                      const double *F_rows, const double *rho_rows, double *sigF_rows,
+                                      double *sigr_rows, void *stream) {
+  using namespace kb;
+  char msg[256];
+  if (!((Ns >= 2 && Ns <= NOALLOC_MAX_NS && Ns % 2 == 0) || Ns == 1)) {
+    snprintf(msg, sizeof msg,
+             "kb_sunset_rows_noalloc: Ns=%d is beyond the maximum of its fixed scratch (Ns must be 1 or even "
+             "in [2,%d])",
+             Ns, NOALLOC_MAX_NS);
+    kb_set_global_error(msg);
+    return KB_ERR_PARAM;
+  }
+  if (N < 1 || (pexp != KB_PEXP_NLO_QUANTUM && pexp != KB_PEXP_NLO_CLASSICAL) || nrows < 0 ||
+      !std::isfinite(lambda)) {
+    kb_set_global_error("kb_sunset_rows_noalloc: needs N >= 1, pexp = KB_PEXP_NLO_QUANTUM or "
+                        "KB_PEXP_NLO_CLASSICAL, nrows >= 0 and a finite lambda");
+    return KB_ERR_PARAM;
+  }
+  if (nrows == 0) return KB_OK;
+  if (!F_rows || !rho_rows || !sigF_rows || !sigr_rows) {
+    kb_set_global_error("kb_sunset_rows_noalloc: null row pointer");
+    return KB_ERR_PARAM;
+  }
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    cudaGetLastError();
+    kb_set_global_error("kb_sunset_rows_noalloc: no current CUDA device");
+    return KB_ERR_NODEV;
+  }
+  double *scratch = nullptr;
+  {
+    // once per device, with that device current: device address of the array
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+      cudaError_t e = cudaGetSymbolAddress((void **)&g_noalloc_ptr[dev], g_noalloc_scratch);
+      if (e != cudaSuccess || !g_noalloc_ptr[dev]) {
+        g_noalloc_ptr[dev] = nullptr;
+        snprintf(msg, sizeof msg, "kb_sunset_rows_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+        kb_set_global_error(msg);
+        return KB_ERR_CUDA;
+      }
+    }
+    scratch = g_noalloc_ptr[dev];
+  }
+  int nsm = 0;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int H = Ns / 2 + 1;
+  const size_t stride = na_slot_elems(H);
+  int grid = nrows < NOALLOC_MAX_CTAS ? nrows : NOALLOC_MAX_CTAS;
+  if (nsm > 0 && grid > nsm) grid = nsm;
+  const double V = (double)Ns * Ns * Ns, iv = 1.0 / V, Nd = (double)N;
+  const double fac_r = iv * iv * iv * (-(lambda * lambda) * (Nd + 2.0) / (6.0 * Nd * Nd));
+  const double fac_F = iv * iv * iv * (-(lambda * lambda) * (Nd + 2.0) / (18.0 * Nd * Nd));
+  SunGeom g(H);
+  const size_t smem = ((size_t)g.H * g.H4 + rup4(g.S)) * sizeof(double) +
+                      (size_t)(g.H + 1 + g.P4 / 4 + 1) * sizeof(int) + (size_t)g.P * sizeof(uint16_t) + 64;
+  sunset_rows_noalloc_kernel<<<grid, SUN_THREADS, smem, (cudaStream_t)stream>>>(
+      Ns, fac_r, fac_F, pexp == KB_PEXP_NLO_CLASSICAL ? 1 : 0, nrows, F_rows, rho_rows, sigF_rows, sigr_rows,
+      scratch, stride);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    snprintf(msg, sizeof msg, "kb_sunset_rows_noalloc: launch failed: %s", cudaGetErrorString(e));
+    kb_set_global_error(msg);
+    return KB_ERR_CUDA;
+  }
+  return KB_OK;
+}

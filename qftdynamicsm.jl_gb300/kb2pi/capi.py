@@ -28,7 +28,7 @@ EXPORTS = [
     "kb_site_orbits", "kb_init", "kb_init_rows", "kb_step", "kb_steps", "kb_expand", "kb_measure",
     "kb_get_traces", "kb_get", "kb_set", "kb_self_energies", "kb_get_sigma", "kb_window",
     "kb_checkpoint_size", "kb_checkpoint_save", "kb_checkpoint_restore", "kb_sync",
-    "kb_get_stream", "kb_profile", "kb_profile_read",
+    "kb_get_stream", "kb_profile", "kb_profile_read", "kb_sunset_rows_noalloc",
 ]
 
 
@@ -97,6 +97,7 @@ def load_library(path: str | None = None):
             "kb_get_stream": (C.c_int, [vp, P(vp)]),
             "kb_profile": (C.c_int, [vp, i32]),
             "kb_profile_read": (C.c_int, [vp, dp, P(i64)]),
+            "kb_sunset_rows_noalloc": (C.c_int, [i32, i32, d, i32, i32, vp, vp, vp, vp, vp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(lib, name)
