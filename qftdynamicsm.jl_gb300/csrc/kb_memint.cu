@@ -51,10 +51,10 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
       "selp.u32 %0, 1, 0, p;\n\t}"
       : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(1000000u)  // suspend up to 1 ms per poll
       : "memory");
   return ok != 0;
 }
@@ -84,27 +84,72 @@ __device__ __forceinline__ void fence_proxy_async() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
-template <typename TS, int T_, int NST_>
+// OPT adjacent orbits per consumer thread: two FP32 values move with one 8-byte
+// shared-memory load and one packed fma.rn.f32x2; FP64 keeps one orbit per thread.
+template <typename TS, int OPT>
+struct Vec;
+template <>
+struct Vec<float, 2> {
+  float2 v;
+  __device__ __forceinline__ static Vec zero() { return Vec{make_float2(0.f, 0.f)}; }
+  __device__ __forceinline__ static Vec ld(const float *p) { return Vec{*reinterpret_cast<const float2 *>(p)}; }
+  __device__ __forceinline__ void fma(const Vec &a, const Vec &b) {
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;"
+        : "=l"(d)
+        : "l"(*reinterpret_cast<const unsigned long long *>(&a.v)),
+          "l"(*reinterpret_cast<const unsigned long long *>(&b.v)),
+          "l"(*reinterpret_cast<const unsigned long long *>(&v)));
+    v = *reinterpret_cast<float2 *>(&d);
+  }
+  __device__ __forceinline__ void scale(float w) {
+    v.x *= w;
+    v.y *= w;
+  }
+  __device__ __forceinline__ double get(int i) const { return i == 0 ? (double)v.x : (double)v.y; }
+  __device__ __forceinline__ void add(const Vec &o) {
+    v.x += o.v.x;
+    v.y += o.v.y;
+  }
+};
+template <>
+struct Vec<double, 1> {
+  double v;
+  __device__ __forceinline__ static Vec zero() { return Vec{0.0}; }
+  __device__ __forceinline__ static Vec ld(const double *p) { return Vec{*p}; }
+  __device__ __forceinline__ void fma(const Vec &a, const Vec &b) { v = fma_rn(a.v, b.v, v); }
+  __device__ __forceinline__ static double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
+  __device__ __forceinline__ void scale(double w) { v *= w; }
+  __device__ __forceinline__ double get(int) const { return v; }
+  __device__ __forceinline__ void add(const Vec &o) { v += o.v; }
+};
+
+template <typename TS, int T_, int NST_, int OPT_>
 struct Cfg {
   static constexpr int T = T_;
   static constexpr int NST = NST_;
-  static constexpr int NT = T * KC;       // threads: one per (column b, orbit j)
-  static constexpr int NW = NT / 32;
-  static constexpr int LPJ = 32 / KC;     // columns per warp
-  static constexpr int RPT = T / LPJ;     // rows per thread after the warp reduce-scatter
-  static constexpr int TILE = T * T * KC; // elements of one field tile
-  static constexpr int XROW = T * KC;
-  static constexpr int STAGE = 2 * TILE + XROW;
+  static constexpr int OPT = OPT_;                          // orbits per consumer thread
+  static constexpr int NJ = KC / OPT;                       // orbit groups per chunk
+  static constexpr int NG = T * NJ;                         // threads per consumer group
+  static constexpr int NT = 2 * NG;                         // column group + row group
+  static constexpr int NW = NT / 32;                        // consumer warps
+  static constexpr int ROWPAD = 32 / sizeof(TS);            // 32-byte pad per tile row: conflict-free rows
+  static constexpr int RS = T * KC + ROWPAD;                // smem stride of one tile row
+  static constexpr int TILE = T * RS;                       // elements of one field tile in smem
+  static constexpr int XV = T * KC;                         // one x vector (T times x KC orbits)
+  static constexpr int STAGE = 2 * TILE + 3 * XV;           // F, rho, x_rho(rows), x_rho(cols), x_F(cols)
   static constexpr uint32_t STAGE_BYTES = STAGE * sizeof(TS);
-  static constexpr size_t RED_BYTES = ((size_t)NW * T * KC * sizeof(TS) + 15) / 16 * 16;
+  static constexpr uint32_t TX_BYTES = (2 * T * T * KC + 3 * XV) * sizeof(TS);  // bytes the TMA delivers
   static_assert((T * KC * sizeof(TS)) % 16 == 0, "bulk copies need 16-byte multiples");
-  static_assert(T <= 32, "one tile row per lane of the issuing warp");
+  static_assert((RS * sizeof(TS)) % 16 == 0, "tile rows must stay 16-byte aligned");
+  static_assert(T <= 32, "one tile row per lane of the producer warp");
+  static_assert(NG % 32 == 0, "whole warps per group");
 };
 
 template <typename C>
 __host__ __device__ constexpr size_t smem_fixed_bytes() {
-  // stages + double-buffered row-reduction buffer + full/empty barriers + small scratch
-  return (size_t)C::NST * C::STAGE_BYTES + 2 * C::RED_BYTES + 2 * C::NST * 8 + 128 * 8 + 16;
+  // stages + full/empty barriers + small scratch
+  return (size_t)C::NST * C::STAGE_BYTES + 2 * C::NST * 8 + 128 * 8 + 16;
 }
 
 // Time tile iterator over the triangle: J = column block, I = row block >= J.
@@ -120,14 +165,15 @@ struct TileIt {
   }
 };
 
-// issued by the producer warp: the T row segments of the F and rho tiles and
-// the Sigma_rho values of the tile's rows, all into one stage
+// issued by the producer warp: the T row segments of the F and rho tiles (each
+// row to a 32-byte padded smem row), Sigma_rho of the tile's rows and
+// Sigma_rho, Sigma_F of its columns, all into one stage
 template <typename TS, typename C>
 __device__ __forceinline__ void issue_tile(int stage, int I, int J, const RunDev &R, int c, TS *stages,
                                            uint64_t *full) {
   const int lane = threadIdx.x & 31;
   uint64_t *bar = full + stage;
-  if (lane == 0) mbar_expect_tx(bar, C::STAGE_BYTES);
+  if (lane == 0) mbar_expect_tx(bar, C::TX_BYTES);
   __syncwarp();
   TS *dst = stages + (size_t)stage * C::STAGE;
   const int sa0 = (I * C::T) % R.Malloc;  // Malloc is a multiple of T: rows stay contiguous
@@ -136,12 +182,15 @@ __device__ __forceinline__ void issue_tile(int stage, int I, int J, const RunDev
   const TS *hR = reinterpret_cast<const TS *>(R.hist_r);
   if (lane < C::T) {
     const size_t off = (((size_t)c * R.Malloc + sa0 + lane) * R.Malloc + sb0) * KC;
-    bulk_g2s(dst + lane * C::T * KC, hF + off, C::T * KC * sizeof(TS), bar);
-    bulk_g2s(dst + C::TILE + lane * C::T * KC, hR + off, C::T * KC * sizeof(TS), bar);
+    bulk_g2s(dst + lane * C::RS, hF + off, C::T * KC * sizeof(TS), bar);
+    bulk_g2s(dst + C::TILE + lane * C::RS, hR + off, C::T * KC * sizeof(TS), bar);
   }
   if (lane == 0) {
-    const TS *sg = reinterpret_cast<const TS *>(R.sig_r) + ((size_t)c * R.Malloc + sa0) * KC;
-    bulk_g2s(dst + 2 * C::TILE, sg, C::XROW * sizeof(TS), bar);
+    const TS *sr = reinterpret_cast<const TS *>(R.sig_r) + (size_t)c * R.Malloc * KC;
+    const TS *sF = reinterpret_cast<const TS *>(R.sig_F) + (size_t)c * R.Malloc * KC;
+    bulk_g2s(dst + 2 * C::TILE, sr + (size_t)sa0 * KC, C::XV * sizeof(TS), bar);
+    bulk_g2s(dst + 2 * C::TILE + C::XV, sr + (size_t)sb0 * KC, C::XV * sizeof(TS), bar);
+    bulk_g2s(dst + 2 * C::TILE + 2 * C::XV, sF + (size_t)sb0 * KC, C::XV * sizeof(TS), bar);
   }
 }
 
@@ -149,48 +198,55 @@ __device__ __forceinline__ void consumer_sync(int nthreads) {
   asm volatile("bar.sync 1, %0;" ::"r"(nthreads) : "memory");
 }
 
-// Block = NT consumer threads (one per column b and orbit j of a tile) + one
-// producer warp that streams tiles through an NST-deep ring of shared-memory
-// stages guarded by full (TMA transaction count) and empty (consumer release)
-// mbarriers. Consumers synchronise once per tile (named barrier 1) for the
-// cross-thread row reduction; the producer never joins it.
-template <typename TS, int T, int NST>
-__global__ void __launch_bounds__(T *KC + 32)
+// Block = column group (NG threads: column b, orbits j) + row group (NG threads:
+// row a, orbits j) + one producer warp. Both consumer groups read every tile
+// from the shared-memory ring: the column group accumulates
+//   acc_F(b) += x_rho(a) F(a,b),  acc_r(b) += x_rho(a) rho(a,b)   over rows a >= b,
+// the row group
+//   acc_F(a) += x_rho(b) F(a,b) + x_F(b) rho(a,b)                  over columns b < a,
+// each in its own registers over the valid index range of the tile, so a tile
+// needs no cross-thread reduction and no block barrier; every consumer warp
+// releases the stage through the empty mbarrier. Once per column block both
+// groups meet at a named barrier: the row sums of that block are complete and
+// the column group runs its leapfrog.
+template <typename TS, int T, int NST, int OPT>
+__global__ void __launch_bounds__(2 * T * (KC / OPT) + 32)
 memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int nruns,
               const int *__restrict__ d_t, int *__restrict__ d_err, int measure) {
-  using C = Cfg<TS, T, NST>;
+  using C = Cfg<TS, T, NST, OPT>;
+  using V = Vec<TS, OPT>;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   TS *stages = reinterpret_cast<TS *>(smem_raw);
-  TS *redbuf = reinterpret_cast<TS *>(smem_raw + (size_t)NST * C::STAGE_BYTES);  // 2 x [NW][T][KC]
-  uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw + (size_t)NST * C::STAGE_BYTES + 2 * C::RED_BYTES);
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw + (size_t)NST * C::STAGE_BYTES);
   uint64_t *empty = full + NST;
   // misc: [0] hartreecont, [1] M^2, [2..2+KC) acc_F(t-1) per orbit, [10] abort flag,
-  // [11] tiles issued, [12] consumer abort flag, [16..16+NW*KC) diagonal partials
+  // [11] tiles issued, [12] consumer abort flag, [16..16+(NG/32)*KC) diagonal partials
   double *misc = reinterpret_cast<double *>(empty + NST);  // 128 doubles
   volatile int *abort_flag = reinterpret_cast<volatile int *>(misc + 10);
   volatile int *issued_count = reinterpret_cast<volatile int *>(misc + 11);
   // consumers leave the tile loop together: the flag is only written by
-  // consumers before the named barrier and read by them after it
+  // consumers and they all meet at the named barrier after the tile loop
   volatile int *cabort = reinterpret_cast<volatile int *>(misc + 12);
-  static_assert(16 + C::NW * KC <= 128, "misc scratch too small");
+  static_assert(16 + (C::NG / 32) * KC <= 128, "misc scratch too small");
 
   const int r = find_run(base, nruns, blockIdx.x);
   const RunDev &R = runs[r];
   const int c = blockIdx.x - R.cta_base_mi;  // chunk
   const int tid = threadIdx.x;
   const bool producer = tid >= C::NT;
-  const int j = tid % KC, bl = tid / KC;
+  const bool colgrp = tid < C::NG;
+  const int gtid = colgrp ? tid : tid - C::NG;  // index inside the group
+  const int jq = gtid % C::NJ, loc = gtid / C::NJ;  // orbit group; column (col group) or row (row group)
+  const int j0 = jq * OPT;                          // first orbit of this thread in the chunk
   const int lane = tid & 31, warp = tid >> 5;
   const int t = *d_t;
   const int M = R.M, Ma = R.Malloc;
   const int tmin = max(1, t - M + 1);
   const size_t rowstride = (size_t)Ma * KC;              // one row of one chunk
   const size_t st_row = (size_t)R.nchunks * rowstride;   // one state row (all chunks)
-  const int k = c * KC + j;                              // orbit of this thread
-  // row sums of this chunk, [Malloc][KC]: entry (slot, j) is only ever touched
-  // by consumer thread (slot mod T, j) -- row a is reduced by thread bl = a mod T
-  // and column b = a is finalised by the same thread -- so it needs no
-  // synchronisation; it lives in a global scratch slot that stays in L2.
+  // row sums of this chunk, [Malloc][KC]: entries (slot, j0..j0+OPT-1) are only
+  // ever written by row-group thread (slot mod T, jq), so they need no atomics;
+  // they live in a global scratch slot that stays in L2.
   double *rowacc = R.rowacc + (size_t)c * rowstride;
 
   // --- tadpole mass M^2(t-1) from the per-chunk sums of F(t-1,t-1) (fixed order)
@@ -211,12 +267,13 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
     *cabort = 0;
     for (int q = 0; q < NST; ++q) {
       mbar_init(full + q, 1);
-      mbar_init(empty + q, 1);
+      mbar_init(empty + q, C::NW);  // one arrival per consumer warp
     }
     fence_proxy_async();
   }
-  if (!producer)
-    for (int q = tid; q < Ma * KC; q += C::NT) rowacc[q] = 0.0;  // entries owned by this thread
+  if (!producer && !colgrp)
+    for (int s = loc; s < Ma; s += T)  // the slots this thread owns
+      for (int o = 0; o < OPT; ++o) rowacc[(size_t)s * KC + j0 + o] = 0.0;
   __syncthreads();
   const double hc = misc[0], M2 = misc[1];
 
@@ -245,153 +302,194 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   } else {
     // ---------------- consumers
     const double dt3 = R.dt3;
-    const double kk = (k < R.S) ? R.k2[k] : 0.0;
-    const double om = (kk + M2) * R.dt2;  // setomega2values!: (kL2 + M^2) * dt^2
-    const double *F1row = R.st_F + (size_t)((t - 1) % 3) * st_row + (size_t)c * rowstride;
-    const double *F2row = R.st_F + (size_t)((t - 2) % 3) * st_row + (size_t)c * rowstride;
-    const double *R1row = R.st_r + (size_t)((t - 1) % 3) * st_row + (size_t)c * rowstride;
-    const double *R2row = R.st_r + (size_t)((t - 2) % 3) * st_row + (size_t)c * rowstride;
-    double *FNrow = R.st_F + (size_t)(t % 3) * st_row + (size_t)c * rowstride;
-    double *RNrow = R.st_r + (size_t)(t % 3) * st_row + (size_t)c * rowstride;
-    TS *hFnew = reinterpret_cast<TS *>(R.hist_F) + ((size_t)c * Ma + (t % Ma)) * rowstride;
-    TS *hRnew = reinterpret_cast<TS *>(R.hist_r) + ((size_t)c * Ma + (t % Ma)) * rowstride;
-    const TS *sigr = reinterpret_cast<const TS *>(R.sig_r) + (size_t)c * rowstride;
-    const TS *sigF = reinterpret_cast<const TS *>(R.sig_F) + (size_t)c * rowstride;
-
-    double diag = 0.0;  // acc_F(t) for the diagonal, partial over this thread's columns
-    double emem = 0.0;  // acc_F(t-1), kept by the thread of column t-1
+    double diag[OPT];  // acc_F(t) for the diagonal, partial over this thread's columns
+    double emem[OPT];  // acc_F(t-1), kept by the thread of column t-1
+    for (int o = 0; o < OPT; ++o) diag[o] = emem[o] = 0.0;
     bool has_emem = false;
     bool aborted = false;
     int n = 0;  // tiles consumed
+    // row group: accumulator of the row of the next tile, loaded one tile ahead
+    double pre[OPT];
+    for (int o = 0; o < OPT; ++o) pre[o] = 0.0;
+    if (!colgrp) {
+      const int a0 = J0 * T + loc;
+      if (a0 >= tmin && a0 <= t - 1)
+        for (int o = 0; o < OPT; ++o) pre[o] = rowacc[(size_t)(a0 % Ma) * KC + j0 + o];
+    }
 
     for (int J = J0; J <= Jn && !aborted; ++J) {
-      const int b = J * T + bl;
-      const bool bvalid = (b >= tmin) && (b <= t - 1);
-      const double wb = (b == tmin) ? 0.5 : 1.0;
-      const double xbr_d = (bvalid && !lo_only) ? wb * (double)sigr[(size_t)(b % Ma) * KC + j] : 0.0;
-      const double xbF_d = (bvalid && !lo_only) ? wb * (double)sigF[(size_t)(b % Ma) * KC + j] : 0.0;
-      const TS xbr = (TS)xbr_d, xbF = (TS)xbF_d;
-      double colF = 0.0, colR = 0.0;
+      const int b = J * T + loc;  // column of a column-group thread
+      const bool bvalid = colgrp && (b >= tmin) && (b <= t - 1);
+      double colF[OPT], colR[OPT];
+      for (int o = 0; o < OPT; ++o) colF[o] = colR[o] = 0.0;
 
       for (int I = lo_only ? Jn + 1 : J; I <= Jn; ++I, ++n) {
         const int stage = n % NST;
-        if (!mbar_wait_bounded(full + stage, (uint32_t)((n / NST) & 1))) {
+        bool ok = !*cabort && mbar_wait_bounded(full + stage, (uint32_t)((n / NST) & 1));
+        ok = __all_sync(0xffffffffu, ok);  // warp-uniform decision
+        if (!ok) {
+          // a wait expired here or in another consumer: leave the tile loop; all
+          // consumers meet at the named barrier that closes this column block
           *abort_flag = 1;  // stops the producer
           *cabort = 1;
           atomicOr(d_err, DEVERR_TIMEOUT);
-        }
-        const TS *tF = stages + (size_t)stage * C::STAGE;
-        const TS *tR = tF + C::TILE;
-        const TS *sx = tF + 2 * C::TILE;
-
-        TS cF0 = 0, cF1 = 0, cR0 = 0, cR1 = 0;
-        TS rp[T];
-        const bool interior = (I > J) && (J * T >= tmin) && (I * T + T - 1 <= t - 1);
-        if (interior) {
-#pragma unroll
-          for (int rr = 0; rr < T; rr += 2) {
-            const TS xa0 = sx[rr * KC + j], xa1 = sx[(rr + 1) * KC + j];
-            const TS f0 = tF[(rr * T + bl) * KC + j], f1 = tF[((rr + 1) * T + bl) * KC + j];
-            const TS q0 = tR[(rr * T + bl) * KC + j], q1 = tR[((rr + 1) * T + bl) * KC + j];
-            cF0 += xa0 * f0;
-            cR0 += xa0 * q0;
-            cF1 += xa1 * f1;
-            cR1 += xa1 * q1;
-            rp[rr] = xbr * f0 + xbF * q0;
-            rp[rr + 1] = xbr * f1 + xbF * q1;
-          }
-        } else {
-#pragma unroll
-          for (int rr = 0; rr < T; ++rr) {
-            const int a = I * T + rr;
-            const bool av = (a >= tmin) && (a <= t - 1);
-            const TS wa = (a == tmin) ? (TS)0.5 : (TS)1;
-            const TS xa = av ? sx[rr * KC + j] * wa : (TS)0;
-            const bool ok = av && bvalid && (b <= a);
-            const TS f = ok ? tF[(rr * T + bl) * KC + j] : (TS)0;
-            const TS q = ok ? tR[(rr * T + bl) * KC + j] : (TS)0;
-            if (rr & 1) {
-              cF1 += xa * f;
-              cR1 += xa * q;
-            } else {
-              cF0 += xa * f;
-              cR0 += xa * q;
-            }
-            rp[rr] = (ok && b < a) ? xbr * f + xbF * q : (TS)0;
-          }
-        }
-        colF += (double)(cF0 + cF1);
-        colR += (double)(cR0 + cR1);
-
-        // reduce-scatter rp over the LPJ columns of this warp that share orbit j
-        int row0 = 0;
-#pragma unroll
-        for (int o = 16, half = T / 2; o >= KC; o >>= 1, half >>= 1) {
-          const bool hi = (lane & o) != 0;
-#pragma unroll
-          for (int i = 0; i < half; ++i) {
-            const TS a0 = rp[i], a1 = rp[i + half];
-            const TS send = hi ? a0 : a1;
-            const TS keep = hi ? a1 : a0;
-            rp[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
-          }
-          if (hi) row0 += half;
-        }
-        TS *red = redbuf + (size_t)(n & 1) * (C::RED_BYTES / sizeof(TS));
-#pragma unroll
-        for (int i = 0; i < C::RPT; ++i) red[((size_t)warp * T + row0 + i) * KC + j] = rp[i];
-        consumer_sync(C::NT);  // every consumer is done with the stage and has written red
-        if (tid == 0) mbar_arrive(empty + stage);
-        {
-          // thread (rr = bl, j): add the CTA-wide row sum of row a = I*T + bl
-          const int a = I * T + bl;
-          TS sum = 0;
-#pragma unroll
-          for (int w = 0; w < C::NW; ++w) sum += red[((size_t)w * T + bl) * KC + j];
-          if (a >= tmin && a <= t - 1) rowacc[(size_t)(a % Ma) * KC + j] += (double)sum;
-        }
-        if (*cabort) {
           aborted = true;
           break;
         }
+        const TS *tF = stages + (size_t)stage * C::STAGE;
+        const TS *tR = tF + C::TILE;
+        const TS *xr_row = tF + 2 * C::TILE;
+        const TS *xr_col = xr_row + C::XV;
+        const TS *xF_col = xr_col + C::XV;
+        if (colgrp) {
+          // column sums over the valid rows a of the tile: a in [max(b, tmin), t-1]
+          int lo = max(b, tmin) - I * T, hi = min(T - 1, t - 1 - I * T);
+          if (!bvalid) hi = -1;
+          lo = max(lo, 0);
+          V cF0 = V::zero(), cF1 = V::zero(), cR0 = V::zero(), cR1 = V::zero();
+          const TS *fb = tF + loc * KC + j0;
+          const TS *qb = tR + loc * KC + j0;
+          const TS *xb = xr_row + j0;
+          int rr = lo;
+          if (rr <= hi && I * T + rr == tmin) {  // trapezoid half weight of z = tmin
+            V x = V::ld(xb + rr * KC);
+            x.scale((TS)0.5);
+            cF0.fma(x, V::ld(fb + rr * C::RS));
+            cR0.fma(x, V::ld(qb + rr * C::RS));
+            ++rr;
+          }
+#pragma unroll 4
+          for (; rr + 1 <= hi; rr += 2) {
+            const V x0 = V::ld(xb + rr * KC), x1 = V::ld(xb + (rr + 1) * KC);
+            cF0.fma(x0, V::ld(fb + rr * C::RS));
+            cR0.fma(x0, V::ld(qb + rr * C::RS));
+            cF1.fma(x1, V::ld(fb + (rr + 1) * C::RS));
+            cR1.fma(x1, V::ld(qb + (rr + 1) * C::RS));
+          }
+          if (rr <= hi) {
+            const V x0 = V::ld(xb + rr * KC);
+            cF0.fma(x0, V::ld(fb + rr * C::RS));
+            cR0.fma(x0, V::ld(qb + rr * C::RS));
+          }
+          cF0.add(cF1);
+          cR0.add(cR1);
+          for (int o = 0; o < OPT; ++o) {
+            colF[o] += cF0.get(o);
+            colR[o] += cR0.get(o);
+          }
+          __syncwarp();
+          if (lane == 0) mbar_arrive(empty + stage);
+        } else {
+          // row sums over the valid columns b of the tile: b in [tmin, a-1]; row a = I*T + loc
+          const int a = I * T + loc;
+          const bool av = (a >= tmin) && (a <= t - 1);
+          double *racc = rowacc + (size_t)(a % Ma) * KC + j0;
+          // the accumulator of this row was loaded during the previous tile; load the
+          // next tile's row now (tile order: (I+1, J), or (J+1, J+1) after the last row block)
+          double prev[OPT];
+          for (int o = 0; o < OPT; ++o) prev[o] = pre[o];
+          const int an = (I < Jn ? (I + 1) : (J + 1)) * T + loc;
+          if (an != a && an >= tmin && an <= t - 1)  // an == a: the value stored below is the next one
+            for (int o = 0; o < OPT; ++o) pre[o] = rowacc[(size_t)(an % Ma) * KC + j0 + o];
+          int lo = max(0, tmin - J * T), hi = min(T - 1, a - 1 - J * T);
+          if (!av) hi = -1;
+          V s0 = V::zero(), s1 = V::zero();
+          const TS *fr = tF + loc * C::RS + j0;
+          const TS *qr = tR + loc * C::RS + j0;
+          const TS *xrc = xr_col + j0;
+          const TS *xFc = xF_col + j0;
+          int bb = lo;
+          if (bb <= hi && J * T + bb == tmin) {  // trapezoid half weight of z = tmin
+            V x = V::ld(xrc + bb * KC), y = V::ld(xFc + bb * KC);
+            x.scale((TS)0.5);
+            y.scale((TS)0.5);
+            s0.fma(x, V::ld(fr + bb * KC));
+            s0.fma(y, V::ld(qr + bb * KC));
+            ++bb;
+          }
+#pragma unroll 4
+          for (; bb + 1 <= hi; bb += 2) {
+            s0.fma(V::ld(xrc + bb * KC), V::ld(fr + bb * KC));
+            s0.fma(V::ld(xFc + bb * KC), V::ld(qr + bb * KC));
+            s1.fma(V::ld(xrc + (bb + 1) * KC), V::ld(fr + (bb + 1) * KC));
+            s1.fma(V::ld(xFc + (bb + 1) * KC), V::ld(qr + (bb + 1) * KC));
+          }
+          if (bb <= hi) {
+            s0.fma(V::ld(xrc + bb * KC), V::ld(fr + bb * KC));
+            s0.fma(V::ld(xFc + bb * KC), V::ld(qr + bb * KC));
+          }
+          s0.add(s1);
+          __syncwarp();
+          if (lane == 0) mbar_arrive(empty + stage);
+          if (av)
+            for (int o = 0; o < OPT; ++o) {
+              const double v = prev[o] + s0.get(o);
+              racc[o] = v;
+              if (an == a) pre[o] = v;
+            }
+        }
       }
-      if (aborted) break;
+      // both groups: the row sums of column block J are final after its diagonal tile
+      consumer_sync(C::NT);
+      if (*cabort) {
+        aborted = true;
+        break;
+      }
 
-      // leapfrog for t' = b (evolve_r!/evolve_F!, Evolution.jl:890-915); rowacc of
-      // row b was last written by this same thread
+      // leapfrog for t' = b (evolve_r!/evolve_F!, Evolution.jl:890-915)
       if (bvalid) {
         const int sb = b % Ma;
-        const double accF = colF + rowacc[(size_t)sb * KC + j];
-        const double accR = colR;
-        const double F1 = F1row[(size_t)sb * KC + j];
-        const double F2 = (b <= t - 2) ? F2row[(size_t)sb * KC + j] : F1row[(size_t)((t - 2) % Ma) * KC + j];
-        const double Fn = (2.0 - om) * F1 - F2 - accF * dt3;
-        double rn;
-        if (b == t - 1) {
-          rn = R.dt;  // phi-pi commutator rho(t, t-1) = dt
-        } else {
-          const double r1 = R1row[(size_t)sb * KC + j];
-          const double r2 = R2row[(size_t)sb * KC + j];
-          rn = (2.0 - om) * r1 - r2 - accR * dt3;
+        const double wb = (b == tmin) ? 0.5 : 1.0;
+        const TS *sigr = reinterpret_cast<const TS *>(R.sig_r) + (size_t)c * rowstride + (size_t)sb * KC;
+        const TS *sigF = reinterpret_cast<const TS *>(R.sig_F) + (size_t)c * rowstride + (size_t)sb * KC;
+        const size_t cs = (size_t)c * rowstride;
+        const double *F1row = R.st_F + (size_t)((t - 1) % 3) * st_row + cs;
+        const double *F2row = R.st_F + (size_t)((t - 2) % 3) * st_row + cs;
+        const double *R1row = R.st_r + (size_t)((t - 1) % 3) * st_row + cs;
+        const double *R2row = R.st_r + (size_t)((t - 2) % 3) * st_row + cs;
+        double *FNrow = R.st_F + (size_t)(t % 3) * st_row + cs;
+        double *RNrow = R.st_r + (size_t)(t % 3) * st_row + cs;
+        TS *hFnew = reinterpret_cast<TS *>(R.hist_F) + ((size_t)c * Ma + (t % Ma)) * rowstride;
+        TS *hRnew = reinterpret_cast<TS *>(R.hist_r) + ((size_t)c * Ma + (t % Ma)) * rowstride;
+        for (int o = 0; o < OPT; ++o) {
+          const int j = j0 + o;
+          const int k = c * KC + j;
+          const double kk = (k < R.S) ? R.k2[k] : 0.0;
+          const double om = (kk + M2) * R.dt2;  // setomega2values!: (kL2 + M^2) * dt^2
+          const double xbr_d = lo_only ? 0.0 : wb * (double)sigr[j];
+          const double xbF_d = lo_only ? 0.0 : wb * (double)sigF[j];
+          const double accF = colF[o] + rowacc[(size_t)sb * KC + j];
+          const double accR = colR[o];
+          const double F1 = F1row[(size_t)sb * KC + j];
+          const double F2 = (b <= t - 2) ? F2row[(size_t)sb * KC + j] : F1row[(size_t)((t - 2) % Ma) * KC + j];
+          const double Fn = (2.0 - om) * F1 - F2 - accF * dt3;
+          double rn;
+          if (b == t - 1) {
+            rn = R.dt;  // phi-pi commutator rho(t, t-1) = dt
+          } else {
+            const double r1 = R1row[(size_t)sb * KC + j];
+            const double r2 = R2row[(size_t)sb * KC + j];
+            rn = (2.0 - om) * r1 - r2 - accR * dt3;
+          }
+          FNrow[(size_t)sb * KC + j] = Fn;
+          RNrow[(size_t)sb * KC + j] = rn;
+          hFnew[(size_t)sb * KC + j] = (TS)Fn;
+          hRnew[(size_t)sb * KC + j] = (TS)rn;
+          diag[o] += xbr_d * Fn + xbF_d * rn;
+          if (b == t - 1) emem[o] = accF;
         }
-        FNrow[(size_t)sb * KC + j] = Fn;
-        RNrow[(size_t)sb * KC + j] = rn;
-        hFnew[(size_t)sb * KC + j] = (TS)Fn;
-        hRnew[(size_t)sb * KC + j] = (TS)rn;
-        diag += xbr_d * Fn + xbF_d * rn;
-        if (b == t - 1) {
-          emem = accF;
-          has_emem = true;
-        }
+        if (b == t - 1) has_emem = true;
       }
     }
-    if (!aborted) {
-      // partial sums of acc_F(t) over this warp's columns
-      double v = diag;
+    if (!aborted && colgrp) {
+      // partial sums of acc_F(t) over this warp's columns (lanes sharing jq)
+      for (int o = 0; o < OPT; ++o) {
+        double v = diag[o];
 #pragma unroll
-      for (int o = 16; o >= KC; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-      if (lane < KC) misc[16 + warp * KC + lane] = v;
-      if (has_emem) misc[2 + j] = emem;
+        for (int off = 16; off >= C::NJ; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+        if (lane < C::NJ) misc[16 + warp * KC + j0 + o] = v;
+        if (has_emem) misc[2 + j0 + o] = emem[o];
+      }
     }
   }
   __syncthreads();  // producer done issuing; consumers done with the triangle
@@ -412,7 +510,7 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
     TS *hFnew = reinterpret_cast<TS *>(R.hist_F) + ((size_t)c * Ma + (t % Ma)) * rowstride;
     TS *hRnew = reinterpret_cast<TS *>(R.hist_r) + ((size_t)c * Ma + (t % Ma)) * rowstride;
     double accd = 0.0;
-    for (int w = 0; w < C::NW; ++w) accd += misc[16 + w * KC + tid];
+    for (int w = 0; w < C::NG / 32; ++w) accd += misc[16 + w * KC + tid];
     const int jj = tid;
     const int kd = c * KC + jj;
     const double kd2 = (kd < R.S) ? R.k2[kd] : 0.0;
@@ -549,8 +647,8 @@ __global__ void measure_init_kernel(const RunDev *__restrict__ runs, int nruns, 
 __global__ void set_t_kernel(int *d_t, int t) { *d_t = t; }
 __global__ void advance_t_kernel(int *d_t) { *d_t += 1; }
 
-using CfgF64 = Cfg<double, 16, 4>;
-using CfgF32 = Cfg<float, 32, 3>;
+using CfgF64 = Cfg<double, 16, 4, 1>;
+using CfgF32 = Cfg<float, 32, 3, 2>;
 
 }  // namespace
 
@@ -563,19 +661,19 @@ size_t memint_smem_bytes(bool fp64, int Malloc) {
 
 cudaError_t configure_memint(bool fp64, size_t smem) {
   if (fp64)
-    return cudaFuncSetAttribute(memint_kernel<double, CfgF64::T, CfgF64::NST>,
+    return cudaFuncSetAttribute(memint_kernel<double, CfgF64::T, CfgF64::NST, CfgF64::OPT>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  return cudaFuncSetAttribute(memint_kernel<float, CfgF32::T, CfgF32::NST>,
+  return cudaFuncSetAttribute(memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
 cudaError_t launch_memint(bool fp64, const RunDev *d_runs, const int *d_base, int nruns, int total_ctas,
                           const int *d_t, int *d_err, int measure, size_t smem, cudaStream_t st) {
   if (fp64)
-    memint_kernel<double, CfgF64::T, CfgF64::NST>
+    memint_kernel<double, CfgF64::T, CfgF64::NST, CfgF64::OPT>
         <<<total_ctas, CfgF64::NT + 32, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure);
   else
-    memint_kernel<float, CfgF32::T, CfgF32::NST>
+    memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT>
         <<<total_ctas, CfgF32::NT + 32, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure);
   return cudaGetLastError();
 }
