@@ -405,7 +405,7 @@ static int put_pair(kb_handle *h, Run &R, int which, int a, int b, const double 
     src = fv.data();
   }
   char *hist = (char *)(which == 0 ? R.hist_F : R.hist_r);
-  char *dst = hist + ((size_t)slot_off(R, a) * R.Malloc + slot_off(R, b)) * KC * R.esz;
+  char *dst = hist + kb::hist_off(R.Malloc, R.T, 0, a, b, 0) * R.esz;  // chunks are Malloc^2 * KC apart
   KB_CUDA(h, cudaMemcpy2DAsync(dst, pitch_hist * R.esz, src, KC * R.esz, KC * R.esz, R.nchunks,
                                cudaMemcpyHostToDevice, h->st));
   if (to_state) {
@@ -563,7 +563,7 @@ static int fetch_pair(kb_handle *h, Run &R, int which, int a, int b, double *out
   } else {
     const size_t pitch_hist = (size_t)R.Malloc * R.Malloc * KC;
     const char *hist = (const char *)(which == 0 ? R.hist_F : R.hist_r);
-    const char *src = hist + ((size_t)slot_off(R, a) * R.Malloc + slot_off(R, b)) * KC * R.esz;
+    const char *src = hist + kb::hist_off(R.Malloc, R.T, 0, a, b, 0) * R.esz;  // chunks are Malloc^2 * KC apart
     if (R.esz == 8) {
       KB_CUDA(h, cudaMemcpy2DAsync(dv.data(), KC * 8, src, pitch_hist * 8, KC * 8, R.nchunks, cudaMemcpyDeviceToHost, h->st));
       KB_CUDA(h, cudaStreamSynchronize(h->st));

@@ -1,10 +1,14 @@
 // kb_internal.cuh -- device data layout shared by the kernels of libkb2pi.
 //
 // Layout in HBM of one run (S orbits padded to nchunks * KC, KC = 8):
-//   hist_F, hist_r  [nchunks][Malloc][Malloc][KC]  storage type TS
-//       element (a, b) with a >= b (later time first) at row slot(a), column
-//       slot(b); slot(t) = t mod Malloc, Malloc = M rounded up to the tile T.
-//       rho holds the true value rho(a, b) of the later-first pair.
+//   hist_F, hist_r  [nchunks][Malloc/T][Malloc/T][T][T][KC]  storage type TS, tile-major
+//       element (a, b) with a >= b (later time first) in the time tile of
+//       slots (slot(a) / T, slot(b) / T), at tile row slot(a) mod T and tile
+//       column (slot(b) mod T) ^ (slot(a) mod 4); slot(t) = t mod Malloc,
+//       Malloc = M rounded up to the tile T. Each T x T x KC tile is contiguous
+//       (one bulk copy), and the XOR swizzle of columns keeps both row-wise and
+//       column-wise shared-memory reads conflict-free. rho holds the true value
+//       rho(a, b) of the later-first pair.
 //   st_F, st_r      [3][nchunks][Malloc][KC]  double: rows t, t-1, t-2 by t mod 3
 //       (the leapfrog state; in KB_PREC_MIXED the only FP64 copy of F, rho)
 //   sig_F, sig_r    [nchunks][Malloc][KC]     TS: Sigma(t-1, z) at slot(z)
@@ -50,6 +54,13 @@ __host__ __device__ inline long long tet3(int c) { return (long long)c * (c + 1)
 __host__ __device__ inline int tri2(int b) { return b * (b + 1) / 2; }
 // orbit index of the sorted triple a <= b <= c
 __host__ __device__ inline int orb3(int a, int b, int c) { return (int)(tet3(c) + tri2(b) + a); }
+
+// element offset of history entry (a, b) of orbit j of chunk c (see the layout above)
+__host__ __device__ inline size_t hist_off(int Malloc, int T, int c, int a, int b, int j) {
+  const int sa = a % Malloc, sb = b % Malloc, nbA = Malloc / T;
+  const int ra = sa % T, cb = sb % T;
+  return ((((size_t)c * nbA + sa / T) * nbA + sb / T) * T + ra) * (size_t)T * KC + (size_t)((cb ^ (ra & 3)) * KC + j);
+}
 
 __device__ inline int find_run(const int *base, int nruns, int bid) {
   int lo = 0, hi = nruns - 1;

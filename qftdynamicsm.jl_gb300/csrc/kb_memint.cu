@@ -133,8 +133,7 @@ struct Cfg {
   static constexpr int NG = T * NJ;                         // threads per consumer group
   static constexpr int NT = 2 * NG;                         // column group + row group
   static constexpr int NW = NT / 32;                        // consumer warps
-  static constexpr int ROWPAD = 32 / sizeof(TS);            // 32-byte pad per tile row: conflict-free rows
-  static constexpr int RS = T * KC + ROWPAD;                // smem stride of one tile row
+  static constexpr int RS = T * KC;                         // smem stride of one tile row (columns swizzled)
   static constexpr int TILE = T * RS;                       // elements of one field tile in smem
   static constexpr int XV = T * KC;                         // one x vector (T times x KC orbits)
   static constexpr int STAGE = 2 * TILE + 3 * XV;           // F, rho, x_rho(rows), x_rho(cols), x_F(cols)
@@ -165,9 +164,9 @@ struct TileIt {
   }
 };
 
-// issued by the producer warp: the T row segments of the F and rho tiles (each
-// row to a 32-byte padded smem row), Sigma_rho of the tile's rows and
-// Sigma_rho, Sigma_F of its columns, all into one stage
+// issued by the producer warp: the F and rho tiles (each one contiguous block in
+// the tile-major history), Sigma_rho of the tile's rows and Sigma_rho, Sigma_F of
+// its columns, all into one stage
 template <typename TS, typename C>
 __device__ __forceinline__ void issue_tile(int stage, int I, int J, const RunDev &R, int c, TS *stages,
                                            uint64_t *full) {
@@ -180,12 +179,10 @@ __device__ __forceinline__ void issue_tile(int stage, int I, int J, const RunDev
   const int sb0 = (J * C::T) % R.Malloc;
   const TS *hF = reinterpret_cast<const TS *>(R.hist_F);
   const TS *hR = reinterpret_cast<const TS *>(R.hist_r);
-  if (lane < C::T) {
-    const size_t off = (((size_t)c * R.Malloc + sa0 + lane) * R.Malloc + sb0) * KC;
-    bulk_g2s(dst + lane * C::RS, hF + off, C::T * KC * sizeof(TS), bar);
-    bulk_g2s(dst + C::TILE + lane * C::RS, hR + off, C::T * KC * sizeof(TS), bar);
-  }
   if (lane == 0) {
+    const size_t off = hist_off(R.Malloc, C::T, c, sa0, sb0, 0);  // start of the tile
+    bulk_g2s(dst, hF + off, C::T * C::T * KC * sizeof(TS), bar);
+    bulk_g2s(dst + C::TILE, hR + off, C::T * C::T * KC * sizeof(TS), bar);
     const TS *sr = reinterpret_cast<const TS *>(R.sig_r) + (size_t)c * R.Malloc * KC;
     const TS *sF = reinterpret_cast<const TS *>(R.sig_F) + (size_t)c * R.Malloc * KC;
     bulk_g2s(dst + 2 * C::TILE, sr + (size_t)sa0 * KC, C::XV * sizeof(TS), bar);
@@ -347,29 +344,30 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
           if (!bvalid) hi = -1;
           lo = max(lo, 0);
           V cF0 = V::zero(), cF1 = V::zero(), cR0 = V::zero(), cR1 = V::zero();
-          const TS *fb = tF + loc * KC + j0;
-          const TS *qb = tR + loc * KC + j0;
+          // column loc of row rr sits at swizzled position loc ^ (rr & 3)
+          auto el = [&](int rr) { return rr * C::RS + (loc ^ (rr & 3)) * KC + j0; };
           const TS *xb = xr_row + j0;
           int rr = lo;
           if (rr <= hi && I * T + rr == tmin) {  // trapezoid half weight of z = tmin
             V x = V::ld(xb + rr * KC);
             x.scale((TS)0.5);
-            cF0.fma(x, V::ld(fb + rr * C::RS));
-            cR0.fma(x, V::ld(qb + rr * C::RS));
+            cF0.fma(x, V::ld(tF + el(rr)));
+            cR0.fma(x, V::ld(tR + el(rr)));
             ++rr;
           }
 #pragma unroll 4
           for (; rr + 1 <= hi; rr += 2) {
             const V x0 = V::ld(xb + rr * KC), x1 = V::ld(xb + (rr + 1) * KC);
-            cF0.fma(x0, V::ld(fb + rr * C::RS));
-            cR0.fma(x0, V::ld(qb + rr * C::RS));
-            cF1.fma(x1, V::ld(fb + (rr + 1) * C::RS));
-            cR1.fma(x1, V::ld(qb + (rr + 1) * C::RS));
+            const int e0 = el(rr), e1 = el(rr + 1);
+            cF0.fma(x0, V::ld(tF + e0));
+            cR0.fma(x0, V::ld(tR + e0));
+            cF1.fma(x1, V::ld(tF + e1));
+            cR1.fma(x1, V::ld(tR + e1));
           }
           if (rr <= hi) {
             const V x0 = V::ld(xb + rr * KC);
-            cF0.fma(x0, V::ld(fb + rr * C::RS));
-            cR0.fma(x0, V::ld(qb + rr * C::RS));
+            cF0.fma(x0, V::ld(tF + el(rr)));
+            cR0.fma(x0, V::ld(tR + el(rr)));
           }
           cF0.add(cF1);
           cR0.add(cR1);
@@ -394,6 +392,8 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
           int lo = max(0, tmin - J * T), hi = min(T - 1, a - 1 - J * T);
           if (!av) hi = -1;
           V s0 = V::zero(), s1 = V::zero();
+          // column bb of row loc sits at swizzled position bb ^ (loc & 3)
+          const int sw = loc & 3;
           const TS *fr = tF + loc * C::RS + j0;
           const TS *qr = tR + loc * C::RS + j0;
           const TS *xrc = xr_col + j0;
@@ -403,20 +403,21 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
             V x = V::ld(xrc + bb * KC), y = V::ld(xFc + bb * KC);
             x.scale((TS)0.5);
             y.scale((TS)0.5);
-            s0.fma(x, V::ld(fr + bb * KC));
-            s0.fma(y, V::ld(qr + bb * KC));
+            s0.fma(x, V::ld(fr + (bb ^ sw) * KC));
+            s0.fma(y, V::ld(qr + (bb ^ sw) * KC));
             ++bb;
           }
 #pragma unroll 4
           for (; bb + 1 <= hi; bb += 2) {
-            s0.fma(V::ld(xrc + bb * KC), V::ld(fr + bb * KC));
-            s0.fma(V::ld(xFc + bb * KC), V::ld(qr + bb * KC));
-            s1.fma(V::ld(xrc + (bb + 1) * KC), V::ld(fr + (bb + 1) * KC));
-            s1.fma(V::ld(xFc + (bb + 1) * KC), V::ld(qr + (bb + 1) * KC));
+            const int e0 = (bb ^ sw) * KC, e1 = ((bb + 1) ^ sw) * KC;
+            s0.fma(V::ld(xrc + bb * KC), V::ld(fr + e0));
+            s0.fma(V::ld(xFc + bb * KC), V::ld(qr + e0));
+            s1.fma(V::ld(xrc + (bb + 1) * KC), V::ld(fr + e1));
+            s1.fma(V::ld(xFc + (bb + 1) * KC), V::ld(qr + e1));
           }
           if (bb <= hi) {
-            s0.fma(V::ld(xrc + bb * KC), V::ld(fr + bb * KC));
-            s0.fma(V::ld(xFc + bb * KC), V::ld(qr + bb * KC));
+            s0.fma(V::ld(xrc + bb * KC), V::ld(fr + (bb ^ sw) * KC));
+            s0.fma(V::ld(xFc + bb * KC), V::ld(qr + (bb ^ sw) * KC));
           }
           s0.add(s1);
           __syncwarp();
@@ -449,8 +450,8 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
         const double *R2row = R.st_r + (size_t)((t - 2) % 3) * st_row + cs;
         double *FNrow = R.st_F + (size_t)(t % 3) * st_row + cs;
         double *RNrow = R.st_r + (size_t)(t % 3) * st_row + cs;
-        TS *hFnew = reinterpret_cast<TS *>(R.hist_F) + ((size_t)c * Ma + (t % Ma)) * rowstride;
-        TS *hRnew = reinterpret_cast<TS *>(R.hist_r) + ((size_t)c * Ma + (t % Ma)) * rowstride;
+        TS *hF = reinterpret_cast<TS *>(R.hist_F);
+        TS *hR = reinterpret_cast<TS *>(R.hist_r);
         for (int o = 0; o < OPT; ++o) {
           const int j = j0 + o;
           const int k = c * KC + j;
@@ -473,8 +474,9 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
           }
           FNrow[(size_t)sb * KC + j] = Fn;
           RNrow[(size_t)sb * KC + j] = rn;
-          hFnew[(size_t)sb * KC + j] = (TS)Fn;
-          hRnew[(size_t)sb * KC + j] = (TS)rn;
+          const size_t ho = hist_off(Ma, T, c, t, b, j);
+          hF[ho] = (TS)Fn;
+          hR[ho] = (TS)rn;
           diag[o] += xbr_d * Fn + xbF_d * rn;
           if (b == t - 1) emem[o] = accF;
         }
@@ -507,8 +509,7 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
     const double *F1row = R.st_F + (size_t)((t - 1) % 3) * st_row + (size_t)c * rowstride;
     double *FNrow = R.st_F + (size_t)(t % 3) * st_row + (size_t)c * rowstride;
     double *RNrow = R.st_r + (size_t)(t % 3) * st_row + (size_t)c * rowstride;
-    TS *hFnew = reinterpret_cast<TS *>(R.hist_F) + ((size_t)c * Ma + (t % Ma)) * rowstride;
-    TS *hRnew = reinterpret_cast<TS *>(R.hist_r) + ((size_t)c * Ma + (t % Ma)) * rowstride;
+    const size_t hdo = hist_off(Ma, T, c, t, t, tid);
     double accd = 0.0;
     for (int w = 0; w < C::NG / 32; ++w) accd += misc[16 + w * KC + tid];
     const int jj = tid;
@@ -520,8 +521,8 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
     const double Ftt = (2.0 - omd) * Ft1 - Ft2 - accd * R.dt3;
     FNrow[(size_t)(t % Ma) * KC + jj] = Ftt;
     RNrow[(size_t)(t % Ma) * KC + jj] = 0.0;
-    hFnew[(size_t)(t % Ma) * KC + jj] = (TS)Ftt;
-    hRnew[(size_t)(t % Ma) * KC + jj] = (TS)0;
+    reinterpret_cast<TS *>(R.hist_F)[hdo] = (TS)Ftt;
+    reinterpret_cast<TS *>(R.hist_r)[hdo] = (TS)0;
     const double dg = (kd < R.S) ? R.deg[kd] : 0.0;
     double tp = dg * Ftt;  // tadpole partial sum of this chunk for the next step
     // measurement (createMeasurement, Measurement.jl:38-64): F(t-1,t-1) from the state
