@@ -39,6 +39,7 @@ namespace kb {
 namespace {
 
 constexpr int SUN_THREADS = 512;
+constexpr int SUN_THREADS_F32 = 1024;
 
 __host__ __device__ inline int rup4(int v) { return (v + 3) & ~3; }
 constexpr int rup4_c(int v) { return (v + 3) & ~3; }
@@ -229,7 +230,7 @@ __device__ void sun_transform(const SunCtx<TC> &c, In in, Out out) {
 }
 
 template <typename TC, typename TS, bool SCRATCH>
-__global__ void __launch_bounds__(SUN_THREADS, 1)
+__global__ void __launch_bounds__(SCRATCH ? SUN_THREADS : SUN_THREADS_F32, 1)
 sunset_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int nruns, int total,
               const int *__restrict__ d_t, TC *__restrict__ scratch, size_t scratch_stride) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -357,8 +358,8 @@ cudaError_t launch_sunset(bool fp64, const RunDev *d_runs, const int *d_base, in
     sunset_kernel<double, double, true><<<grid, SUN_THREADS, smem, st>>>(
         d_runs, d_base, nruns, total_rows, d_t, reinterpret_cast<double *>(scratch), scratch_stride);
   else
-    sunset_kernel<float, float, false><<<grid, SUN_THREADS, smem, st>>>(d_runs, d_base, nruns, total_rows, d_t,
-                                                                         nullptr, 0);
+    sunset_kernel<float, float, false><<<grid, SUN_THREADS_F32, smem, st>>>(d_runs, d_base, nruns, total_rows, d_t,
+                                                                             nullptr, 0);
   return cudaGetLastError();
 }
 
