@@ -250,6 +250,54 @@ def cpu_baseline(steps=1, Msample=128, budget_s=None):
                       f"(M/{Msample})^2 to M=1000"}
 
 
+def run_batched(args):
+    """Config 3: 64 independent runs with uneven Ns, lambda, T and memory windows in one
+    launch per kernel (mixed precision, graph-captured steps). Reports run-steps/s."""
+    import torch
+
+    from kb2pi import capi
+
+    ws, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    rng = np.random.default_rng(args.seed)
+    runs = []
+    for r in range(64):
+        runs.append(dict(Ns=int(rng.choice([16, 24, 32, 48])), lam=float(rng.uniform(0.5, 8.0)),
+                         T=float(rng.uniform(0.5, 3.0)), M=int(rng.integers(100, 501))))
+    ps = [capi.KbParams(Ns=c["Ns"], sdim=3, M=c["M"], N=4, pexp=1, precision=capi.KB_PREC_MIXED, device=local,
+                        flags=0, dt=0.05, lam=c["lam"], mass2=1.0, mass=1.0) for c in runs]
+    h = capi.Handle(ps)
+    for r, c in enumerate(runs):
+        _, k2, _ = h.orbits(r)
+        n = 1.0 / (np.exp(np.sqrt(k2 + 1.0) / c["T"]) - 1.0)
+        h.init(r, n, 1.0)
+    # 500 steps each: the first 500 - K - W fill every memory window, W warm up, K are timed
+    total = 500
+    fill = max(0, total - args.steps - args.warmup)
+    h.steps(3, fill, 0)
+    t = 2 + fill
+    h.steps(t + 1, args.warmup, 0)
+    t += args.warmup
+    stream = h.stream()
+    barrier(ws)
+    with ClockSampler(local) as clk:
+        ms = timed_graph_steps(h, t + 1, args.steps, stream)
+    ms = max_over_ranks(ws, ms)
+    if rank != 0:
+        return 0
+    value = ws * 64 * args.steps / (ms / 1000.0)
+    line = {"metric": "run-steps/s, 64 uneven runs in one launch (config 3)", "value": value,
+            "unit": "run-steps/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 history/sunset, f64 accumulation/leapfrog/diagnostics",
+            "data": f"synthetic: thermal states, per-run draws seeded with {args.seed}",
+            "config": {"workload": "64 runs, Ns in {16,24,32,48}, lambda U[0.5,8], T U[0.5,3], M U{100..500}, "
+                                   "dt=0.05, steps 478..500 of 500", "runs": runs},
+            "clocks": clk.summary(), "gpu_launches": 3 * args.steps}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_reference(args):
     ws, rank, _ = dist_setup()
     if rank != 0:
@@ -395,9 +443,13 @@ def main():
     ap.add_argument("--cpu-window", type=int, default=128)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--config", default="c5", choices=["c5", "small"],
-                    help="c5: the benchmark workload; small: Ns=40, M=400 for profiler captures")
+    ap.add_argument("--config", default="c5", choices=["c5", "small", "c3"],
+                    help="c5: the benchmark workload; small: Ns=40, M=400 for profiler captures; "
+                         "c3: 64 uneven runs in one launch")
+    ap.add_argument("--seed", type=int, default=12345)
     args = ap.parse_args()
+    if args.config == "c3" and args.impl == "ours":
+        return run_batched(args)
     if args.config == "small":
         CFG.update(SMALL)
     if args.warmup < 3:

@@ -292,3 +292,51 @@ def test_host_mirror_run_simulation():
     assert len(got) == 21
     assert rel(got, Es) <= TOL64
     assert problem.model.Mass2 < 1.0  # RMass counterterm applied
+
+
+def c3_runs(nruns, seed, Ns_choices, M_range):
+    """Config 3 style batch: per-run seeded draws of Ns, lambda, T and the memory window."""
+    rng = np.random.default_rng(seed)
+    runs = []
+    for r in range(nruns):
+        runs.append(dict(Ns=int(rng.choice(Ns_choices)), lam=float(rng.uniform(0.5, 8.0)),
+                         T=float(rng.uniform(0.5, 3.0)), M=int(rng.integers(M_range[0], M_range[1] + 1)),
+                         dt=0.05, N=4))
+    return runs
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_batched_config3_style(precision):
+    """Uneven runs in one launch per kernel: each run of the batch is bit-identical to
+    the same run alone, and follows the FP64 oracle (1e-10 plain, 1e-5 mixed)."""
+    from kb2pi import capi
+
+    runs = c3_runs(12, 2024, [6, 8, 12, 16], (8, 40))
+    ps = [capi.KbParams(Ns=c["Ns"], sdim=3, M=c["M"], N=4, pexp=1, precision=precision, device=0, flags=0,
+                        dt=c["dt"], lam=c["lam"], mass2=1.0, mass=1.0) for c in runs]
+    batch = capi.Handle(ps)
+    alone = [make_gpu(c, precision) for c in runs[:3]]
+    oracles = [make_oracle(c) for c in runs]
+    for r, c in enumerate(runs):
+        _, k2, _ = batch.orbits(r)
+        n = occupation(c, k2)
+        batch.init(r, n, 1.0)
+        oracles[r].init_occupation(n, 1.0)
+        if r < 3:
+            alone[r].init(0, n, 1.0)
+    steps = 50
+    batch.steps(3, steps, 0)
+    for a in alone:
+        a.steps(3, steps, 0)
+    for o in oracles:
+        for t in range(3, 3 + steps):
+            o.step(t)
+    t = 2 + steps
+    tol = TOL64 if precision == 0 else TOL_MIXED
+    for r in range(len(runs)):
+        mb, mo = batch.measure(r, t), oracles[r].measure(t)
+        assert abs(mb["E"] - mo["E"]) <= tol * abs(mo["E"]), r
+        assert rel(mb["n"], mo["n"]) <= tol, r
+        if r < 3:
+            assert mb["E"] == alone[r].measure(0, t)["E"]
+            assert np.array_equal(mb["n"], alone[r].measure(0, t)["n"])
