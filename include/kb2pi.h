@@ -58,7 +58,8 @@ typedef struct kb_params {
   int32_t pexp;      /* KB_PEXP_* */
   int32_t precision; /* KB_PREC_*; must be equal for all runs of one handle */
   int32_t device;    /* CUDA device ordinal */
-  int32_t flags;     /* reserved, 0 */
+  int32_t flags;     /* bits 0-15: extra ring slots kept beyond the memory
+                      * window (kb_adjoint needs >= its ckpt_every); 0 otherwise */
   double dt;         /* disc.dt */
   double lambda;     /* model.Lambda */
   double mass2;      /* model.Mass2: m^2 used in the evolution (after Renormalize) */
@@ -160,6 +161,27 @@ int kb_sync(kb_handle *h);
 int kb_get_stream(const kb_handle *h, void **stream);
 int kb_profile(kb_handle *h, int32_t enable);
 int kb_profile_read(kb_handle *h, double *ms, int64_t *launches);
+
+/* Gradient of a late-time loss by the discrete adjoint of the step. No
+ * counterpart in the reference (its ChainRulesCore rrule would wrap this):
+ *   L = sum_k w_n[k] n(k, t_final) + w_E E(t_final)
+ * over orbits k (kb_get_orbits order), with n and E as kb_measure reports them
+ * at t_final, for the run that kb_init(h, 0, n_init, init_mass) starts and
+ * kb_step evolves to t_final (>= 3). Returns dL/dlambda, dL/dm^2 (kb_params.mass2),
+ * dL/dn_init[k] for every orbit (S values) and, if grad_init_mass is not NULL,
+ * dL/d init_mass at fixed n_init (chain it through the gap equation when
+ * init_mass is the gap mass), and L itself in *loss if loss is not NULL.
+ * w_n may be NULL (energy only).
+ * Checkpointing: the forward run keeps a device copy of the state every
+ * ckpt_every steps; the reverse sweep recomputes each block of ckpt_every steps
+ * from its copy and runs the block's adjoint steps backwards. The handle must
+ * hold one run in KB_PREC_FP64, created with (kb_params.flags & 0xffff) >=
+ * ckpt_every. Memory: two more history rings plus
+ * ceil((t_final - 2) / ckpt_every) state copies. The handle's state is
+ * consumed: afterwards it needs kb_init before the next kb_step. */
+int kb_adjoint(kb_handle *h, const double *n_init, double init_mass, int32_t t_final, const double *w_n, double w_E,
+               int32_t ckpt_every, double *grad_lambda, double *grad_mass2, double *grad_n, double *grad_init_mass,
+               double *loss);
 
 /* Self-energies of caller-owned rows, allocating nothing. No counterpart in
  * the reference: it is for callers that cannot call cudaMalloc -- a host

@@ -135,6 +135,7 @@ int validate(const kb_params &p, std::string &why) {
   if ((p.Ns < 2 || p.Ns > 64 || (p.Ns % 2) != 0) && p.Ns != 1) { snprintf(b, sizeof b, "Ns=%d must be 1 or even in [2,64]", p.Ns); why = b; return -1; }
   if (p.M < 3 || p.M > 1024) { snprintf(b, sizeof b, "NstepsinMemory=%d must be in [3,1024]", p.M); why = b; return -1; }
   if (p.N < 1) { why = "ONgroup must be >= 1"; return -1; }
+  if (p.flags < 0 || p.flags > 1024) { why = "flags: only bits 0-15 (extra ring slots, at most 1024) are defined"; return -1; }
   if (!(p.dt > 0.0) || !std::isfinite(p.dt)) { why = "dt must be positive"; return -1; }
   if (p.pexp < 0 || p.pexp > 2) { why = "pexp must be KB_PEXP_LO, _NLO_QUANTUM or _NLO_CLASSICAL"; return -1; }
   if (p.precision != KB_PREC_FP64 && p.precision != KB_PREC_MIXED) { why = "unknown precision"; return -1; }
@@ -204,7 +205,7 @@ int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out) {
     R.p = p[r];
     build_orbits(R);
     R.T = T;
-    R.Malloc = ((R.p.M + T - 1) / T) * T;
+    R.Malloc = ((R.p.M + (R.p.flags & 0xffff) + T - 1) / T) * T;  // extra slots for kb_adjoint
     R.esz = h->fp64 ? 8 : 4;
     smem_sun = std::max(smem_sun, kb::sunset_smem_bytes(h->fp64, R.H));
     smem_mi = std::max(smem_mi, kb::memint_smem_bytes(h->fp64, R.Malloc));
@@ -836,6 +837,131 @@ int kb_checkpoint_save(kb_handle *h, void *buf, size_t bytes) {
 int kb_checkpoint_restore(kb_handle *h, const void *buf, size_t bytes) {
   if (!h || !buf) return KB_ERR_PARAM;
   return ckpt_copy(h, (char *)const_cast<void *>(buf), bytes, false);
+}
+
+// ---------------------------------------------------------------------------
+// kb_adjoint: forward run with device state copies every ckpt_every steps,
+// then blocks of ckpt_every steps recomputed from their copy and reversed
+// (kernels in kb_adjoint.cu). The ring keeps ckpt_every slots beyond the window
+// so that a recomputed block leaves the rows of its first reverse step intact.
+int kb_adjoint(kb_handle *h, const double *n_init, double init_mass, int32_t t_final, const double *w_n, double w_E,
+               int32_t ckpt_every, double *grad_lambda, double *grad_mass2, double *grad_n, double *grad_init_mass,
+               double *loss) {
+  if (!h) return KB_ERR_PARAM;
+  if (!n_init || !grad_lambda || !grad_mass2 || !grad_n) return fail(h, KB_ERR_PARAM, "kb_adjoint: null argument");
+  if (h->runs.size() != 1) return fail(h, KB_ERR_PARAM, "kb_adjoint: the handle must hold a single run");
+  if (!h->fp64) return fail(h, KB_ERR_PARAM, "kb_adjoint: needs a KB_PREC_FP64 handle");
+  if (t_final < 3) return fail(h, KB_ERR_PARAM, "kb_adjoint: t_final=%d must be >= 3", t_final);
+  Run &R = h->runs[0];
+  const int k = ckpt_every;
+  if (k < 1 || R.Malloc - R.p.M < k)
+    return fail(h, KB_ERR_PARAM,
+                "kb_adjoint: ckpt_every=%d needs a handle created with kb_params.flags >= %d extra ring slots "
+                "(this one keeps %d)", k, std::max(k, 1), R.Malloc - R.p.M);
+  if (!std::isfinite(w_E)) return fail(h, KB_ERR_PARAM, "kb_adjoint: non-finite w_E");
+  cudaSetDevice(h->device);
+  int rc = kb_sync(h);
+  if (rc) return rc;
+  h->t_cur = 0;  // the state is consumed from here on
+  h->sigma_valid = false;
+  const RunDev &D = R.dev;
+  const int nsnap = (t_final - 2 + k - 1) / k;  // state copies at t = 2, 2 + k, ... < t_final
+  struct Part { void *d; size_t n; } parts[] = {
+      {R.hist_F, R.hist_elems * 8}, {R.hist_r, R.hist_elems * 8}, {R.st_F, R.st_elems * 8},
+      {R.st_r, R.st_elems * 8},     {R.tad, (size_t)2 * R.nchunks * 8},
+  };
+  size_t snap_bytes = 0;
+  for (auto &q : parts) snap_bytes += (q.n + 255) / 256 * 256;
+  const size_t adj_bytes = kb::adjoint_buffer_bytes(D);
+  char *snaps = nullptr, *adj = nullptr;
+  double *d_vec = nullptr;  // w_n [Spad], n_init [Spad], output [2][S]
+  auto release = [&]() {
+    cudaStreamSynchronize(h->st);
+    if (snaps) cudaFree(snaps);
+    if (adj) cudaFree(adj);
+    if (d_vec) cudaFree(d_vec);
+    cudaGetLastError();
+  };
+  if (cudaMalloc((void **)&snaps, snap_bytes * nsnap) != cudaSuccess ||
+      cudaMalloc((void **)&adj, adj_bytes) != cudaSuccess ||
+      cudaMalloc((void **)&d_vec, (size_t)(2 * R.Spad + 2 * R.S) * 8) != cudaSuccess) {
+    release();
+    return fail(h, KB_ERR_OOM, "kb_adjoint: cudaMalloc of %zu + %zu bytes (state copies + adjoint) failed",
+                snap_bytes * nsnap, adj_bytes);
+  }
+  auto copy_state = [&](int i, bool save) -> int {
+    size_t off = 0;
+    for (auto &q : parts) {
+      char *dev = snaps + (size_t)i * snap_bytes + off;
+      KB_CUDA(h, cudaMemcpyAsync(save ? dev : q.d, save ? q.d : dev, q.n, cudaMemcpyDeviceToDevice, h->st));
+      off += (q.n + 255) / 256 * 256;
+    }
+    return KB_OK;
+  };
+  kb::AdjBuffers A{};
+  kb::adjoint_carve(D, adj, &A);
+  double *d_wn = d_vec, *d_n0 = d_vec + R.Spad, *d_out = d_vec + 2 * R.Spad;
+  auto run = [&]() -> int {
+    KB_CUDA(h, cudaMemsetAsync(adj, 0, adj_bytes, h->st));
+    if (w_n) KB_CUDA(h, cudaMemcpyAsync(d_wn, w_n, R.S * 8, cudaMemcpyHostToDevice, h->st));
+    KB_CUDA(h, cudaMemcpyAsync(d_n0, n_init, R.S * 8, cudaMemcpyHostToDevice, h->st));
+    // forward, keeping the state copies
+    int r = kb_init(h, 0, n_init, init_mass);
+    if (r) return r;
+    if ((r = copy_state(0, true))) return r;
+    for (int t = 3; t <= t_final; ++t) {
+      if ((r = kb_step(h, t))) return r;
+      if ((t - 2) % k == 0 && t < t_final && (r = copy_state((t - 2) / k, true))) return r;
+    }
+    if (loss) {  // L at t_final from the forward measurement
+      kb_meas_scalars ms{};
+      std::vector<double> nv(R.S);
+      if ((r = kb_measure(h, 0, t_final, &ms, nullptr, nullptr, nv.data(), nullptr, nullptr))) return r;
+      double L = w_E * ms.E;
+      if (w_n)
+        for (int q = 0; q < R.S; ++q) L += w_n[q] * nv[q];
+      *loss = L;
+    }
+    const double N = (double)R.p.N;
+    const double dpref_ivol = (N + 2.0) / (6.0 * N) * D.ivol;  // d(pref ivol)/dlambda
+    KB_CUDA(h, kb::launch_adjoint_seed(D, A, t_final, w_n ? d_wn : nullptr, w_E, dpref_ivol, h->st));
+    const kb::SunsetLaunch sl{h->d_runs, h->d_base_sun, 1, h->total_sun, h->grid_sun, h->d_t,
+                              h->sun_scratch, h->sun_scratch_stride, h->smem_sun};
+    for (int i = nsnap - 1; i >= 0; --i) {
+      const int s0 = 2 + i * k, e = std::min(s0 + k, t_final);
+      if (i != nsnap - 1) {  // recompute the block from its copy
+        if ((r = copy_state(i, false))) return r;
+        h->t_cur = s0;
+        for (int t = s0 + 1; t <= e; ++t)
+          if ((r = kb_step(h, t))) return r;
+      }
+      for (int t = e; t > s0; --t)
+        KB_CUDA(h, kb::launch_adjoint_step(D, A, t, t == t_final ? w_E : 0.0, R.p.lambda, dpref_ivol, sl,
+                                           h->num_sms, h->st));
+    }
+    KB_CUDA(h, kb::launch_adjoint_init_grad(D, A, d_n0, init_mass, d_out, h->st));
+    double scal[8];
+    std::vector<double> out((size_t)2 * R.S);
+    KB_CUDA(h, cudaMemcpyAsync(scal, A.scal, sizeof scal, cudaMemcpyDeviceToHost, h->st));
+    KB_CUDA(h, cudaMemcpyAsync(out.data(), d_out, out.size() * 8, cudaMemcpyDeviceToHost, h->st));
+    if ((r = kb_sync(h))) return r;
+    *grad_mass2 = scal[2];
+    *grad_lambda = scal[3];
+    std::copy(out.begin(), out.begin() + R.S, grad_n);
+    if (grad_init_mass) {
+      double gm = 0.0;
+      for (int q = 0; q < R.S; ++q) gm += out[R.S + q];
+      *grad_init_mass = gm;
+    }
+    if (!std::isfinite(*grad_lambda) || !std::isfinite(*grad_mass2))
+      return fail(h, KB_ERR_NAN, "kb_adjoint: non-finite gradient");
+    return KB_OK;
+  };
+  rc = run();
+  release();
+  h->t_cur = 0;
+  h->sigma_valid = false;
+  return rc;
 }
 
 }  // extern "C"

@@ -86,6 +86,37 @@ int memint_tile(bool fp64);
 cudaError_t launch_measure_init(const RunDev *d_runs, int nruns, int t, cudaStream_t st);
 cudaError_t launch_set_t(int *d_t, int t, cudaStream_t st);
 cudaError_t launch_advance_t(int *d_t, cudaStream_t st);
+// adjoint of the sunset (kb_sunset.cu), FP64 handles only
+size_t sunset_adjoint_smem_bytes(int H);
+cudaError_t launch_sunset_adjoint(const RunDev &R, int t, const double *sbar_r, const double *sbar_F, double *adjF,
+                                  double *adjR, double *lam_part, void *scratch, size_t stride, int grid,
+                                  double lambda, cudaStream_t st);
+
+// reverse sweep of kb_adjoint (kb_adjoint.cu), FP64 single-run handles
+struct AdjBuffers {
+  double *adjF, *adjR;  // adjoint history, the layout of hist_F / hist_r
+  double *xbr, *xbF;    // [Malloc][Spad]: adjoints of x_rho(z), x_F(z), then of Sigma(t-1, z)
+  double *accF, *accR;  // [Malloc][Spad]: adjoints of acc_F(t'), acc_rho(t')
+  double *omb;          // [Spad]: adjoint of omega^2 dt^2
+  double *lamp;         // [Malloc]: dL/dlambda of each sunset row
+  double *scal;         // [8]: 0 M^2(t-1), 1 hartreecont, 2 dL/dm^2, 3 dL/dlambda
+};
+struct SunsetLaunch {  // the handle's forward sunset launch
+  const RunDev *runs;
+  const int *base;
+  int nruns, total_rows, grid;
+  int *d_t;
+  void *scratch;
+  size_t stride, smem;
+};
+size_t adjoint_buffer_bytes(const RunDev &R);
+void adjoint_carve(const RunDev &R, void *base, AdjBuffers *A);
+cudaError_t launch_adjoint_seed(const RunDev &R, const AdjBuffers &A, int t_final, const double *d_wn, double w_E,
+                                double dpref_ivol, cudaStream_t st);
+cudaError_t launch_adjoint_step(const RunDev &R, const AdjBuffers &A, int t, double emem_weight, double lambda,
+                                double dpref_ivol, const SunsetLaunch &sl, int num_sms, cudaStream_t st);
+cudaError_t launch_adjoint_init_grad(const RunDev &R, const AdjBuffers &A, const double *d_n0, double init_mass,
+                                     double *d_out, cudaStream_t st);
 // message returned by kb_last_error(NULL) (kb_api.cu)
 void kb_set_global_error(const char *msg);
 

@@ -528,3 +528,139 @@ extern "C" int kb_sunset_rows_noalloc(int32_t Ns, int32_t N, double lambda, int3
   }
   return KB_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Adjoint of the sunset (reverse mode, FP64), used by kb_adjoint.
+//
+// Forward, per t' row z: Fx = A F, rx = A rho (A: orbit-level cosine transform),
+// g_r = rx (Fx^2 - rx^2/12), g_F = Fx (Fx^2 - 3/4 rx^2),
+// Sigma_rho = f_r A g_r, Sigma_F = f_F A g_F (classical: without the rx^2 terms).
+// On the full lattice the transform is a symmetric matrix; on orbits its
+// transpose is A^T = diag(deg) A diag(deg)^-1, so every adjoint transform
+// divides by the orbit degeneracy, applies A and multiplies back.
+// Given orbit adjoints Sbar_rho, Sbar_F of Sigma(t-1, z) (already weighted),
+// this adds the adjoints of F(t-1, z), rho(t-1, z) into the adjoint history and
+// writes the row's d L / d lambda partial (Sigma ~ lambda^2).
+// ---------------------------------------------------------------------------
+namespace kb {
+namespace {
+
+__global__ void __launch_bounds__(SUN_THREADS, 1)
+sunset_adjoint_kernel(RunDev R, int t, const double *__restrict__ sbar_r, const double *__restrict__ sbar_F,
+                      double *__restrict__ adjF, double *__restrict__ adjR, double *__restrict__ lam_part,
+                      double *scratch, size_t stride, double lambda) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int tmin = max(1, t - R.M + 1);
+  SunGeom g(R.H);
+  double *CT = reinterpret_cast<double *>(smem_raw);
+  double *bFx = CT + g.H * g.H4;      // Fx, then adjoint of Fx / deg
+  double *brx = bFx + rup4(g.S);      // rx, then adjoint of rx / deg
+  double *bgr = brx + rup4(g.S);      // adjoint of g_r
+  double *bgF = bgr + rup4(g.S);      // adjoint of g_F
+  int *off2 = reinterpret_cast<int *>(bgF + rup4(g.S));
+  int *off3 = off2 + (g.H + 1);
+  uint16_t *pr = reinterpret_cast<uint16_t *>(off3 + (g.P4 / 4 + 1));
+  double *R1 = scratch + (size_t)blockIdx.x * stride;
+  double *R2 = R1 + g.r1;
+  __shared__ double red[SUN_THREADS / 32];
+  for (int i = threadIdx.x; i < g.H * g.H4; i += blockDim.x) {
+    const int x = i / g.H4, X = i - x * g.H4;
+    CT[i] = (X < g.H) ? R.Cm[X * g.H + x] : 0.0;
+  }
+  for (int z = threadIdx.x; z < g.H; z += blockDim.x)
+    for (int y = 0; y <= z; ++y) pr[tri2(z) + y] = (uint16_t)(y | (z << 8));
+  if (threadIdx.x == 0) {
+    const int nzb = g.H4 / 4;
+    off2[0] = 0;
+    for (int X = 0; X < g.H; ++X) off2[X + 1] = off2[X] + (g.H4 / 4 - X / 4) * nzb;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int nqb = g.P4 / 4;
+    off3[0] = 0;
+    for (int qb = 0; qb < nqb; ++qb) {
+      const int Ymin = pr[min(4 * qb, g.P - 1)] >> 8;
+      off3[qb + 1] = off3[qb] + (g.H4 / 4 - Ymin / 4);
+    }
+  }
+  __syncthreads();
+  const SunCtx<double> c{CT, pr, off2, off3, R1, R2, bFx, g};
+  const int S = g.S, Spad = R.nchunks * KC;
+  const bool classical = (R.pexp == 2);
+  const size_t rowstride = (size_t)R.Malloc * KC;
+  const int r3 = (t - 1) % 3;
+  const double *deg = R.deg;
+  const double *sigr = reinterpret_cast<const double *>(R.sig_r);
+  const double *sigF = reinterpret_cast<const double *>(R.sig_F);
+  auto gidx = [&](int o) { return (size_t)(o / KC) * rowstride + (o % KC); };
+  for (int u = blockIdx.x; u < t - tmin; u += gridDim.x) {
+    const int z = tmin + u;
+    const int slot = z % R.Malloc;
+    const double *stF = R.st_F + (size_t)r3 * R.nchunks * rowstride + (size_t)slot * KC;
+    const double *stR = R.st_r + (size_t)r3 * R.nchunks * rowstride + (size_t)slot * KC;
+    const double *sr = sbar_r + (size_t)slot * Spad;
+    const double *sF = sbar_F + (size_t)slot * Spad;
+    // Fx, rx of row t-1 (recomputed), and the adjoints of g_r, g_F
+    sun_transform<double>(c, [&](int o) { return stF[gidx(o)]; }, [&](int o, double v) { bFx[o] = v; });
+    sun_transform<double>(c, [&](int o) { return stR[gidx(o)]; }, [&](int o, double v) { brx[o] = v; });
+    sun_transform<double>(c, [&](int o) { return sr[o] / deg[o]; },
+                          [&](int o, double v) { bgr[o] = R.fac_r * v * deg[o]; });
+    sun_transform<double>(c, [&](int o) { return sF[o] / deg[o]; },
+                          [&](int o, double v) { bgF[o] = R.fac_F * v * deg[o]; });
+    // pointwise Jacobian of (g_r, g_F) with respect to (Fx, rx); dL/dlambda partial
+    double lam_acc = 0.0;
+    for (int k = threadIdx.x; k < S; k += blockDim.x) {
+      const double Fx = bFx[k], rx = brx[k], gr = bgr[k], gF = bgF[k];
+      double dFx, drx;
+      if (classical) {
+        dFx = gr * 2 * rx * Fx + gF * 3 * Fx * Fx;
+        drx = gr * Fx * Fx;
+      } else {
+        dFx = gr * 2 * rx * Fx + gF * (3 * Fx * Fx - 0.75 * rx * rx);
+        drx = gr * (Fx * Fx - 0.25 * rx * rx) - gF * 1.5 * Fx * rx;
+      }
+      bFx[k] = dFx / deg[k];
+      brx[k] = drx / deg[k];
+      const size_t gi = gidx(k) + (size_t)slot * KC;
+      lam_acc += sr[k] * sigr[gi] + sF[k] * sigF[gi];
+    }
+    for (int o = 16; o > 0; o >>= 1) lam_acc += __shfl_xor_sync(0xffffffffu, lam_acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = lam_acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double s = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+      lam_part[slot] = (lambda != 0.0) ? 2.0 * s / lambda : 0.0;  // Sigma ~ lambda^2
+    }
+    // adjoints of F(t-1, z) and rho(t-1, z), added into the adjoint history
+    const int T = R.T;
+    sun_transform<double>(c, [&](int o) { return bFx[o]; }, [&](int o, double v) {
+      adjF[hist_off(R.Malloc, T, o / KC, t - 1, z, o % KC)] += v * deg[o];
+    });
+    if (z < t - 1)
+      sun_transform<double>(c, [&](int o) { return brx[o]; }, [&](int o, double v) {
+        adjR[hist_off(R.Malloc, T, o / KC, t - 1, z, o % KC)] += v * deg[o];
+      });
+  }
+}
+
+}  // namespace
+
+size_t sunset_adjoint_smem_bytes(int H) {
+  SunGeom g(H);
+  return ((size_t)g.H * g.H4 + 4 * (size_t)rup4(g.S)) * sizeof(double) +
+         (size_t)(g.H + 1 + g.P4 / 4 + 1) * sizeof(int) + (size_t)g.P * sizeof(uint16_t) + 64;
+}
+
+cudaError_t launch_sunset_adjoint(const RunDev &R, int t, const double *sbar_r, const double *sbar_F, double *adjF,
+                                  double *adjR, double *lam_part, void *scratch, size_t stride, int grid,
+                                  double lambda, cudaStream_t st) {
+  const size_t smem = sunset_adjoint_smem_bytes(R.H);
+  cudaError_t e = cudaFuncSetAttribute(sunset_adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  sunset_adjoint_kernel<<<grid, SUN_THREADS, smem, st>>>(R, t, sbar_r, sbar_F, adjF, adjR, lam_part,
+                                                         reinterpret_cast<double *>(scratch), stride, lambda);
+  return cudaGetLastError();
+}
+
+}  // namespace kb

@@ -1,9 +1,10 @@
 """kb2pi -- Python host mirror of the TwoPIScalar GPU numerics (libkb2pi).
 
 ``capi`` binds the C ABI of include/kb2pi.h; ``twopiscalar`` mirrors the
-reference's problem/solution/initialize!/evolve!/measure! interface over it.
+reference's problem/solution/initialize!/evolve!/measure! interface over it;
+``adjoint`` holds the gradient entry point (kb_adjoint) and its loss helpers.
 """
-from . import capi  # noqa: F401
+from . import adjoint, capi  # noqa: F401
 from .capi import Handle, KbError, KbParams, load_library  # noqa: F401
 from .twopiscalar import (  # noqa: F401
     QFTdynamicsProblem, QFTdynamicsSolution, TwoPIScalarfile, createMeasurement, evolve, getGapMass,

@@ -28,7 +28,7 @@ EXPORTS = [
     "kb_site_orbits", "kb_init", "kb_init_rows", "kb_step", "kb_steps", "kb_expand", "kb_measure",
     "kb_get_traces", "kb_get", "kb_set", "kb_self_energies", "kb_get_sigma", "kb_window",
     "kb_checkpoint_size", "kb_checkpoint_save", "kb_checkpoint_restore", "kb_sync",
-    "kb_get_stream", "kb_profile", "kb_profile_read", "kb_sunset_rows_noalloc",
+    "kb_get_stream", "kb_profile", "kb_profile_read", "kb_adjoint", "kb_sunset_rows_noalloc",
 ]
 
 
@@ -97,6 +97,7 @@ def load_library(path: str | None = None):
             "kb_get_stream": (C.c_int, [vp, P(vp)]),
             "kb_profile": (C.c_int, [vp, i32]),
             "kb_profile_read": (C.c_int, [vp, dp, P(i64)]),
+            "kb_adjoint": (C.c_int, [vp, dp, d, i32, dp, d, i32, dp, dp, dp, dp, dp]),
             "kb_sunset_rows_noalloc": (C.c_int, [i32, i32, d, i32, i32, vp, vp, vp, vp, vp]),
         }
         for name, (res, args) in sig.items():
@@ -245,3 +246,17 @@ class Handle:
         n = np.zeros(2, np.int64)
         self._check(self.lib.kb_profile_read(self.h, dptr(ms), n.ctypes.data_as(C.POINTER(C.c_int64))))
         return {"sunset": (ms[0], int(n[0])), "memint": (ms[1], int(n[1]))}
+
+    def adjoint(self, n_init, init_mass, t_final, w_n=None, w_E=0.0, ckpt_every=20):
+        """Gradients of sum_k w_n[k] n(k, t_final) + w_E E(t_final) (kb_adjoint).
+
+        Returns {"loss", "lambda", "mass2", "n_init" (per orbit), "init_mass"}.
+        The handle's state is consumed (call init() before stepping again)."""
+        n0 = np.ascontiguousarray(n_init, dtype=np.float64)
+        wn = None if w_n is None else np.ascontiguousarray(w_n, dtype=np.float64)
+        gl, gm, gi, L = C.c_double(), C.c_double(), C.c_double(), C.c_double()
+        gn = np.zeros(n0.shape[0])
+        self._check(self.lib.kb_adjoint(self.h, dptr(n0), float(init_mass), int(t_final), dptr(wn), float(w_E),
+                                        int(ckpt_every), C.byref(gl), C.byref(gm), dptr(gn), C.byref(gi),
+                                        C.byref(L)))
+        return {"loss": L.value, "lambda": gl.value, "mass2": gm.value, "n_init": gn, "init_mass": gi.value}

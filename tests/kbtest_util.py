@@ -27,7 +27,7 @@ def make_gpu(cfg, precision=0, device=0):
     from kb2pi import capi
 
     p = capi.KbParams(Ns=cfg["Ns"], sdim=3, M=cfg["M"], N=cfg.get("N", 4), pexp=cfg.get("pexp", 1),
-                      precision=precision, device=device, flags=0, dt=cfg["dt"], lam=cfg["lam"],
+                      precision=precision, device=device, flags=cfg.get("flags", 0), dt=cfg["dt"], lam=cfg["lam"],
                       mass2=cfg.get("mass2", 1.0), mass=cfg.get("mass", 1.0))
     return capi.Handle([p])
 
