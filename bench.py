@@ -131,7 +131,8 @@ def max_over_ranks(ws, v):
     import torch
     import torch.distributed as dist
 
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dev = "cpu" if dist.get_backend() == "gloo" else "cuda"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -298,6 +299,78 @@ def run_batched(args):
     return 0
 
 
+
+def run_adjoint(args):
+    """Config 4: gradient of the shell-averaged late-time occupation (8 radial
+    shells) plus the total energy at Ns=24, window 300, 300 steps, with respect
+    to lambda, m^2 and 8 Gaussian-bump amplitudes of the initial occupation;
+    checkpoint every 20 steps, FP64. Reports gradients/s of kb_adjoint and the
+    agreement with central finite differences of the GPU forward run."""
+    import torch
+
+    from kb2pi import adjoint as adj
+    from kb2pi import capi
+
+    ws, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    cfg = dict(Ns=24, N=4, lam=2.0, mass2=1.0, mass=1.0, dt=0.05, M=300, pexp=1, device=local)
+    tf, ckpt, nb = 302, 20, 8
+    h = capi.Handle([adj.params_for(cfg, 0)])
+    _, k2, deg = h.orbits()
+    h.close()
+    rng = np.random.default_rng(args.seed)
+    amps = rng.uniform(0.0, 5.0, nb)
+    B = adj.bump_basis(k2, nb)
+    wn = adj.shell_weights(k2, deg, nb)
+    n0 = amps @ B
+
+    def fwd(c, n):
+        hh = capi.Handle([adj.params_for(c, 0)])
+        hh.init(0, n, 1.0)
+        hh.steps(3, tf - 2, 0)
+        m = hh.measure(0, tf)
+        hh.close()
+        return float(np.dot(wn, m["n"]) + m["E"])
+
+    r = adj.loss_and_grad(cfg, n0, tf, w_n=wn, w_E=1.0, ckpt_every=ckpt)  # warm-up
+    K = max(1, min(args.steps, 3))
+    barrier(ws)
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for _ in range(K):
+            r = adj.loss_and_grad(cfg, n0, tf, w_n=wn, w_E=1.0, ckpt_every=ckpt)
+        torch.cuda.synchronize()
+        dt_adj = (time.perf_counter() - t0) / K
+    t0 = time.perf_counter()
+    L = fwd(cfg, n0)
+    dt_fwd = time.perf_counter() - t0
+    dt_adj = max_over_ranks(ws, dt_adj)
+    if rank != 0:
+        return 0
+    # central finite differences (step 1e-5 relative) of the GPU forward run
+    def cd(f, x):
+        e = 1e-5 * max(abs(x), 1.0)
+        return (f(x + e) - f(x - e)) / (2 * e)
+    fd = {"lambda": cd(lambda v: fwd(dict(cfg, lam=v), n0), cfg["lam"]),
+          "mass2": cd(lambda v: fwd(dict(cfg, mass2=v), n0), cfg["mass2"])}
+    ga = B @ r["n_init"]
+    fd_a = np.array([cd(lambda s, b=b: fwd(cfg, (amps + s * np.eye(nb)[b]) @ B), 0.0) for b in range(nb)])
+    errs = {"lambda": abs(r["lambda"] - fd["lambda"]) / abs(fd["lambda"]),
+            "mass2": abs(r["mass2"] - fd["mass2"]) / abs(fd["mass2"]),
+            "amplitudes": float(np.max(np.abs(ga - fd_a)) / np.max(np.abs(fd_a)))}
+    line = {"metric": "adjoint gradients/s (config 4: Ns=24, window 300, 300 steps, checkpoint every 20)",
+            "value": ws / dt_adj, "unit": "gradients/s", "n_gpus": ws, "steps": K, "warmup": 1,
+            "ms_per_step": 1000.0 * dt_adj, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": f"synthetic: 8 bump amplitudes U[0,5] seeded with {args.seed}",
+            "config": {"workload": "loss = sum over 8 radial shells of the mean n(p, t=302) + E(302); "
+                                   "Ns=24, N=4, lambda=2, m^2=1, dt=0.05, M=300, 300 steps, ckpt_every=20"},
+            "loss": r["loss"], "loss_forward": L, "forward_s": dt_fwd,
+            "grad": {"lambda": r["lambda"], "mass2": r["mass2"], "amplitudes": ga.tolist()},
+            "fd": {"lambda": fd["lambda"], "mass2": fd["mass2"], "amplitudes": fd_a.tolist()},
+            "rel_err_vs_fd": errs, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    return 0
+
 def run_reference(args):
     ws, rank, _ = dist_setup()
     if rank != 0:
@@ -401,7 +474,8 @@ def run_ours(args):
     alg = algorithmic_bytes(M, S, 4, 4)
     peak, peak_kind = read_peaks()
     achieved = alg / (mi_ms / 1000.0) / 1e9
-    traffic = read_traffic("traffic_bytes_per_launch")
+    # the committed capture covers this workload only
+    traffic = read_traffic("traffic_bytes_per_launch") if (CFG["Ns"], CFG["M"]) == (64, 1000) else None
     line = {
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -416,7 +490,7 @@ def run_ours(args):
         "kernels_ms": {"memint": mi_ms, "sunset": sun_ms},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                     "kernel": "memint_kernel<float,32,2>", "algorithmic_bytes": alg},
+                     "kernel": "memint_kernel<float,32,3,2>", "algorithmic_bytes": alg},
         "clocks": clk.summary(),
         "e2e": {"value": e2e_val, "unit": "steps/s", "h2d_bytes_per_step": 4, "d2h_bytes_per_step": d2h,
                 "path": "kb_step + kb_measure through the C ABI, host buffers, wall clock"},
@@ -443,13 +517,15 @@ def main():
     ap.add_argument("--cpu-window", type=int, default=128)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--config", default="c5", choices=["c5", "small", "c3"],
+    ap.add_argument("--config", default="c5", choices=["c5", "small", "c3", "c4"],
                     help="c5: the benchmark workload; small: Ns=40, M=400 for profiler captures; "
-                         "c3: 64 uneven runs in one launch")
+                         "c3: 64 uneven runs in one launch; c4: adjoint gradients")
     ap.add_argument("--seed", type=int, default=12345)
     args = ap.parse_args()
     if args.config == "c3" and args.impl == "ours":
         return run_batched(args)
+    if args.config == "c4" and args.impl == "ours":
+        return run_adjoint(args)
     if args.config == "small":
         CFG.update(SMALL)
     if args.warmup < 3:

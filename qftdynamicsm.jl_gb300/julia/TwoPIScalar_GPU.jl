@@ -141,3 +141,44 @@ function getGapMass_orbits(model, pexp, disc, n, simdata)
     D(f) = x -> ForwardDiff.derivative(f, float(x))
     return find_zero((g, D(g)), 0.5, Roots.Newton())
 end
+
+# Gradients by the discrete adjoint (kb_adjoint): L = sum_k w_n[k] n(k, t_final) + w_E E(t_final) on orbits,
+# for the run started from occupation n_init at init_mass. A handle with NstepsinMemory M and extra ring
+# slots (kb_params.flags) >= ckpt_every is created per call; its state is consumed.
+function kb_loss_and_grad(problem, n_init::Vector{Float64}, init_mass, t_final, w_n, w_E; ckpt_every = 20)
+    d, m = problem.disc, problem.model
+    pexp = problem.pexp isa TwoPIScalarLambdaLO ? 0 : (problem.pexp isa TwoPIScalarLambdaNLOclassical ? 2 : 1)
+    p = Ref(KbParams(d.Nx, d.sdim, problem.simsetup.NstepsinMemory, m.ONgroup, pexp, 0, 0, ckpt_every,
+                     d.dt, m.Lambda, m.Mass2, d.Mass))
+    hr = Ref{Ptr{Cvoid}}(C_NULL)
+    kbcheck(ccall((:kb_create, libkb2pi), Cint, (Ref{KbParams}, Ref{Ptr{Cvoid}}), p, hr), C_NULL)
+    gl = Ref(0.0); gm = Ref(0.0); gi = Ref(0.0); L = Ref(0.0); gn = zeros(length(n_init))
+    try
+        kbcheck(ccall((:kb_adjoint, libkb2pi), Cint,
+                      (Ptr{Cvoid}, Ptr{Float64}, Float64, Int32, Ptr{Float64}, Float64, Int32,
+                       Ref{Float64}, Ref{Float64}, Ptr{Float64}, Ref{Float64}, Ref{Float64}),
+                      hr[], n_init, init_mass, t_final, w_n === nothing ? C_NULL : w_n, w_E, ckpt_every,
+                      gl, gm, gn, gi, L), hr[])
+    finally
+        ccall((:kb_destroy, libkb2pi), Cvoid, (Ptr{Cvoid},), hr[])
+    end
+    return L[], (lambda = gl[], mass2 = gm[], n_init = gn, init_mass = gi[])
+end
+
+# ChainRulesCore rrule: late-time loss as a function of (lambda, m^2, n_init) with the adjoint as pullback.
+# `kb_late_time_loss(problem, lambda, mass2, n_init, init_mass, t_final, w_n, w_E)` runs the forward pass.
+# ChainRulesCore and ConstructionBase are already in the reference's Manifest.toml (as indirect
+# dependencies, :136 and :210); add both to Project.toml [deps] with this file.
+using ChainRulesCore
+using ConstructionBase: setproperties
+function kb_late_time_loss(problem, lambda, mass2, n_init, init_mass, t_final, w_n, w_E)
+    pr = setproperties(problem, model = setproperties(problem.model, Lambda = lambda, Mass2 = mass2))
+    return first(kb_loss_and_grad(pr, n_init, init_mass, t_final, w_n, w_E))
+end
+function ChainRulesCore.rrule(::typeof(kb_late_time_loss), problem, lambda, mass2, n_init, init_mass, t_final, w_n, w_E)
+    pr = setproperties(problem, model = setproperties(problem.model, Lambda = lambda, Mass2 = mass2))
+    L, g = kb_loss_and_grad(pr, n_init, init_mass, t_final, w_n, w_E)
+    pullback(dL) = (NoTangent(), NoTangent(), dL * g.lambda, dL * g.mass2, dL .* g.n_init, dL * g.init_mass,
+                    NoTangent(), NoTangent(), NoTangent())
+    return L, pullback
+end
