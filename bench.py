@@ -145,6 +145,18 @@ def make_handle(precision, device):
     return capi.Handle([p])
 
 
+def apply_tuning(h, args, fp64=False):
+    """Autotune the launch configuration on the filled window (untimed), unless fixed on the command line."""
+    if args.memint_variant is not None or args.sunset_grid is not None:
+        h.set_tuning(memint_variant=None if fp64 else args.memint_variant, sunset_grid=args.sunset_grid)
+        d = h.tuning()
+        d["source"] = "command line"
+        return d
+    d = h.autotune(trials=3)
+    d["source"] = "kb_autotune"
+    return d
+
+
 def init_and_fill(h):
     _, k2, deg = h.orbits(0)
     n = tsunami_n(k2)
@@ -405,6 +417,7 @@ def run_ours(args):
     S = h.S[0]
     t = init_and_fill(h)
     meas_mixed = h.measure(0, t)
+    tuning = apply_tuning(h, args)
     for i in range(args.warmup):
         h.step(t + 1 + i)
     t += args.warmup
@@ -448,6 +461,7 @@ def run_ours(args):
         h64 = make_handle(capi.KB_PREC_FP64, dev)
         t64 = init_and_fill(h64)
         meas64 = h64.measure(0, t64)
+        tuning64 = apply_tuning(h64, args, fp64=True)
         for i in range(min(args.warmup, 3)):
             h64.step(t64 + 1 + i)
         t64 += min(args.warmup, 3)
@@ -459,6 +473,7 @@ def run_ours(args):
         ms64 = max_over_ranks(ws, ms64)
         nn = meas64["n"]
         fp64 = {"steps_per_s": ws * k64 / (ms64 / 1000.0), "ms_per_step": ms64 / k64, "steps": k64,
+                "tuning": tuning64,
                 "memint_ms": prof64["memint"][0] / max(1, prof64["memint"][1]),
                 "sunset_ms": prof64["sunset"][0] / max(1, prof64["sunset"][1]),
                 "mixed_vs_fp64_rel_err": {
@@ -488,6 +503,7 @@ def run_ours(args):
         "mode_steps_per_s": value * M * CFG["Ns"] ** 3,
         "graph_ms_per_step": gms / args.steps,
         "kernels_ms": {"memint": mi_ms, "sunset": sun_ms},
+        "tuning": tuning,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                      "kernel": "memint_kernel<float,32,3,2>", "algorithmic_bytes": alg},
@@ -521,6 +537,11 @@ def main():
                     help="c5: the benchmark workload; small: Ns=40, M=400 for profiler captures; "
                          "c3: 64 uneven runs in one launch; c4: adjoint gradients")
     ap.add_argument("--seed", type=int, default=12345)
+    ap.add_argument("--ns", type=int, default=None, help="override Ns of the c5/small workload (sweeps)")
+    ap.add_argument("--m", type=int, default=None, help="override the memory window M (sweeps)")
+    ap.add_argument("--memint-variant", type=int, default=None,
+                    help="fix the mixed-precision memory-integral variant instead of autotuning")
+    ap.add_argument("--sunset-grid", type=int, default=None, help="fix the sunset grid instead of autotuning")
     args = ap.parse_args()
     if args.config == "c3" and args.impl == "ours":
         return run_batched(args)
@@ -528,6 +549,10 @@ def main():
         return run_adjoint(args)
     if args.config == "small":
         CFG.update(SMALL)
+    if args.ns:
+        CFG["Ns"] = args.ns
+    if args.m:
+        CFG["M"] = args.m
     if args.warmup < 3:
         ap.error("at least 3 warm-up steps")
     if args.impl == "reference":

@@ -162,6 +162,25 @@ int kb_get_stream(const kb_handle *h, void **stream);
 int kb_profile(kb_handle *h, int32_t enable);
 int kb_profile_read(kb_handle *h, double *ms, int64_t *launches);
 
+/* Launch configuration of a handle's kernels. No counterpart in the reference
+ * (it has no tunables). Every choice computes the same step; the memory-integral
+ * variant only changes the order of the FP32 tile partial sums (KB_PREC_MIXED). */
+typedef struct kb_tuning {
+  int32_t memint_variant; /* KB_PREC_MIXED: 1 column/row consumer groups (default), 0 register-blocked
+                           * consumers; KB_PREC_FP64: 0 (one kernel) */
+  int32_t sunset_grid;    /* CTAs of the persistent sunset kernel; 0 = one per SM */
+  int32_t reserved[2];
+} kb_tuning;
+int kb_get_tuning(const kb_handle *h, kb_tuning *out);
+int kb_set_tuning(kb_handle *h, const kb_tuning *in);
+/* Autotuner: times every candidate configuration (memory-integral variants;
+ * sunset grids of 1..4 CTAs per SM that fit) by re-running the last evolved
+ * step t -- which reads rows < t and rewrites row t, so the state is unchanged
+ * -- `trials` times each, keeps the fastest kernel configurations, re-runs step
+ * t once with them and returns the choice and its time per step (ms) if the
+ * pointers are not NULL. Needs t >= 3. */
+int kb_autotune(kb_handle *h, int32_t trials, kb_tuning *chosen, double *ms_per_step);
+
 /* Gradient of a late-time loss by the discrete adjoint of the step. No
  * counterpart in the reference (its ChainRulesCore rrule would wrap this):
  *   L = sum_k w_n[k] n(k, t_final) + w_E E(t_final)

@@ -51,7 +51,8 @@ struct kb_handle {
   int total_sun = 0, total_mi = 0;
   int *d_t = nullptr, *d_err = nullptr;
   size_t smem_sun = 0, smem_mi = 0;
-  int num_sms = 0, grid_sun = 0;
+  int num_sms = 0, grid_sun = 0, grid_sun_max = 0;
+  int memint_variant = 0;         // FP32 consumer layout of the memory-integral kernel
   void *sun_scratch = nullptr;    // FP64 cosine-transform intermediates, one slot per CTA
   size_t sun_scratch_stride = 0;  // elements per slot
   int t_cur = 0;      // last evolved (or initialised) step; window is [tmin(t_cur), t_cur]
@@ -190,6 +191,7 @@ int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out) {
   kb_handle *h = new kb_handle();
   h->device = p[0].device;
   h->fp64 = (p[0].precision == KB_PREC_FP64);
+  h->memint_variant = h->fp64 ? 0 : 1;  // FP32: two consumer groups unless kb_set_tuning/kb_autotune choose
   if (cudaSetDevice(h->device) != cudaSuccess) { delete h; return fail(nullptr, KB_ERR_CUDA, "cudaSetDevice failed"); }
   if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) {
     delete h;
@@ -208,7 +210,7 @@ int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out) {
     R.Malloc = ((R.p.M + (R.p.flags & 0xffff) + T - 1) / T) * T;  // extra slots for kb_adjoint
     R.esz = h->fp64 ? 8 : 4;
     smem_sun = std::max(smem_sun, kb::sunset_smem_bytes(h->fp64, R.H));
-    smem_mi = std::max(smem_mi, kb::memint_smem_bytes(h->fp64, R.Malloc));
+    smem_mi = std::max({smem_mi, kb::memint_smem_bytes(h->fp64, R.Malloc, 0), kb::memint_smem_bytes(h->fp64, R.Malloc, 1)});
     bsun[r] = base_sun;
     bmi[r] = base_mi;
     base_sun += R.p.M;
@@ -306,18 +308,6 @@ int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out) {
   }
   cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
   h->grid_sun = kb::sunset_grid(h->fp64, h->num_sms, h->total_sun);
-  if (h->fp64 && h->any_nlo) {
-    int Hmax = 1;
-    for (auto &R : h->runs) Hmax = std::max(Hmax, R.H);
-    h->sun_scratch_stride = kb::sunset_scratch_elems(Hmax);
-    const size_t bytes = (size_t)h->grid_sun * h->sun_scratch_stride * sizeof(double);
-    if (cudaMalloc(&h->sun_scratch, bytes) != cudaSuccess) {
-      cudaGetLastError();
-      fail(nullptr, KB_ERR_OOM, "cudaMalloc of %zu bytes of sunset scratch failed", bytes);
-      kb_destroy(h);
-      return KB_ERR_OOM;
-    }
-  }
   cudaMemcpy(h->d_runs, devs.data(), sizeof(RunDev) * nruns, cudaMemcpyHostToDevice);
   cudaMemcpy(h->d_base_sun, bsun.data(), sizeof(int) * nruns, cudaMemcpyHostToDevice);
   cudaMemcpy(h->d_base_mi, bmi.data(), sizeof(int) * nruns, cudaMemcpyHostToDevice);
@@ -330,6 +320,21 @@ int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out) {
     fail(nullptr, KB_ERR_CUDA, "kernel configuration failed: %s", cudaGetErrorString(e1 != cudaSuccess ? e1 : e2));
     kb_destroy(h);
     return KB_ERR_CUDA;
+  }
+  // the largest sunset grid the tuner may pick: up to 4 resident CTAs per SM
+  h->grid_sun_max = std::max(1, std::min(h->total_sun, h->num_sms * std::min(4, kb::sunset_max_ctas_per_sm(
+                                                                                    h->fp64, h->smem_sun))));
+  if (h->fp64 && h->any_nlo) {
+    int Hmax = 1;
+    for (auto &R : h->runs) Hmax = std::max(Hmax, R.H);
+    h->sun_scratch_stride = kb::sunset_scratch_elems(Hmax);
+    const size_t bytes = (size_t)h->grid_sun_max * h->sun_scratch_stride * sizeof(double);
+    if (cudaMalloc(&h->sun_scratch, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      fail(nullptr, KB_ERR_OOM, "cudaMalloc of %zu bytes of sunset scratch failed", bytes);
+      kb_destroy(h);
+      return KB_ERR_OOM;
+    }
   }
   if (cudaDeviceSynchronize() != cudaSuccess) {
     fail(nullptr, KB_ERR_CUDA, "device error during kb_create: %s", cudaGetErrorString(cudaGetLastError()));
@@ -481,8 +486,8 @@ static int launch_step(kb_handle *h, int measure) {
     KB_CUDA(h, cudaEventRecord(e1, h->st));
     if (h->any_nlo) h->ev_pending.push_back({0, {e0, e1}});
   }
-  KB_CUDA(h, kb::launch_memint(h->fp64, h->d_runs, h->d_base_mi, (int)h->runs.size(), h->total_mi, h->d_t,
-                               h->d_err, measure, h->smem_mi, h->st));
+  KB_CUDA(h, kb::launch_memint(h->fp64, h->memint_variant, h->d_runs, h->d_base_mi, (int)h->runs.size(),
+                               h->total_mi, h->d_t, h->d_err, measure, h->smem_mi, h->st));
   if (h->profiling) {
     KB_CUDA(h, cudaEventRecord(e2, h->st));
     h->ev_pending.push_back({1, {e1, e2}});
@@ -837,6 +842,108 @@ int kb_checkpoint_save(kb_handle *h, void *buf, size_t bytes) {
 int kb_checkpoint_restore(kb_handle *h, const void *buf, size_t bytes) {
   if (!h || !buf) return KB_ERR_PARAM;
   return ckpt_copy(h, (char *)const_cast<void *>(buf), bytes, false);
+}
+
+// ---------------------------------------------------------------------------
+// Tuning: launch configuration of the two step kernels, and an autotuner that
+// times candidates by re-running the last step (idempotent: step t reads rows
+// < t, the FP64 state rows t-1, t-2 and the tadpole sums of t-1, and rewrites
+// row t, Sigma(t-1, .), the tadpole sums of t and the measurement).
+int kb_get_tuning(const kb_handle *h, kb_tuning *out) {
+  if (!h || !out) return KB_ERR_PARAM;
+  *out = kb_tuning{};
+  out->memint_variant = h->memint_variant;
+  out->sunset_grid = h->grid_sun;
+  return KB_OK;
+}
+
+int kb_set_tuning(kb_handle *h, const kb_tuning *in) {
+  if (!h || !in) return KB_ERR_PARAM;
+  if (in->memint_variant < 0 || in->memint_variant > 1 || (h->fp64 && in->memint_variant != 0))
+    return fail(h, KB_ERR_PARAM, "memint_variant=%d: 0 or 1, and 0 for KB_PREC_FP64", in->memint_variant);
+  const int g = in->sunset_grid == 0 ? kb::sunset_grid(h->fp64, h->num_sms, h->total_sun) : in->sunset_grid;
+  if (g < 1 || g > h->grid_sun_max)
+    return fail(h, KB_ERR_PARAM, "sunset_grid=%d: at most %d CTAs fit on this device", in->sunset_grid,
+                h->grid_sun_max);
+  h->memint_variant = in->memint_variant;
+  h->grid_sun = g;
+  if (h->graph) {  // captured with the old configuration
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+  }
+  return KB_OK;
+}
+
+int kb_autotune(kb_handle *h, int32_t trials, kb_tuning *chosen, double *ms_per_step) {
+  if (!h || trials < 1) return KB_ERR_PARAM;
+  if (h->t_cur < 3) return fail(h, KB_ERR_PARAM, "kb_autotune needs an evolved step (t >= 3)");
+  cudaSetDevice(h->device);
+  int rc = kb_sync(h);
+  if (rc) return rc;
+  const int t = h->t_cur;
+  cudaEvent_t e[3];
+  for (auto &x : e) KB_CUDA(h, cudaEventCreate(&x));
+  auto time_cfg = [&](int variant, int grid, float *ms_sun, float *ms_mi) -> int {
+    h->memint_variant = variant;
+    h->grid_sun = grid;
+    float best_s = 1e30f, best_m = 1e30f;
+    for (int q = 0; q < trials; ++q) {
+      KB_CUDA(h, kb::launch_set_t(h->d_t, t, h->st));
+      KB_CUDA(h, cudaEventRecord(e[0], h->st));
+      if (h->any_nlo)
+        KB_CUDA(h, kb::launch_sunset(h->fp64, h->d_runs, h->d_base_sun, (int)h->runs.size(), h->total_sun,
+                                     h->grid_sun, h->d_t, h->sun_scratch, h->sun_scratch_stride, h->smem_sun, h->st));
+      KB_CUDA(h, cudaEventRecord(e[1], h->st));
+      KB_CUDA(h, kb::launch_memint(h->fp64, h->memint_variant, h->d_runs, h->d_base_mi, (int)h->runs.size(),
+                                   h->total_mi, h->d_t, h->d_err, 1, h->smem_mi, h->st));
+      KB_CUDA(h, cudaEventRecord(e[2], h->st));
+      KB_CUDA(h, cudaEventSynchronize(e[2]));
+      float a = 0, b = 0;
+      KB_CUDA(h, cudaEventElapsedTime(&a, e[0], e[1]));
+      KB_CUDA(h, cudaEventElapsedTime(&b, e[1], e[2]));
+      best_s = std::min(best_s, a);
+      best_m = std::min(best_m, b);
+    }
+    *ms_sun = best_s;
+    *ms_mi = best_m;
+    return KB_OK;
+  };
+  // sunset grids: 1..4 CTAs per SM as far as they fit; memint variants: FP32 only
+  std::vector<int> grids;
+  for (int k = 1; k <= 4; ++k) {
+    const int g = std::min(h->total_sun, k * h->num_sms);
+    if (g <= h->grid_sun_max && (grids.empty() || g != grids.back())) grids.push_back(g);
+  }
+  if (grids.empty()) grids.push_back(h->grid_sun);
+  const int nvar = h->fp64 ? 1 : 2;
+  int best_g = grids[0], best_v = 0;
+  float bs = 1e30f, bm = 1e30f;
+  for (int g : grids) {
+    float ms_s, ms_m;
+    if ((rc = time_cfg(0, g, &ms_s, &ms_m))) break;
+    if (ms_s < bs) { bs = ms_s; best_g = g; }
+    if (g == grids[0]) bm = ms_m;
+  }
+  for (int v = 1; v < nvar && !rc; ++v) {
+    float ms_s, ms_m;
+    if ((rc = time_cfg(v, best_g, &ms_s, &ms_m))) break;
+    if (ms_m < bm) { bm = ms_m; best_v = v; }
+  }
+  for (auto &x : e) cudaEventDestroy(x);
+  if (rc) return rc;
+  h->memint_variant = best_v;
+  h->grid_sun = best_g;
+  if (h->graph) {
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+  }
+  // step t once more with the chosen kernels, so the state is theirs
+  KB_CUDA(h, kb::launch_set_t(h->d_t, t, h->st));
+  if ((rc = launch_step(h, 1))) return rc;
+  if ((rc = kb_sync(h))) return rc;
+  if (chosen) kb_get_tuning(h, chosen);
+  if (ms_per_step) *ms_per_step = (double)(bs + bm);
+  return KB_OK;
 }
 
 // ---------------------------------------------------------------------------

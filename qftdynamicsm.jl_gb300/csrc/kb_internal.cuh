@@ -77,10 +77,11 @@ cudaError_t launch_sunset(bool fp64, const RunDev *d_runs, const int *d_base, in
 size_t sunset_smem_bytes(bool fp64, int H);
 size_t sunset_scratch_elems(int H);
 int sunset_grid(bool fp64, int num_sms, int total_rows);
+int sunset_max_ctas_per_sm(bool fp64, size_t smem);
 cudaError_t configure_sunset(bool fp64, size_t smem);
-cudaError_t launch_memint(bool fp64, const RunDev *d_runs, const int *d_base, int nruns, int total_ctas,
-                          const int *d_t, int *d_err, int measure, size_t smem, cudaStream_t st);
-size_t memint_smem_bytes(bool fp64, int Malloc);
+cudaError_t launch_memint(bool fp64, int variant, const RunDev *d_runs, const int *d_base, int nruns,
+                          int total_ctas, const int *d_t, int *d_err, int measure, size_t smem, cudaStream_t st);
+size_t memint_smem_bytes(bool fp64, int Malloc, int variant);
 cudaError_t configure_memint(bool fp64, size_t smem);
 int memint_tile(bool fp64);
 cudaError_t launch_measure_init(const RunDev *d_runs, int nruns, int t, cudaStream_t st);

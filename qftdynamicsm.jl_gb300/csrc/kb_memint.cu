@@ -195,6 +195,73 @@ __device__ __forceinline__ void consumer_sync(int nthreads) {
   asm volatile("bar.sync 1, %0;" ::"r"(nthreads) : "memory");
 }
 
+// Diagonal F(t,t) (Evolution.jl:969-974), its tadpole partial for the next
+// step and the measurement of the chunk's orbits (createMeasurement,
+// Measurement.jl:38-64); threads 0..KC-1 of the CTA, one orbit each. misc holds
+// hartreecont, acc_F(t-1) per orbit and the nwarps x KC partial sums of acc_F(t).
+template <typename TS>
+__device__ void memint_epilogue(const RunDev &R, int c, int t, int tid, const double *misc, int nwarps,
+                                double M2, int measure) {
+  const double hc = misc[0];
+  const int Ma = R.Malloc, T = R.T;
+  const size_t rowstride = (size_t)Ma * KC;
+  const size_t st_row = (size_t)R.nchunks * rowstride;
+  const double *F1row = R.st_F + (size_t)((t - 1) % 3) * st_row + (size_t)c * rowstride;
+  double *FNrow = R.st_F + (size_t)(t % 3) * st_row + (size_t)c * rowstride;
+  double *RNrow = R.st_r + (size_t)(t % 3) * st_row + (size_t)c * rowstride;
+  const size_t hdo = hist_off(Ma, T, c, t, t, tid);
+  double accd = 0.0;
+  for (int w = 0; w < nwarps; ++w) accd += misc[16 + w * KC + tid];
+  const int jj = tid;
+  const int kd = c * KC + jj;
+  const double kd2 = (kd < R.S) ? R.k2[kd] : 0.0;
+  const double omd = (kd2 + M2) * R.dt2;
+  const double Ft1 = FNrow[(size_t)((t - 1) % Ma) * KC + jj];  // F(t, t-1)
+  const double Ft2 = FNrow[(size_t)((t - 2) % Ma) * KC + jj];  // F(t, t-2)
+  const double Ftt = (2.0 - omd) * Ft1 - Ft2 - accd * R.dt3;
+  FNrow[(size_t)(t % Ma) * KC + jj] = Ftt;
+  RNrow[(size_t)(t % Ma) * KC + jj] = 0.0;
+  reinterpret_cast<TS *>(R.hist_F)[hdo] = (TS)Ftt;
+  reinterpret_cast<TS *>(R.hist_r)[hdo] = (TS)0;
+  const double dg = (kd < R.S) ? R.deg[kd] : 0.0;
+  double tp = dg * Ftt;  // tadpole partial sum of this chunk for the next step
+  // measurement (createMeasurement, Measurement.jl:38-64): F(t-1,t-1) from the state
+  const double Fmm = F1row[(size_t)((t - 1) % Ma) * KC + jj];
+  const double dt = R.dt, dt2 = R.dt2;
+  const double ddF = (Ftt - 2 * Ft1 + Fmm) / dt2;
+  const double omg = (ddF / Fmm > 0) ? sqrt(ddF / Fmm) : 0.0;
+  const double cc = (0.25 * dt2 * (omg * omg) < 1) ? sqrt(1. - 0.25 * dt2 * (omg * omg)) : 1.0;
+  const double nn = (ddF * Fmm > 0) ? (cc * sqrt(ddF * Fmm)) - 0.5 : 0.0;
+  double ek = 0.5 * ddF * dg;
+  double ep = 0.5 * (R.mass2 + kd2 + 0.5 * R.pref_ivol * hc) * Fmm * dg;
+  double em = 0.25 * dt * dg * misc[2 + jj];
+  if (kd < R.S && measure) {
+    const int Sp = R.nchunks * KC;
+    R.meas[0 * Sp + kd] = Fmm;
+    R.meas[1 * Sp + kd] = ddF;
+    R.meas[2 * Sp + kd] = nn;
+    R.meas[3 * Sp + kd] = omg;
+    R.meas[4 * Sp + kd] = cc;
+  }
+  // fixed-order reduction over the KC orbits (lanes 0..KC-1 of warp 0)
+#pragma unroll
+  for (int o = KC / 2; o > 0; o >>= 1) {
+    tp += __shfl_xor_sync((1u << KC) - 1, tp, o);
+    ek += __shfl_xor_sync((1u << KC) - 1, ek, o);
+    ep += __shfl_xor_sync((1u << KC) - 1, ep, o);
+    em += __shfl_xor_sync((1u << KC) - 1, em, o);
+  }
+  if (jj == 0) {
+    R.tad[(size_t)(t & 1) * R.nchunks + c] = tp;
+    if (measure) {
+      R.epart[(size_t)c * 4 + 0] = ek;
+      R.epart[(size_t)c * 4 + 1] = ep;
+      R.epart[(size_t)c * 4 + 2] = em;
+      R.epart[(size_t)c * 4 + 3] = M2;
+    }
+  }
+}
+
 // Block = column group (NG threads: column b, orbits j) + row group (NG threads:
 // row a, orbits j) + one producer warp. Both consumer groups read every tile
 // from the shared-memory ring: the column group accumulates
@@ -504,63 +571,341 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
     return;
   }
 
-  // --- diagonal F(t,t) (Evolution.jl:969-974)
-  if (tid < KC) {
-    const double *F1row = R.st_F + (size_t)((t - 1) % 3) * st_row + (size_t)c * rowstride;
-    double *FNrow = R.st_F + (size_t)(t % 3) * st_row + (size_t)c * rowstride;
-    double *RNrow = R.st_r + (size_t)(t % 3) * st_row + (size_t)c * rowstride;
-    const size_t hdo = hist_off(Ma, T, c, t, t, tid);
-    double accd = 0.0;
-    for (int w = 0; w < C::NG / 32; ++w) accd += misc[16 + w * KC + tid];
-    const int jj = tid;
-    const int kd = c * KC + jj;
-    const double kd2 = (kd < R.S) ? R.k2[kd] : 0.0;
-    const double omd = (kd2 + M2) * R.dt2;
-    const double Ft1 = FNrow[(size_t)((t - 1) % Ma) * KC + jj];  // F(t, t-1)
-    const double Ft2 = FNrow[(size_t)((t - 2) % Ma) * KC + jj];  // F(t, t-2)
-    const double Ftt = (2.0 - omd) * Ft1 - Ft2 - accd * R.dt3;
-    FNrow[(size_t)(t % Ma) * KC + jj] = Ftt;
-    RNrow[(size_t)(t % Ma) * KC + jj] = 0.0;
-    reinterpret_cast<TS *>(R.hist_F)[hdo] = (TS)Ftt;
-    reinterpret_cast<TS *>(R.hist_r)[hdo] = (TS)0;
-    const double dg = (kd < R.S) ? R.deg[kd] : 0.0;
-    double tp = dg * Ftt;  // tadpole partial sum of this chunk for the next step
-    // measurement (createMeasurement, Measurement.jl:38-64): F(t-1,t-1) from the state
-    const double Fmm = F1row[(size_t)((t - 1) % Ma) * KC + jj];
-    const double dt = R.dt, dt2 = R.dt2;
-    const double ddF = (Ftt - 2 * Ft1 + Fmm) / dt2;
-    const double omg = (ddF / Fmm > 0) ? sqrt(ddF / Fmm) : 0.0;
-    const double cc = (0.25 * dt2 * (omg * omg) < 1) ? sqrt(1. - 0.25 * dt2 * (omg * omg)) : 1.0;
-    const double nn = (ddF * Fmm > 0) ? (cc * sqrt(ddF * Fmm)) - 0.5 : 0.0;
-    double ek = 0.5 * ddF * dg;
-    double ep = 0.5 * (R.mass2 + kd2 + 0.5 * R.pref_ivol * hc) * Fmm * dg;
-    double em = 0.25 * dt * dg * misc[2 + jj];
-    if (kd < R.S && measure) {
-      const int Sp = R.nchunks * KC;
-      R.meas[0 * Sp + kd] = Fmm;
-      R.meas[1 * Sp + kd] = ddF;
-      R.meas[2 * Sp + kd] = nn;
-      R.meas[3 * Sp + kd] = omg;
-      R.meas[4 * Sp + kd] = cc;
-    }
-    // fixed-order reduction over the KC orbits (lanes 0..KC-1 of warp 0)
-#pragma unroll
-    for (int o = KC / 2; o > 0; o >>= 1) {
-      tp += __shfl_xor_sync((1u << KC) - 1, tp, o);
-      ek += __shfl_xor_sync((1u << KC) - 1, ek, o);
-      ep += __shfl_xor_sync((1u << KC) - 1, ep, o);
-      em += __shfl_xor_sync((1u << KC) - 1, em, o);
-    }
-    if (jj == 0) {
-      R.tad[(size_t)(t & 1) * R.nchunks + c] = tp;
-      if (measure) {
-        R.epart[(size_t)c * 4 + 0] = ek;
-        R.epart[(size_t)c * 4 + 1] = ep;
-        R.epart[(size_t)c * 4 + 2] = em;
-        R.epart[(size_t)c * 4 + 3] = M2;
-      }
+  if (tid < KC) memint_epilogue<TS>(R, c, t, tid, misc, C::NG / 32, M2, measure);
+}
+
+// ---------------------------------------------------------------------------
+// FP32 history, register-blocked consumers. Same pipeline, tile order, row
+// accumulator and epilogue as memint_kernel, but every consumer thread owns a
+// 4 x 4 block of (row, column) pairs of each tile for 2 adjacent orbits, so
+// each F and rho element is read from shared memory once (memint_kernel reads
+// it twice, once per consumer group; shared-memory wavefronts bound its CTA).
+//   warp w        : tile rows 4w .. 4w+3
+//   lane          : columns (lane >> 2) + 8k, k = 0..3; orbits 2 (lane & 3) + {0,1}
+// A warp-wide 8-byte load covers 8 consecutive columns of one row (256
+// contiguous bytes under the XOR swizzle, conflict-free). Row sums of a tile
+// are reduce-scattered over the 8 column lanes (7 shuffles) so that every lane
+// ends with one (row, orbit) sum, which it adds to its FP64 row accumulator.
+// Column partials are summed in FP32 over at most 8 tiles (32 rows, as the
+// per-tile partials of memint_kernel), then in FP64; at the end of a column
+// block the 8 warps' column sums meet in shared memory and one thread per
+// (column, orbit) runs the leapfrog.
+// ---------------------------------------------------------------------------
+constexpr int BLK_COLBUF_BYTES = 8 * 32 * KC * (int)sizeof(double);
+
+template <int NST>
+__global__ void __launch_bounds__(288)
+memint_blk_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int nruns,
+                  const int *__restrict__ d_t, int *__restrict__ d_err, int measure) {
+  using C = Cfg<float, 32, NST, 2>;
+  using V = Vec<float, 2>;
+  constexpr int T = 32, NT = 256;
+  static_assert(C::NT == NT, "256 consumer threads");
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  float *stages = reinterpret_cast<float *>(smem_raw);
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw + (size_t)NST * C::STAGE_BYTES);
+  uint64_t *empty = full + NST;
+  // misc: [0] hartreecont, [1] M^2, [2..2+KC) acc_F(t-1) per orbit, [10] abort flag,
+  // [11] tiles issued, [12] consumer abort flag, [16..16+8*KC) diagonal partials
+  double *misc = reinterpret_cast<double *>(empty + NST);
+  double *colbuf = misc + 128;  // [8 warps][32 columns][KC] column partials of one field
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(misc + 10);
+  volatile int *issued_count = reinterpret_cast<volatile int *>(misc + 11);
+  volatile int *cabort = reinterpret_cast<volatile int *>(misc + 12);
+
+  const int r = find_run(base, nruns, blockIdx.x);
+  const RunDev &R = runs[r];
+  const int c = blockIdx.x - R.cta_base_mi;  // chunk
+  const int tid = threadIdx.x;
+  const bool producer = tid >= NT;
+  const int lane = tid & 31, warp = tid >> 5;
+  const int jq = lane & 3, c8 = lane >> 2;
+  const int j0 = 2 * jq;
+  // (row, orbit) owned after the reduce-scatter of the row sums
+  const int own_rr = 4 * warp + 2 * ((lane >> 4) & 1) + ((lane >> 3) & 1);
+  const int own_j = j0 + ((lane >> 2) & 1);
+  const int t = *d_t;
+  const int M = R.M, Ma = R.Malloc;
+  const int tmin = max(1, t - M + 1);
+  const size_t rowstride = (size_t)Ma * KC;
+  const size_t st_row = (size_t)R.nchunks * rowstride;
+  double *rowacc = R.rowacc + (size_t)c * rowstride;
+
+  if (warp == 0) {
+    const double *tad = R.tad + (size_t)((t - 1) & 1) * R.nchunks;
+    double s = 0.0;
+    for (int q = lane; q < R.nchunks; q += 32) s += tad[q];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) {
+      misc[0] = s;
+      misc[1] = s * R.pref_ivol + R.mass2;
     }
   }
+  if (tid < KC) misc[2 + tid] = 0.0;
+  if (tid == 0) {
+    *abort_flag = 0;
+    *issued_count = 0;
+    *cabort = 0;
+    for (int q = 0; q < NST; ++q) {
+      mbar_init(full + q, 1);
+      mbar_init(empty + q, C::NW);
+    }
+    fence_proxy_async();
+  }
+  if (!producer)
+    for (int s = own_rr; s < Ma; s += T) rowacc[(size_t)s * KC + own_j] = 0.0;
+  __syncthreads();
+  const double M2 = misc[1];
+
+  const bool lo_only = (R.pexp == 0);
+  const int J0 = tmin / T, Jn = (t - 1) / T;
+  const int nb = Jn - J0 + 1;
+  const int ntiles = lo_only ? 0 : nb * (nb + 1) / 2;
+
+  if (producer) {
+    TileIt it{J0, J0, Jn};
+    for (int n = 0; n < ntiles; ++n, it.next()) {
+      const int stage = n % NST;
+      if (n >= NST && !mbar_wait_bounded(empty + stage, (uint32_t)(((n / NST) - 1) & 1))) {
+        if (lane == 0) {
+          *abort_flag = 1;
+          atomicOr(d_err, DEVERR_TIMEOUT);
+        }
+        break;
+      }
+      if (*abort_flag) break;
+      issue_tile<float, C>(stage, it.I, it.J, R, c, stages, full);
+      if (lane == 0) *issued_count = n + 1;
+    }
+    __syncwarp();
+  } else {
+    const double dt3 = R.dt3;
+    double diag = 0.0, emem = 0.0;  // for (column loc, orbit jj) of the leapfrog thread
+    bool has_emem = false, aborted = false;
+    const int lf_loc = tid >> 3, lf_j = tid & 7;  // leapfrog thread: column, orbit
+    int n = 0;
+    double pre = 0.0;  // row accumulator of the owned row of the current tile
+    {
+      const int a0 = J0 * T + own_rr;
+      if (a0 >= tmin && a0 <= t - 1) pre = rowacc[(size_t)(a0 % Ma) * KC + own_j];
+    }
+    for (int J = J0; J <= Jn && !aborted; ++J) {
+      double colD[2][4][2];  // [F, rho][k][orbit]: FP64 column sums of this thread
+      V colP[2][4];          // FP32 partials, flushed to colD every 8 tiles
+      for (int k = 0; k < 4; ++k) {
+        colP[0][k] = V::zero();
+        colP[1][k] = V::zero();
+        for (int o = 0; o < 2; ++o) colD[0][k][o] = colD[1][k][o] = 0.0;
+      }
+      int nin = 0;  // tiles of this column block consumed
+      for (int I = lo_only ? Jn + 1 : J; I <= Jn; ++I, ++n, ++nin) {
+        const int stage = n % NST;
+        bool ok = !*cabort && mbar_wait_bounded(full + stage, (uint32_t)((n / NST) & 1));
+        ok = __all_sync(0xffffffffu, ok);
+        if (!ok) {
+          *abort_flag = 1;
+          *cabort = 1;
+          atomicOr(d_err, DEVERR_TIMEOUT);
+          aborted = true;
+          break;
+        }
+        const float *tF = stages + (size_t)stage * C::STAGE;
+        const float *tR = tF + C::TILE;
+        const float *xr_row = tF + 2 * C::TILE;
+        const float *xr_col = xr_row + C::XV;
+        const float *xF_col = xr_col + C::XV;
+        // x of this thread's rows and columns; zero outside the window, half at tmin
+        V xr[4], xc[4], xf[4];
+        bool rv[4], cv[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int a = I * T + 4 * warp + q;
+          rv[q] = (a >= tmin) && (a <= t - 1);
+          xr[q] = V::ld(xr_row + (4 * warp + q) * KC + j0);
+          xr[q].scale(rv[q] ? (a == tmin ? 0.5f : 1.0f) : 0.0f);
+          const int cc = c8 + 8 * q;
+          const int b = J * T + cc;
+          cv[q] = (b >= tmin) && (b <= t - 1);
+          xc[q] = V::ld(xr_col + cc * KC + j0);
+          xf[q] = V::ld(xF_col + cc * KC + j0);
+          const float wb = cv[q] ? (b == tmin ? 0.5f : 1.0f) : 0.0f;
+          xc[q].scale(wb);
+          xf[q].scale(wb);
+        }
+        const bool interior = (I > J) && rv[0] && rv[1] && rv[2] && rv[3] && cv[0] && cv[1] && cv[2] && cv[3];
+        const bool all_interior = __all_sync(0xffffffffu, interior);
+        V rp[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) rp[q] = V::zero();
+        if (all_interior) {
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const int rr = 4 * warp + q;
+            const float *fr = tF + rr * C::RS + j0;
+            const float *qr = tR + rr * C::RS + j0;
+            const int sw = rr & 3;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              const int e = ((c8 + 8 * k) ^ sw) * KC;
+              const V f = V::ld(fr + e), g = V::ld(qr + e);
+              colP[0][k].fma(xr[q], f);
+              colP[1][k].fma(xr[q], g);
+              rp[q].fma(xc[k], f);
+              rp[q].fma(xf[k], g);
+            }
+          }
+        } else {
+          // edge tiles: rows/columns outside the window and, on the diagonal
+          // tile, pairs above it (column sums take a >= b, row sums b < a)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const int rr = 4 * warp + q;
+            const float *fr = tF + rr * C::RS + j0;
+            const float *qr = tR + rr * C::RS + j0;
+            const int sw = rr & 3;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              const int cc = c8 + 8 * k;
+              const int e = (cc ^ sw) * KC;
+              V f = V::ld(fr + e), g = V::ld(qr + e);
+              const bool in = rv[q] && cv[k];
+              const bool vc = in && (I > J || rr >= cc);
+              const bool vr = in && (I > J || rr > cc);
+              const V zero = V::zero();
+              const V fc = vc ? f : zero, gc = vc ? g : zero;
+              const V fw = vr ? f : zero, gw = vr ? g : zero;
+              colP[0][k].fma(xr[q], fc);
+              colP[1][k].fma(xr[q], gc);
+              rp[q].fma(xc[k], fw);
+              rp[q].fma(xf[k], gw);
+            }
+          }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(empty + stage);
+        // reduce-scatter the row sums over the 8 column lanes (lane bits 4, 3, 2)
+        const bool b4 = (lane >> 4) & 1, b3 = (lane >> 3) & 1, b2 = (lane >> 2) & 1;
+        float h[4];  // rows 2*b4 + {0,1}, orbits {0,1}
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+          const V mine = b4 ? rp[2 + i] : rp[i], theirs = b4 ? rp[i] : rp[2 + i];
+          h[2 * i] = mine.v.x + __shfl_xor_sync(0xffffffffu, theirs.v.x, 16);
+          h[2 * i + 1] = mine.v.y + __shfl_xor_sync(0xffffffffu, theirs.v.y, 16);
+        }
+        float g2[2];  // row 2*b4 + b3, orbits {0,1}
+#pragma unroll
+        for (int o = 0; o < 2; ++o) {
+          const float mine = b3 ? h[2 + o] : h[o], theirs = b3 ? h[o] : h[2 + o];
+          g2[o] = mine + __shfl_xor_sync(0xffffffffu, theirs, 8);
+        }
+        const float rsum = (b2 ? g2[1] : g2[0]) + __shfl_xor_sync(0xffffffffu, b2 ? g2[0] : g2[1], 4);
+        // this lane's (row, orbit) accumulator; the next tile's row is loaded one tile ahead
+        {
+          const int a = I * T + own_rr;
+          const double prev = pre;
+          const int an = (I < Jn ? (I + 1) : (J + 1)) * T + own_rr;
+          if (an != a && an >= tmin && an <= t - 1) pre = rowacc[(size_t)(an % Ma) * KC + own_j];
+          if (a >= tmin && a <= t - 1) {
+            const double v = prev + (double)rsum;
+            rowacc[(size_t)(a % Ma) * KC + own_j] = v;
+            if (an == a) pre = v;
+          }
+        }
+        if ((nin & 7) == 7)
+#pragma unroll
+          for (int f = 0; f < 2; ++f)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              colD[f][k][0] += (double)colP[f][k].v.x;
+              colD[f][k][1] += (double)colP[f][k].v.y;
+              colP[f][k] = V::zero();
+            }
+      }
+      // all consumers: the row sums of column block J are complete
+      consumer_sync(NT);
+      if (*cabort) {
+        aborted = true;
+        break;
+      }
+      // column sums of the block: FP64 partials of the 8 warps meet in shared memory
+      double accF = 0.0, accR = 0.0;
+#pragma unroll
+      for (int f = 0; f < 2; ++f) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          double *dst = colbuf + ((size_t)warp * 32 + (c8 + 8 * k)) * KC + j0;
+          dst[0] = colD[f][k][0] + (double)colP[f][k].v.x;
+          dst[1] = colD[f][k][1] + (double)colP[f][k].v.y;
+        }
+        consumer_sync(NT);
+        double s = 0.0;
+#pragma unroll
+        for (int w = 0; w < 8; ++w) s += colbuf[((size_t)w * 32 + lf_loc) * KC + lf_j];
+        if (f == 0) accF = s; else accR = s;
+        consumer_sync(NT);
+      }
+      // leapfrog for t' = b (evolve_r!/evolve_F!, Evolution.jl:890-915)
+      const int b = J * T + lf_loc;
+      if (b >= tmin && b <= t - 1) {
+        const int sb = b % Ma;
+        const double wb = (b == tmin) ? 0.5 : 1.0;
+        const float *sigr = reinterpret_cast<const float *>(R.sig_r) + (size_t)c * rowstride + (size_t)sb * KC;
+        const float *sigF = reinterpret_cast<const float *>(R.sig_F) + (size_t)c * rowstride + (size_t)sb * KC;
+        const size_t cs = (size_t)c * rowstride;
+        const double *F1row = R.st_F + (size_t)((t - 1) % 3) * st_row + cs;
+        const double *F2row = R.st_F + (size_t)((t - 2) % 3) * st_row + cs;
+        const double *R1row = R.st_r + (size_t)((t - 1) % 3) * st_row + cs;
+        const double *R2row = R.st_r + (size_t)((t - 2) % 3) * st_row + cs;
+        double *FNrow = R.st_F + (size_t)(t % 3) * st_row + cs;
+        double *RNrow = R.st_r + (size_t)(t % 3) * st_row + cs;
+        const int j = lf_j;
+        const int k = c * KC + j;
+        const double kk = (k < R.S) ? R.k2[k] : 0.0;
+        const double om = (kk + M2) * R.dt2;
+        const double xbr_d = lo_only ? 0.0 : wb * (double)sigr[j];
+        const double xbF_d = lo_only ? 0.0 : wb * (double)sigF[j];
+        const double aF = accF + rowacc[(size_t)sb * KC + j];
+        const double F1 = F1row[(size_t)sb * KC + j];
+        const double F2 = (b <= t - 2) ? F2row[(size_t)sb * KC + j] : F1row[(size_t)((t - 2) % Ma) * KC + j];
+        const double Fn = (2.0 - om) * F1 - F2 - aF * dt3;
+        double rn;
+        if (b == t - 1) {
+          rn = R.dt;
+        } else {
+          const double r1 = R1row[(size_t)sb * KC + j];
+          const double r2 = R2row[(size_t)sb * KC + j];
+          rn = (2.0 - om) * r1 - r2 - accR * dt3;
+        }
+        FNrow[(size_t)sb * KC + j] = Fn;
+        RNrow[(size_t)sb * KC + j] = rn;
+        const size_t ho = hist_off(Ma, T, c, t, b, j);
+        reinterpret_cast<float *>(R.hist_F)[ho] = (float)Fn;
+        reinterpret_cast<float *>(R.hist_r)[ho] = (float)rn;
+        diag += xbr_d * Fn + xbF_d * rn;
+        if (b == t - 1) {
+          emem = aF;
+          has_emem = true;
+        }
+      }
+    }
+    if (!aborted) {
+      // partial sums of acc_F(t) over this warp's columns, per orbit (lanes sharing lf_j)
+      double v = diag;
+      v += __shfl_xor_sync(0xffffffffu, v, 8);
+      v += __shfl_xor_sync(0xffffffffu, v, 16);
+      if (lane < KC) misc[16 + warp * KC + lane] = v;
+      if (has_emem) misc[2 + lf_j] = emem;
+    }
+  }
+  __syncthreads();
+  if (*abort_flag) {
+    if (tid == 0)
+      for (int q = 0; q < *issued_count; ++q)
+        (void)mbar_wait_bounded(full + (q % NST), (uint32_t)((q / NST) & 1));
+    __syncthreads();
+    return;
+  }
+  if (tid < KC) memint_epilogue<float>(R, c, t, tid, misc, 8, M2, measure);
 }
 
 // t = 2 measurement after initSimData! (Measurement.jl:31-64 with E_mem = 0):
@@ -655,27 +1000,38 @@ using CfgF32 = Cfg<float, 32, 3, 2>;
 
 int memint_tile(bool fp64) { return fp64 ? CfgF64::T : CfgF32::T; }
 
-size_t memint_smem_bytes(bool fp64, int Malloc) {
+// FP32 variants: 1 = two consumer groups (memint_kernel, the default), 0 =
+// register-blocked consumers (memint_blk_kernel: half the shared-memory
+// wavefronts but more instructions per tile; slower on GB300 at Ns = 16..64,
+// where both are latency-bound at about a third of the issue rate). Both stream
+// the same tiles in the same order.
+size_t memint_smem_bytes(bool fp64, int Malloc, int variant) {
   (void)Malloc;
-  return fp64 ? smem_fixed_bytes<CfgF64>() : smem_fixed_bytes<CfgF32>();
+  if (fp64) return smem_fixed_bytes<CfgF64>();
+  return variant == 1 ? smem_fixed_bytes<CfgF32>() : smem_fixed_bytes<CfgF32>() + BLK_COLBUF_BYTES;
 }
 
 cudaError_t configure_memint(bool fp64, size_t smem) {
   if (fp64)
     return cudaFuncSetAttribute(memint_kernel<double, CfgF64::T, CfgF64::NST, CfgF64::OPT>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  return cudaFuncSetAttribute(memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT>,
-                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = cudaFuncSetAttribute(memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(memint_blk_kernel<CfgF32::NST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)smem);
 }
 
-cudaError_t launch_memint(bool fp64, const RunDev *d_runs, const int *d_base, int nruns, int total_ctas,
-                          const int *d_t, int *d_err, int measure, size_t smem, cudaStream_t st) {
+cudaError_t launch_memint(bool fp64, int variant, const RunDev *d_runs, const int *d_base, int nruns,
+                          int total_ctas, const int *d_t, int *d_err, int measure, size_t smem, cudaStream_t st) {
   if (fp64)
     memint_kernel<double, CfgF64::T, CfgF64::NST, CfgF64::OPT>
         <<<total_ctas, CfgF64::NT + 32, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure);
-  else
+  else if (variant == 1)
     memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT>
         <<<total_ctas, CfgF32::NT + 32, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure);
+  else
+    memint_blk_kernel<CfgF32::NST><<<total_ctas, 288, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure);
   return cudaGetLastError();
 }
 

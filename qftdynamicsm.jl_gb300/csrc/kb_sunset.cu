@@ -343,6 +343,19 @@ int sunset_grid(bool fp64, int num_sms, int total_rows) {
   return total_rows < num_sms ? total_rows : num_sms;
 }
 
+int sunset_max_ctas_per_sm(bool fp64, size_t smem) {
+  int n = 0;
+  cudaError_t e = fp64 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sunset_kernel<double, double, true>,
+                                                                       SUN_THREADS, smem)
+                       : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sunset_kernel<float, float, false>,
+                                                                       SUN_THREADS_F32, smem);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return 1;
+  }
+  return n < 1 ? 1 : n;
+}
+
 cudaError_t configure_sunset(bool fp64, size_t smem) {
   if (fp64)
     return cudaFuncSetAttribute(sunset_kernel<double, double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,

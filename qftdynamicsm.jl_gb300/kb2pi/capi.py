@@ -28,7 +28,8 @@ EXPORTS = [
     "kb_site_orbits", "kb_init", "kb_init_rows", "kb_step", "kb_steps", "kb_expand", "kb_measure",
     "kb_get_traces", "kb_get", "kb_set", "kb_self_energies", "kb_get_sigma", "kb_window",
     "kb_checkpoint_size", "kb_checkpoint_save", "kb_checkpoint_restore", "kb_sync",
-    "kb_get_stream", "kb_profile", "kb_profile_read", "kb_adjoint", "kb_sunset_rows_noalloc",
+    "kb_get_stream", "kb_profile", "kb_profile_read", "kb_get_tuning", "kb_set_tuning", "kb_autotune",
+    "kb_adjoint", "kb_sunset_rows_noalloc",
 ]
 
 
@@ -45,6 +46,13 @@ class KbMeasScalars(C.Structure):
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class KbTuning(C.Structure):
+    _fields_ = [("memint_variant", C.c_int32), ("sunset_grid", C.c_int32), ("reserved", C.c_int32 * 2)]
+
+    def as_dict(self):
+        return {"memint_variant": self.memint_variant, "sunset_grid": self.sunset_grid}
 
 
 class KbError(RuntimeError):
@@ -97,6 +105,9 @@ def load_library(path: str | None = None):
             "kb_get_stream": (C.c_int, [vp, P(vp)]),
             "kb_profile": (C.c_int, [vp, i32]),
             "kb_profile_read": (C.c_int, [vp, dp, P(i64)]),
+            "kb_get_tuning": (C.c_int, [vp, P(KbTuning)]),
+            "kb_set_tuning": (C.c_int, [vp, P(KbTuning)]),
+            "kb_autotune": (C.c_int, [vp, i32, P(KbTuning), dp]),
             "kb_adjoint": (C.c_int, [vp, dp, d, i32, dp, d, i32, dp, dp, dp, dp, dp]),
             "kb_sunset_rows_noalloc": (C.c_int, [i32, i32, d, i32, i32, vp, vp, vp, vp, vp]),
         }
@@ -246,6 +257,29 @@ class Handle:
         n = np.zeros(2, np.int64)
         self._check(self.lib.kb_profile_read(self.h, dptr(ms), n.ctypes.data_as(C.POINTER(C.c_int64))))
         return {"sunset": (ms[0], int(n[0])), "memint": (ms[1], int(n[1]))}
+
+    def tuning(self):
+        out = KbTuning()
+        self._check(self.lib.kb_get_tuning(self.h, C.byref(out)))
+        return out.as_dict()
+
+    def set_tuning(self, memint_variant=None, sunset_grid=None):
+        cur = KbTuning()
+        self._check(self.lib.kb_get_tuning(self.h, C.byref(cur)))
+        if memint_variant is not None:
+            cur.memint_variant = int(memint_variant)
+        if sunset_grid is not None:
+            cur.sunset_grid = int(sunset_grid)
+        self._check(self.lib.kb_set_tuning(self.h, C.byref(cur)))
+
+    def autotune(self, trials=3):
+        """Time the candidate launch configurations on the last evolved step; keep the fastest."""
+        out = KbTuning()
+        ms = C.c_double()
+        self._check(self.lib.kb_autotune(self.h, int(trials), C.byref(out), C.byref(ms)))
+        d = out.as_dict()
+        d["ms_per_step"] = ms.value
+        return d
 
     def adjoint(self, n_init, init_mass, t_final, w_n=None, w_E=0.0, ckpt_every=20):
         """Gradients of sum_k w_n[k] n(k, t_final) + w_E E(t_final) (kb_adjoint).
