@@ -147,8 +147,9 @@ def make_handle(precision, device):
 
 def apply_tuning(h, args, fp64=False):
     """Autotune the launch configuration on the filled window (untimed), unless fixed on the command line."""
-    if args.memint_variant is not None or args.sunset_grid is not None:
-        h.set_tuning(memint_variant=None if fp64 else args.memint_variant, sunset_grid=args.sunset_grid)
+    if any(v is not None for v in (args.memint_variant, args.sunset_grid, args.batch_order, args.sunset_variant)):
+        h.set_tuning(memint_variant=None if fp64 else args.memint_variant, sunset_grid=args.sunset_grid,
+                     batch_order=args.batch_order, sunset_variant=None if fp64 else args.sunset_variant)
         d = h.tuning()
         d["source"] = "command line"
         return d
@@ -291,11 +292,19 @@ def run_batched(args):
     t = 2 + fill
     h.steps(t + 1, args.warmup, 0)
     t += args.warmup
+    tuning = apply_tuning(h, args)
     stream = h.stream()
     barrier(ws)
     with ClockSampler(local) as clk:
         ms = timed_graph_steps(h, t + 1, args.steps, stream)
+    t += args.steps
     ms = max_over_ranks(ws, ms)
+    # per-kernel times of a few more steps (events around each launch)
+    h.profile(True)
+    for i in range(3):
+        h.step(t + 1 + i)
+    prof = h.profile_read()
+    h.profile(False)
     if rank != 0:
         return 0
     value = ws * 64 * args.steps / (ms / 1000.0)
@@ -306,7 +315,9 @@ def run_batched(args):
             "data": f"synthetic: thermal states, per-run draws seeded with {args.seed}",
             "config": {"workload": "64 runs, Ns in {16,24,32,48}, lambda U[0.5,8], T U[0.5,3], M U{100..500}, "
                                    "dt=0.05, steps 478..500 of 500", "runs": runs},
-            "clocks": clk.summary(), "gpu_launches": 3 * args.steps}
+            "clocks": clk.summary(), "gpu_launches": 3 * args.steps, "tuning": tuning,
+            "kernels_ms": {"memint": prof["memint"][0] / max(1, prof["memint"][1]),
+                           "sunset": prof["sunset"][0] / max(1, prof["sunset"][1])}}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -542,6 +553,8 @@ def main():
     ap.add_argument("--memint-variant", type=int, default=None,
                     help="fix the mixed-precision memory-integral variant instead of autotuning")
     ap.add_argument("--sunset-grid", type=int, default=None, help="fix the sunset grid instead of autotuning")
+    ap.add_argument("--batch-order", type=int, default=None, help="fix the run order of the batched grids (c3)")
+    ap.add_argument("--sunset-variant", type=int, default=None, help="fix the FP32 sunset variant (0: 1024, 1: 512 threads)")
     args = ap.parse_args()
     if args.config == "c3" and args.impl == "ours":
         return run_batched(args)

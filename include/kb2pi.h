@@ -169,12 +169,15 @@ typedef struct kb_tuning {
   int32_t memint_variant; /* KB_PREC_MIXED: 1 column/row consumer groups (default), 0 register-blocked
                            * consumers; KB_PREC_FP64: 0 (one kernel) */
   int32_t sunset_grid;    /* CTAs of the persistent sunset kernel; 0 = one per SM */
-  int32_t reserved[2];
+  int32_t batch_order;    /* batched handles: 0 runs in order, 1 costliest runs first in both grids */
+  int32_t sunset_variant; /* KB_PREC_MIXED: 0 1024 threads per CTA, 1 512 threads (two CTAs per SM where
+                           * their shared memory fits); KB_PREC_FP64: 0 */
 } kb_tuning;
 int kb_get_tuning(const kb_handle *h, kb_tuning *out);
 int kb_set_tuning(kb_handle *h, const kb_tuning *in);
 /* Autotuner: times every candidate configuration (memory-integral variants;
- * sunset grids of 1..4 CTAs per SM that fit) by re-running the last evolved
+ * sunset variants with grids of 1..4 CTAs per SM that fit; both run orders of a batched
+ * handle) by re-running the last evolved
  * step t -- which reads rows < t and rewrites row t, so the state is unchanged
  * -- `trials` times each, keeps the fastest kernel configurations, re-runs step
  * t once with them and returns the choice and its time per step (ms) if the

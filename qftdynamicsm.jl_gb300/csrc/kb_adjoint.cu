@@ -325,7 +325,7 @@ cudaError_t launch_adjoint_step(const RunDev &R, const AdjBuffers &A, int t, dou
   adj_scalars_kernel<<<1, 256, 0, st>>>(R, t, A);
   const bool nlo = (R.pexp != 0);
   if (nlo) {
-    e = launch_sunset(true, sl.runs, sl.base, sl.nruns, sl.total_rows, sl.grid, sl.d_t, sl.scratch, sl.stride,
+    e = launch_sunset(true, 0, sl.runs, sl.base, sl.nruns, sl.total_rows, sl.grid, sl.d_t, sl.scratch, sl.stride,
                       sl.smem, st);
     if (e != cudaSuccess) return e;
   }

@@ -53,6 +53,8 @@ struct kb_handle {
   size_t smem_sun = 0, smem_mi = 0;
   int num_sms = 0, grid_sun = 0, grid_sun_max = 0;
   int memint_variant = 0;         // FP32 consumer layout of the memory-integral kernel
+  int batch_order = 0;            // order of the runs' CTA ranges in the batched grids
+  int sunset_variant = 0;         // FP32 sunset: 0 1024 threads per CTA, 1 512 threads (2 CTAs per SM)
   void *sun_scratch = nullptr;    // FP64 cosine-transform intermediates, one slot per CTA
   size_t sun_scratch_stride = 0;  // elements per slot
   int t_cur = 0;      // last evolved (or initialised) step; window is [tmin(t_cur), t_cur]
@@ -166,6 +168,50 @@ void gather_host(const std::vector<TS> &chunked, int S, double *out) {
 
 void kb::kb_set_global_error(const char *msg) { g_create_err = msg; }
 
+// Batched grids: run r owns a contiguous range of CTAs (memory integrals: one
+// per chunk) and of persistent-loop items (sunset: one per row t'). The device
+// schedule arrays hold [0, nruns) the first item of each position and
+// [nruns, 2 nruns) the run at that position. order 0 keeps the runs in order;
+// order 1 puts the costliest runs first (memory integrals ~ tiles per chunk,
+// sunset ~ H^4 per row), so the longest CTAs start in the first wave and the
+// cheap ones fill the tail.
+static int apply_schedule(kb_handle *h, int order) {
+  const int nr = (int)h->runs.size();
+  std::vector<int> pos_mi(nr), pos_sun(nr);
+  for (int r = 0; r < nr; ++r) pos_mi[r] = pos_sun[r] = r;
+  if (order == 1) {
+    auto cost_mi = [&](int r) {
+      const double nb = std::ceil((double)h->runs[r].p.M / h->runs[r].T) + 1;
+      return nb * (nb + 1) / 2;
+    };
+    auto cost_sun = [&](int r) { return std::pow((double)h->runs[r].H, 4); };
+    std::stable_sort(pos_mi.begin(), pos_mi.end(), [&](int a, int b) { return cost_mi(a) > cost_mi(b); });
+    std::stable_sort(pos_sun.begin(), pos_sun.end(), [&](int a, int b) { return cost_sun(a) > cost_sun(b); });
+  }
+  std::vector<int> smi(2 * nr), ssun(2 * nr);
+  int bm = 0, bs = 0;
+  for (int q = 0; q < nr; ++q) {
+    Run &Rm = h->runs[pos_mi[q]];
+    smi[q] = bm;
+    smi[nr + q] = pos_mi[q];
+    Rm.dev.cta_base_mi = bm;
+    bm += Rm.nchunks;
+    Run &Rs = h->runs[pos_sun[q]];
+    ssun[q] = bs;
+    ssun[nr + q] = pos_sun[q];
+    Rs.dev.cta_base_sun = bs;
+    bs += Rs.p.M;
+  }
+  std::vector<RunDev> devs(nr);
+  for (int r = 0; r < nr; ++r) devs[r] = h->runs[r].dev;
+  if (cudaMemcpy(h->d_runs, devs.data(), sizeof(RunDev) * nr, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(h->d_base_mi, smi.data(), sizeof(int) * 2 * nr, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(h->d_base_sun, ssun.data(), sizeof(int) * 2 * nr, cudaMemcpyHostToDevice) != cudaSuccess)
+    return KB_ERR_CUDA;
+  h->batch_order = order;
+  return KB_OK;
+}
+
 // ------------------------------------------------------------------------
 extern "C" {
 
@@ -201,7 +247,6 @@ int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out) {
   h->runs.resize(nruns);
   size_t smem_sun = 0, smem_mi = 0;
   int base_sun = 0, base_mi = 0;
-  std::vector<int> bsun(nruns), bmi(nruns);
   for (int r = 0; r < nruns; ++r) {
     Run &R = h->runs[r];
     R.p = p[r];
@@ -211,8 +256,6 @@ int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out) {
     R.esz = h->fp64 ? 8 : 4;
     smem_sun = std::max(smem_sun, kb::sunset_smem_bytes(h->fp64, R.H));
     smem_mi = std::max({smem_mi, kb::memint_smem_bytes(h->fp64, R.Malloc, 0), kb::memint_smem_bytes(h->fp64, R.Malloc, 1)});
-    bsun[r] = base_sun;
-    bmi[r] = base_mi;
     base_sun += R.p.M;
     base_mi += R.nchunks;
     if (R.p.pexp != KB_PEXP_LO) h->any_nlo = true;
@@ -291,14 +334,10 @@ int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out) {
     D.meas = R.meas;
     D.epart = R.epart;
     D.rowacc = R.rowacc;
-    D.cta_base_sun = bsun[r];
-    D.cta_base_mi = bmi[r];
   }
-  std::vector<RunDev> devs(nruns);
-  for (int r = 0; r < nruns; ++r) devs[r] = h->runs[r].dev;
   bool ok = cudaMalloc(&h->d_runs, sizeof(RunDev) * nruns) == cudaSuccess &&
-            cudaMalloc(&h->d_base_sun, sizeof(int) * nruns) == cudaSuccess &&
-            cudaMalloc(&h->d_base_mi, sizeof(int) * nruns) == cudaSuccess &&
+            cudaMalloc(&h->d_base_sun, sizeof(int) * 2 * nruns) == cudaSuccess &&
+            cudaMalloc(&h->d_base_mi, sizeof(int) * 2 * nruns) == cudaSuccess &&
             cudaMalloc(&h->d_t, sizeof(int)) == cudaSuccess && cudaMalloc(&h->d_err, sizeof(int)) == cudaSuccess;
   if (!ok) {
     cudaGetLastError();
@@ -308,9 +347,11 @@ int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out) {
   }
   cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
   h->grid_sun = kb::sunset_grid(h->fp64, h->num_sms, h->total_sun);
-  cudaMemcpy(h->d_runs, devs.data(), sizeof(RunDev) * nruns, cudaMemcpyHostToDevice);
-  cudaMemcpy(h->d_base_sun, bsun.data(), sizeof(int) * nruns, cudaMemcpyHostToDevice);
-  cudaMemcpy(h->d_base_mi, bmi.data(), sizeof(int) * nruns, cudaMemcpyHostToDevice);
+  if (apply_schedule(h, 0) != KB_OK) {  // runs in order
+    fail(nullptr, KB_ERR_CUDA, "upload of the run table failed");
+    kb_destroy(h);
+    return KB_ERR_CUDA;
+  }
   cudaMemset(h->d_t, 0, sizeof(int));
   cudaMemset(h->d_err, 0, sizeof(int));
   // the attribute is per kernel, shared by all handles: allow the device maximum
@@ -322,8 +363,11 @@ int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out) {
     return KB_ERR_CUDA;
   }
   // the largest sunset grid the tuner may pick: up to 4 resident CTAs per SM
-  h->grid_sun_max = std::max(1, std::min(h->total_sun, h->num_sms * std::min(4, kb::sunset_max_ctas_per_sm(
-                                                                                    h->fp64, h->smem_sun))));
+  {
+    int per_sm = kb::sunset_max_ctas_per_sm(h->fp64, 0, h->smem_sun);
+    if (!h->fp64) per_sm = std::max(per_sm, kb::sunset_max_ctas_per_sm(false, 1, h->smem_sun));
+    h->grid_sun_max = std::max(1, std::min(h->total_sun, h->num_sms * std::min(4, per_sm)));
+  }
   if (h->fp64 && h->any_nlo) {
     int Hmax = 1;
     for (auto &R : h->runs) Hmax = std::max(Hmax, R.H);
@@ -480,7 +524,7 @@ static int launch_step(kb_handle *h, int measure) {
     KB_CUDA(h, cudaEventRecord(e0, h->st));
   }
   if (h->any_nlo)
-    KB_CUDA(h, kb::launch_sunset(h->fp64, h->d_runs, h->d_base_sun, (int)h->runs.size(), h->total_sun, h->grid_sun,
+    KB_CUDA(h, kb::launch_sunset(h->fp64, h->sunset_variant, h->d_runs, h->d_base_sun, (int)h->runs.size(), h->total_sun, h->grid_sun,
                                  h->d_t, h->sun_scratch, h->sun_scratch_stride, h->smem_sun, h->st));
   if (h->profiling) {
     KB_CUDA(h, cudaEventRecord(e1, h->st));
@@ -616,7 +660,7 @@ int kb_self_energies(kb_handle *h, int32_t tmone) {
   cudaSetDevice(h->device);
   KB_CUDA(h, kb::launch_set_t(h->d_t, h->t_cur, h->st));
   if (h->any_nlo)
-    KB_CUDA(h, kb::launch_sunset(h->fp64, h->d_runs, h->d_base_sun, (int)h->runs.size(), h->total_sun, h->grid_sun,
+    KB_CUDA(h, kb::launch_sunset(h->fp64, h->sunset_variant, h->d_runs, h->d_base_sun, (int)h->runs.size(), h->total_sun, h->grid_sun,
                                  h->d_t, h->sun_scratch, h->sun_scratch_stride, h->smem_sun, h->st));
   h->sigma_valid = true;
   return kb_sync(h);
@@ -854,6 +898,8 @@ int kb_get_tuning(const kb_handle *h, kb_tuning *out) {
   *out = kb_tuning{};
   out->memint_variant = h->memint_variant;
   out->sunset_grid = h->grid_sun;
+  out->batch_order = h->batch_order;
+  out->sunset_variant = h->sunset_variant;
   return KB_OK;
 }
 
@@ -865,7 +911,20 @@ int kb_set_tuning(kb_handle *h, const kb_tuning *in) {
   if (g < 1 || g > h->grid_sun_max)
     return fail(h, KB_ERR_PARAM, "sunset_grid=%d: at most %d CTAs fit on this device", in->sunset_grid,
                 h->grid_sun_max);
+  if (in->sunset_variant < 0 || in->sunset_variant > 1 || (h->fp64 && in->sunset_variant != 0))
+    return fail(h, KB_ERR_PARAM, "sunset_variant=%d: 0 or 1, and 0 for KB_PREC_FP64", in->sunset_variant);
+  if (in->sunset_grid != 0 &&
+      in->sunset_grid > h->num_sms * kb::sunset_max_ctas_per_sm(h->fp64, in->sunset_variant, h->smem_sun) * 4)
+    return fail(h, KB_ERR_PARAM, "sunset_grid=%d: too large for this variant", in->sunset_grid);
+  if (in->batch_order < 0 || in->batch_order > 1)
+    return fail(h, KB_ERR_PARAM, "batch_order=%d: 0 (runs in order) or 1 (costliest first)", in->batch_order);
+  cudaSetDevice(h->device);
+  int rc = kb_sync(h);
+  if (rc) return rc;
+  if (in->batch_order != h->batch_order && apply_schedule(h, in->batch_order) != KB_OK)
+    return fail(h, KB_ERR_CUDA, "upload of the run schedule failed");
   h->memint_variant = in->memint_variant;
+  h->sunset_variant = in->sunset_variant;
   h->grid_sun = g;
   if (h->graph) {  // captured with the old configuration
     cudaGraphExecDestroy(h->graph);
@@ -883,15 +942,16 @@ int kb_autotune(kb_handle *h, int32_t trials, kb_tuning *chosen, double *ms_per_
   const int t = h->t_cur;
   cudaEvent_t e[3];
   for (auto &x : e) KB_CUDA(h, cudaEventCreate(&x));
-  auto time_cfg = [&](int variant, int grid, float *ms_sun, float *ms_mi) -> int {
+  auto time_cfg = [&](int variant, int svar, int grid, float *ms_sun, float *ms_mi) -> int {
     h->memint_variant = variant;
+    h->sunset_variant = svar;
     h->grid_sun = grid;
     float best_s = 1e30f, best_m = 1e30f;
     for (int q = 0; q < trials; ++q) {
       KB_CUDA(h, kb::launch_set_t(h->d_t, t, h->st));
       KB_CUDA(h, cudaEventRecord(e[0], h->st));
       if (h->any_nlo)
-        KB_CUDA(h, kb::launch_sunset(h->fp64, h->d_runs, h->d_base_sun, (int)h->runs.size(), h->total_sun,
+        KB_CUDA(h, kb::launch_sunset(h->fp64, h->sunset_variant, h->d_runs, h->d_base_sun, (int)h->runs.size(), h->total_sun,
                                      h->grid_sun, h->d_t, h->sun_scratch, h->sun_scratch_stride, h->smem_sun, h->st));
       KB_CUDA(h, cudaEventRecord(e[1], h->st));
       KB_CUDA(h, kb::launch_memint(h->fp64, h->memint_variant, h->d_runs, h->d_base_mi, (int)h->runs.size(),
@@ -908,31 +968,62 @@ int kb_autotune(kb_handle *h, int32_t trials, kb_tuning *chosen, double *ms_per_
     *ms_mi = best_m;
     return KB_OK;
   };
-  // sunset grids: 1..4 CTAs per SM as far as they fit; memint variants: FP32 only
-  std::vector<int> grids;
-  for (int k = 1; k <= 4; ++k) {
-    const int g = std::min(h->total_sun, k * h->num_sms);
-    if (g <= h->grid_sun_max && (grids.empty() || g != grids.back())) grids.push_back(g);
+  // sunset variants x grids of 1..4 resident CTAs per SM; memint variants:
+  // FP32 only; run orders: batched handles only
+  std::vector<std::pair<int, int>> sun_cands;  // (variant, grid)
+  for (int sv = 0; sv < (h->fp64 ? 1 : 2); ++sv) {
+    const int occ = std::min(4, kb::sunset_max_ctas_per_sm(h->fp64, sv, h->smem_sun));
+    int last = -1;
+    for (int k = 1; k <= occ; ++k) {
+      const int g = std::min(h->total_sun, k * h->num_sms);
+      if (g <= h->grid_sun_max && g != last) sun_cands.push_back({sv, g});
+      last = g;
+    }
   }
-  if (grids.empty()) grids.push_back(h->grid_sun);
+  if (sun_cands.empty()) sun_cands.push_back({h->sunset_variant, h->grid_sun});
   const int nvar = h->fp64 ? 1 : 2;
-  int best_g = grids[0], best_v = 0;
-  float bs = 1e30f, bm = 1e30f;
-  for (int g : grids) {
-    float ms_s, ms_m;
-    if ((rc = time_cfg(0, g, &ms_s, &ms_m))) break;
-    if (ms_s < bs) { bs = ms_s; best_g = g; }
-    if (g == grids[0]) bm = ms_m;
-  }
-  for (int v = 1; v < nvar && !rc; ++v) {
-    float ms_s, ms_m;
-    if ((rc = time_cfg(v, best_g, &ms_s, &ms_m))) break;
-    if (ms_m < bm) { bm = ms_m; best_v = v; }
+  const int norder = h->runs.size() > 1 ? 2 : 1;
+  const int v0 = h->fp64 ? 0 : 1;  // default memint variant first
+  int best_o = h->batch_order, best_v = v0;
+  std::pair<int, int> best_sc = sun_cands[0];
+  float best_total = 1e30f, best_s_all = 0, best_m_all = 0;
+  for (int o = 0; o < norder && !rc; ++o) {
+    const int order = (norder == 1) ? h->batch_order : o;
+    if (order != h->batch_order && apply_schedule(h, order) != KB_OK) {
+      rc = fail(h, KB_ERR_CUDA, "upload of the run schedule failed");
+      break;
+    }
+    std::pair<int, int> sc_o = sun_cands[0];
+    int v_o = v0;
+    float bs = 1e30f, bm = 1e30f;
+    for (size_t q = 0; q < sun_cands.size(); ++q) {
+      float ms_s, ms_m;
+      if ((rc = time_cfg(v0, sun_cands[q].first, sun_cands[q].second, &ms_s, &ms_m))) break;
+      if (ms_s < bs) { bs = ms_s; sc_o = sun_cands[q]; }
+      if (q == 0) bm = ms_m;
+    }
+    for (int v = 0; v < nvar && !rc; ++v) {
+      if (v == v0) continue;
+      float ms_s, ms_m;
+      if ((rc = time_cfg(v, sc_o.first, sc_o.second, &ms_s, &ms_m))) break;
+      if (ms_m < bm) { bm = ms_m; v_o = v; }
+    }
+    if (!rc && bs + bm < best_total) {
+      best_total = bs + bm;
+      best_o = order;
+      best_sc = sc_o;
+      best_v = v_o;
+      best_s_all = bs;
+      best_m_all = bm;
+    }
   }
   for (auto &x : e) cudaEventDestroy(x);
   if (rc) return rc;
+  if (best_o != h->batch_order && apply_schedule(h, best_o) != KB_OK)
+    return fail(h, KB_ERR_CUDA, "upload of the run schedule failed");
   h->memint_variant = best_v;
-  h->grid_sun = best_g;
+  h->sunset_variant = best_sc.first;
+  h->grid_sun = best_sc.second;
   if (h->graph) {
     cudaGraphExecDestroy(h->graph);
     h->graph = nullptr;
@@ -942,7 +1033,7 @@ int kb_autotune(kb_handle *h, int32_t trials, kb_tuning *chosen, double *ms_per_
   if ((rc = launch_step(h, 1))) return rc;
   if ((rc = kb_sync(h))) return rc;
   if (chosen) kb_get_tuning(h, chosen);
-  if (ms_per_step) *ms_per_step = (double)(bs + bm);
+  if (ms_per_step) *ms_per_step = (double)(best_s_all + best_m_all);
   return KB_OK;
 }
 

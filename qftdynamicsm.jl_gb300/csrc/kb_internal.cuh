@@ -62,22 +62,25 @@ __host__ __device__ inline size_t hist_off(int Malloc, int T, int c, int a, int 
   return ((((size_t)c * nbA + sa / T) * nbA + sb / T) * T + ra) * (size_t)T * KC + (size_t)((cb ^ (ra & 3)) * KC + j);
 }
 
-__device__ inline int find_run(const int *base, int nruns, int bid) {
+// Batched grids: sched[0, nruns) is the first item (CTA or row) of each
+// position, increasing; sched[nruns, 2 nruns) the run at that position.
+__device__ inline int run_at(const int *sched, int nruns, int item) {
   int lo = 0, hi = nruns - 1;
   while (lo < hi) {
     int mid = (lo + hi + 1) >> 1;
-    if (base[mid] <= bid) lo = mid; else hi = mid - 1;
+    if (sched[mid] <= item) lo = mid; else hi = mid - 1;
   }
-  return lo;
+  return sched[nruns + lo];
 }
 
 // host launchers (kb_sunset.cu, kb_memint.cu)
-cudaError_t launch_sunset(bool fp64, const RunDev *d_runs, const int *d_base, int nruns, int total_rows, int grid,
-                          const int *d_t, void *scratch, size_t scratch_stride, size_t smem, cudaStream_t st);
+cudaError_t launch_sunset(bool fp64, int variant, const RunDev *d_runs, const int *d_base, int nruns,
+                          int total_rows, int grid, const int *d_t, void *scratch, size_t scratch_stride, size_t smem,
+                          cudaStream_t st);
 size_t sunset_smem_bytes(bool fp64, int H);
 size_t sunset_scratch_elems(int H);
 int sunset_grid(bool fp64, int num_sms, int total_rows);
-int sunset_max_ctas_per_sm(bool fp64, size_t smem);
+int sunset_max_ctas_per_sm(bool fp64, int variant, size_t smem);
 cudaError_t configure_sunset(bool fp64, size_t smem);
 cudaError_t launch_memint(bool fp64, int variant, const RunDev *d_runs, const int *d_base, int nruns,
                           int total_ctas, const int *d_t, int *d_err, int measure, size_t smem, cudaStream_t st);

@@ -293,7 +293,7 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   volatile int *cabort = reinterpret_cast<volatile int *>(misc + 12);
   static_assert(16 + (C::NG / 32) * KC <= 128, "misc scratch too small");
 
-  const int r = find_run(base, nruns, blockIdx.x);
+  const int r = run_at(base, nruns, blockIdx.x);
   const RunDev &R = runs[r];
   const int c = blockIdx.x - R.cta_base_mi;  // chunk
   const int tid = threadIdx.x;
@@ -613,7 +613,7 @@ memint_blk_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base,
   volatile int *issued_count = reinterpret_cast<volatile int *>(misc + 11);
   volatile int *cabort = reinterpret_cast<volatile int *>(misc + 12);
 
-  const int r = find_run(base, nruns, blockIdx.x);
+  const int r = run_at(base, nruns, blockIdx.x);
   const RunDev &R = runs[r];
   const int c = blockIdx.x - R.cta_base_mi;  // chunk
   const int tid = threadIdx.x;

@@ -229,8 +229,9 @@ __device__ void sun_transform(const SunCtx<TC> &c, In in, Out out) {
   __syncthreads();
 }
 
-template <typename TC, typename TS, bool SCRATCH>
-__global__ void __launch_bounds__(SCRATCH ? SUN_THREADS : SUN_THREADS_F32, 1)
+// NTHR threads per CTA; MINB resident CTAs per SM the register budget allows
+template <typename TC, typename TS, bool SCRATCH, int NTHR, int MINB>
+__global__ void __launch_bounds__(NTHR, MINB)
 sunset_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int nruns, int total,
               const int *__restrict__ d_t, TC *__restrict__ scratch, size_t scratch_stride) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -238,7 +239,7 @@ sunset_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   int cur_run = -1;
   SunCtx<TC> c{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, SunGeom(1)};
   for (int w = blockIdx.x; w < total; w += gridDim.x) {
-    const int r = find_run(base, nruns, w);
+    const int r = run_at(base, nruns, w);
     const RunDev &R = runs[r];
     const int tmin = max(1, t - R.M + 1);
     const int tp = tmin + (w - R.cta_base_sun);
@@ -343,12 +344,20 @@ int sunset_grid(bool fp64, int num_sms, int total_rows) {
   return total_rows < num_sms ? total_rows : num_sms;
 }
 
-int sunset_max_ctas_per_sm(bool fp64, size_t smem) {
+// Kernel variants: FP64 (512 threads, global scratch); FP32 0: 1024 threads,
+// 1 CTA per SM (the whole Ns = 64 octant in shared memory); FP32 1: 512 threads
+// with registers for 2 CTAs per SM, which hide each other's barrier waits when
+// the shared memory of two fits (Ns <= 48).
+#define KB_SUNSET_F64 sunset_kernel<double, double, true, SUN_THREADS, 1>
+#define KB_SUNSET_F32 sunset_kernel<float, float, false, SUN_THREADS_F32, 1>
+#define KB_SUNSET_F32_HALF sunset_kernel<float, float, false, SUN_THREADS, 2>
+
+int sunset_max_ctas_per_sm(bool fp64, int variant, size_t smem) {
   int n = 0;
-  cudaError_t e = fp64 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sunset_kernel<double, double, true>,
-                                                                       SUN_THREADS, smem)
-                       : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sunset_kernel<float, float, false>,
-                                                                       SUN_THREADS_F32, smem);
+  cudaError_t e = fp64 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, KB_SUNSET_F64, SUN_THREADS, smem)
+                  : variant == 1
+                      ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, KB_SUNSET_F32_HALF, SUN_THREADS, smem)
+                      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, KB_SUNSET_F32, SUN_THREADS_F32, smem);
   if (e != cudaSuccess) {
     cudaGetLastError();
     return 1;
@@ -357,22 +366,23 @@ int sunset_max_ctas_per_sm(bool fp64, size_t smem) {
 }
 
 cudaError_t configure_sunset(bool fp64, size_t smem) {
-  if (fp64)
-    return cudaFuncSetAttribute(sunset_kernel<double, double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)smem);
-  return cudaFuncSetAttribute(sunset_kernel<float, float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)smem);
+  if (fp64) return cudaFuncSetAttribute(KB_SUNSET_F64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = cudaFuncSetAttribute(KB_SUNSET_F32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(KB_SUNSET_F32_HALF, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
-cudaError_t launch_sunset(bool fp64, const RunDev *d_runs, const int *d_base, int nruns, int total_rows, int grid,
-                          const int *d_t, void *scratch, size_t scratch_stride, size_t smem, cudaStream_t st) {
+cudaError_t launch_sunset(bool fp64, int variant, const RunDev *d_runs, const int *d_base, int nruns,
+                          int total_rows, int grid, const int *d_t, void *scratch, size_t scratch_stride, size_t smem,
+                          cudaStream_t st) {
   if (total_rows <= 0 || grid <= 0) return cudaSuccess;
   if (fp64)
-    sunset_kernel<double, double, true><<<grid, SUN_THREADS, smem, st>>>(
-        d_runs, d_base, nruns, total_rows, d_t, reinterpret_cast<double *>(scratch), scratch_stride);
+    KB_SUNSET_F64<<<grid, SUN_THREADS, smem, st>>>(d_runs, d_base, nruns, total_rows, d_t,
+                                                   reinterpret_cast<double *>(scratch), scratch_stride);
+  else if (variant == 1)
+    KB_SUNSET_F32_HALF<<<grid, SUN_THREADS, smem, st>>>(d_runs, d_base, nruns, total_rows, d_t, nullptr, 0);
   else
-    sunset_kernel<float, float, false><<<grid, SUN_THREADS_F32, smem, st>>>(d_runs, d_base, nruns, total_rows, d_t,
-                                                                             nullptr, 0);
+    KB_SUNSET_F32<<<grid, SUN_THREADS_F32, smem, st>>>(d_runs, d_base, nruns, total_rows, d_t, nullptr, 0);
   return cudaGetLastError();
 }
 

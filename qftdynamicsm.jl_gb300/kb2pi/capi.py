@@ -49,10 +49,12 @@ class KbMeasScalars(C.Structure):
 
 
 class KbTuning(C.Structure):
-    _fields_ = [("memint_variant", C.c_int32), ("sunset_grid", C.c_int32), ("reserved", C.c_int32 * 2)]
+    _fields_ = [("memint_variant", C.c_int32), ("sunset_grid", C.c_int32), ("batch_order", C.c_int32),
+                ("sunset_variant", C.c_int32)]
 
     def as_dict(self):
-        return {"memint_variant": self.memint_variant, "sunset_grid": self.sunset_grid}
+        return {"memint_variant": self.memint_variant, "sunset_grid": self.sunset_grid,
+                "batch_order": self.batch_order, "sunset_variant": self.sunset_variant}
 
 
 class KbError(RuntimeError):
@@ -263,13 +265,17 @@ class Handle:
         self._check(self.lib.kb_get_tuning(self.h, C.byref(out)))
         return out.as_dict()
 
-    def set_tuning(self, memint_variant=None, sunset_grid=None):
+    def set_tuning(self, memint_variant=None, sunset_grid=None, batch_order=None, sunset_variant=None):
         cur = KbTuning()
         self._check(self.lib.kb_get_tuning(self.h, C.byref(cur)))
         if memint_variant is not None:
             cur.memint_variant = int(memint_variant)
         if sunset_grid is not None:
             cur.sunset_grid = int(sunset_grid)
+        if batch_order is not None:
+            cur.batch_order = int(batch_order)
+        if sunset_variant is not None:
+            cur.sunset_variant = int(sunset_variant)
         self._check(self.lib.kb_set_tuning(self.h, C.byref(cur)))
 
     def autotune(self, trials=3):
