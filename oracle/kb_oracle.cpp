@@ -19,6 +19,7 @@
 #include <functional>
 #include <stdexcept>
 #include <thread>
+#include <type_traits>
 #include <vector>
 
 namespace {
@@ -733,6 +734,285 @@ struct Oracle {
   }
 };
 
+// ---------------------------------------------------------------------------
+// Forward-mode derivatives (the stand-in for ForwardDiff through the reference,
+// which cannot run here): dual numbers carrying K directional derivatives
+// through a templated restatement of the orbit/octant engine above -- the same
+// ring (mod1 slots, thesign), the same evolve! order of operations, the same
+// octant sunset and createMeasurement -- single-threaded, orbit values only.
+// ---------------------------------------------------------------------------
+template <int K>
+struct Dual {
+  double v = 0.0;
+  double d[K] = {};
+  Dual() = default;
+  Dual(double x) : v(x) {}  // NOLINT: constants promote to duals
+  friend Dual operator+(const Dual &a, const Dual &b) {
+    Dual r(a.v + b.v);
+    for (int k = 0; k < K; ++k) r.d[k] = a.d[k] + b.d[k];
+    return r;
+  }
+  friend Dual operator-(const Dual &a, const Dual &b) {
+    Dual r(a.v - b.v);
+    for (int k = 0; k < K; ++k) r.d[k] = a.d[k] - b.d[k];
+    return r;
+  }
+  friend Dual operator-(const Dual &a) {
+    Dual r(-a.v);
+    for (int k = 0; k < K; ++k) r.d[k] = -a.d[k];
+    return r;
+  }
+  friend Dual operator*(const Dual &a, const Dual &b) {
+    Dual r(a.v * b.v);
+    for (int k = 0; k < K; ++k) r.d[k] = a.d[k] * b.v + a.v * b.d[k];
+    return r;
+  }
+  friend Dual operator/(const Dual &a, const Dual &b) {
+    Dual r(a.v / b.v);
+    for (int k = 0; k < K; ++k) r.d[k] = (a.d[k] * b.v - a.v * b.d[k]) / (b.v * b.v);
+    return r;
+  }
+  Dual &operator+=(const Dual &b) { return *this = *this + b; }
+  Dual &operator-=(const Dual &b) { return *this = *this - b; }
+  Dual &operator*=(const Dual &b) { return *this = *this * b; }
+};
+template <int K>
+Dual<K> dsqrt(const Dual<K> &a) {
+  Dual<K> r(std::sqrt(a.v));
+  for (int k = 0; k < K; ++k) r.d[k] = a.d[k] / (2.0 * r.v);
+  return r;
+}
+inline double val(double x) { return x; }
+template <int K>
+double val(const Dual<K> &x) {
+  return x.v;
+}
+
+template <class T>
+struct DualEngine {
+  orc_params p{};
+  Orbits orb;
+  int S = 0, M = 0, tmin = 0, tmax = 0;
+  T lam, mass2;
+  std::vector<std::vector<T>> Fst, rst, SigF, Sigr;
+  std::vector<T> omega2;
+  T hm2;
+  std::vector<double> Coct;
+
+  int mod1(int i) const { return ((i - 1) % M + M) % M + 1; }
+  double thesign(int i, int j) const { return mod1(i) >= mod1(j) ? 1.0 : -1.0; }
+  size_t slot(int i, int j) const {
+    int a = mod1(i) - 1, b = mod1(j) - 1;
+    if (a < b) std::swap(a, b);
+    return (size_t)a * (a + 1) / 2 + b;
+  }
+  std::vector<T> &F(int i, int j) { return Fst[slot(i, j)]; }
+  std::vector<T> &r(int i, int j) { return rst[slot(i, j)]; }
+  std::vector<T> &sF(int z) { return SigF[mod1(z) - 1]; }
+  std::vector<T> &sr(int z) { return Sigr[mod1(z) - 1]; }
+
+  void setup(const orc_params &pp, T lam_, T mass2_) {
+    p = pp;
+    orb.build(p.Ns, 3);
+    S = orb.S;
+    M = p.M;
+    lam = lam_;
+    mass2 = mass2_;
+    Fst.assign((size_t)M * (M + 1) / 2, std::vector<T>(S, T(1.0)));
+    rst.assign((size_t)M * (M + 1) / 2, std::vector<T>(S, T(1.0)));
+    SigF.assign(M, std::vector<T>(S, T(0.0)));
+    Sigr.assign(M, std::vector<T>(S, T(0.0)));
+    omega2.assign(S, T(0.0));
+    Coct = octant_matrix(p.Ns);
+  }
+  void expand() {
+    if (tmax + 1 > M) {
+      tmin += 1;
+      tmax += 1;
+    } else {
+      tmin = 1;
+      tmax += 1;
+    }
+  }
+  T pref() const { return lam * T((double)(p.N + 2) / (double)(6 * p.N)); }
+  double ivol() const { return 1.0 / (double)orb.V; }
+  T hartree(int a, int b) {
+    T h(0.0);
+    const std::vector<T> &f = F(a, b);
+    for (int o = 0; o < S; ++o) h += f[o] * T((double)orb.deg[o]);
+    return h * (pref() * T(ivol())) + mass2;
+  }
+  void octant(std::vector<T> &a, std::vector<T> &tmp) {
+    const int H = orb.H;
+    const long npt = (long)H * H * H;
+    long stride = 1;
+    for (int d = 0; d < 3; ++d) {
+      for (long q = 0; q < npt; ++q) {
+        const long xi = (q / stride) % H, base = q - xi * stride;
+        T acc(0.0);
+        for (int x = 0; x < H; ++x) acc += T(Coct[(size_t)xi * H + x]) * a[base + (long)x * stride];
+        tmp[q] = acc;
+      }
+      std::swap(a, tmp);
+      stride *= H;
+    }
+  }
+  void sunset(const std::vector<T> &Fin, const std::vector<T> &rin, std::vector<T> &oF, std::vector<T> &orr) {
+    const int H = orb.H;
+    const long npt = (long)H * H * H;
+    std::vector<T> fa(npt), ra(npt), tmp(npt);
+    for (long q = 0; q < npt; ++q) {
+      int g[3] = {(int)(q % H), (int)((q / H) % H), (int)(q / ((long)H * H))};
+      std::sort(g, g + 3);
+      const long o = Orbits::tri_index(3, g[0], g[1], g[2]);
+      fa[q] = Fin[o];
+      ra[q] = rin[o];
+    }
+    octant(fa, tmp);
+    octant(ra, tmp);
+    const double iv = ivol(), Nn = (double)p.N;
+    const T lam2 = lam * lam;
+    const T fr = T(iv * iv * iv) * (-lam2 * T((Nn + 2.0) / (6.0 * Nn * Nn)));
+    const T fF = T(iv * iv * iv) * (-lam2 * T((Nn + 2.0) / (18.0 * Nn * Nn)));
+    const bool classical = (p.pexp == ORC_PEXP_NLO_CLASSICAL);
+    for (long q = 0; q < npt; ++q) {
+      const T rx = ra[q], Fx = fa[q];
+      ra[q] = classical ? rx * (Fx * Fx) : rx * (Fx * Fx - T(1 / 12.) * (rx * rx));
+      fa[q] = classical ? Fx * (Fx * Fx) : Fx * (Fx * Fx - T(0.75) * (rx * rx));
+    }
+    octant(fa, tmp);
+    octant(ra, tmp);
+    for (int o = 0; o < S; ++o) {
+      const long q = (long)orb.rep[3 * o] + (long)orb.rep[3 * o + 1] * H + (long)orb.rep[3 * o + 2] * H * H;
+      orr[o] = fr * ra[q];
+      oF[o] = fF * fa[q];
+    }
+  }
+  void self_energies(int tmone) {
+    if (p.pexp == ORC_PEXP_LO) return;
+    std::vector<T> rs(S);
+    for (int tp = tmin; tp <= tmax - 1; ++tp) {
+      const double sg = thesign(tmone, tp);
+      const std::vector<T> &rr = r(tmone, tp);
+      for (int o = 0; o < S; ++o) rs[o] = rr[o] * T(sg);
+      sunset(F(tmone, tp), rs, sF(tp), sr(tp));
+    }
+  }
+  void rhs_r(std::vector<T> &Mem, int t, int tp) {
+    for (auto &x : Mem) x = T(0.0);
+    if (p.pexp == ORC_PEXP_LO) return;
+    for (int z = tp + 1; z <= t - 2; ++z) {
+      const double sg = thesign(z, tp);
+      for (int o = 0; o < S; ++o) Mem[o] -= sr(z)[o] * r(z, tp)[o] * T(sg);
+    }
+  }
+  void rhs_F(std::vector<T> &Mem, int t, int tp) {
+    if (p.pexp == ORC_PEXP_LO) {
+      for (auto &x : Mem) x = T(0.0);
+      return;
+    }
+    for (int o = 0; o < S; ++o) Mem[o] = sr(tmin)[o] * F(tmin, tp)[o] * T(-0.5);
+    for (int z = tmin + 1; z <= t - 2; ++z)
+      for (int o = 0; o < S; ++o) Mem[o] -= sr(z)[o] * F(z, tp)[o];
+    {
+      const double sg = thesign(tmin, tp);
+      for (int o = 0; o < S; ++o) Mem[o] += T(0.5) * sF(tmin)[o] * r(tmin, tp)[o] * T(sg);
+    }
+    for (int z = tmin + 1; z <= tp - 1; ++z) {
+      const double sg = thesign(z, tp);
+      for (int o = 0; o < S; ++o) Mem[o] += sF(z)[o] * r(z, tp)[o] * T(sg);
+    }
+  }
+  void evolve_r(std::vector<T> &R, int t, int tp) {
+    std::vector<T> &out = r(t, tp);
+    const double st = thesign(t, tp);
+    if (tp == t - 1) {
+      for (auto &x : out) x = T(st * p.dt);
+    } else if (tp == t) {
+      for (auto &x : out) x = T(0.0);
+    } else {
+      const double dt3 = p.dt * p.dt * p.dt, s1 = thesign(t - 1, tp), s2 = thesign(t - 2, tp);
+      for (int o = 0; o < S; ++o) {
+        const T rhs = R[o] * T(dt3);
+        out[o] = ((T(2.0) - omega2[o]) * r(t - 1, tp)[o] * T(s1) - r(t - 2, tp)[o] * T(s2) + rhs) * T(st);
+      }
+    }
+  }
+  void evolve_F(std::vector<T> &R, int t, int tp) {
+    const double dt3 = p.dt * p.dt * p.dt;
+    std::vector<T> &out = F(t, tp);
+    for (int o = 0; o < S; ++o)
+      out[o] = (T(2.0) - omega2[o]) * F(t - 1, tp)[o] - F(t - 2, tp)[o] + R[o] * T(dt3);
+  }
+  void evolve(int t) {
+    expand();
+    self_energies(t - 1);
+    hm2 = hartree(t - 1, t - 1);
+    for (int o = 0; o < S; ++o) omega2[o] = (T(orb.k2[o]) + hm2) * T(p.dt * p.dt);
+    std::vector<T> R(S);
+    for (int tp = tmin; tp <= tmax - 1; ++tp) {
+      rhs_r(R, t, tp);
+      evolve_r(R, t, tp);
+      rhs_F(R, t, tp);
+      evolve_F(R, t, tp);
+    }
+    evolve_r(R, t, t);
+    rhs_F(R, t, t);
+    evolve_F(R, t, t);
+  }
+  void init(const std::vector<T> &n, double initmass) {
+    expand();
+    expand();
+    for (int o = 0; o < S; ++o) {
+      const double om = std::sqrt(orb.k2[o] + initmass * initmass);
+      F(1, 1)[o] = T(1 / om) * (n[o] + T(0.5));
+      F(2, 1)[o] = T(1 / om) * (n[o] + T(0.5));
+      F(2, 2)[o] = T(om) * (n[o] + T(0.5)) * T(p.dt * p.dt) + T(1 / om) * (n[o] + T(0.5));
+      r(1, 1)[o] = T(0.0);
+      r(2, 1)[o] = T(p.dt * thesign(2, 1));
+      r(2, 2)[o] = T(0.0);
+    }
+    hm2 = hartree(2, 2);
+  }
+  // createMeasurement: L = sum_o w_n[o] n_o + w_E E at t
+  T loss(int t, const double *w_n, double w_E) {
+    const double dt = p.dt;
+    T E_kin(0.0), E_pot(0.0), E_mem(0.0), hc(0.0), Lw(0.0);
+    std::vector<T> ddF(S);
+    for (int o = 0; o < S; ++o) {
+      const T Fmm = F(t - 1, t - 1)[o];
+      ddF[o] = (F(t, t)[o] - T(2.0) * F(t - 1, t)[o] + Fmm) / T(dt * dt);
+      const T ow2 = ddF[o] / Fmm;
+      const T om = val(ow2) > 0 ? dsqrt_any(ow2) : T(0.0);
+      const T c = (0.25 * dt * dt * val(om * om) < 1) ? dsqrt_any(T(1.0) - T(0.25 * dt * dt) * (om * om)) : T(1.0);
+      const T nn = (val(ddF[o] * Fmm) > 0) ? c * dsqrt_any(ddF[o] * Fmm) - T(0.5) : T(0.0);
+      if (w_n) Lw += T(w_n[o]) * nn;
+      E_kin += T(0.5) * ddF[o] * T((double)orb.deg[o]);
+      hc += Fmm * T((double)orb.deg[o]);
+    }
+    for (int o = 0; o < S; ++o)
+      E_pot += T(0.5) * (mass2 + T(orb.k2[o]) + T(0.5 * ivol()) * pref() * hc) * F(t - 1, t - 1)[o] *
+               T((double)orb.deg[o]);
+    if (t != 2) {
+      const int tp0 = tmin;
+      const double s = thesign(tp0, t - 1);
+      for (int o = 0; o < S; ++o)
+        E_mem += T(0.5 * 0.25 * dt * (double)orb.deg[o]) *
+                 (sr(tp0)[o] * F(tp0, t - 1)[o] - sF(tp0)[o] * r(tp0, t - 1)[o] * T(s));
+      for (int o = 0; o < S; ++o)
+        for (int tp = tp0 + 1; tp <= t - 2; ++tp) {
+          const double st = thesign(tp, t - 1);
+          E_mem += T(0.25 * dt * (double)orb.deg[o]) * (sr(tp)[o] * F(tp, t - 1)[o] - sF(tp)[o] * r(tp, t - 1)[o] * T(st));
+        }
+    }
+    return Lw + T(w_E) * (E_kin + E_pot + E_mem);
+  }
+  static T dsqrt_any(const T &x) {
+    if constexpr (std::is_same<T, double>::value) return std::sqrt(x);
+    else return dsqrt(x);
+  }
+};
+
 template <class Fn>
 int guarded(Fn f) {
   try {
@@ -864,6 +1144,31 @@ int orc_sunset_rows(void *h, const double *F, const double *rho, double *sig_F, 
     } else {
       o->sunset_rows(F, rho, sig_F, sig_r, o->scratch[0]);
     }
+  });
+}
+
+// Forward-mode loss derivatives (dual numbers, K = 3 directions: lambda,
+// m^2 and the occupation direction dn)
+int orc_dual_loss(const orc_params *p, const double *n_init, double init_mass, int32_t t_final, const double *w_n,
+                  double w_E, const double *dn, double *L, double *dL) {
+  return guarded([&] {
+    using D = Dual<3>;
+    if (p->sdim != 3 || t_final < 3) throw std::invalid_argument("sdim 3 and t_final >= 3");
+    DualEngine<D> e;
+    D lam(p->lambda), m2(p->mass2);
+    lam.d[0] = 1.0;
+    m2.d[1] = 1.0;
+    e.setup(*p, lam, m2);
+    std::vector<D> n(e.S);
+    for (int o = 0; o < e.S; ++o) {
+      n[o] = D(n_init[o]);
+      n[o].d[2] = dn ? dn[o] : 0.0;
+    }
+    e.init(n, init_mass);
+    for (int t = 3; t <= t_final; ++t) e.evolve(t);
+    const D l = e.loss(t_final, w_n, w_E);
+    *L = l.v;
+    for (int k = 0; k < 3; ++k) dL[k] = l.d[k];
   });
 }
 

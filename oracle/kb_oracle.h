@@ -108,6 +108,15 @@ double orc_gap_mass(void *h, const double *n_orbit, double x0);
 int orc_sunset_rows(void *h, const double *F, const double *rho, double *sig_F,
                     double *sig_r);
 
+/* Forward-mode derivatives through a templated restatement of the orbit/octant
+ * engine with dual numbers (the stand-in for ForwardDiff through the Julia
+ * reference): L = sum_o w_n[o] n(o, t_final) + w_E E(t_final) for the run
+ * orc_init_occupation(n_init, init_mass) + orc_step(3..t_final), and
+ * dL[0] = dL/dlambda, dL[1] = dL/dm^2, dL[2] = sum_o dL/dn_init[o] dn[o].
+ * sdim = 3; single-threaded; w_n and dn may be NULL. */
+int orc_dual_loss(const orc_params *p, const double *n_init, double init_mass, int32_t t_final,
+                  const double *w_n, double w_E, const double *dn, double *L, double *dL);
+
 #ifdef __cplusplus
 }
 #endif

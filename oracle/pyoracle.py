@@ -76,6 +76,7 @@ def _lib():
             lib.orc_gap_mass.restype = d
             lib.orc_sunset_rows.argtypes = [C.c_void_p, P(d), P(d), P(d), P(d)]
             lib.orc_step_times.argtypes = [C.c_void_p, P(d), P(d)]
+            lib.orc_dual_loss.argtypes = [P(OracleParams), P(d), d, i32, P(d), d, P(d), P(d), P(d)]
             _LIB = lib
     return _LIB
 
@@ -87,6 +88,23 @@ def _dp(a):
 def _check(rc, what):
     if rc != 0:
         raise RuntimeError(f"oracle {what} failed with code {rc}")
+
+
+def dual_loss(Ns, M, n_init, init_mass, t_final, w_n=None, w_E=0.0, dn=None, N=4, dt=0.1, lam=1.0, mass2=1.0,
+              mass=1.0, pexp=PEXP_NLO_QUANTUM):
+    """Forward-mode (dual-number) derivatives of L = sum w_n n(t_final) + w_E E(t_final):
+    returns (L, dL/dlambda, dL/dm^2, dL/dn_init . dn) from the templated orbit/octant engine."""
+    lib = _lib()
+    p = OracleParams(Ns=Ns, sdim=3, M=M, N=N, pexp=pexp, engine=ENGINE_OCTANT, nthreads=1, pad_=0, dt=dt,
+                     lam=lam, mass2=mass2, mass=mass)
+    n0 = np.ascontiguousarray(n_init, dtype=np.float64)
+    wn = None if w_n is None else np.ascontiguousarray(w_n, dtype=np.float64)
+    d = None if dn is None else np.ascontiguousarray(dn, dtype=np.float64)
+    L = C.c_double()
+    dL = np.zeros(3)
+    _check(lib.orc_dual_loss(C.byref(p), _dp(n0), float(init_mass), int(t_final), _dp(wn), float(w_E), _dp(d),
+                             C.byref(L), _dp(dL)), "dual_loss")
+    return L.value, dL[0], dL[1], dL[2]
 
 
 class Oracle:

@@ -175,3 +175,23 @@ def test_torch_function_backward():
     e[3] = 1.0
     fd_a = central(lambda s: gpu_loss(cfg, (amps.detach().numpy() + s * e) @ B, 20, wn, 1.0), 0.0)
     assert rel(amps.grad[3].item(), fd_a) <= TOL
+
+
+@pytest.mark.parametrize("pexp", [1, 2, 0])
+def test_adjoint_matches_dual_number_oracle(pexp):
+    """Exact derivatives on both sides: the GPU adjoint against forward-mode dual
+    numbers through the CPU oracle (the stand-in for ForwardDiff through the
+    reference), to 1e-8 relative -- far below what finite differences resolve."""
+    from oracle.pyoracle import dual_loss
+
+    cfg = dict(BASE, Ns=8, M=9, lam=2.5, pexp=pexp)
+    tf, wE, ckpt = 26, 0.6, 4
+    _, _, n0, wn = setup(cfg, 21 + pexp)
+    dn = np.random.default_rng(31).random(len(n0)) - 0.3
+    g = adjoint(cfg, n0, tf, wn, wE, ckpt)
+    L, dlam, dm2, ddn = dual_loss(cfg["Ns"], cfg["M"], n0, 1.0, tf, wn, wE, dn, N=cfg["N"], dt=cfg["dt"],
+                                  lam=cfg["lam"], mass2=cfg["mass2"], pexp=pexp)
+    assert abs(g["loss"] - L) <= 1e-11 * abs(L)
+    assert abs(g["lambda"] - dlam) <= 1e-8 * abs(dlam) + 1e-12
+    assert abs(g["mass2"] - dm2) <= 1e-8 * abs(dm2)
+    assert abs(np.dot(g["n_init"], dn) - ddn) <= 1e-8 * abs(ddn)

@@ -12,6 +12,7 @@ import numpy as np
 import pytest
 
 from oracle import ENGINE_FULL, ENGINE_OCTANT, ENGINE_ORBIT, PEXP_LO, PEXP_NLO_CLASSICAL, Oracle
+from kbtest_util import make_oracle, thermal_n
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
@@ -180,3 +181,43 @@ def test_gap_mass_newton():
     pref = 4.0 * 6 / 24
     g = np.sum((n + 0.5) * deg / np.sqrt(k2 + m_or ** 2)) / 16 ** 3 * pref + 1.0 - m_or ** 2
     assert abs(g) < 1e-12
+
+
+def _loss_plain(cfg, n0, tf, wn, wE):
+    o = make_oracle(cfg)
+    o.init_occupation(n0, 1.0)
+    for t in range(3, tf + 1):
+        o.step(t)
+    m = o.measure(tf)
+    o.close()
+    return float(np.dot(wn, m["n"]) + wE * m["E"])
+
+
+@pytest.mark.parametrize("pexp", [1, 2, 0])
+def test_dual_oracle_values_and_derivatives(pexp):
+    """The dual-number engine reproduces the plain oracle's loss and its central
+    finite differences (forward-mode derivatives pinned by FD on the oracle)."""
+    from oracle.pyoracle import dual_loss
+
+    cfg = dict(Ns=6, M=8, N=4, lam=2.0, dt=0.1, mass2=1.0, pexp=pexp)
+    o = make_oracle(cfg)
+    _, k2, deg = o.orbits()
+    o.close()
+    rng = np.random.default_rng(7 + pexp)
+    n0 = thermal_n(k2, 1.5)
+    wn = rng.random(len(k2)) * deg / deg.sum()
+    dn = rng.random(len(k2))
+    tf, wE = 20, 0.7
+    L, dlam, dm2, ddn = dual_loss(cfg["Ns"], cfg["M"], n0, 1.0, tf, wn, wE, dn, N=4, dt=0.1, lam=2.0, mass2=1.0,
+                                  pexp=pexp)
+    L0 = _loss_plain(cfg, n0, tf, wn, wE)
+    assert abs(L - L0) <= 1e-12 * abs(L0)
+    h = 1e-5
+    fl = (_loss_plain(dict(cfg, lam=2.0 + h * 2), n0, tf, wn, wE) - _loss_plain(dict(cfg, lam=2.0 - h * 2), n0, tf,
+                                                                               wn, wE)) / (4 * h)
+    fm = (_loss_plain(dict(cfg, mass2=1.0 + h), n0, tf, wn, wE) - _loss_plain(dict(cfg, mass2=1.0 - h), n0, tf, wn,
+                                                                             wE)) / (2 * h)
+    fn = (_loss_plain(cfg, n0 + h * dn, tf, wn, wE) - _loss_plain(cfg, n0 - h * dn, tf, wn, wE)) / (2 * h)
+    assert abs(dlam - fl) <= 1e-6 * max(abs(fl), 1e-8) + 1e-10
+    assert abs(dm2 - fm) <= 1e-6 * abs(fm)
+    assert abs(ddn - fn) <= 1e-6 * abs(fn)
