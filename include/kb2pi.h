@@ -138,6 +138,18 @@ int kb_get_sigma(kb_handle *h, int32_t run, int32_t which, int32_t z, double *ou
 /* simdata.indices after the last step: [tmin, tmax] */
 int kb_window(const kb_handle *h, int32_t run, int32_t *tmin, int32_t *tmax);
 
+/* Device measurement stream: evolves t0 .. t0+count-1 like kb_steps, and every
+ * step with (t - 2) % measure_every == 0 (measure! of the reference's drivers,
+ * G_SimulationArgs.jl:96-101) appends its createMeasurement record
+ * (TwoPIScalar_Measurement.jl:31-99) to a device buffer from inside the
+ * captured step graph; the host reads all records once at the end. Record m of
+ * run r: out[m * nruns + r] (scalars) and, if arrays is not NULL, the per-orbit
+ * F, ddF, n, omega, c at arrays + m * sum_r 5 S_r + sum_{r' < r} 5 S_r'
+ * (each S_r values). Fails with KB_ERR_PARAM if more than capacity steps are
+ * measured; *n_recorded (if not NULL) receives the number recorded. */
+int kb_steps_recorded(kb_handle *h, int32_t t0, int32_t count, int32_t measure_every, kb_meas_scalars *out,
+                      double *arrays, int32_t capacity, int32_t *n_recorded);
+
 /* Snapshot of the full state (history, self-energies, window) into a host
  * buffer and back; replaces the serialisation the reference could not do
  * ("Serialization broke because of pointers in simdata", G_SimulationArgs.jl:117). */

@@ -63,6 +63,13 @@ struct kb_handle {
   bool sigma_valid = false;
   cudaGraphExec_t graph = nullptr;
   int graph_measure = -1;
+  // device measurement stream (kb_steps_recorded): step graph with the record
+  // kernel, control block {first t, every, capacity}, per-run record offsets
+  cudaGraphExec_t graph_rec = nullptr;
+  int *d_rec_ctl = nullptr;
+  long long *d_rec_off = nullptr;
+  double *d_rec = nullptr;
+  size_t rec_cap_doubles = 0;
   // profiling: event pairs around each kernel launch, summed on read
   bool profiling = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -394,6 +401,10 @@ void kb_destroy(kb_handle *h) {
   cudaSetDevice(h->device);
   if (h->st) cudaStreamSynchronize(h->st);
   if (h->graph) cudaGraphExecDestroy(h->graph);
+  if (h->graph_rec) cudaGraphExecDestroy(h->graph_rec);
+  if (h->d_rec_ctl) cudaFree(h->d_rec_ctl);
+  if (h->d_rec_off) cudaFree(h->d_rec_off);
+  if (h->d_rec) cudaFree(h->d_rec);
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
   for (auto &R : h->runs) free_run(R);
   void *ptrs[] = {h->d_runs, h->d_base_sun, h->d_base_mi, h->d_t, h->d_err, h->sun_scratch};
@@ -778,6 +789,105 @@ int kb_steps(kb_handle *h, int32_t t0, int32_t count, int32_t measure_every, kb_
   return kb_sync(h);
 }
 
+// Device measurement stream: count steps from a captured graph that also
+// appends the measurement of every measured step to a device buffer; one
+// copy to the host at the end (createMeasurement records, Measurement.jl:31-99).
+int kb_steps_recorded(kb_handle *h, int32_t t0, int32_t count, int32_t measure_every, kb_meas_scalars *out,
+                      double *arrays, int32_t capacity, int32_t *n_recorded) {
+  if (!h || count < 0 || measure_every < 1 || capacity < 0) return KB_ERR_PARAM;
+  if (h->t_cur < 2) return fail(h, KB_ERR_PARAM, "kb_steps_recorded before kb_init");
+  if (t0 != h->t_cur + 1)
+    return fail(h, KB_ERR_PARAM, "kb_steps_recorded(t0=%d): expected t0 = %d", t0, h->t_cur + 1);
+  if (n_recorded) *n_recorded = 0;
+  if (count == 0) return KB_OK;
+  cudaSetDevice(h->device);
+  const int nr = (int)h->runs.size();
+  // measured steps: (t - 2) % measure_every == 0 (the reference's NstepsbetweenNmeas)
+  const int rem = ((t0 - 2) % measure_every + measure_every) % measure_every;
+  const int tf = t0 + (rem == 0 ? 0 : measure_every - rem);
+  const int t_last = t0 + count - 1;
+  const int nmeas = (tf <= t_last) ? (t_last - tf) / measure_every + 1 : 0;
+  if (nmeas > capacity)
+    return fail(h, KB_ERR_PARAM, "kb_steps_recorded: %d measurements, capacity %d", nmeas, capacity);
+  std::vector<long long> off(nr);
+  long long block = 0;
+  for (int r = 0; r < nr; ++r) {
+    off[r] = block;
+    block += 6 + 5LL * h->runs[r].S;
+  }
+  const size_t need = (size_t)std::max(1, nmeas) * (size_t)block;
+  if (!h->d_rec_ctl) {
+    if (cudaMalloc(&h->d_rec_ctl, 4 * sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&h->d_rec_off, sizeof(long long) * nr) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(h, KB_ERR_OOM, "kb_steps_recorded: cudaMalloc of the control block failed");
+    }
+    KB_CUDA(h, cudaMemcpy(h->d_rec_off, off.data(), sizeof(long long) * nr, cudaMemcpyHostToDevice));
+  }
+  if (need > h->rec_cap_doubles) {
+    if (h->graph_rec) {  // the graph holds the old buffer's address
+      cudaGraphExecDestroy(h->graph_rec);
+      h->graph_rec = nullptr;
+    }
+    KB_CUDA(h, cudaStreamSynchronize(h->st));
+    if (h->d_rec) cudaFree(h->d_rec);
+    h->d_rec = nullptr;
+    h->rec_cap_doubles = 0;
+    if (cudaMalloc(&h->d_rec, need * sizeof(double)) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(h, KB_ERR_OOM, "kb_steps_recorded: cudaMalloc of %zu record bytes failed", need * sizeof(double));
+    }
+    h->rec_cap_doubles = need;
+  }
+  const int ctl[4] = {tf, measure_every, nmeas, 0};
+  KB_CUDA(h, cudaMemcpyAsync(h->d_rec_ctl, ctl, sizeof ctl, cudaMemcpyHostToDevice, h->st));
+  if (!h->graph_rec) {
+    cudaGraph_t g;
+    const bool prof = h->profiling;  // no profiling events inside the graph
+    h->profiling = false;
+    KB_CUDA(h, cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+    int rc = launch_step(h, 1);
+    h->profiling = prof;
+    cudaError_t ea = cudaSuccess;
+    if (rc == 0) ea = kb::launch_record(h->d_runs, nr, h->d_t, h->d_rec_ctl, h->d_rec, h->d_rec_off, block, h->st);
+    if (rc == 0 && ea == cudaSuccess) ea = kb::launch_advance_t(h->d_t, h->st);
+    cudaError_t ec = cudaStreamEndCapture(h->st, &g);
+    if (rc) return rc;
+    if (ea != cudaSuccess || ec != cudaSuccess) return fail(h, KB_ERR_CUDA, "graph capture failed");
+    cudaError_t ei = cudaGraphInstantiate(&h->graph_rec, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) return fail(h, KB_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(ei));
+  }
+  KB_CUDA(h, kb::launch_set_t(h->d_t, t0, h->st));
+  for (int i = 0; i < count; ++i) KB_CUDA(h, cudaGraphLaunch(h->graph_rec, h->st));
+  h->t_cur = t_last;
+  h->sigma_valid = h->any_nlo;
+  std::vector<double> host((size_t)nmeas * block);
+  if (nmeas > 0)
+    KB_CUDA(h, cudaMemcpyAsync(host.data(), h->d_rec, host.size() * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  int rc = kb_sync(h);
+  if (rc) return rc;
+  size_t aoff = 0;
+  for (int m = 0; m < nmeas; ++m)
+    for (int r = 0; r < nr; ++r) {
+      const double *rec = host.data() + (size_t)m * block + off[r];
+      if (out) {
+        kb_meas_scalars &o = out[(size_t)m * nr + r];
+        o.time = rec[0];
+        o.E = rec[1];
+        o.E_pot = rec[2];
+        o.E_kin = rec[3];
+        o.E_mem = rec[4];
+        o.M2 = rec[5];
+      }
+      const size_t n5 = 5 * (size_t)h->runs[r].S;
+      if (arrays) std::memcpy(arrays + aoff, rec + 6, n5 * sizeof(double));
+      aoff += n5;
+    }
+  if (n_recorded) *n_recorded = nmeas;
+  return KB_OK;
+}
+
 int kb_get_stream(const kb_handle *h, void **stream) {
   if (!h || !stream) return KB_ERR_PARAM;
   *stream = (void *)h->st;
@@ -930,6 +1040,10 @@ int kb_set_tuning(kb_handle *h, const kb_tuning *in) {
     cudaGraphExecDestroy(h->graph);
     h->graph = nullptr;
   }
+  if (h->graph_rec) {
+    cudaGraphExecDestroy(h->graph_rec);
+    h->graph_rec = nullptr;
+  }
   return KB_OK;
 }
 
@@ -1027,6 +1141,10 @@ int kb_autotune(kb_handle *h, int32_t trials, kb_tuning *chosen, double *ms_per_
   if (h->graph) {
     cudaGraphExecDestroy(h->graph);
     h->graph = nullptr;
+  }
+  if (h->graph_rec) {
+    cudaGraphExecDestroy(h->graph_rec);
+    h->graph_rec = nullptr;
   }
   // step t once more with the chosen kernels, so the state is theirs
   KB_CUDA(h, kb::launch_set_t(h->d_t, t, h->st));

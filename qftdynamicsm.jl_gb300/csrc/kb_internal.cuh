@@ -89,6 +89,8 @@ cudaError_t configure_memint(bool fp64, size_t smem);
 int memint_tile(bool fp64);
 cudaError_t launch_measure_init(const RunDev *d_runs, int nruns, int t, cudaStream_t st);
 cudaError_t launch_set_t(int *d_t, int t, cudaStream_t st);
+cudaError_t launch_record(const RunDev *d_runs, int nruns, const int *d_t, const int *d_ctl, double *rec,
+                          const long long *d_off, long long block, cudaStream_t st);
 cudaError_t launch_advance_t(int *d_t, cudaStream_t st);
 // adjoint of the sunset (kb_sunset.cu), FP64 handles only
 size_t sunset_adjoint_smem_bytes(int H);

@@ -990,6 +990,45 @@ __global__ void measure_init_kernel(const RunDev *__restrict__ runs, int nruns, 
   }
 }
 
+// Device measurement stream: after a step t with (t - 2) % every == 0, one
+// block per run appends the createMeasurement record of that step -- the
+// scalars (time, E, E_pot, E_kin, E_mem, M2, summed over chunks in order as
+// kb_measure does on the host) and the per-orbit F, ddF, n, omega, c -- to a
+// device buffer, so a captured multi-step graph needs no host round trip.
+// ctl = {first measured t, every, capacity}; record m of run r starts at
+// rec + m * block + off[r] and holds 6 + 5 S doubles.
+__global__ void record_kernel(const RunDev *__restrict__ runs, const int *__restrict__ d_t,
+                              const int *__restrict__ ctl, double *__restrict__ rec,
+                              const long long *__restrict__ off, long long block) {
+  const int t = *d_t;
+  const int tf = ctl[0], every = ctl[1], cap = ctl[2];
+  if (t < tf || (t - tf) % every != 0) return;
+  const int m = (t - tf) / every;
+  if (m >= cap) return;
+  const RunDev &R = runs[blockIdx.x];
+  double *out = rec + (long long)m * block + off[blockIdx.x];
+  if (threadIdx.x == 0) {
+    double ek = 0, ep = 0, em = 0;
+    for (int c = 0; c < R.nchunks; ++c) {
+      ek += R.epart[(size_t)c * 4 + 0];
+      ep += R.epart[(size_t)c * 4 + 1];
+      em += R.epart[(size_t)c * 4 + 2];
+    }
+    if (t == 2) em = 0.0;
+    out[0] = (t - 1) * R.dt * R.mass;
+    out[1] = ek + ep + em;
+    out[2] = ep;
+    out[3] = ek;
+    out[4] = em;
+    out[5] = R.epart[3];
+  }
+  const int Sp = R.nchunks * KC;
+  for (int i = threadIdx.x; i < 5 * R.S; i += blockDim.x) {
+    const int q = i / R.S, k = i - q * R.S;
+    out[6 + i] = R.meas[(size_t)q * Sp + k];
+  }
+}
+
 __global__ void set_t_kernel(int *d_t, int t) { *d_t = t; }
 __global__ void advance_t_kernel(int *d_t) { *d_t += 1; }
 
@@ -1037,6 +1076,11 @@ cudaError_t launch_memint(bool fp64, int variant, const RunDev *d_runs, const in
 
 cudaError_t launch_measure_init(const RunDev *d_runs, int nruns, int t, cudaStream_t st) {
   measure_init_kernel<<<nruns, 256, 0, st>>>(d_runs, nruns, t);
+  return cudaGetLastError();
+}
+cudaError_t launch_record(const RunDev *d_runs, int nruns, const int *d_t, const int *d_ctl, double *rec,
+                          const long long *d_off, long long block, cudaStream_t st) {
+  record_kernel<<<nruns, 256, 0, st>>>(d_runs, d_t, d_ctl, rec, d_off, block);
   return cudaGetLastError();
 }
 cudaError_t launch_set_t(int *d_t, int t, cudaStream_t st) {

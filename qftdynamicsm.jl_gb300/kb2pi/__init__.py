@@ -8,5 +8,6 @@ from . import adjoint, capi  # noqa: F401
 from .capi import Handle, KbError, KbParams, load_library  # noqa: F401
 from .twopiscalar import (  # noqa: F401
     QFTdynamicsProblem, QFTdynamicsSolution, TwoPIScalarfile, createMeasurement, evolve, getGapMass,
-    getparticlenr, initialize, lattice_orbits, make_problem, measure, run_simulation,
+    evolve_recorded, getparticlenr, initialize, lattice_orbits, load_measurearray, make_problem, measure,
+    run_simulation, save_measurearray,
 )

@@ -28,7 +28,7 @@ EXPORTS = [
     "kb_site_orbits", "kb_init", "kb_init_rows", "kb_step", "kb_steps", "kb_expand", "kb_measure",
     "kb_get_traces", "kb_get", "kb_set", "kb_self_energies", "kb_get_sigma", "kb_window",
     "kb_checkpoint_size", "kb_checkpoint_save", "kb_checkpoint_restore", "kb_sync",
-    "kb_get_stream", "kb_profile", "kb_profile_read", "kb_get_tuning", "kb_set_tuning", "kb_autotune",
+    "kb_get_stream", "kb_profile", "kb_profile_read", "kb_steps_recorded", "kb_get_tuning", "kb_set_tuning", "kb_autotune",
     "kb_adjoint", "kb_sunset_rows_noalloc",
 ]
 
@@ -107,6 +107,7 @@ def load_library(path: str | None = None):
             "kb_get_stream": (C.c_int, [vp, P(vp)]),
             "kb_profile": (C.c_int, [vp, i32]),
             "kb_profile_read": (C.c_int, [vp, dp, P(i64)]),
+            "kb_steps_recorded": (C.c_int, [vp, i32, i32, i32, P(KbMeasScalars), dp, i32, P(i32)]),
             "kb_get_tuning": (C.c_int, [vp, P(KbTuning)]),
             "kb_set_tuning": (C.c_int, [vp, P(KbTuning)]),
             "kb_autotune": (C.c_int, [vp, i32, P(KbTuning), dp]),
@@ -189,6 +190,36 @@ class Handle:
         out = (KbMeasScalars * cap)()
         self._check(self.lib.kb_steps(self.h, int(t0), int(count), int(measure_every), out, cap))
         return [[out[r * nm + i].as_dict() for i in range(nm)] for r in range(self.nruns)]
+
+    def steps_recorded(self, t0, count, measure_every, arrays=True):
+        """kb_steps_recorded: evolve count steps from t0 with the measurements of every
+        measure_every-th step recorded on the device; returns per measured step a list
+        (one dict per run) of the scalars and, with arrays=True, F, ddF, n, omega, c."""
+        rem = (t0 - 2) % measure_every
+        tf = t0 + (0 if rem == 0 else measure_every - rem)
+        nmeas = max(0, (t0 + count - 1 - tf) // measure_every + 1) if tf <= t0 + count - 1 else 0
+        cap = max(1, nmeas)
+        out = (KbMeasScalars * (cap * self.nruns))()
+        per = [5 * S for S in self.S]
+        arr = np.zeros(cap * sum(per)) if arrays else None
+        nrec = C.c_int32()
+        self._check(self.lib.kb_steps_recorded(self.h, int(t0), int(count), int(measure_every), out, dptr(arr),
+                                               int(cap), C.byref(nrec)))
+        res = []
+        off = 0
+        for m in range(nrec.value):
+            row = []
+            for r in range(self.nruns):
+                d = out[m * self.nruns + r].as_dict()
+                d["t"] = tf + m * measure_every
+                if arrays:
+                    a = arr[off:off + per[r]].reshape(5, self.S[r])
+                    for q, k in enumerate(("F", "ddF", "n", "omega", "c")):
+                        d[k] = a[q].copy()
+                off += per[r]
+                row.append(d)
+            res.append(row)
+        return res
 
     def expand(self):
         self._check(self.lib.kb_expand(self.h))

@@ -309,14 +309,81 @@ def measure(thesolution: QFTdynamicsSolutionTwoPIScalar, t: int) -> None:
     thesolution.measurearray[int((t - 2) / ss.NstepsbetweenNmeas)] = createMeasurement(t, thesolution)
 
 
-def run_simulation(parameters: dict, evolveto: int | None = None, device: int = 0):
-    """TwoPIScalar_testevolution (TwoPIScalar_Testhelpers.jl:27-48) on the GPU numerics."""
+def evolve_recorded(thesolution: QFTdynamicsSolutionTwoPIScalar, tlast: int) -> None:
+    """evolve! from lastEvolStep + 1 to tlast with measure! of every NstepsbetweenNmeas-th
+    step taken from the device measurement stream (kb_steps_recorded): one graph launch per
+    step and a single host read at the end. The records carry the scalars and per-orbit
+    arrays of createMeasurement; the site-1 traces are only available for the last step."""
+    ss = thesolution.problem.simsetup
+    h = thesolution.simdata.handle
+    t0 = ss.lastEvolStep + 1
+    if tlast < t0:
+        return
+    for row in h.steps_recorded(t0, tlast - t0 + 1, ss.NstepsbetweenNmeas):
+        m = row[0]
+        t = m.pop("t")
+        m["r"] = np.zeros_like(m["F"])
+        thesolution.measurearray[int((t - 2) / ss.NstepsbetweenNmeas)] = m
+    ss.lastEvolStep = tlast
+    if (tlast - 2) % ss.NstepsbetweenNmeas == 0:
+        thesolution.measurearray[int((tlast - 2) / ss.NstepsbetweenNmeas)].update(h.traces(0))
+
+
+def run_simulation(parameters: dict, evolveto: int | None = None, device: int = 0, stream: bool = False):
+    """TwoPIScalar_testevolution (TwoPIScalar_Testhelpers.jl:27-48) on the GPU numerics.
+    stream=True takes the measurements from the device measurement stream."""
     problem = make_problem(TwoPIScalarfile(), parameters)
     sol, tmp = QFTdynamicsSolution(TwoPIScalarfile(), problem, device)
     initialize(sol, tmp)
     last = evolveto if evolveto is not None else problem.simsetup.Nsteps + 2
+    if stream:
+        evolve_recorded(sol, last)
+        return sol
     for t in range(problem.simsetup.lastEvolStep + 1, last + 1):
         evolve(sol, tmp, t)
         if (t - 2) % problem.simsetup.NstepsbetweenNmeas == 0:
             measure(sol, t)
     return sol
+
+
+# Measurearray serialisation. The reference saves Vector{MeasurementTwoPIScalar}
+# with JLD (G_SimulationArgs.jl); here each record keeps its MeasurementTwoPIScalar
+# field names (TwoPIScalar_Measurement.jl:2-23) in one .npz archive, with the
+# simulation parameters as JSON, so analysis code can read GPU runs field by field.
+MEASUREMENT_FIELDS = ("time", "E", "E_pot", "E_kin", "E_mem", "M2", "F", "ddF", "n", "omega", "c", "r",
+                      "Fonet", "ronet", "SigF", "Sigr")
+
+
+def save_measurearray(path: str, thesolution: QFTdynamicsSolutionTwoPIScalar, parameters: dict | None = None):
+    import json
+
+    arrays = {"parameters": np.array(json.dumps(parameters or {}))}
+    count = 0
+    for i, m in enumerate(thesolution.measurearray):
+        if m is None:
+            continue
+        count += 1
+        for k in MEASUREMENT_FIELDS:
+            if k in m:
+                arrays[f"{i}/{k}"] = np.asarray(m[k])
+    arrays["indices"] = np.array([i for i, m in enumerate(thesolution.measurearray) if m is not None], dtype=np.int64)
+    np.savez(path, **arrays)
+    return count
+
+
+def load_measurearray(path: str):
+    """Returns (measurearray, parameters): a list with None where nothing was measured."""
+    import json
+
+    z = np.load(path, allow_pickle=False)
+    idx = [int(i) for i in z["indices"]]
+    out = [None] * ((max(idx) + 1) if idx else 0)
+    for i in idx:
+        rec = {}
+        for k in MEASUREMENT_FIELDS:
+            key = f"{i}/{k}"
+            if key in z.files:
+                v = z[key]
+                rec[k] = float(v) if v.ndim == 0 else v
+        out[i] = rec
+    return out, json.loads(str(z["parameters"]))

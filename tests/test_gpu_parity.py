@@ -340,3 +340,49 @@ def test_batched_config3_style(precision):
         if r < 3:
             assert mb["E"] == alone[r].measure(0, t)["E"]
             assert np.array_equal(mb["n"], alone[r].measure(0, t)["n"])
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_device_measurement_stream(precision, tmp_path):
+    """kb_steps_recorded: the measurements recorded on the device inside the step
+    graph equal kb_measure after single steps, bitwise; the host mirror's
+    stream path fills the same measurearray, which round-trips through save/load."""
+    import kb2pi
+
+    cfg = dict(Ns=10, M=30, N=4, lam=3.0, dt=0.1, pexp=1, T=1.5)
+    a = make_gpu(cfg, precision)
+    b = make_gpu(cfg, precision)
+    _, k2, _ = a.orbits()
+    n0 = occupation(cfg, k2)
+    a.init(0, n0, 1.0)
+    b.init(0, n0, 1.0)
+    every = 7
+    rec = a.steps_recorded(3, 50, every)
+    ref = []
+    for t in range(3, 53):
+        b.step(t)
+        if (t - 2) % every == 0:
+            ref.append((t, b.measure(0, t)))
+    assert len(rec) == len(ref) == 7
+    for row, (t, m) in zip(rec, ref):
+        d = row[0]
+        assert d["t"] == t
+        for k in ("time", "E", "E_pot", "E_kin", "E_mem", "M2"):
+            assert d[k] == m[k], k
+        for k in ("F", "ddF", "n", "omega", "c"):
+            assert np.array_equal(d[k], m[k]), k
+    a.close()
+    b.close()
+    params = {"Mass": 1.0, "Nx": 10, "sdim": 3, "dt": 0.1, "Nsteps": 60, "NstepsinMemory": 30, "Nmeas": 6,
+              "Mod": "phi4", "Lambda": 3.0, "ONgroup": 4, "init": "Thermal", "T": 1.5, "Reno": "RNone",
+              "Pexp": "LambdaNLO", "Num": "GPU" if precision == 0 else "GPUmixed"}
+    s1 = kb2pi.run_simulation(params)
+    s2 = kb2pi.run_simulation(params, stream=True)
+    for m1, m2 in zip(s1.measurearray, s2.measurearray):
+        assert m1["E"] == m2["E"] and np.array_equal(m1["n"], m2["n"])
+    path = str(tmp_path / "Measurearray.npz")
+    assert kb2pi.save_measurearray(path, s2, params) == 7
+    back, p2 = kb2pi.load_measurearray(path)
+    assert p2 == params and len(back) == 7
+    for m1, m2 in zip(s2.measurearray, back):
+        assert m1["E"] == m2["E"] and np.array_equal(m1["n"], m2["n"])
