@@ -41,8 +41,10 @@ enum {
   KB_ERR_NODEV = -7    /* no CUDA device / library built without a device */
 };
 
-/* Perturbative expansion (src/TwoPIScalar/TwoPIScalar_Problemdefinition.jl:115-118) */
-enum { KB_PEXP_LO = 0, KB_PEXP_NLO_QUANTUM = 1, KB_PEXP_NLO_CLASSICAL = 2 };
+/* Perturbative expansion (src/TwoPIScalar/TwoPIScalar_Problemdefinition.jl:41-49, 115-118):
+ * LambdaLO, LambdaNLO (quantum), LambdaNLOclassical, NinverseLO, NinverseNLO.
+ * KB_PEXP_NINV_NLO needs KB_PREC_FP64. */
+enum { KB_PEXP_LO = 0, KB_PEXP_NLO_QUANTUM = 1, KB_PEXP_NLO_CLASSICAL = 2, KB_PEXP_NINV_LO = 3, KB_PEXP_NINV_NLO = 4 };
 /* Precision: plain FP64 everywhere, or FP32 history/transforms/sunset with
  * FP64 leapfrog state, accumulation of the memory integrals, tadpole and
  * diagnostics. */

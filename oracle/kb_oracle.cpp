@@ -216,6 +216,7 @@ struct Oracle {
   int tmin = 0, tmax = 0;  // simdata.indices
   std::vector<double> Fst, rst;      // M(M+1)/2 slots of nv values
   std::vector<double> SigF, Sigr;    // M slots of nv values
+  std::vector<double> IrS, IFS;      // 1/N: M slots of I_rho, I_F (FULL: x-space lattice; else orbit momenta)
   std::vector<double> kL2, omega2;   // per stored value
   double hartreemass2 = 0.0;
   std::vector<double> Coct;          // octant cosine matrix
@@ -254,7 +255,7 @@ struct Oracle {
 
   void setup(const orc_params &pp) {
     p = pp;
-    if (p.sdim < 1 || p.sdim > 3 || p.Ns < 1 || p.M < 3 || p.N < 1)
+    if (p.sdim < 1 || p.sdim > 3 || p.Ns < 1 || p.M < 3 || p.N < 1 || p.pexp < 0 || p.pexp > ORC_PEXP_NINV_NLO)
       throw std::invalid_argument("bad parameters");
     if (p.nthreads < 1) p.nthreads = 1;
     orb.build(p.Ns, p.sdim);
@@ -266,6 +267,12 @@ struct Oracle {
     rst.assign(npairs * nv, 1.0);
     SigF.assign((size_t)M * nv, 0.0);
     Sigr.assign((size_t)M * nv, 0.0);
+    if (p.pexp == ORC_PEXP_NINV_NLO) {
+      if (p.engine == ORC_ENGINE_ORBIT) throw std::invalid_argument("1/N NLO: FULL or OCTANT engine");
+      if (p.sdim != 3) throw std::invalid_argument("1/N NLO: sdim 3");
+      IrS.assign((size_t)M * nv, 0.0);
+      IFS.assign((size_t)M * nv, 0.0);
+    }
     kL2.assign(nv, 0.0);
     omega2.assign(nv, 0.0);
     // getTwoPISimData (TwoPIScalar_SimDataStruct.jl:669-687)
@@ -300,9 +307,12 @@ struct Oracle {
   }
 
   double hartree_prefactor() const {
-    // Hartreeprefactor for the lambda expansion (TwoPIScalar_Initialization.jl:245)
+    // Hartreeprefactor (TwoPIScalar_Initialization.jl:245-247): lambda/6 for the
+    // 1/N expansion at LO, lambda (N+2)/(6N) otherwise
+    if (p.pexp == ORC_PEXP_NINV_LO) return p.lambda * (1.0 / 6.0);
     return p.lambda * (double)(p.N + 2) / (double)(6 * p.N);
   }
+  bool lo() const { return p.pexp == ORC_PEXP_LO || p.pexp == ORC_PEXP_NINV_LO; }
   double ivol() const { return 1.0 / (double)orb.V; }
 
   // getHartreeMass2 (TwoPIScalar_Initialization.jl:207-229)
@@ -473,6 +483,219 @@ struct Oracle {
     }
   }
 
+  // ------------------------------------------------------------------------
+  // 1/N expansion at NLO (TwoPIScalar_Evolution.jl:144-758)
+  // ------------------------------------------------------------------------
+  double *Irp(int z) { return IrS.data() + (size_t)(mod1(z) - 1) * nv; }
+  double *IFp(int z) { return IFS.data() + (size_t)(mod1(z) - 1) * nv; }
+  // rfft of a real even lattice, real part with the half-spectrum extension
+  void Kf(const double *in, double *out, FFTScratch &sc) {
+    std::vector<cplx> &X = sc.lat;
+    for (long q = 0; q < orb.V; ++q) X[q] = cplx(in[q], 0.0);
+    fft_lattice(X.data(), -1, sc);
+    real_half_spectrum(X);
+    for (long q = 0; q < orb.V; ++q) out[q] = X[q].real();
+  }
+  // brfft of a real half spectrum (stored extended on the full lattice)
+  void Kb(const double *in, double *out, FFTScratch &sc) {
+    std::vector<cplx> &X = sc.lat;
+    for (long q = 0; q < orb.V; ++q) X[q] = cplx(in[q], 0.0);
+    fft_lattice(X.data(), +1, sc);
+    for (long q = 0; q < orb.V; ++q) out[q] = X[q].real();
+  }
+  // CPUfull: calcIrs! (:170-206), calcIFs! (:354-436), calcSelfEnergyattp! (:683-698)
+  void ninv_full(int tmone) {
+    FFTScratch &sc = scratch[0];
+    const long V = orb.V;
+    const double iv = ivol(), lam = p.lambda, dt = p.dt, N = (double)p.N;
+    std::vector<double> Fx(V), rx(V), A(V), B(V), R2(V), R3(V), RHS(V), T(V);
+    {  // calcIrs!
+      double *I0 = Irp(tmone);
+      for (long q = 0; q < V; ++q) I0[q] = 0.0;
+      const double f1 = (lam / 3.) * iv * iv, f2 = dt * (lam / 3.) * iv, f3 = iv * iv;
+      for (int tp = tmone - 1; tp >= tmin; --tp) {
+        Kf(Fp(tmone, tp), Fx.data(), sc);
+        Kf(rp(tmone, tp), rx.data(), sc);
+        const double s = thesign(tmone, tp);
+        double *I = Irp(tp);
+        for (long q = 0; q < V; ++q) I[q] = s * f1 * Fx[q] * rx[q];
+        for (long q = 0; q < V; ++q) RHS[q] = 0.0;
+        for (int z = tp + 1; z <= tmone - 1; ++z) {
+          Kf(Fp(z, tp), A.data(), sc);
+          Kf(rp(z, tp), B.data(), sc);
+          const double sz = thesign(z, tp);
+          for (long q = 0; q < V; ++q) T[q] = A[q] * B[q];
+          Kb(T.data(), R2.data(), sc);
+          Kb(Irp(z), R3.data(), sc);
+          for (long q = 0; q < V; ++q) RHS[q] -= f3 * sz * R2[q] * R3[q];
+        }
+        Kf(RHS.data(), T.data(), sc);
+        for (long q = 0; q < V; ++q) I[q] += f2 * T[q];
+      }
+    }
+    {  // calcIFs!
+      const double f1 = lam / 6. * iv * iv, f2 = lam / 6. * dt, f3 = lam / 3. * dt;
+      for (int tp = tmin; tp <= tmone; ++tp) {
+        Kf(Fp(tmone, tp), Fx.data(), sc);
+        Kf(rp(tmone, tp), rx.data(), sc);
+        double *IF = IFp(tp);
+        for (long q = 0; q < V; ++q) IF[q] = f1 * (Fx[q] * Fx[q] - 0.25 * rx[q] * rx[q]);
+        for (long q = 0; q < V; ++q) RHS[q] = 0.0;
+        for (int z = tmin + 1; z <= tp - 1; ++z) {  // first integral
+          Kf(Fp(z, tp), A.data(), sc);
+          Kf(rp(z, tp), B.data(), sc);
+          for (long q = 0; q < V; ++q) {
+            A[q] *= iv;
+            B[q] *= iv;
+          }
+          Kb(Irp(z), R3.data(), sc);
+          for (long q = 0; q < V; ++q) T[q] = A[q] * A[q] - 0.25 * B[q] * B[q];
+          Kb(T.data(), R2.data(), sc);
+          for (long q = 0; q < V; ++q) RHS[q] -= f2 * R3[q] * R2[q];  // nr 1
+          for (long q = 0; q < V; ++q) T[q] = A[q] * B[q];
+          const double sz = thesign(z, tp);
+          Kb(T.data(), R3.data(), sc);
+          Kb(IFp(z), R2.data(), sc);
+          for (long q = 0; q < V; ++q) RHS[q] += f3 * sz * R2[q] * R3[q];  // nr 2
+        }
+        const int beginning = (tp == tmin) ? tmin + 1 : tp;
+        for (int z = beginning; z <= tmone - 1; ++z) {  // second integral
+          Kf(Fp(z, tp), A.data(), sc);
+          Kf(rp(z, tp), B.data(), sc);
+          for (long q = 0; q < V; ++q) {
+            A[q] *= iv;
+            B[q] *= iv;
+          }
+          for (long q = 0; q < V; ++q) T[q] = A[q] * A[q] - 0.25 * B[q] * B[q];
+          Kb(T.data(), R3.data(), sc);
+          Kb(Irp(z), R2.data(), sc);
+          for (long q = 0; q < V; ++q) RHS[q] -= f2 * R2[q] * R3[q];
+        }
+        {  // border part
+          Kf(Fp(tmin, tp), A.data(), sc);
+          Kf(rp(tmin, tp), B.data(), sc);
+          for (long q = 0; q < V; ++q) T[q] = A[q] * A[q] - 0.25 * B[q] * B[q];
+          Kb(T.data(), R3.data(), sc);
+          for (long q = 0; q < V; ++q) R3[q] *= iv * iv;
+          Kb(Irp(tmin), R2.data(), sc);
+          for (long q = 0; q < V; ++q) RHS[q] -= 0.5 * dt * lam / 6. * R2[q] * R3[q];
+          if (tp > tmin) {
+            const double sz = thesign(tmin, tp);
+            for (long q = 0; q < V; ++q) T[q] = sz * A[q] * B[q];
+            Kb(T.data(), R3.data(), sc);
+            Kb(IFp(tmin), R2.data(), sc);
+            for (long q = 0; q < V; ++q) RHS[q] += 0.5 * dt * lam / 3. * iv * iv * R2[q] * R3[q];
+          }
+        }
+        Kf(RHS.data(), T.data(), sc);
+        for (long q = 0; q < V; ++q) IF[q] += iv * T[q];
+      }
+    }
+    // calcSelfEnergyattp! for every t' of the window
+    const double fac = -lam / (3. * N) * iv;
+    for (int tp = tmin; tp <= tmone; ++tp) {
+      Kf(Fp(tmone, tp), Fx.data(), sc);
+      Kf(rp(tmone, tp), rx.data(), sc);
+      const double s = thesign(tmone, tp);
+      for (long q = 0; q < V; ++q) rx[q] *= s;
+      const double *I = Irp(tp), *IF = IFp(tp);
+      for (long q = 0; q < V; ++q) T[q] = Fx[q] * I[q] + rx[q] * IF[q];
+      Kb(T.data(), sigrp(tp), sc);
+      for (long q = 0; q < V; ++q) sigrp(tp)[q] *= fac;
+      for (long q = 0; q < V; ++q) T[q] = Fx[q] * IF[q] - 0.25 * rx[q] * I[q];
+      Kb(T.data(), sigFp(tp), sc);
+      for (long q = 0; q < V; ++q) sigFp(tp)[q] *= fac;
+    }
+  }
+  // Orbit form: the resummed kernels are diagonal in momentum, so with the orbit
+  // cosine transform A (A A = V) and the bubbles
+  //   Pr(a,b) = ivol^2 A[A F(a,b) . A rho(a,b)],  PF(a,b) = ivol^2 A[(A F)^2 - (A rho)^2 / 4]
+  // the momentum-space kernels I_k = A I_rho^x, J_k = A I_F^x obey
+  //   I_k(t') = lam/3 Pr(t-1,t') - dt lam/3 sum_{z=t'+1}^{t-2} I_k(z) Pr(z,t')
+  //   J_k(t') = lam/6 PF(t-1,t') - sum_{z=tmin}^{t-2} w_z lam/6 I_k(z) PF(z,t')
+  //                             + sum_{z=tmin}^{t'-1} w_z lam/3 J_k(z) Pr(z,t')
+  // (w = dt/2 at tmin, dt otherwise) and
+  //   Sigma_rho = -lam/(3N) ivol^2 A[A F . A I_k + A rho . A J_k]
+  //   Sigma_F   = -lam/(3N) ivol^2 A[A F . A J_k - A rho . A I_k / 4]
+  void A_orbit(const double *in, double *out) {
+    const int H = orb.H;
+    const long npt = (long)H * H * H;
+    std::vector<double> a(npt), tmp(npt);
+    for (long q = 0; q < npt; ++q) {
+      int g[3] = {(int)(q % H), (int)((q / H) % H), (int)(q / ((long)H * H))};
+      std::sort(g, g + 3);
+      a[q] = in[Orbits::tri_index(3, g[0], g[1], g[2])];
+    }
+    octant_transform(a, tmp);
+    for (int o = 0; o < orb.S; ++o)
+      out[o] = a[(long)orb.rep[3 * o] + (long)orb.rep[3 * o + 1] * H + (long)orb.rep[3 * o + 2] * H * H];
+  }
+  void bubbles(int a, int b, double *Pr, double *PF) {
+    const int S = orb.S;
+    const double iv = ivol();
+    std::vector<double> Fx(S), rx(S), g(S), rt(S);
+    const double s = thesign(a, b);
+    for (int o = 0; o < S; ++o) rt[o] = rp(a, b)[o] * s;  // the true rho(a, b)
+    A_orbit(Fp(a, b), Fx.data());
+    A_orbit(rt.data(), rx.data());
+    if (Pr) {
+      for (int o = 0; o < S; ++o) g[o] = Fx[o] * rx[o];
+      A_orbit(g.data(), Pr);
+      for (int o = 0; o < S; ++o) Pr[o] *= iv * iv;
+    }
+    if (PF) {
+      for (int o = 0; o < S; ++o) g[o] = Fx[o] * Fx[o] - 0.25 * rx[o] * rx[o];
+      A_orbit(g.data(), PF);
+      for (int o = 0; o < S; ++o) PF[o] *= iv * iv;
+    }
+  }
+  void ninv_octant(int tmone) {
+    const int S = orb.S;
+    const double iv = ivol(), lam = p.lambda, dt = p.dt, N = (double)p.N;
+    std::vector<double> Pr(S), PF(S), acc(S);
+    for (int o = 0; o < S; ++o) Irp(tmone)[o] = 0.0;
+    for (int tp = tmone - 1; tp >= tmin; --tp) {
+      for (int o = 0; o < S; ++o) acc[o] = 0.0;
+      for (int z = tp + 1; z <= tmone - 1; ++z) {
+        bubbles(z, tp, Pr.data(), nullptr);
+        for (int o = 0; o < S; ++o) acc[o] += Irp(z)[o] * Pr[o];
+      }
+      bubbles(tmone, tp, Pr.data(), nullptr);
+      for (int o = 0; o < S; ++o) Irp(tp)[o] = lam / 3. * Pr[o] - dt * lam / 3. * acc[o];
+    }
+    for (int tp = tmin; tp <= tmone; ++tp) {
+      std::vector<double> a1(S, 0.0), a2(S, 0.0);
+      for (int z = tmin; z <= tmone - 1; ++z) {
+        const double w = (z == tmin) ? 0.5 * dt : dt;
+        bubbles(z, tp, nullptr, PF.data());
+        for (int o = 0; o < S; ++o) a1[o] += w * Irp(z)[o] * PF[o];
+      }
+      for (int z = tmin; z <= tp - 1; ++z) {
+        const double w = (z == tmin) ? 0.5 * dt : dt;
+        bubbles(z, tp, Pr.data(), nullptr);
+        for (int o = 0; o < S; ++o) a2[o] += w * IFp(z)[o] * Pr[o];
+      }
+      bubbles(tmone, tp, nullptr, PF.data());
+      for (int o = 0; o < S; ++o) IFp(tp)[o] = lam / 6. * PF[o] - lam / 6. * a1[o] + lam / 3. * a2[o];
+    }
+    const double fac = -lam / (3. * N) * iv * iv;
+    std::vector<double> Fx(S), rx(S), Ix(S), Jx(S), g(S), rt(S);
+    for (int tp = tmin; tp <= tmone; ++tp) {
+      const double s = thesign(tmone, tp);
+      for (int o = 0; o < S; ++o) rt[o] = rp(tmone, tp)[o] * s;
+      A_orbit(Fp(tmone, tp), Fx.data());
+      A_orbit(rt.data(), rx.data());
+      A_orbit(Irp(tp), Ix.data());
+      A_orbit(IFp(tp), Jx.data());
+      for (int o = 0; o < S; ++o) g[o] = Fx[o] * Ix[o] + rx[o] * Jx[o];
+      A_orbit(g.data(), sigrp(tp));
+      for (int o = 0; o < S; ++o) sigrp(tp)[o] *= fac;
+      for (int o = 0; o < S; ++o) g[o] = Fx[o] * Jx[o] - 0.25 * rx[o] * Ix[o];
+      A_orbit(g.data(), sigFp(tp));
+      for (int o = 0; o < S; ++o) sigFp(tp)[o] *= fac;
+    }
+  }
+
   // calcSelfEnergyattp! (TwoPIScalar_Evolution.jl:25-31 / 91-105)
   void self_energy_at(int tmone, int tp, int ichunk) {
     std::vector<double> rs(nv);
@@ -484,7 +707,12 @@ struct Oracle {
 
   // calcSelfEnergies! (TwoPIScalar_Evolution.jl:8-23)
   void self_energies(int tmone) {
-    if (p.pexp == ORC_PEXP_LO) return;  // LO: no self-energy (:8-9)
+    if (lo()) return;  // LO: no self-energy (:8-11)
+    if (p.pexp == ORC_PEXP_NINV_NLO) {
+      if (p.engine == ORC_ENGINE_FULL) ninv_full(tmone);
+      else ninv_octant(tmone);
+      return;
+    }
     int n = (tmax - 1) - tmin + 1;
     auto ranges = splitter(tmin, n, p.nthreads);
     parallel_chunks(ranges, [&](int c, int lo, int hi) {
@@ -495,7 +723,7 @@ struct Oracle {
   // getRHS_r! (TwoPIScalar_Evolution.jl:846-865); LO: zero (:842-844)
   void rhs_r(double *Mem, int t, int tp) {
     for (int v = 0; v < nv; ++v) Mem[v] = 0.0;
-    if (p.pexp == ORC_PEXP_LO) return;
+    if (lo()) return;
     for (int z = tp + 1; z <= t - 2; ++z) {
       const double *S = sigrp(z), *r = rp(z, tp);
       const double s = thesign(z, tp);
@@ -504,7 +732,7 @@ struct Oracle {
   }
   // getRHS_F! (TwoPIScalar_Evolution.jl:766-801); LO: zero (:763-765)
   void rhs_F(double *Mem, int t, int tp) {
-    if (p.pexp == ORC_PEXP_LO) {
+    if (lo()) {
       for (int v = 0; v < nv; ++v) Mem[v] = 0.0;
       return;
     }
@@ -1153,7 +1381,8 @@ int orc_dual_loss(const orc_params *p, const double *n_init, double init_mass, i
                   double w_E, const double *dn, double *L, double *dL) {
   return guarded([&] {
     using D = Dual<3>;
-    if (p->sdim != 3 || t_final < 3) throw std::invalid_argument("sdim 3 and t_final >= 3");
+    if (p->sdim != 3 || t_final < 3 || p->pexp > ORC_PEXP_NLO_CLASSICAL)
+      throw std::invalid_argument("sdim 3, t_final >= 3, lambda expansion");
     DualEngine<D> e;
     D lam(p->lambda), m2(p->mass2);
     lam.d[0] = 1.0;

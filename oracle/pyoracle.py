@@ -14,7 +14,7 @@ import threading
 import numpy as np
 
 ENGINE_FULL, ENGINE_ORBIT, ENGINE_OCTANT = 0, 1, 2
-PEXP_LO, PEXP_NLO_QUANTUM, PEXP_NLO_CLASSICAL = 0, 1, 2
+PEXP_LO, PEXP_NLO_QUANTUM, PEXP_NLO_CLASSICAL, PEXP_NINV_LO, PEXP_NINV_NLO = 0, 1, 2, 3, 4
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB = None

@@ -131,7 +131,7 @@ __global__ void adj_step_kernel(RunDev R, int t, AdjBuffers A, double emem_weigh
   const double om = (R.k2[k] + A.scal[0]) * R.dt2;
   double *aF = A.adjF, *aR = A.adjR;
   auto off = [&](int a, int b) { return hist_off(Ma, T, c, a, b, j); };
-  const bool nlo = (R.pexp != 0);
+  const bool nlo = pexp_sunset(R.pexp);
   const double *sgr = reinterpret_cast<const double *>(R.sig_r) + (size_t)c * Ma * KC + j;
   const double *sgF = reinterpret_cast<const double *>(R.sig_F) + (size_t)c * Ma * KC + j;
   // diagonal F(t,t) = (2 - om) F(t,t-1) - F(t,t-2) - dt^3 sum_z [x_rho(z) F(t,z) + x_F(z) rho(t,z)]
@@ -323,7 +323,7 @@ cudaError_t launch_adjoint_step(const RunDev &R, const AdjBuffers &A, int t, dou
   if (e != cudaSuccess) return e;
   adj_refill_kernel<<<grid_for((long long)n * Spad, 256, cap), 256, 0, st>>>(R, t);
   adj_scalars_kernel<<<1, 256, 0, st>>>(R, t, A);
-  const bool nlo = (R.pexp != 0);
+  const bool nlo = pexp_sunset(R.pexp);
   if (nlo) {
     e = launch_sunset(true, 0, sl.runs, sl.base, sl.nruns, sl.total_rows, sl.grid, sl.d_t, sl.scratch, sl.stride,
                       sl.smem, st);

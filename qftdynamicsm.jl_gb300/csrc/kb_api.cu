@@ -34,6 +34,7 @@ struct Run {
   void *hist_F = nullptr, *hist_r = nullptr, *sig_F = nullptr, *sig_r = nullptr;
   double *st_F = nullptr, *st_r = nullptr, *k2_d = nullptr, *deg_d = nullptr, *Cm_d = nullptr;
   double *tad = nullptr, *meas = nullptr, *epart = nullptr, *rowacc = nullptr;
+  double *pi_r = nullptr, *pi_F = nullptr, *Ik = nullptr, *Jk = nullptr;  // 1/N NLO only
   size_t hist_elems = 0, st_elems = 0, sig_elems = 0;
   RunDev dev{};
 };
@@ -59,7 +60,9 @@ struct kb_handle {
   size_t sun_scratch_stride = 0;  // elements per slot
   int t_cur = 0;      // last evolved (or initialised) step; window is [tmin(t_cur), t_cur]
   int inited_runs = 0;
-  bool any_nlo = false;
+  bool any_nlo = false;   // runs with the sunset (lambda expansion at NLO)
+  bool any_ninv = false;  // runs of the 1/N expansion at NLO
+  size_t smem_ninv = 0, smem_nv = 0;
   bool sigma_valid = false;
   cudaGraphExec_t graph = nullptr;
   int graph_measure = -1;
@@ -147,7 +150,8 @@ int validate(const kb_params &p, std::string &why) {
   if (p.N < 1) { why = "ONgroup must be >= 1"; return -1; }
   if (p.flags < 0 || p.flags > 1024) { why = "flags: only bits 0-15 (extra ring slots, at most 1024) are defined"; return -1; }
   if (!(p.dt > 0.0) || !std::isfinite(p.dt)) { why = "dt must be positive"; return -1; }
-  if (p.pexp < 0 || p.pexp > 2) { why = "pexp must be KB_PEXP_LO, _NLO_QUANTUM or _NLO_CLASSICAL"; return -1; }
+  if (p.pexp < 0 || p.pexp > 4) { why = "pexp must be one of KB_PEXP_LO .. KB_PEXP_NINV_NLO"; return -1; }
+  if (p.pexp == KB_PEXP_NINV_NLO && p.precision != KB_PREC_FP64) { why = "the 1/N expansion at NLO runs in KB_PREC_FP64"; return -1; }
   if (p.precision != KB_PREC_FP64 && p.precision != KB_PREC_MIXED) { why = "unknown precision"; return -1; }
   if (!std::isfinite(p.lambda) || !std::isfinite(p.mass2) || !std::isfinite(p.mass)) { why = "non-finite coupling or mass"; return -1; }
   return 0;
@@ -157,7 +161,7 @@ size_t slot_off(const Run &R, int a) { return (size_t)(a % R.Malloc); }
 
 void free_run(Run &R) {
   void *ptrs[] = {R.hist_F, R.hist_r, R.sig_F, R.sig_r, R.st_F, R.st_r, R.k2_d, R.deg_d, R.Cm_d, R.tad, R.meas, R.epart,
-                  R.rowacc};
+                  R.rowacc, R.pi_r, R.pi_F, R.Ik, R.Jk};
   for (void *q : ptrs)
     if (q) cudaFree(q);
 }
@@ -265,7 +269,12 @@ int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out) {
     smem_mi = std::max({smem_mi, kb::memint_smem_bytes(h->fp64, R.Malloc, 0), kb::memint_smem_bytes(h->fp64, R.Malloc, 1)});
     base_sun += R.p.M;
     base_mi += R.nchunks;
-    if (R.p.pexp != KB_PEXP_LO) h->any_nlo = true;
+    if (kb::pexp_sunset(R.p.pexp)) h->any_nlo = true;
+    if (R.p.pexp == KB_PEXP_NINV_NLO) {
+      h->any_ninv = true;
+      h->smem_ninv = std::max(h->smem_ninv, kb::ninv_smem_bytes(R.H));
+      h->smem_nv = std::max(h->smem_nv, kb::ninv_volterra_smem_bytes(R.Malloc));
+    }
   }
   h->total_sun = base_sun;
   h->total_mi = base_mi;
@@ -273,7 +282,7 @@ int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out) {
   h->smem_mi = smem_mi;
   int maxsm = 0;
   cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
-  if ((int)smem_mi > maxsm || (int)smem_sun > maxsm) {
+  if ((int)smem_mi > maxsm || (int)smem_sun > maxsm || (int)h->smem_ninv > maxsm || (int)h->smem_nv > maxsm) {
     fail(nullptr, KB_ERR_PARAM, "shared memory need (%zu / %zu B) exceeds the device limit %d B", smem_sun, smem_mi, maxsm);
     kb_destroy(h);
     return KB_ERR_PARAM;
@@ -293,7 +302,14 @@ int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out) {
         {(void **)&R.meas, (size_t)5 * R.Spad * 8}, {(void **)&R.epart, (size_t)4 * R.nchunks * 8},
         {(void **)&R.rowacc, (size_t)R.nchunks * R.Malloc * KC * 8},
     };
-    for (auto &a : al) {
+    std::vector<A> all(std::begin(al), std::end(al));
+    if (R.p.pexp == KB_PEXP_NINV_NLO) {  // bubble rings and the resummed kernels of the window
+      all.push_back({(void **)&R.pi_r, R.hist_elems * 8});
+      all.push_back({(void **)&R.pi_F, R.hist_elems * 8});
+      all.push_back({(void **)&R.Ik, (size_t)R.Malloc * R.Spad * 8});
+      all.push_back({(void **)&R.Jk, (size_t)R.Malloc * R.Spad * 8});
+    }
+    for (auto &a : all) {
       if (cudaMalloc(a.p, a.bytes) != cudaSuccess) {
         cudaGetLastError();
         fail(nullptr, KB_ERR_OOM, "cudaMalloc of %zu bytes failed (run %d)", a.bytes, r);
@@ -324,7 +340,10 @@ int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out) {
     const double ivol = 1.0 / (double)R.V;
     const double N = (double)R.p.N, lam = R.p.lambda;
     D.ivol = ivol;
-    D.pref_ivol = (lam * (N + 2.0) / (6.0 * N)) * ivol;
+    // Hartreeprefactor (TwoPIScalar_Initialization.jl:245-247): lambda/6 for NinverseLO
+    D.pref_ivol = (R.p.pexp == KB_PEXP_NINV_LO ? lam * (1.0 / 6.0) : lam * (N + 2.0) / (6.0 * N)) * ivol;
+    D.lam = lam;
+    D.ninv_fac = -lam / (3.0 * N) * ivol * ivol;
     D.fac_r = ivol * ivol * ivol * (-(lam * lam) * (N + 2.0) / (6.0 * N * N));
     D.fac_F = ivol * ivol * ivol * (-(lam * lam) * (N + 2.0) / (18.0 * N * N));
     D.mass = R.p.mass;
@@ -341,6 +360,10 @@ int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out) {
     D.meas = R.meas;
     D.epart = R.epart;
     D.rowacc = R.rowacc;
+    D.pi_r = R.pi_r;
+    D.pi_F = R.pi_F;
+    D.Ik = R.Ik;
+    D.Jk = R.Jk;
   }
   bool ok = cudaMalloc(&h->d_runs, sizeof(RunDev) * nruns) == cudaSuccess &&
             cudaMalloc(&h->d_base_sun, sizeof(int) * 2 * nruns) == cudaSuccess &&
@@ -375,7 +398,15 @@ int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out) {
     if (!h->fp64) per_sm = std::max(per_sm, kb::sunset_max_ctas_per_sm(false, 1, h->smem_sun));
     h->grid_sun_max = std::max(1, std::min(h->total_sun, h->num_sms * std::min(4, per_sm)));
   }
-  if (h->fp64 && h->any_nlo) {
+  if (h->any_ninv) {
+    cudaError_t e3 = kb::configure_ninv((size_t)maxsm);
+    if (e3 != cudaSuccess) {
+      fail(nullptr, KB_ERR_CUDA, "kernel configuration failed: %s", cudaGetErrorString(e3));
+      kb_destroy(h);
+      return KB_ERR_CUDA;
+    }
+  }
+  if (h->fp64 && (h->any_nlo || h->any_ninv)) {
     int Hmax = 1;
     for (auto &R : h->runs) Hmax = std::max(Hmax, R.H);
     h->sun_scratch_stride = kb::sunset_scratch_elems(Hmax);
@@ -525,6 +556,20 @@ static cudaEvent_t next_event(kb_handle *h) {
   return h->ev_pool[h->ev_next++];
 }
 
+// Sigma(t-1, .) of every run: the sunset (lambda expansion) and/or the 1/N
+// kernels; each kernel skips the runs of the other expansion.
+static int launch_self_energies(kb_handle *h) {
+  if (h->any_nlo)
+    KB_CUDA(h, kb::launch_sunset(h->fp64, h->sunset_variant, h->d_runs, h->d_base_sun, (int)h->runs.size(),
+                                 h->total_sun, h->grid_sun, h->d_t, h->sun_scratch, h->sun_scratch_stride, h->smem_sun,
+                                 h->st));
+  if (h->any_ninv)
+    KB_CUDA(h, kb::launch_ninv(h->d_runs, h->d_base_sun, h->d_base_mi, (int)h->runs.size(), h->total_sun, h->total_mi,
+                               std::min(h->grid_sun, h->grid_sun_max), h->d_t, h->sun_scratch, h->sun_scratch_stride,
+                               h->smem_ninv, h->smem_nv, h->st));
+  return KB_OK;
+}
+
 static int launch_step(kb_handle *h, int measure) {
   cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
   if (h->profiling) {
@@ -534,12 +579,13 @@ static int launch_step(kb_handle *h, int measure) {
     if (!e0 || !e1 || !e2) return fail(h, KB_ERR_CUDA, "cudaEventCreate failed");
     KB_CUDA(h, cudaEventRecord(e0, h->st));
   }
-  if (h->any_nlo)
-    KB_CUDA(h, kb::launch_sunset(h->fp64, h->sunset_variant, h->d_runs, h->d_base_sun, (int)h->runs.size(), h->total_sun, h->grid_sun,
-                                 h->d_t, h->sun_scratch, h->sun_scratch_stride, h->smem_sun, h->st));
+  {
+    const int rc = launch_self_energies(h);
+    if (rc) return rc;
+  }
   if (h->profiling) {
     KB_CUDA(h, cudaEventRecord(e1, h->st));
-    if (h->any_nlo) h->ev_pending.push_back({0, {e0, e1}});
+    if (h->any_nlo || h->any_ninv) h->ev_pending.push_back({0, {e0, e1}});
   }
   KB_CUDA(h, kb::launch_memint(h->fp64, h->memint_variant, h->d_runs, h->d_base_mi, (int)h->runs.size(),
                                h->total_mi, h->d_t, h->d_err, measure, h->smem_mi, h->st));
@@ -559,7 +605,7 @@ int kb_step(kb_handle *h, int32_t t) {
   int rc = launch_step(h, 1);
   if (rc) return rc;
   h->t_cur = t;
-  h->sigma_valid = h->any_nlo;
+  h->sigma_valid = h->any_nlo || h->any_ninv;
   return KB_OK;
 }
 
@@ -670,9 +716,10 @@ int kb_self_energies(kb_handle *h, int32_t tmone) {
     return fail(h, KB_ERR_PARAM, "kb_self_energies(%d): tmone must be the current tmax - 1 = %d", tmone, h->t_cur - 1);
   cudaSetDevice(h->device);
   KB_CUDA(h, kb::launch_set_t(h->d_t, h->t_cur, h->st));
-  if (h->any_nlo)
-    KB_CUDA(h, kb::launch_sunset(h->fp64, h->sunset_variant, h->d_runs, h->d_base_sun, (int)h->runs.size(), h->total_sun, h->grid_sun,
-                                 h->d_t, h->sun_scratch, h->sun_scratch_stride, h->smem_sun, h->st));
+  {
+    const int rc = launch_self_energies(h);
+    if (rc) return rc;
+  }
   h->sigma_valid = true;
   return kb_sync(h);
 }
@@ -785,7 +832,7 @@ int kb_steps(kb_handle *h, int32_t t0, int32_t count, int32_t measure_every, kb_
       ++nm;
     }
   }
-  h->sigma_valid = h->any_nlo;
+  h->sigma_valid = h->any_nlo || h->any_ninv;
   return kb_sync(h);
 }
 
@@ -861,7 +908,7 @@ int kb_steps_recorded(kb_handle *h, int32_t t0, int32_t count, int32_t measure_e
   KB_CUDA(h, kb::launch_set_t(h->d_t, t0, h->st));
   for (int i = 0; i < count; ++i) KB_CUDA(h, cudaGraphLaunch(h->graph_rec, h->st));
   h->t_cur = t_last;
-  h->sigma_valid = h->any_nlo;
+  h->sigma_valid = h->any_nlo || h->any_ninv;
   std::vector<double> host((size_t)nmeas * block);
   if (nmeas > 0)
     KB_CUDA(h, cudaMemcpyAsync(host.data(), h->d_rec, host.size() * sizeof(double), cudaMemcpyDeviceToHost, h->st));
@@ -945,8 +992,10 @@ static const uint64_t kCkptMagic = 0x6b623270692d636bull;
 int kb_checkpoint_size(const kb_handle *h, size_t *bytes) {
   if (!h || !bytes) return KB_ERR_PARAM;
   size_t b = sizeof(CkptHeader);
-  for (const Run &R : h->runs)
+  for (const Run &R : h->runs) {
     b += (2 * R.hist_elems + 2 * R.sig_elems) * R.esz + 2 * R.st_elems * 8 + (2 * R.nchunks + 5 * R.Spad + 4 * R.nchunks) * 8;
+    if (R.pi_r) b += (2 * R.hist_elems + 2 * (size_t)R.Malloc * R.Spad) * 8;
+  }
   *bytes = b;
   return KB_OK;
 }
@@ -975,7 +1024,14 @@ static int ckpt_copy(kb_handle *h, char *host, size_t bytes, bool save) {
         {R.sig_r, R.sig_elems * R.esz},   {R.st_F, R.st_elems * 8},         {R.st_r, R.st_elems * 8},
         {R.tad, (size_t)2 * R.nchunks * 8}, {R.meas, (size_t)5 * R.Spad * 8}, {R.epart, (size_t)4 * R.nchunks * 8},
     };
-    for (auto &q : bufs) {
+    std::vector<B> bl(std::begin(bufs), std::end(bufs));
+    if (R.pi_r) {
+      bl.push_back({R.pi_r, R.hist_elems * 8});
+      bl.push_back({R.pi_F, R.hist_elems * 8});
+      bl.push_back({R.Ik, (size_t)R.Malloc * R.Spad * 8});
+      bl.push_back({R.Jk, (size_t)R.Malloc * R.Spad * 8});
+    }
+    for (auto &q : bl) {
       if (save) KB_CUDA(h, cudaMemcpyAsync(host + off, q.d, q.n, cudaMemcpyDeviceToHost, h->st));
       else KB_CUDA(h, cudaMemcpyAsync(q.d, host + off, q.n, cudaMemcpyHostToDevice, h->st));
       off += q.n;
@@ -1064,9 +1120,7 @@ int kb_autotune(kb_handle *h, int32_t trials, kb_tuning *chosen, double *ms_per_
     for (int q = 0; q < trials; ++q) {
       KB_CUDA(h, kb::launch_set_t(h->d_t, t, h->st));
       KB_CUDA(h, cudaEventRecord(e[0], h->st));
-      if (h->any_nlo)
-        KB_CUDA(h, kb::launch_sunset(h->fp64, h->sunset_variant, h->d_runs, h->d_base_sun, (int)h->runs.size(), h->total_sun,
-                                     h->grid_sun, h->d_t, h->sun_scratch, h->sun_scratch_stride, h->smem_sun, h->st));
+      if ((rc = launch_self_energies(h))) return rc;
       KB_CUDA(h, cudaEventRecord(e[1], h->st));
       KB_CUDA(h, kb::launch_memint(h->fp64, h->memint_variant, h->d_runs, h->d_base_mi, (int)h->runs.size(),
                                    h->total_mi, h->d_t, h->d_err, 1, h->smem_mi, h->st));
@@ -1167,6 +1221,8 @@ int kb_adjoint(kb_handle *h, const double *n_init, double init_mass, int32_t t_f
   if (!n_init || !grad_lambda || !grad_mass2 || !grad_n) return fail(h, KB_ERR_PARAM, "kb_adjoint: null argument");
   if (h->runs.size() != 1) return fail(h, KB_ERR_PARAM, "kb_adjoint: the handle must hold a single run");
   if (!h->fp64) return fail(h, KB_ERR_PARAM, "kb_adjoint: needs a KB_PREC_FP64 handle");
+  if (h->runs[0].p.pexp > KB_PEXP_NLO_CLASSICAL)
+    return fail(h, KB_ERR_PARAM, "kb_adjoint: the 1/N expansion has no adjoint (lambda expansion only)");
   if (t_final < 3) return fail(h, KB_ERR_PARAM, "kb_adjoint: t_final=%d must be >= 3", t_final);
   Run &R = h->runs[0];
   const int k = ckpt_every;

@@ -48,7 +48,17 @@ struct RunDev {
   double *rowacc;           // [nchunks][Malloc][KC] scratch of the memory-integral kernel
   int cta_base_sun, cta_base_mi;  // first CTA of this run in the batched grids
   int pad0, pad1;
+  // 1/N expansion at NLO (pexp 4), FP64: bubble rings (layout of hist_F) and the
+  // momentum-space resummed kernels I_k, J_k of the window ([Malloc][Spad])
+  double *pi_r, *pi_F, *Ik, *Jk;
+  double lam;       // lambda
+  double ninv_fac;  // -lambda / (3 N) * ivol^2
 };
+
+// perturbative expansions (kb2pi.h): 0 LambdaLO, 1 LambdaNLO, 2 LambdaNLOclassical,
+// 3 NinverseLO, 4 NinverseNLO
+__host__ __device__ inline bool pexp_lo(int pexp) { return pexp == 0 || pexp == 3; }
+__host__ __device__ inline bool pexp_sunset(int pexp) { return pexp == 1 || pexp == 2; }
 
 __host__ __device__ inline long long tet3(int c) { return (long long)c * (c + 1) * (c + 2) / 6; }
 __host__ __device__ inline int tri2(int b) { return b * (b + 1) / 2; }
@@ -92,6 +102,14 @@ cudaError_t launch_set_t(int *d_t, int t, cudaStream_t st);
 cudaError_t launch_record(const RunDev *d_runs, int nruns, const int *d_t, const int *d_ctl, double *rec,
                           const long long *d_off, long long block, cudaStream_t st);
 cudaError_t launch_advance_t(int *d_t, cudaStream_t st);
+// 1/N NLO self-energies (kb_sunset.cu), FP64: bubbles of row t-1, resummed
+// kernels per chunk, then Sigma(t-1, .)
+size_t ninv_smem_bytes(int H);
+size_t ninv_volterra_smem_bytes(int Malloc);
+cudaError_t configure_ninv(size_t smem);
+cudaError_t launch_ninv(const RunDev *d_runs, const int *d_sched_sun, const int *d_sched_mi, int nruns,
+                        int total_rows, int total_ctas, int grid, const int *d_t, void *scratch, size_t scratch_stride,
+                        size_t smem_rows, size_t smem_volterra, cudaStream_t st);
 // adjoint of the sunset (kb_sunset.cu), FP64 handles only
 size_t sunset_adjoint_smem_bytes(int H);
 cudaError_t launch_sunset_adjoint(const RunDev &R, int t, const double *sbar_r, const double *sbar_F, double *adjF,

@@ -341,7 +341,7 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   __syncthreads();
   const double hc = misc[0], M2 = misc[1];
 
-  const bool lo_only = (R.pexp == 0);
+  const bool lo_only = pexp_lo(R.pexp);
   const int J0 = tmin / T, Jn = (t - 1) / T;
   const int nb = Jn - J0 + 1;
   const int ntiles = lo_only ? 0 : nb * (nb + 1) / 2;
@@ -657,7 +657,7 @@ memint_blk_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base,
   __syncthreads();
   const double M2 = misc[1];
 
-  const bool lo_only = (R.pexp == 0);
+  const bool lo_only = pexp_lo(R.pexp);
   const int J0 = tmin / T, Jn = (t - 1) / T;
   const int nb = Jn - J0 + 1;
   const int ntiles = lo_only ? 0 : nb * (nb + 1) / 2;

@@ -243,7 +243,7 @@ sunset_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
     const RunDev &R = runs[r];
     const int tmin = max(1, t - R.M + 1);
     const int tp = tmin + (w - R.cta_base_sun);
-    if (R.pexp == 0 || tp > t - 1 || t < 3) continue;
+    if (!pexp_sunset(R.pexp) || tp > t - 1 || t < 3) continue;
     if (r != cur_run) {
       // per-run tables: cosine matrix, pair list, pass offsets
       __syncthreads();
@@ -683,6 +683,236 @@ cudaError_t launch_sunset_adjoint(const RunDev &R, int t, const double *sbar_r, 
   if (e != cudaSuccess) return e;
   sunset_adjoint_kernel<<<grid, SUN_THREADS, smem, st>>>(R, t, sbar_r, sbar_F, adjF, adjR, lam_part,
                                                          reinterpret_cast<double *>(scratch), stride, lambda);
+  return cudaGetLastError();
+}
+
+}  // namespace kb
+
+// ---------------------------------------------------------------------------
+// 1/N expansion at NLO (calcSelfEnergies! for TwoPIScalarNinverseNLO,
+// TwoPIScalar_Evolution.jl:144-758), FP64.
+//
+// The resummed kernels of the reference, I_rho^x (calcIrs!) and I_F^x
+// (calcIFs!), are products and convolutions of x-space quantities; with the
+// orbit cosine transform A (A A = V on orbits) they are diagonal in momentum.
+// With the bubbles of every stored pair
+//   Pr(a,b) = ivol^2 A[A F(a,b) . A rho(a,b)],   PF(a,b) = ivol^2 A[(A F)^2 - (A rho)^2 / 4]
+// the momentum-space kernels I_k = A I_rho^x, J_k = A I_F^x of step t obey
+//   I_k(t') = lam/3 Pr(t-1,t') - dt lam/3 sum_{z=t'+1}^{t-2} I_k(z) Pr(z,t'),      I_k(t-1) = 0
+//   J_k(t') = lam/6 PF(t-1,t') - sum_{z=tmin}^{t-2} w_z lam/6 I_k(z) PF(z,t')
+//                               + sum_{z=tmin}^{t'-1} w_z lam/3 J_k(z) Pr(z,t')
+// (w_z = dt/2 at tmin, dt otherwise; Pr(z,t') = -Pr(t',z)), and the self-energies are
+//   Sigma_rho = -lam/(3N) ivol^2 A[A F . A I_k + A rho . A J_k]
+//   Sigma_F   = -lam/(3N) ivol^2 A[A F . A J_k - A rho . A I_k / 4]
+// Three kernels per step: the bubbles of the new row t-1 (4 transforms per t',
+// stored in two more rings with the history layout, so each pair's bubble is
+// computed once), the two triangular Volterra solves per orbit chunk (one CTA
+// per chunk, sequential in t', the sums over z split across 32 lanes), and the
+// self-energies (6 transforms per t').
+// ---------------------------------------------------------------------------
+namespace kb {
+namespace {
+
+// cosine matrix and pass tables of one lattice size (as sunset_kernel builds them)
+__device__ void ninv_tables(const RunDev &R, const SunGeom &g, double *CT, uint16_t *pr, int *off2, int *off3) {
+  for (int i = threadIdx.x; i < g.H * g.H4; i += blockDim.x) {
+    const int x = i / g.H4, X = i - x * g.H4;
+    CT[i] = (X < g.H) ? R.Cm[X * g.H + x] : 0.0;
+  }
+  for (int z = threadIdx.x; z < g.H; z += blockDim.x)
+    for (int y = 0; y <= z; ++y) pr[tri2(z) + y] = (uint16_t)(y | (z << 8));
+  if (threadIdx.x == 0) {
+    const int nzb = g.H4 / 4;
+    off2[0] = 0;
+    for (int X = 0; X < g.H; ++X) off2[X + 1] = off2[X] + (g.H4 / 4 - X / 4) * nzb;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int nqb = g.P4 / 4;
+    off3[0] = 0;
+    for (int qb = 0; qb < nqb; ++qb) {
+      const int Ymin = pr[min(4 * qb, g.P - 1)] >> 8;
+      off3[qb + 1] = off3[qb] + (g.H4 / 4 - Ymin / 4);
+    }
+  }
+  __syncthreads();
+}
+
+// shared memory: CT, NB orbit buffers, pass tables
+__host__ __device__ inline size_t ninv_rows_smem(int H, int NB) {
+  SunGeom g(H);
+  return ((size_t)g.H * g.H4 + (size_t)NB * rup4(g.S)) * sizeof(double) +
+         (size_t)(g.H + 1 + g.P4 / 4 + 1) * sizeof(int) + (size_t)g.P * sizeof(uint16_t) + 64;
+}
+
+// MODE 0: bubbles of row t-1 (and of the pair (1,1) at t = 3); MODE 1: self-energies
+template <int MODE>
+__global__ void __launch_bounds__(SUN_THREADS, 1)
+ninv_rows_kernel(const RunDev *__restrict__ runs, const int *__restrict__ sched, int nruns, int total,
+                 const int *__restrict__ d_t, double *__restrict__ scratch, size_t stride) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int t = *d_t;
+  int cur_run = -1;
+  SunCtx<double> c{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, SunGeom(1)};
+  double *buf[4] = {nullptr, nullptr, nullptr, nullptr};
+  for (int w = blockIdx.x; w < total; w += gridDim.x) {
+    const int r = run_at(sched, nruns, w);
+    const RunDev &R = runs[r];
+    if (R.pexp != 4 || t < 3) continue;
+    const int tmin = max(1, t - R.M + 1), tmone = t - 1;
+    const int u = w - R.cta_base_sun;
+    int a = tmone, tp = tmin + u;
+    if (tp > tmone) {
+      if (MODE == 0 && t == 3 && u == 2) {  // F(1,1) enters the first step's kernels
+        a = 1;
+        tp = 1;
+      } else {
+        continue;
+      }
+    }
+    if (r != cur_run) {
+      __syncthreads();
+      cur_run = r;
+      SunGeom g(R.H);
+      double *p = reinterpret_cast<double *>(smem_raw);
+      double *CT = p;
+      p += g.H * g.H4;
+      for (int q = 0; q < (MODE == 0 ? 2 : 4); ++q) {
+        buf[q] = p;
+        p += rup4(g.S);
+      }
+      int *off2 = reinterpret_cast<int *>(p);
+      int *off3 = off2 + (g.H + 1);
+      uint16_t *pr = reinterpret_cast<uint16_t *>(off3 + (g.P4 / 4 + 1));
+      ninv_tables(R, g, CT, pr, off2, off3);
+      double *R1 = scratch + (size_t)blockIdx.x * stride;
+      c = SunCtx<double>{CT, pr, off2, off3, R1, R1 + g.r1, buf[0], g};
+    }
+    const int S = c.g.S, Spad = R.nchunks * KC;
+    const size_t rowstride = (size_t)R.Malloc * KC;
+    const int slot = tp % R.Malloc;
+    const double *stF = R.st_F + (size_t)(a % 3) * R.nchunks * rowstride + (size_t)slot * KC;
+    const double *stR = R.st_r + (size_t)(a % 3) * R.nchunks * rowstride + (size_t)slot * KC;
+    auto gidx = [&](int o) { return (size_t)(o / KC) * rowstride + (o % KC); };
+    double *Fx = buf[0], *rx = buf[1];
+    sun_transform<double>(c, [&](int o) { return stF[gidx(o)]; }, [&](int o, double v) { Fx[o] = v; });
+    sun_transform<double>(c, [&](int o) { return stR[gidx(o)]; }, [&](int o, double v) { rx[o] = v; });
+    if (MODE == 0) {
+      const double iv2 = R.ivol * R.ivol;
+      const int T = R.T;
+      sun_transform<double>(c, [&](int o) { return Fx[o] * rx[o]; },
+                            [&](int o, double v) { R.pi_r[hist_off(R.Malloc, T, o / KC, a, tp, o % KC)] = iv2 * v; });
+      sun_transform<double>(c, [&](int o) { return Fx[o] * Fx[o] - 0.25 * (rx[o] * rx[o]); },
+                            [&](int o, double v) { R.pi_F[hist_off(R.Malloc, T, o / KC, a, tp, o % KC)] = iv2 * v; });
+    } else {
+      double *Ix = buf[2], *Jx = buf[3];
+      const double *Ik = R.Ik + (size_t)slot * Spad, *Jk = R.Jk + (size_t)slot * Spad;
+      sun_transform<double>(c, [&](int o) { return Ik[o]; }, [&](int o, double v) { Ix[o] = v; });
+      sun_transform<double>(c, [&](int o) { return Jk[o]; }, [&](int o, double v) { Jx[o] = v; });
+      double *sigr = reinterpret_cast<double *>(R.sig_r) + (size_t)slot * KC;
+      double *sigF = reinterpret_cast<double *>(R.sig_F) + (size_t)slot * KC;
+      const double fac = R.ninv_fac;
+      sun_transform<double>(c, [&](int o) { return Fx[o] * Ix[o] + rx[o] * Jx[o]; },
+                            [&](int o, double v) { sigr[gidx(o)] = fac * v; });
+      sun_transform<double>(c, [&](int o) { return Fx[o] * Jx[o] - 0.25 * (rx[o] * Ix[o]); },
+                            [&](int o, double v) { sigF[gidx(o)] = fac * v; });
+    }
+    (void)S;
+  }
+}
+
+// One CTA per chunk of KC orbits: thread (lane z-group zl in [0,32), orbit j).
+// I_k descending in t', then J_k ascending; each t' is one block-wide sum over z.
+constexpr int NV_THREADS = 32 * KC;
+
+__global__ void __launch_bounds__(NV_THREADS, 1)
+ninv_volterra_kernel(const RunDev *__restrict__ runs, const int *__restrict__ sched, int nruns,
+                     const int *__restrict__ d_t) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int r = run_at(sched, nruns, blockIdx.x);
+  const RunDev &R = runs[r];
+  const int t = *d_t;
+  if (R.pexp != 4 || t < 3) return;
+  const int c = blockIdx.x - R.cta_base_mi;
+  const int Ma = R.Malloc, T = R.T, Spad = R.nchunks * KC;
+  double *Iv = reinterpret_cast<double *>(smem_raw);  // [Ma][KC]
+  double *Jv = Iv + (size_t)Ma * KC;                    // [Ma][KC]
+  double *red = Jv + (size_t)Ma * KC;                   // [32][KC] x 2
+  const int tid = threadIdx.x, zl = tid / KC, j = tid % KC;
+  const int tmin = max(1, t - R.M + 1), tmone = t - 1;
+  const double lam = R.lam, dt = R.dt;
+  const double *PR = R.pi_r, *PF = R.pi_F;
+  auto pr_at = [&](int z, int tp) {  // Pr(z, t') for z > t' from the stored pair, antisymmetric
+    return z >= tp ? PR[hist_off(Ma, T, c, z, tp, j)] : -PR[hist_off(Ma, T, c, tp, z, j)];
+  };
+  auto pf_at = [&](int z, int tp) {
+    return z >= tp ? PF[hist_off(Ma, T, c, z, tp, j)] : PF[hist_off(Ma, T, c, tp, z, j)];
+  };
+  if (zl == 0) Iv[(size_t)(tmone % Ma) * KC + j] = 0.0;
+  __syncthreads();
+  for (int tp = tmone - 1; tp >= tmin; --tp) {
+    double s = 0.0;
+    for (int z = tp + 1 + zl; z <= tmone - 1; z += 32) s += Iv[(size_t)(z % Ma) * KC + j] * pr_at(z, tp);
+    red[zl * KC + j] = s;
+    __syncthreads();
+    if (zl == 0) {
+      double tot = 0.0;
+      for (int q = 0; q < 32; ++q) tot += red[q * KC + j];
+      Iv[(size_t)(tp % Ma) * KC + j] = lam / 3. * pr_at(tmone, tp) - dt * lam / 3. * tot;
+    }
+    __syncthreads();
+  }
+  double *red2 = red + 32 * KC;
+  for (int tp = tmin; tp <= tmone; ++tp) {
+    double s1 = 0.0, s2 = 0.0;
+    for (int z = tmin + zl; z <= tmone - 1; z += 32) {
+      const double wz = (z == tmin) ? 0.5 * dt : dt;
+      s1 += wz * Iv[(size_t)(z % Ma) * KC + j] * pf_at(z, tp);
+      if (z <= tp - 1) s2 += wz * Jv[(size_t)(z % Ma) * KC + j] * pr_at(z, tp);
+    }
+    red[zl * KC + j] = s1;
+    red2[zl * KC + j] = s2;
+    __syncthreads();
+    if (zl == 0) {
+      double a1 = 0.0, a2 = 0.0;
+      for (int q = 0; q < 32; ++q) {
+        a1 += red[q * KC + j];
+        a2 += red2[q * KC + j];
+      }
+      Jv[(size_t)(tp % Ma) * KC + j] = lam / 6. * pf_at(tmone, tp) - lam / 6. * a1 + lam / 3. * a2;
+    }
+    __syncthreads();
+  }
+  for (int tp = tmin + zl; tp <= tmone; tp += 32) {
+    const size_t o = (size_t)(tp % Ma) * Spad + (size_t)c * KC + j;
+    R.Ik[o] = Iv[(size_t)(tp % Ma) * KC + j];
+    R.Jk[o] = Jv[(size_t)(tp % Ma) * KC + j];
+  }
+}
+
+}  // namespace
+
+size_t ninv_smem_bytes(int H) { return ninv_rows_smem(H, 4); }
+size_t ninv_volterra_smem_bytes(int Malloc) { return ((size_t)2 * Malloc * KC + 2 * 32 * KC) * sizeof(double); }
+
+cudaError_t configure_ninv(size_t smem) {
+  cudaError_t e = cudaFuncSetAttribute(ninv_rows_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(ninv_rows_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(ninv_volterra_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+cudaError_t launch_ninv(const RunDev *d_runs, const int *d_sched_sun, const int *d_sched_mi, int nruns,
+                        int total_rows, int total_ctas, int grid, const int *d_t, void *scratch, size_t scratch_stride,
+                        size_t smem_rows, size_t smem_volterra, cudaStream_t st) {
+  if (total_rows <= 0 || grid <= 0) return cudaSuccess;
+  double *sc = reinterpret_cast<double *>(scratch);
+  ninv_rows_kernel<0><<<grid, SUN_THREADS, smem_rows, st>>>(d_runs, d_sched_sun, nruns, total_rows, d_t, sc,
+                                                             scratch_stride);
+  ninv_volterra_kernel<<<total_ctas, NV_THREADS, smem_volterra, st>>>(d_runs, d_sched_mi, nruns, d_t);
+  ninv_rows_kernel<1><<<grid, SUN_THREADS, smem_rows, st>>>(d_runs, d_sched_sun, nruns, total_rows, d_t, sc,
+                                                             scratch_stride);
   return cudaGetLastError();
 }
 

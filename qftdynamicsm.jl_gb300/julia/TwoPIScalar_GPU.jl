@@ -48,7 +48,8 @@ mutable struct TwoPIScalarSimDataGPUkb <: TwoPIScalarSimDataGPU
     hartreemass2::Vector{Float64}
     function TwoPIScalarSimDataGPUkb(problem)
         d, m = problem.disc, problem.model
-        pexp = problem.pexp isa TwoPIScalarLambdaLO ? 0 : (problem.pexp isa TwoPIScalarLambdaNLOclassical ? 2 : 1)
+        pexp = problem.pexp isa TwoPIScalarLambdaLO ? 0 : problem.pexp isa TwoPIScalarLambdaNLOclassical ? 2 :
+               problem.pexp isa TwoPIScalarNinverseLO ? 3 : problem.pexp isa TwoPIScalarNinverseNLO ? 4 : 1
         p = Ref(KbParams(d.Nx, d.sdim, problem.simsetup.NstepsinMemory, m.ONgroup, pexp, problem.num.precision, 0, 0,
                          d.dt, m.Lambda, m.Mass2, d.Mass))
         hr = Ref{Ptr{Cvoid}}(C_NULL)

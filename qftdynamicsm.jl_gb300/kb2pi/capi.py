@@ -19,7 +19,7 @@ KB_ERR = {
     -1: "KB_ERR_PARAM", -2: "KB_ERR_OOM", -3: "KB_ERR_CUDA", -4: "KB_ERR_NAN",
     -5: "KB_ERR_TIMEOUT", -6: "KB_ERR_RANGE", -7: "KB_ERR_NODEV",
 }
-KB_PEXP_LO, KB_PEXP_NLO_QUANTUM, KB_PEXP_NLO_CLASSICAL = 0, 1, 2
+KB_PEXP_LO, KB_PEXP_NLO_QUANTUM, KB_PEXP_NLO_CLASSICAL, KB_PEXP_NINV_LO, KB_PEXP_NINV_NLO = 0, 1, 2, 3, 4
 KB_PREC_FP64, KB_PREC_MIXED = 0, 1
 
 # every symbol include/kb2pi.h declares

@@ -29,7 +29,8 @@ from . import capi
 # problem definition (TwoPIScalar_Problemdefinition.jl, _Modelfile.jl)
 # ---------------------------------------------------------------------------
 PEXP = {"LambdaLO": capi.KB_PEXP_LO, "LambdaNLO": capi.KB_PEXP_NLO_QUANTUM,
-        "LambdaNLOclassical": capi.KB_PEXP_NLO_CLASSICAL}
+        "LambdaNLOclassical": capi.KB_PEXP_NLO_CLASSICAL, "NinverseLO": capi.KB_PEXP_NINV_LO,
+        "NinverseNLO": capi.KB_PEXP_NINV_NLO}
 NUM = {"GPU": capi.KB_PREC_FP64, "GPUfull": capi.KB_PREC_FP64, "GPUmixed": capi.KB_PREC_MIXED}
 
 
@@ -112,7 +113,10 @@ def lattice_orbits(Ns: int):
 
 
 def hartree_prefactor(model: Phi4, pexp: str) -> float:
-    """Hartreeprefactor for the lambda expansion (TwoPIScalar_Initialization.jl:245)."""
+    """Hartreeprefactor (TwoPIScalar_Initialization.jl:245-247): lambda/6 for NinverseLO,
+    lambda (N+2)/(6N) for the lambda expansion and NinverseNLO."""
+    if pexp == "NinverseLO":
+        return model.Lambda * (1 / 6)
     return model.Lambda * (model.ONgroup + 2) / (6 * model.ONgroup)
 
 

@@ -386,3 +386,73 @@ def test_device_measurement_stream(precision, tmp_path):
     assert p2 == params and len(back) == 7
     for m1, m2 in zip(s2.measurearray, back):
         assert m1["E"] == m2["E"] and np.array_equal(m1["n"], m2["n"])
+
+
+# --- 1/N expansion (NinverseLO, NinverseNLO) -----------------------------------
+
+@pytest.mark.parametrize("cfg,steps", [
+    (dict(Ns=6, M=8, dt=0.1, lam=4.0, T=2.0, pexp=4), 24),            # ring wraps
+    (dict(Ns=8, M=20, dt=0.1, lam=2.0, T=1.5, pexp=4), 30),
+    (dict(Ns=12, M=14, dt=0.05, lam=3.0, init="tsunami", init_mass=1.2, pexp=4), 20),
+    (dict(Ns=8, M=9, dt=0.1, lam=3.0, T=2.0, pexp=3), 20),            # NinverseLO: tadpole lambda/6
+])
+def test_ninverse_parity_fp64(cfg, steps):
+    worst, _, _ = run_pair(cfg, steps)
+    for k, v in worst.items():
+        assert v <= TOL64, (k, v)
+
+
+def test_ninverse_full_lattice_engine():
+    """GPU bubbles + Volterra solves vs the literal full-lattice restatement of
+    calcIrs!/calcIFs!/calcSelfEnergyattp! (CPUfull)."""
+    cfg = dict(Ns=4, M=6, dt=0.1, lam=4.0, T=2.0, pexp=4)
+    worst, _, _ = run_pair(cfg, 14, engine=ENGINE_FULL)
+    for k, v in worst.items():
+        assert v <= TOL64, (k, v)
+
+
+def test_ninverse_batched_with_lambda_runs_and_checkpoint():
+    """One FP64 handle holding a LambdaNLO run and two NinverseNLO runs equals the
+    single-run handles bitwise; a checkpoint restores the bubble rings too."""
+    from kb2pi import capi
+
+    cfgs = [dict(Ns=6, M=8, lam=2.0, pexp=1, T=1.5), dict(Ns=8, M=11, lam=3.0, pexp=4, T=2.0),
+            dict(Ns=6, M=7, lam=1.5, pexp=4, T=1.0)]
+
+    def params(c):
+        return capi.KbParams(Ns=c["Ns"], sdim=3, M=c["M"], N=4, pexp=c["pexp"], precision=0, device=0, flags=0,
+                             dt=0.1, lam=c["lam"], mass2=1.0, mass=1.0)
+
+    hb = capi.Handle([params(c) for c in cfgs])
+    singles = [capi.Handle([params(c)]) for c in cfgs]
+    for r, c in enumerate(cfgs):
+        _, k2, _ = hb.orbits(r)
+        n = occupation(c, k2)
+        hb.init(r, n, 1.0)
+        singles[r].init(0, n, 1.0)
+    for t in range(3, 15):
+        hb.step(t)
+        for s in singles:
+            s.step(t)
+    buf = hb.checkpoint()
+    for t in range(15, 25):
+        hb.step(t)
+        for s in singles:
+            s.step(t)
+    for r, s in enumerate(singles):
+        a, b = hb.measure(r, 24), s.measure(0, 24)
+        assert a["E"] == b["E"] and np.array_equal(a["n"], b["n"])
+    e_before = [hb.measure(r, 24)["E"] for r in range(3)]
+    hb.restore(buf)
+    for t in range(15, 25):
+        hb.step(t)
+    assert [hb.measure(r, 24)["E"] for r in range(3)] == e_before
+    for h in [hb] + singles:
+        h.close()
+
+
+def test_ninverse_mixed_precision_is_rejected():
+    from kb2pi import capi
+
+    with pytest.raises(capi.KbError, match="1/N"):
+        make_gpu(dict(Ns=6, M=8, dt=0.1, lam=2.0, pexp=4), precision=1)

@@ -221,3 +221,43 @@ def test_dual_oracle_values_and_derivatives(pexp):
     assert abs(dlam - fl) <= 1e-6 * max(abs(fl), 1e-8) + 1e-10
     assert abs(dm2 - fm) <= 1e-6 * abs(fm)
     assert abs(ddn - fn) <= 1e-6 * abs(fn)
+
+
+@pytest.mark.parametrize("Ns,M,steps", [(4, 6, 14), (6, 7, 12)])
+@pytest.mark.parametrize("pexp", [4, 3])
+def test_ninverse_engines_agree(Ns, M, steps, pexp):
+    """1/N expansion: the literal full-lattice restatement of calcIrs!/calcIFs!/
+    calcSelfEnergyattp! (CPUfull, with the reference's rfft/brfft pattern) and the
+    orbit form (diagonal in momentum, triangular Volterra solves) agree."""
+    res = []
+    for eng in (ENGINE_FULL, ENGINE_OCTANT):
+        o = Oracle(Ns, 3, M=M, N=4, dt=0.1, lam=4.0, mass2=1.0, pexp=pexp, engine=eng)
+        _, k2, _ = o.orbits()
+        o.init_occupation(thermal_n(k2, 2.0), 1.0)
+        for t in range(3, steps + 3):
+            o.step(t)
+        res.append((o.measure(steps + 2), o.sigma(0, steps + 1) if pexp == 4 else None))
+        o.close()
+    (a, sa), (b, sb) = res
+    assert np.max(np.abs(a["n"] - b["n"])) <= 1e-12 * np.max(np.abs(b["n"]))
+    assert abs(a["E"] - b["E"]) <= 1e-12 * abs(b["E"])
+    if pexp == 4:
+        assert abs(b["E_mem"]) > 0
+        assert np.max(np.abs(sa - sb)) <= 1e-12 * np.max(np.abs(sb))
+
+
+def test_ninverse_energy_drift_matches_lambda_nlo_scale():
+    """A 1/N NLO run conserves energy to the same order as the lambda expansion."""
+    drifts = []
+    for pexp in (1, 4):
+        o = Oracle(6, 3, M=60, N=4, dt=0.05, lam=2.0, mass2=1.0, pexp=pexp, engine=ENGINE_OCTANT)
+        _, k2, _ = o.orbits()
+        o.init_occupation(thermal_n(k2, 1.5), 1.0)
+        E = []
+        for t in range(3, 123):
+            o.step(t)
+            if t % 20 == 0:
+                E.append(o.measure(t)["E"])
+        o.close()
+        drifts.append(abs(E[-1] - E[0]) / abs(E[0]))
+    assert drifts[1] < 5e-3
