@@ -394,6 +394,52 @@ def run_adjoint(args):
     print(json.dumps(line), flush=True)
     return 0
 
+
+def run_ninverse(args):
+    """1/N expansion at NLO (NinverseNLO), FP64: Ns=32, N=4, lambda=4, dt=0.05, M=400,
+    tsunami state; steps/s at a full window, the self-energy share (bubbles, Volterra
+    solves, Sigma) and the memory integrals timed with events."""
+    import torch
+
+    from kb2pi import capi
+
+    ws, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    Ns, M = args.ns or 32, args.m or 400
+    p = capi.KbParams(Ns=Ns, sdim=3, M=M, N=4, pexp=capi.KB_PEXP_NINV_NLO, precision=capi.KB_PREC_FP64,
+                      device=local, flags=0, dt=0.05, lam=4.0, mass2=1.0, mass=1.0)
+    h = capi.Handle([p])
+    _, k2, deg = h.orbits(0)
+    n = tsunami_n(k2)
+    h.init(0, n, gap_mass(k2, deg, n, 4.0, 4, 1.0, Ns ** 3))
+    h.steps(3, M - 2, 0)
+    t = M
+    h.steps(t + 1, args.warmup, 0)
+    t += args.warmup
+    tuning = apply_tuning(h, args, fp64=True)
+    stream = h.stream()
+    barrier(ws)
+    h.profile(True)
+    with ClockSampler(local) as clk:
+        ms = timed_steps(h, t + 1, args.steps, stream)
+    prof = h.profile_read()
+    h.profile(False)
+    m = h.measure(0, t + args.steps)
+    h.close()
+    ms = max_over_ranks(ws, ms)
+    if rank != 0:
+        return 0
+    line = {"metric": "KB steps/s, 1/N expansion at NLO (NinverseNLO), FP64", "value": ws * args.steps / (ms / 1e3),
+            "unit": "steps/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic: tsunami initial state, gap-mass init",
+            "config": {"workload": f"NinverseNLO, Ns={Ns}, N=4, lambda=4, dt=0.05, M={M}, full window"},
+            "kernels_ms": {"self_energies": prof["sunset"][0] / max(1, prof["sunset"][1]),
+                           "memint": prof["memint"][0] / max(1, prof["memint"][1])},
+            "E": m["E"], "tuning": tuning, "clocks": clk.summary(), "gpu_launches": 5 * args.steps}
+    print(json.dumps(line), flush=True)
+    return 0
+
 def run_reference(args):
     ws, rank, _ = dist_setup()
     if rank != 0:
@@ -544,9 +590,9 @@ def main():
     ap.add_argument("--cpu-window", type=int, default=128)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--config", default="c5", choices=["c5", "small", "c3", "c4"],
+    ap.add_argument("--config", default="c5", choices=["c5", "small", "c3", "c4", "ninv"],
                     help="c5: the benchmark workload; small: Ns=40, M=400 for profiler captures; "
-                         "c3: 64 uneven runs in one launch; c4: adjoint gradients")
+                         "c3: 64 uneven runs in one launch; c4: adjoint gradients; ninv: 1/N expansion at NLO")
     ap.add_argument("--seed", type=int, default=12345)
     ap.add_argument("--ns", type=int, default=None, help="override Ns of the c5/small workload (sweeps)")
     ap.add_argument("--m", type=int, default=None, help="override the memory window M (sweeps)")
@@ -560,6 +606,8 @@ def main():
         return run_batched(args)
     if args.config == "c4" and args.impl == "ours":
         return run_adjoint(args)
+    if args.config == "ninv" and args.impl == "ours":
+        return run_ninverse(args)
     if args.config == "small":
         CFG.update(SMALL)
     if args.ns:

@@ -821,10 +821,66 @@ ninv_rows_kernel(const RunDev *__restrict__ runs, const int *__restrict__ sched,
   }
 }
 
-// One CTA per chunk of KC orbits: thread (lane z-group zl in [0,32), orbit j).
-// I_k descending in t', then J_k ascending; each t' is one block-wide sum over z.
-constexpr int NV_THREADS = 32 * KC;
+// One CTA per chunk of KC orbits solves both triangular systems of its orbits,
+// blocked by the time tiles of the history layout (T times per block):
+//   I_k, descending: for time block TB, the contributions of the solved blocks
+//   above it (tiles (ZB, TB), ZB > TB) are summed by all threads -- thread
+//   (group g, tile column tl, orbit j) -- with coalesced loads; then the
+//   diagonal tile, staged in shared memory, is resolved t' by t' by KC threads.
+//   J_k, ascending: the I_k term for every t' first (no dependence on J_k),
+//   then the same blocked scheme for the J_k term over the blocks below.
+constexpr int NV_T = 16;                  // the FP64 time tile
+constexpr int NV_G = 8;                   // thread groups splitting the off-diagonal tiles
+constexpr int NV_THREADS = NV_G * NV_T * KC;
 
+// sum over the T rows zr in [0, nz) of tile (ZB, TB) at column tl, orbit j of
+// v[z] * P(z, TB*T + tl): T independent loads (one tile row each, coalesced
+// across the 4 columns x KC orbits of a warp), no branch for whole tiles
+__device__ __forceinline__ double ninv_col_dot(const double *P, const double *v, size_t tile0, int Ma, int zbase,
+                                               int tl, int j, int nz) {
+  const double *vb = v + (size_t)(zbase % Ma) * KC + j;  // zbase is a block start: slots stay contiguous
+  const double *pb = P + tile0 + j;
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+  if (nz == NV_T) {
+#pragma unroll
+    for (int zr = 0; zr < NV_T; zr += 4) {
+      a0 += vb[zr * KC] * pb[(zr * NV_T + (tl ^ 0)) * KC];
+      a1 += vb[(zr + 1) * KC] * pb[((zr + 1) * NV_T + (tl ^ 1)) * KC];
+      a2 += vb[(zr + 2) * KC] * pb[((zr + 2) * NV_T + (tl ^ 2)) * KC];
+      a3 += vb[(zr + 3) * KC] * pb[((zr + 3) * NV_T + (tl ^ 3)) * KC];
+    }
+  } else {
+    for (int zr = 0; zr < nz; ++zr) a0 += vb[zr * KC] * pb[(zr * NV_T + (tl ^ (zr & 3))) * KC];
+  }
+  return (a0 + a1) + (a2 + a3);
+}
+
+// same along a tile row: sum over columns cl in [c0, c1) of v[z] * P(TB*T + row, zbase + cl)
+__device__ __forceinline__ double ninv_row_dot(const double *P, const double *v, size_t tile0, int Ma, int zbase,
+                                               int row, int j, int c0, int c1, const double *w) {
+  const double *vb = v + (size_t)(zbase % Ma) * KC + j;
+  const double *pb = P + tile0 + (size_t)row * NV_T * KC + j;
+  const int sw = row & 3;
+  double a0 = 0.0, a1 = 0.0;
+  if (c0 == 0 && c1 == NV_T) {
+#pragma unroll
+    for (int cl = 0; cl < NV_T; cl += 2) {
+      a0 += w[cl] * vb[cl * KC] * pb[(cl ^ sw) * KC];
+      a1 += w[cl + 1] * vb[(cl + 1) * KC] * pb[((cl + 1) ^ sw) * KC];
+    }
+  } else {
+    for (int cl = c0; cl < c1; ++cl) a0 += w[cl] * vb[cl * KC] * pb[(cl ^ sw) * KC];
+  }
+  return a0 + a1;
+}
+
+// One CTA per chunk of KC orbits solves both triangular systems of its orbits,
+// blocked by the time tiles of the history layout:
+//   I_k, descending in blocks: the contributions of the solved blocks above
+//   (tiles (ZB, TB), ZB > TB) are column sums shared by two thread groups;
+//   the diagonal tile, staged in shared memory, is resolved t' by t'.
+//   J_k: its I_k term for every t' first (tile-wise, no dependence on J_k),
+//   then ascending in blocks with the J_k term of the blocks below (row sums).
 __global__ void __launch_bounds__(NV_THREADS, 1)
 ninv_volterra_kernel(const RunDev *__restrict__ runs, const int *__restrict__ sched, int nruns,
                      const int *__restrict__ d_t) {
@@ -832,68 +888,140 @@ ninv_volterra_kernel(const RunDev *__restrict__ runs, const int *__restrict__ sc
   const int r = run_at(sched, nruns, blockIdx.x);
   const RunDev &R = runs[r];
   const int t = *d_t;
-  if (R.pexp != 4 || t < 3) return;
+  if (R.pexp != 4 || t < 3 || R.T != NV_T) return;
   const int c = blockIdx.x - R.cta_base_mi;
-  const int Ma = R.Malloc, T = R.T, Spad = R.nchunks * KC;
+  const int Ma = R.Malloc, Spad = R.nchunks * KC, nbA = Ma / NV_T;
+  constexpr int T = NV_T;
   double *Iv = reinterpret_cast<double *>(smem_raw);  // [Ma][KC]
   double *Jv = Iv + (size_t)Ma * KC;                    // [Ma][KC]
-  double *red = Jv + (size_t)Ma * KC;                   // [32][KC] x 2
-  const int tid = threadIdx.x, zl = tid / KC, j = tid % KC;
+  double *T1 = Jv + (size_t)Ma * KC;                    // [Ma][KC]: the I_k term of J_k
+  double *red = T1 + (size_t)Ma * KC;                   // [NV_G][T][KC]
+  double *tile = red + NV_G * T * KC;                   // [T][T][KC] diagonal tile
+  double *prow = tile + T * T * KC;                     // [T][KC]: Pr or PF of (t-1, t') of the block
+  double *wv = prow + T * KC;                           // [Ma]: trapezoid weights by slot
+  const int tid = threadIdx.x, j = tid % KC, tl = (tid / KC) % T, g = tid / (KC * T);
   const int tmin = max(1, t - R.M + 1), tmone = t - 1;
   const double lam = R.lam, dt = R.dt;
   const double *PR = R.pi_r, *PF = R.pi_F;
-  auto pr_at = [&](int z, int tp) {  // Pr(z, t') for z > t' from the stored pair, antisymmetric
-    return z >= tp ? PR[hist_off(Ma, T, c, z, tp, j)] : -PR[hist_off(Ma, T, c, tp, z, j)];
+  auto redsum = [&](int l, int jj) {  // the NV_G group sums of column l, fixed order
+    double a = 0.0;
+    for (int q = 0; q < NV_G; ++q) a += red[(q * T + l) * KC + jj];
+    return a;
   };
-  auto pf_at = [&](int z, int tp) {
-    return z >= tp ? PF[hist_off(Ma, T, c, z, tp, j)] : PF[hist_off(Ma, T, c, tp, z, j)];
+  // start of tile (A, B) of this chunk (absolute time blocks)
+  auto tile0 = [&](int A, int B) {
+    return (((size_t)c * nbA + (size_t)((A * T) % Ma) / T) * nbA + (size_t)((B * T) % Ma) / T) * (size_t)T * T * KC;
   };
-  if (zl == 0) Iv[(size_t)(tmone % Ma) * KC + j] = 0.0;
+  const int J0 = tmin / T, Jn = tmone / T;
+  for (int z = tid; z < Ma; z += NV_THREADS) wv[z] = 0.0;
   __syncthreads();
-  for (int tp = tmone - 1; tp >= tmin; --tp) {
+  for (int z = tmin + tid; z <= tmone; z += NV_THREADS) wv[z % Ma] = (z == tmin) ? 0.5 * dt : dt;
+  if (tid < KC) Iv[(size_t)(tmone % Ma) * KC + j] = 0.0;
+  __syncthreads();
+  // ---- I_k(t') = lam/3 Pr(t-1,t') - dt lam/3 sum_{t' < z < t-1} I_k(z) Pr(z,t')
+  for (int TB = Jn; TB >= J0; --TB) {
     double s = 0.0;
-    for (int z = tp + 1 + zl; z <= tmone - 1; z += 32) s += Iv[(size_t)(z % Ma) * KC + j] * pr_at(z, tp);
-    red[zl * KC + j] = s;
-    __syncthreads();
-    if (zl == 0) {
-      double tot = 0.0;
-      for (int q = 0; q < 32; ++q) tot += red[q * KC + j];
-      Iv[(size_t)(tp % Ma) * KC + j] = lam / 3. * pr_at(tmone, tp) - dt * lam / 3. * tot;
+    for (int ZB = TB + 1 + g; ZB <= Jn; ZB += NV_G) {
+      const int nz = min(T, tmone - ZB * T);  // rows z <= t-2 (I_k(t-1) = 0)
+      if (nz > 0) s += ninv_col_dot(PR, Iv, tile0(ZB, TB), Ma, ZB * T, tl, j, nz);
+    }
+    red[(g * T + tl) * KC + j] = s;
+    for (int q = tid; q < T * T * KC; q += NV_THREADS) {
+      const int zr = q / (T * KC), cl = (q / KC) % T, jj = q % KC;
+      tile[q] = PR[tile0(TB, TB) + (size_t)(zr * T + (cl ^ (zr & 3))) * KC + jj];
+    }
+    if (tid < T * KC) {  // Pr(t-1, t') of the block's columns
+      const int l = tid / KC, p = TB * T + l;
+      prow[tid] = (p >= tmin && p <= tmone) ? PR[hist_off(Ma, T, c, tmone, p, j)] : 0.0;
     }
     __syncthreads();
-  }
-  double *red2 = red + 32 * KC;
-  for (int tp = tmin; tp <= tmone; ++tp) {
-    double s1 = 0.0, s2 = 0.0;
-    for (int z = tmin + zl; z <= tmone - 1; z += 32) {
-      const double wz = (z == tmin) ? 0.5 * dt : dt;
-      s1 += wz * Iv[(size_t)(z % Ma) * KC + j] * pf_at(z, tp);
-      if (z <= tp - 1) s2 += wz * Jv[(size_t)(z % Ma) * KC + j] * pr_at(z, tp);
-    }
-    red[zl * KC + j] = s1;
-    red2[zl * KC + j] = s2;
-    __syncthreads();
-    if (zl == 0) {
-      double a1 = 0.0, a2 = 0.0;
-      for (int q = 0; q < 32; ++q) {
-        a1 += red[q * KC + j];
-        a2 += red2[q * KC + j];
+    if (tid < KC)
+      for (int l = T - 1; l >= 0; --l) {
+        const int p = TB * T + l;
+        if (p < tmin || p > tmone - 1) continue;
+        double d = redsum(l, j);
+        const int zmax = min(T - 1, tmone - 1 - TB * T);
+        const double *ib = Iv + (size_t)((TB * T) % Ma) * KC + j;
+        for (int zr = l + 1; zr <= zmax; ++zr) d += ib[zr * KC] * tile[(zr * T + l) * KC + j];
+        Iv[(size_t)((TB * T) % Ma + l) * KC + j] = lam / 3. * prow[l * KC + j] - dt * lam / 3. * d;
       }
-      Jv[(size_t)(tp % Ma) * KC + j] = lam / 6. * pf_at(tmone, tp) - lam / 6. * a1 + lam / 3. * a2;
-    }
     __syncthreads();
   }
-  for (int tp = tmin + zl; tp <= tmone; tp += 32) {
-    const size_t o = (size_t)(tp % Ma) * Spad + (size_t)c * KC + j;
-    R.Ik[o] = Iv[(size_t)(tp % Ma) * KC + j];
-    R.Jk[o] = Jv[(size_t)(tp % Ma) * KC + j];
+  // ---- T1(t') = sum_{tmin <= z <= t-2} w_z I_k(z) PF(z, t') (PF symmetric): tile-wise,
+  //      column sums for z >= t' (tiles (ZB, TB), ZB >= TB) and row sums for z < t'
+  for (int TB = J0; TB <= Jn; ++TB) {
+    double s = 0.0;
+    const int p = TB * T + tl;
+    if (p >= tmin && p <= tmone) {
+      for (int ZB = TB + g; ZB <= Jn; ZB += NV_G) {
+        // rows z = ZB*T + zr with z >= p, tmin <= z <= t-2, weighted
+        const int zlo = max(ZB * T, max(p, tmin)), zhi = min(ZB * T + T - 1, tmone - 1);
+        const size_t t0 = tile0(ZB, TB);
+        const int sb = (ZB * T) % Ma;
+        for (int z = zlo; z <= zhi; ++z) {
+          const int zr = z - ZB * T;
+          s += wv[sb + zr] * Iv[(size_t)(sb + zr) * KC + j] * PF[t0 + (size_t)(zr * T + (tl ^ (zr & 3))) * KC + j];
+        }
+      }
+      for (int ZB = J0 + g; ZB <= TB; ZB += NV_G) {
+        // columns z = ZB*T + cl with tmin <= z < p: row p of tile (TB, ZB)
+        const int c0 = max(0, tmin - ZB * T), c1 = min(T, p - ZB * T);
+        if (c1 > c0) s += ninv_row_dot(PF, Iv, tile0(TB, ZB), Ma, ZB * T, tl, j, c0, c1, wv + ((ZB * T) % Ma));
+      }
+    }
+    red[(g * T + tl) * KC + j] = s;
+    __syncthreads();
+    if (g == 0 && p >= tmin && p <= tmone) T1[(size_t)(p % Ma) * KC + j] = redsum(tl, j);
+    __syncthreads();
+  }
+  // ---- J_k(t') = lam/6 PF(t-1,t') - lam/6 T1(t') + lam/3 sum_{tmin <= z < t'} w_z J_k(z) Pr(z,t'),
+  //      Pr(z,t') = -Pr(t',z) for z < t'
+  for (int TB = J0; TB <= Jn; ++TB) {
+    const int p = TB * T + tl;
+    double s = 0.0;
+    if (p >= tmin && p <= tmone)
+      for (int ZB = J0 + g; ZB < TB; ZB += NV_G) {
+        const int c0 = max(0, tmin - ZB * T);
+        s -= ninv_row_dot(PR, Jv, tile0(TB, ZB), Ma, ZB * T, tl, j, c0, T, wv + ((ZB * T) % Ma));
+      }
+    red[(g * T + tl) * KC + j] = s;
+    for (int q = tid; q < T * T * KC; q += NV_THREADS) {
+      const int pr_ = q / (T * KC), cl = (q / KC) % T, jj = q % KC;
+      tile[q] = PR[tile0(TB, TB) + (size_t)(pr_ * T + (cl ^ (pr_ & 3))) * KC + jj];
+    }
+    if (tid < T * KC) {
+      const int l = tid / KC, pp = TB * T + l;
+      prow[tid] = (pp >= tmin && pp <= tmone) ? PF[hist_off(Ma, T, c, tmone, pp, j)] : 0.0;
+    }
+    __syncthreads();
+    if (tid < KC)
+      for (int l = 0; l < T; ++l) {
+        const int pp = TB * T + l;
+        if (pp < tmin || pp > tmone) continue;
+        double d = redsum(l, j);
+        const int sb = (TB * T) % Ma;
+        for (int zr = max(0, tmin - TB * T); zr < l; ++zr)
+          d -= wv[sb + zr] * Jv[(size_t)(sb + zr) * KC + j] * tile[(l * T + zr) * KC + j];
+        Jv[(size_t)(sb + l) * KC + j] =
+            lam / 6. * prow[l * KC + j] - lam / 6. * T1[(size_t)(sb + l) * KC + j] + lam / 3. * d;
+      }
+    __syncthreads();
+  }
+  for (int q = tid; q < (tmone - tmin + 1) * KC; q += NV_THREADS) {
+    const int tp = tmin + q / KC, jj = q % KC;
+    const size_t o = (size_t)(tp % Ma) * Spad + (size_t)c * KC + jj;
+    R.Ik[o] = Iv[(size_t)(tp % Ma) * KC + jj];
+    R.Jk[o] = Jv[(size_t)(tp % Ma) * KC + jj];
   }
 }
 
 }  // namespace
 
 size_t ninv_smem_bytes(int H) { return ninv_rows_smem(H, 4); }
-size_t ninv_volterra_smem_bytes(int Malloc) { return ((size_t)2 * Malloc * KC + 2 * 32 * KC) * sizeof(double); }
+size_t ninv_volterra_smem_bytes(int Malloc) {
+  // I_k, J_k, their I_k term, block sums, one diagonal tile, a row of the block, weights
+  return ((size_t)3 * Malloc * KC + NV_G * NV_T * KC + NV_T * NV_T * KC + NV_T * KC + Malloc) * sizeof(double);
+}
 
 cudaError_t configure_ninv(size_t smem) {
   cudaError_t e = cudaFuncSetAttribute(ninv_rows_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
