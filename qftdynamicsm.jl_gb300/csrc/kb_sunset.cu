@@ -935,16 +935,19 @@ ninv_volterra_kernel(const RunDev *__restrict__ runs, const int *__restrict__ sc
       prow[tid] = (p >= tmin && p <= tmone) ? PR[hist_off(Ma, T, c, tmone, p, j)] : 0.0;
     }
     __syncthreads();
-    if (tid < KC)
+    if (tid < 4 * 32) {
+      // the diagonal tile, t' by t': warp w resolves orbits 2w, 2w+1 with one lane per row zr
+      const int lane = tid & 31, jj = 2 * (tid >> 5) + (lane >> 4), zr = lane & 15;
+      const int zmax = min(T - 1, tmone - 1 - TB * T), sb = (TB * T) % Ma;
       for (int l = T - 1; l >= 0; --l) {
         const int p = TB * T + l;
         if (p < tmin || p > tmone - 1) continue;
-        double d = redsum(l, j);
-        const int zmax = min(T - 1, tmone - 1 - TB * T);
-        const double *ib = Iv + (size_t)((TB * T) % Ma) * KC + j;
-        for (int zr = l + 1; zr <= zmax; ++zr) d += ib[zr * KC] * tile[(zr * T + l) * KC + j];
-        Iv[(size_t)((TB * T) % Ma + l) * KC + j] = lam / 3. * prow[l * KC + j] - dt * lam / 3. * d;
+        double v = (zr > l && zr <= zmax) ? Iv[(size_t)(sb + zr) * KC + jj] * tile[(zr * T + l) * KC + jj] : 0.0;
+        for (int o = 8; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (zr == 0) Iv[(size_t)(sb + l) * KC + jj] = lam / 3. * prow[l * KC + jj] - dt * lam / 3. * (redsum(l, jj) + v);
+        __syncwarp();
       }
+    }
     __syncthreads();
   }
   // ---- T1(t') = sum_{tmin <= z <= t-2} w_z I_k(z) PF(z, t') (PF symmetric): tile-wise,
@@ -994,17 +997,22 @@ ninv_volterra_kernel(const RunDev *__restrict__ runs, const int *__restrict__ sc
       prow[tid] = (pp >= tmin && pp <= tmone) ? PF[hist_off(Ma, T, c, tmone, pp, j)] : 0.0;
     }
     __syncthreads();
-    if (tid < KC)
+    if (tid < 4 * 32) {
+      const int lane = tid & 31, jj = 2 * (tid >> 5) + (lane >> 4), zr = lane & 15;
+      const int zmin = max(0, tmin - TB * T), sb = (TB * T) % Ma;
       for (int l = 0; l < T; ++l) {
         const int pp = TB * T + l;
         if (pp < tmin || pp > tmone) continue;
-        double d = redsum(l, j);
-        const int sb = (TB * T) % Ma;
-        for (int zr = max(0, tmin - TB * T); zr < l; ++zr)
-          d -= wv[sb + zr] * Jv[(size_t)(sb + zr) * KC + j] * tile[(l * T + zr) * KC + j];
-        Jv[(size_t)(sb + l) * KC + j] =
-            lam / 6. * prow[l * KC + j] - lam / 6. * T1[(size_t)(sb + l) * KC + j] + lam / 3. * d;
+        double v = (zr < l && zr >= zmin)
+                       ? -wv[sb + zr] * Jv[(size_t)(sb + zr) * KC + jj] * tile[(l * T + zr) * KC + jj]
+                       : 0.0;
+        for (int o = 8; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (zr == 0)
+          Jv[(size_t)(sb + l) * KC + jj] = lam / 6. * prow[l * KC + jj] -
+                                           lam / 6. * T1[(size_t)(sb + l) * KC + jj] + lam / 3. * (redsum(l, jj) + v);
+        __syncwarp();
       }
+    }
     __syncthreads();
   }
   for (int q = tid; q < (tmone - tmin + 1) * KC; q += NV_THREADS) {
