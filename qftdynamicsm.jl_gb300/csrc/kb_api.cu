@@ -772,7 +772,12 @@ int kb_get_traces(kb_handle *h, int32_t run, double *Fonet, double *ronet, doubl
       ronet[q] = v[0];
     }
   }
-  if (SigF || Sigr) {
+  if ((SigF || Sigr) && kb::pexp_lo(R.p.pexp)) {  // LO: no self-energy, the traces are zero
+    for (int tp = t - 1, q = 0; tp >= tmin; --tp, ++q) {
+      if (SigF) SigF[q] = 0.0;
+      if (Sigr) Sigr[q] = 0.0;
+    }
+  } else if (SigF || Sigr) {
     for (int tp = t - 1, q = 0; tp >= tmin; --tp, ++q) {
       int rc;
       if (SigF) {

@@ -294,6 +294,29 @@ def test_host_mirror_run_simulation():
     assert problem.model.Mass2 < 1.0  # RMass counterterm applied
 
 
+@pytest.mark.parametrize("pexp_name,pexp", [("NinverseNLO", 4), ("NinverseLO", 3)])
+def test_host_mirror_ninverse(pexp_name, pexp):
+    """The driver loop with Pexp = NinverseNLO / NinverseLO and RMass renormalisation
+    (its counterterm uses the 1/N Hartree prefactor), against the oracle."""
+    import kb2pi
+    from oracle import Oracle
+
+    parameters = {"Mass": 1.0, "Nx": 6, "sdim": 3, "dt": 0.1, "Nsteps": 16, "NstepsinMemory": 9, "Nmeas": 0,
+                  "Mod": "phi4", "Lambda": 3.0, "ONgroup": 4, "init": "Thermal", "T": 1.5, "Reno": "RMass",
+                  "Pexp": pexp_name, "Num": "GPU"}
+    sol = kb2pi.run_simulation(dict(parameters))
+    problem = sol.problem
+    o = Oracle(6, 3, M=9, N=4, dt=0.1, lam=3.0, mass2=problem.model.Mass2, mass=1.0, pexp=pexp)
+    _, k2, _ = o.orbits()
+    o.init_occupation(1.0 / (np.exp(np.sqrt(k2 + 1.0) / 1.5) - 1.0), 1.0)
+    Es = [o.measure(2)["E"]]
+    for t in range(3, 19):
+        o.step(t)
+        Es.append(o.measure(t)["E"])
+    assert rel([m["E"] for m in sol.measurearray], Es) <= TOL64
+    assert problem.model.Mass2 < 1.0
+
+
 def c3_runs(nruns, seed, Ns_choices, M_range):
     """Config 3 style batch: per-run seeded draws of Ns, lambda, T and the memory window."""
     rng = np.random.default_rng(seed)
