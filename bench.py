@@ -147,9 +147,11 @@ def make_handle(precision, device):
 
 def apply_tuning(h, args, fp64=False):
     """Autotune the launch configuration on the filled window (untimed), unless fixed on the command line."""
-    if any(v is not None for v in (args.memint_variant, args.sunset_grid, args.batch_order, args.sunset_variant)):
+    if any(v is not None for v in (args.memint_variant, args.sunset_grid, args.batch_order, args.sunset_variant,
+                                   args.memint_split)):
         h.set_tuning(memint_variant=None if fp64 else args.memint_variant, sunset_grid=args.sunset_grid,
-                     batch_order=args.batch_order, sunset_variant=None if fp64 else args.sunset_variant)
+                     batch_order=args.batch_order, sunset_variant=None if fp64 else args.sunset_variant,
+                     memint_split=args.memint_split)
         d = h.tuning()
         d["source"] = "command line"
         return d
@@ -600,6 +602,7 @@ def main():
                     help="fix the mixed-precision memory-integral variant instead of autotuning")
     ap.add_argument("--sunset-grid", type=int, default=None, help="fix the sunset grid instead of autotuning")
     ap.add_argument("--batch-order", type=int, default=None, help="fix the run order of the batched grids (c3)")
+    ap.add_argument("--memint-split", type=int, default=None, help="fix the split mode of the memory integrals")
     ap.add_argument("--sunset-variant", type=int, default=None, help="fix the FP32 sunset variant (0: 1024, 1: 512 threads)")
     args = ap.parse_args()
     if args.config == "c3" and args.impl == "ours":

@@ -186,10 +186,16 @@ typedef struct kb_tuning {
   int32_t batch_order;    /* batched handles: 0 runs in order, 1 costliest runs first in both grids */
   int32_t sunset_variant; /* KB_PREC_MIXED: 0 1024 threads per CTA, 1 512 threads (two CTAs per SM where
                            * their shared memory fits); KB_PREC_FP64: 0 */
+  int32_t memint_split;   /* 1: each chunk's triangle of history tiles is streamed by two CTAs (equal
+                           * halves by column blocks), then a finishing kernel adds their sums and runs
+                           * the leapfrog; 0: one CTA per chunk. Needs memint_variant 1 in
+                           * KB_PREC_MIXED */
+  int32_t reserved[3];
 } kb_tuning;
 int kb_get_tuning(const kb_handle *h, kb_tuning *out);
 int kb_set_tuning(kb_handle *h, const kb_tuning *in);
-/* Autotuner: times every candidate configuration (memory-integral variants;
+/* Autotuner: times every candidate configuration (memory-integral variants,
+ * whole or split;
  * sunset variants with grids of 1..4 CTAs per SM that fit; both run orders of a batched
  * handle) by re-running the last evolved
  * step t -- which reads rows < t and rewrites row t, so the state is unchanged

@@ -33,7 +33,7 @@ struct Run {
   // device allocations
   void *hist_F = nullptr, *hist_r = nullptr, *sig_F = nullptr, *sig_r = nullptr;
   double *st_F = nullptr, *st_r = nullptr, *k2_d = nullptr, *deg_d = nullptr, *Cm_d = nullptr;
-  double *tad = nullptr, *meas = nullptr, *epart = nullptr, *rowacc = nullptr;
+  double *tad = nullptr, *meas = nullptr, *epart = nullptr, *rowacc = nullptr, *colacc = nullptr;
   double *pi_r = nullptr, *pi_F = nullptr, *Ik = nullptr, *Jk = nullptr;  // 1/N NLO only
   size_t hist_elems = 0, st_elems = 0, sig_elems = 0;
   RunDev dev{};
@@ -54,6 +54,7 @@ struct kb_handle {
   size_t smem_sun = 0, smem_mi = 0;
   int num_sms = 0, grid_sun = 0, grid_sun_max = 0;
   int memint_variant = 0;         // FP32 consumer layout of the memory-integral kernel
+  int memint_split = 0;           // 1: two half-triangle CTAs per chunk and a finishing kernel
   int batch_order = 0;            // order of the runs' CTA ranges in the batched grids
   int sunset_variant = 0;         // FP32 sunset: 0 1024 threads per CTA, 1 512 threads (2 CTAs per SM)
   void *sun_scratch = nullptr;    // FP64 cosine-transform intermediates, one slot per CTA
@@ -161,7 +162,7 @@ size_t slot_off(const Run &R, int a) { return (size_t)(a % R.Malloc); }
 
 void free_run(Run &R) {
   void *ptrs[] = {R.hist_F, R.hist_r, R.sig_F, R.sig_r, R.st_F, R.st_r, R.k2_d, R.deg_d, R.Cm_d, R.tad, R.meas, R.epart,
-                  R.rowacc, R.pi_r, R.pi_F, R.Ik, R.Jk};
+                  R.rowacc, R.colacc, R.pi_r, R.pi_F, R.Ik, R.Jk};
   for (void *q : ptrs)
     if (q) cudaFree(q);
 }
@@ -300,7 +301,8 @@ int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out) {
         {(void **)&R.k2_d, (size_t)R.Spad * 8}, {(void **)&R.deg_d, (size_t)R.Spad * 8},
         {(void **)&R.Cm_d, (size_t)R.H * R.H * 8}, {(void **)&R.tad, (size_t)2 * R.nchunks * 8},
         {(void **)&R.meas, (size_t)5 * R.Spad * 8}, {(void **)&R.epart, (size_t)4 * R.nchunks * 8},
-        {(void **)&R.rowacc, (size_t)R.nchunks * R.Malloc * KC * 8},
+        {(void **)&R.rowacc, (size_t)2 * R.nchunks * R.Malloc * KC * 8},
+        {(void **)&R.colacc, (size_t)2 * R.nchunks * R.Malloc * KC * 8},
     };
     std::vector<A> all(std::begin(al), std::end(al));
     if (R.p.pexp == KB_PEXP_NINV_NLO) {  // bubble rings and the resummed kernels of the window
@@ -360,6 +362,7 @@ int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out) {
     D.meas = R.meas;
     D.epart = R.epart;
     D.rowacc = R.rowacc;
+    D.colacc = R.colacc;
     D.pi_r = R.pi_r;
     D.pi_F = R.pi_F;
     D.Ik = R.Ik;
@@ -587,7 +590,7 @@ static int launch_step(kb_handle *h, int measure) {
     KB_CUDA(h, cudaEventRecord(e1, h->st));
     if (h->any_nlo || h->any_ninv) h->ev_pending.push_back({0, {e0, e1}});
   }
-  KB_CUDA(h, kb::launch_memint(h->fp64, h->memint_variant, h->d_runs, h->d_base_mi, (int)h->runs.size(),
+  KB_CUDA(h, kb::launch_memint(h->fp64, h->memint_variant, h->memint_split, h->d_runs, h->d_base_mi, (int)h->runs.size(),
                                h->total_mi, h->d_t, h->d_err, measure, h->smem_mi, h->st));
   if (h->profiling) {
     KB_CUDA(h, cudaEventRecord(e2, h->st));
@@ -1071,6 +1074,7 @@ int kb_get_tuning(const kb_handle *h, kb_tuning *out) {
   out->sunset_grid = h->grid_sun;
   out->batch_order = h->batch_order;
   out->sunset_variant = h->sunset_variant;
+  out->memint_split = h->memint_split;
   return KB_OK;
 }
 
@@ -1087,6 +1091,9 @@ int kb_set_tuning(kb_handle *h, const kb_tuning *in) {
   if (in->sunset_grid != 0 &&
       in->sunset_grid > h->num_sms * kb::sunset_max_ctas_per_sm(h->fp64, in->sunset_variant, h->smem_sun) * 4)
     return fail(h, KB_ERR_PARAM, "sunset_grid=%d: too large for this variant", in->sunset_grid);
+  if (in->memint_split < 0 || in->memint_split > 1 || (in->memint_split && !h->fp64 && in->memint_variant != 1))
+    return fail(h, KB_ERR_PARAM, "memint_split=%d: 0 or 1, and 1 only with memint_variant 1 in KB_PREC_MIXED",
+                in->memint_split);
   if (in->batch_order < 0 || in->batch_order > 1)
     return fail(h, KB_ERR_PARAM, "batch_order=%d: 0 (runs in order) or 1 (costliest first)", in->batch_order);
   cudaSetDevice(h->device);
@@ -1095,6 +1102,7 @@ int kb_set_tuning(kb_handle *h, const kb_tuning *in) {
   if (in->batch_order != h->batch_order && apply_schedule(h, in->batch_order) != KB_OK)
     return fail(h, KB_ERR_CUDA, "upload of the run schedule failed");
   h->memint_variant = in->memint_variant;
+  h->memint_split = in->memint_split;
   h->sunset_variant = in->sunset_variant;
   h->grid_sun = g;
   if (h->graph) {  // captured with the old configuration
@@ -1117,8 +1125,9 @@ int kb_autotune(kb_handle *h, int32_t trials, kb_tuning *chosen, double *ms_per_
   const int t = h->t_cur;
   cudaEvent_t e[3];
   for (auto &x : e) KB_CUDA(h, cudaEventCreate(&x));
-  auto time_cfg = [&](int variant, int svar, int grid, float *ms_sun, float *ms_mi) -> int {
+  auto time_cfg = [&](int variant, int split, int svar, int grid, float *ms_sun, float *ms_mi) -> int {
     h->memint_variant = variant;
+    h->memint_split = split;
     h->sunset_variant = svar;
     h->grid_sun = grid;
     float best_s = 1e30f, best_m = 1e30f;
@@ -1127,7 +1136,7 @@ int kb_autotune(kb_handle *h, int32_t trials, kb_tuning *chosen, double *ms_per_
       KB_CUDA(h, cudaEventRecord(e[0], h->st));
       if ((rc = launch_self_energies(h))) return rc;
       KB_CUDA(h, cudaEventRecord(e[1], h->st));
-      KB_CUDA(h, kb::launch_memint(h->fp64, h->memint_variant, h->d_runs, h->d_base_mi, (int)h->runs.size(),
+      KB_CUDA(h, kb::launch_memint(h->fp64, h->memint_variant, h->memint_split, h->d_runs, h->d_base_mi, (int)h->runs.size(),
                                    h->total_mi, h->d_t, h->d_err, 1, h->smem_mi, h->st));
       KB_CUDA(h, cudaEventRecord(e[2], h->st));
       KB_CUDA(h, cudaEventSynchronize(e[2]));
@@ -1141,8 +1150,9 @@ int kb_autotune(kb_handle *h, int32_t trials, kb_tuning *chosen, double *ms_per_
     *ms_mi = best_m;
     return KB_OK;
   };
-  // sunset variants x grids of 1..4 resident CTAs per SM; memint variants:
-  // FP32 only; run orders: batched handles only
+  // sunset variants x grids of 1..4 resident CTAs per SM; memint (variant,
+  // split): the whole or split two-group kernel, and for FP32 the
+  // register-blocked one; run orders: batched handles only
   std::vector<std::pair<int, int>> sun_cands;  // (variant, grid)
   for (int sv = 0; sv < (h->fp64 ? 1 : 2); ++sv) {
     const int occ = std::min(4, kb::sunset_max_ctas_per_sm(h->fp64, sv, h->smem_sun));
@@ -1154,10 +1164,11 @@ int kb_autotune(kb_handle *h, int32_t trials, kb_tuning *chosen, double *ms_per_
     }
   }
   if (sun_cands.empty()) sun_cands.push_back({h->sunset_variant, h->grid_sun});
-  const int nvar = h->fp64 ? 1 : 2;
   const int norder = h->runs.size() > 1 ? 2 : 1;
   const int v0 = h->fp64 ? 0 : 1;  // default memint variant first
-  int best_o = h->batch_order, best_v = v0;
+  std::vector<std::pair<int, int>> mi_cands = {{v0, 1}};  // (variant, split) after (v0, 0)
+  if (!h->fp64) mi_cands.push_back({0, 0});
+  int best_o = h->batch_order, best_v = v0, best_split = 0;
   std::pair<int, int> best_sc = sun_cands[0];
   float best_total = 1e30f, best_s_all = 0, best_m_all = 0;
   for (int o = 0; o < norder && !rc; ++o) {
@@ -1167,25 +1178,25 @@ int kb_autotune(kb_handle *h, int32_t trials, kb_tuning *chosen, double *ms_per_
       break;
     }
     std::pair<int, int> sc_o = sun_cands[0];
-    int v_o = v0;
+    int v_o = v0, sp_o = 0;
     float bs = 1e30f, bm = 1e30f;
     for (size_t q = 0; q < sun_cands.size(); ++q) {
       float ms_s, ms_m;
-      if ((rc = time_cfg(v0, sun_cands[q].first, sun_cands[q].second, &ms_s, &ms_m))) break;
+      if ((rc = time_cfg(v0, 0, sun_cands[q].first, sun_cands[q].second, &ms_s, &ms_m))) break;
       if (ms_s < bs) { bs = ms_s; sc_o = sun_cands[q]; }
       if (q == 0) bm = ms_m;
     }
-    for (int v = 0; v < nvar && !rc; ++v) {
-      if (v == v0) continue;
+    for (size_t q = 0; q < mi_cands.size() && !rc; ++q) {
       float ms_s, ms_m;
-      if ((rc = time_cfg(v, sc_o.first, sc_o.second, &ms_s, &ms_m))) break;
-      if (ms_m < bm) { bm = ms_m; v_o = v; }
+      if ((rc = time_cfg(mi_cands[q].first, mi_cands[q].second, sc_o.first, sc_o.second, &ms_s, &ms_m))) break;
+      if (ms_m < bm) { bm = ms_m; v_o = mi_cands[q].first; sp_o = mi_cands[q].second; }
     }
     if (!rc && bs + bm < best_total) {
       best_total = bs + bm;
       best_o = order;
       best_sc = sc_o;
       best_v = v_o;
+      best_split = sp_o;
       best_s_all = bs;
       best_m_all = bm;
     }
@@ -1195,6 +1206,7 @@ int kb_autotune(kb_handle *h, int32_t trials, kb_tuning *chosen, double *ms_per_
   if (best_o != h->batch_order && apply_schedule(h, best_o) != KB_OK)
     return fail(h, KB_ERR_CUDA, "upload of the run schedule failed");
   h->memint_variant = best_v;
+  h->memint_split = best_split;
   h->sunset_variant = best_sc.first;
   h->grid_sun = best_sc.second;
   if (h->graph) {

@@ -16,7 +16,9 @@
 //                                              by t mod 2
 //   meas            [5][Spad]                 double: F(t-1,t-1), ddF, n, omega, c
 //   epart           [nchunks][4]              double: E_kin, E_pot, E_mem partials
-//   rowacc          [nchunks][Malloc][KC]     double: row sums of the memory integrals
+//   rowacc          [2][nchunks][Malloc][KC]  double: row sums of the memory integrals
+//                                              (the second half only in split mode)
+//   colacc          [2][nchunks][Malloc][KC]  double: column sums (F, rho) of a split step
 //   sunset scratch  [grid][R1 + R2]           double: FP64 cosine-transform intermediates
 #pragma once
 #include <cstdint>
@@ -45,7 +47,8 @@ struct RunDev {
   double *tad;              // [2][nchunks]
   double *meas;             // [5][Spad]
   double *epart;            // [nchunks][4]
-  double *rowacc;           // [nchunks][Malloc][KC] scratch of the memory-integral kernel
+  double *rowacc;           // [2][nchunks][Malloc][KC] row sums of the memory integrals (one per half when split)
+  double *colacc;           // [2][nchunks][Malloc][KC] column sums F, rho of a split step
   int cta_base_sun, cta_base_mi;  // first CTA of this run in the batched grids
   int pad0, pad1;
   // 1/N expansion at NLO (pexp 4), FP64: bubble rings (layout of hist_F) and the
@@ -92,7 +95,7 @@ size_t sunset_scratch_elems(int H);
 int sunset_grid(bool fp64, int num_sms, int total_rows);
 int sunset_max_ctas_per_sm(bool fp64, int variant, size_t smem);
 cudaError_t configure_sunset(bool fp64, size_t smem);
-cudaError_t launch_memint(bool fp64, int variant, const RunDev *d_runs, const int *d_base, int nruns,
+cudaError_t launch_memint(bool fp64, int variant, int split, const RunDev *d_runs, const int *d_base, int nruns,
                           int total_ctas, const int *d_t, int *d_err, int measure, size_t smem, cudaStream_t st);
 size_t memint_smem_bytes(bool fp64, int Malloc, int variant);
 cudaError_t configure_memint(bool fp64, size_t smem);

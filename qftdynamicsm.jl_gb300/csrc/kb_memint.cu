@@ -262,6 +262,19 @@ __device__ void memint_epilogue(const RunDev &R, int c, int t, int tid, const do
   }
 }
 
+// Split mode: the triangle of a chunk is cut between column blocks into two
+// halves with (nearly) equal tile counts; half 0 takes blocks [J0, Js), half 1
+// blocks [Js, Jn]. Both kernels of the split step compute Js the same way.
+__host__ __device__ inline int split_block(int J0, int Jn) {
+  const int nb = Jn - J0 + 1, total = nb * (nb + 1) / 2;
+  int acc = 0;
+  for (int J = J0; J <= Jn; ++J) {
+    acc += Jn - J + 1;
+    if (2 * acc >= total) return J + 1;
+  }
+  return Jn + 1;
+}
+
 // Block = column group (NG threads: column b, orbits j) + row group (NG threads:
 // row a, orbits j) + one producer warp. Both consumer groups read every tile
 // from the shared-memory ring: the column group accumulates
@@ -273,7 +286,12 @@ __device__ void memint_epilogue(const RunDev &R, int c, int t, int tid, const do
 // releases the stage through the empty mbarrier. Once per column block both
 // groups meet at a named barrier: the row sums of that block are complete and
 // the column group runs its leapfrog.
-template <typename TS, int T, int NST, int OPT>
+// SPLIT: CTA 2k + h streams half h of chunk k's triangle, keeps its row sums in
+// row buffer h and stores the column sums of its column blocks instead of
+// running the leapfrog; memint_finish_kernel completes the step. Two CTAs per
+// chunk fill the partial last wave of a large grid and double the CTAs of a
+// small one.
+template <typename TS, int T, int NST, int OPT, bool SPLIT>
 __global__ void __launch_bounds__(2 * T * (KC / OPT) + 32)
 memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int nruns,
               const int *__restrict__ d_t, int *__restrict__ d_err, int measure) {
@@ -293,9 +311,11 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   volatile int *cabort = reinterpret_cast<volatile int *>(misc + 12);
   static_assert(16 + (C::NG / 32) * KC <= 128, "misc scratch too small");
 
-  const int r = run_at(base, nruns, blockIdx.x);
+  const int item = SPLIT ? (int)(blockIdx.x >> 1) : (int)blockIdx.x;
+  const int half = SPLIT ? (int)(blockIdx.x & 1) : 0;
+  const int r = run_at(base, nruns, item);
   const RunDev &R = runs[r];
-  const int c = blockIdx.x - R.cta_base_mi;  // chunk
+  const int c = item - R.cta_base_mi;  // chunk
   const int tid = threadIdx.x;
   const bool producer = tid >= C::NT;
   const bool colgrp = tid < C::NG;
@@ -310,8 +330,8 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   const size_t st_row = (size_t)R.nchunks * rowstride;   // one state row (all chunks)
   // row sums of this chunk, [Malloc][KC]: entries (slot, j0..j0+OPT-1) are only
   // ever written by row-group thread (slot mod T, jq), so they need no atomics;
-  // they live in a global scratch slot that stays in L2.
-  double *rowacc = R.rowacc + (size_t)c * rowstride;
+  // they live in a global scratch slot that stays in L2 (one per half in split mode).
+  double *rowacc = R.rowacc + (size_t)half * R.nchunks * rowstride + (size_t)c * rowstride;
 
   // --- tadpole mass M^2(t-1) from the per-chunk sums of F(t-1,t-1) (fixed order)
   if (warp == 0) {
@@ -343,12 +363,17 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
 
   const bool lo_only = pexp_lo(R.pexp);
   const int J0 = tmin / T, Jn = (t - 1) / T;
-  const int nb = Jn - J0 + 1;
-  const int ntiles = lo_only ? 0 : nb * (nb + 1) / 2;
+  // column blocks of this CTA: all of them, or one half of the triangle
+  const int Js = SPLIT ? split_block(J0, Jn) : J0;
+  const int Jlo = (SPLIT && half == 1) ? Js : J0;
+  const int Jhi = (SPLIT && half == 0) ? Js - 1 : Jn;
+  int ntiles = 0;
+  if (!lo_only)
+    for (int J = Jlo; J <= Jhi; ++J) ntiles += Jn - J + 1;
 
   if (producer) {
-    // ---------------- producer warp: stream every tile of the triangle once
-    TileIt it{J0, J0, Jn};
+    // ---------------- producer warp: stream every tile of its column blocks once
+    TileIt it{Jlo, Jlo, Jn};
     for (int n = 0; n < ntiles; ++n, it.next()) {
       const int stage = n % NST;
       if (n >= NST && !mbar_wait_bounded(empty + stage, (uint32_t)(((n / NST) - 1) & 1))) {
@@ -376,12 +401,12 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
     double pre[OPT];
     for (int o = 0; o < OPT; ++o) pre[o] = 0.0;
     if (!colgrp) {
-      const int a0 = J0 * T + loc;
+      const int a0 = Jlo * T + loc;
       if (a0 >= tmin && a0 <= t - 1)
         for (int o = 0; o < OPT; ++o) pre[o] = rowacc[(size_t)(a0 % Ma) * KC + j0 + o];
     }
 
-    for (int J = J0; J <= Jn && !aborted; ++J) {
+    for (int J = Jlo; J <= Jhi && !aborted; ++J) {
       const int b = J * T + loc;  // column of a column-group thread
       const bool bvalid = colgrp && (b >= tmin) && (b <= t - 1);
       double colF[OPT], colR[OPT];
@@ -504,6 +529,14 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
         break;
       }
 
+      if (SPLIT) {  // column sums of this block, for memint_finish_kernel
+        if (bvalid)
+          for (int o = 0; o < OPT; ++o) {
+            R.colacc[(size_t)c * rowstride + (size_t)(b % Ma) * KC + j0 + o] = colF[o];
+            R.colacc[(size_t)(R.nchunks + c) * rowstride + (size_t)(b % Ma) * KC + j0 + o] = colR[o];
+          }
+        continue;
+      }
       // leapfrog for t' = b (evolve_r!/evolve_F!, Evolution.jl:890-915)
       if (bvalid) {
         const int sb = b % Ma;
@@ -550,7 +583,7 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
         if (b == t - 1) has_emem = true;
       }
     }
-    if (!aborted && colgrp) {
+    if (!SPLIT && !aborted && colgrp) {
       // partial sums of acc_F(t) over this warp's columns (lanes sharing jq)
       for (int o = 0; o < OPT; ++o) {
         double v = diag[o];
@@ -571,7 +604,84 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
     return;
   }
 
-  if (tid < KC) memint_epilogue<TS>(R, c, t, tid, misc, C::NG / 32, M2, measure);
+  if (!SPLIT && tid < KC) memint_epilogue<TS>(R, c, t, tid, misc, C::NG / 32, M2, measure);
+}
+
+// Second kernel of a split step: one CTA per chunk adds the column sums and
+// the two halves' row sums, runs the leapfrog of every t' of the window (the
+// same arithmetic as memint_kernel's), then the diagonal and measurement.
+constexpr int FIN_THREADS = 256;
+
+template <typename TS>
+__global__ void __launch_bounds__(FIN_THREADS)
+memint_finish_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int nruns,
+                     const int *__restrict__ d_t, int measure) {
+  __shared__ double misc[16 + (FIN_THREADS / 32) * KC];
+  const int r = run_at(base, nruns, blockIdx.x);
+  const RunDev &R = runs[r];
+  const int c = blockIdx.x - R.cta_base_mi;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int t = *d_t;
+  const int Ma = R.Malloc, T = R.T;
+  const int tmin = max(1, t - R.M + 1);
+  const size_t rowstride = (size_t)Ma * KC, st_row = (size_t)R.nchunks * rowstride, cs = (size_t)c * rowstride;
+  if (warp == 0) {
+    const double *tad = R.tad + (size_t)((t - 1) & 1) * R.nchunks;
+    double s = 0.0;
+    for (int q = lane; q < R.nchunks; q += 32) s += tad[q];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) {
+      misc[0] = s;
+      misc[1] = s * R.pref_ivol + R.mass2;
+    }
+  }
+  if (tid < KC) misc[2 + tid] = 0.0;
+  __syncthreads();
+  const double M2 = misc[1], dt3 = R.dt3;
+  const bool lo_only = pexp_lo(R.pexp);
+  const double *colF = R.colacc + cs, *colR = R.colacc + (size_t)R.nchunks * rowstride + cs;
+  const double *rowA = R.rowacc + cs, *rowB = R.rowacc + (size_t)R.nchunks * rowstride + cs;
+  const TS *sigr = reinterpret_cast<const TS *>(R.sig_r) + cs;
+  const TS *sigF = reinterpret_cast<const TS *>(R.sig_F) + cs;
+  const double *F1row = R.st_F + (size_t)((t - 1) % 3) * st_row + cs;
+  const double *F2row = R.st_F + (size_t)((t - 2) % 3) * st_row + cs;
+  const double *R1row = R.st_r + (size_t)((t - 1) % 3) * st_row + cs;
+  const double *R2row = R.st_r + (size_t)((t - 2) % 3) * st_row + cs;
+  double *FNrow = R.st_F + (size_t)(t % 3) * st_row + cs;
+  double *RNrow = R.st_r + (size_t)(t % 3) * st_row + cs;
+  TS *hF = reinterpret_cast<TS *>(R.hist_F);
+  TS *hR = reinterpret_cast<TS *>(R.hist_r);
+  const int j = tid % KC;  // FIN_THREADS is a multiple of KC: each thread keeps one orbit
+  const int k = c * KC + j;
+  const double kk = (k < R.S) ? R.k2[k] : 0.0;
+  const double om = (kk + M2) * R.dt2;
+  double diag = 0.0;
+  for (int q = tid; q < (t - tmin) * KC; q += FIN_THREADS) {
+    const int b = tmin + q / KC, sb = b % Ma;
+    const size_t e = (size_t)sb * KC + j;
+    const double wb = (b == tmin) ? 0.5 : 1.0;
+    const double xbr_d = lo_only ? 0.0 : wb * (double)sigr[e];
+    const double xbF_d = lo_only ? 0.0 : wb * (double)sigF[e];
+    const double accF = colF[e] + (rowA[e] + rowB[e]);
+    const double accR = colR[e];
+    const double F1 = F1row[e];
+    const double F2 = (b <= t - 2) ? F2row[e] : F1row[(size_t)((t - 2) % Ma) * KC + j];
+    const double Fn = (2.0 - om) * F1 - F2 - accF * dt3;
+    const double rn = (b == t - 1) ? R.dt : (2.0 - om) * R1row[e] - R2row[e] - accR * dt3;
+    FNrow[e] = Fn;
+    RNrow[e] = rn;
+    const size_t ho = hist_off(Ma, T, c, t, b, j);
+    hF[ho] = (TS)Fn;
+    hR[ho] = (TS)rn;
+    diag += xbr_d * Fn + xbF_d * rn;
+    if (b == t - 1) misc[2 + j] = accF;
+  }
+  // partial sums of acc_F(t) per orbit: lanes l, l^8, l^16, l^24 share an orbit
+  diag += __shfl_xor_sync(0xffffffffu, diag, 8);
+  diag += __shfl_xor_sync(0xffffffffu, diag, 16);
+  if (lane < KC) misc[16 + warp * KC + lane] = diag;
+  __syncthreads();
+  if (tid < KC) memint_epilogue<TS>(R, c, t, tid, misc, FIN_THREADS / 32, M2, measure);
 }
 
 // ---------------------------------------------------------------------------
@@ -1051,23 +1161,42 @@ size_t memint_smem_bytes(bool fp64, int Malloc, int variant) {
 }
 
 cudaError_t configure_memint(bool fp64, size_t smem) {
-  if (fp64)
-    return cudaFuncSetAttribute(memint_kernel<double, CfgF64::T, CfgF64::NST, CfgF64::OPT>,
+  if (fp64) {
+    cudaError_t e = cudaFuncSetAttribute(memint_kernel<double, CfgF64::T, CfgF64::NST, CfgF64::OPT, false>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(memint_kernel<double, CfgF64::T, CfgF64::NST, CfgF64::OPT, true>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  cudaError_t e = cudaFuncSetAttribute(memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT>,
+  }
+  cudaError_t e = cudaFuncSetAttribute(memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT, false>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT, true>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   return cudaFuncSetAttribute(memint_blk_kernel<CfgF32::NST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)smem);
 }
 
-cudaError_t launch_memint(bool fp64, int variant, const RunDev *d_runs, const int *d_base, int nruns,
+cudaError_t launch_memint(bool fp64, int variant, int split, const RunDev *d_runs, const int *d_base, int nruns,
                           int total_ctas, const int *d_t, int *d_err, int measure, size_t smem, cudaStream_t st) {
+  if (split && (fp64 || variant == 1)) {  // two half-triangle CTAs per chunk, then the finishing kernel
+    if (fp64) {
+      memint_kernel<double, CfgF64::T, CfgF64::NST, CfgF64::OPT, true>
+          <<<2 * total_ctas, CfgF64::NT + 32, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure);
+      memint_finish_kernel<double><<<total_ctas, FIN_THREADS, 0, st>>>(d_runs, d_base, nruns, d_t, measure);
+    } else {
+      memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT, true>
+          <<<2 * total_ctas, CfgF32::NT + 32, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure);
+      memint_finish_kernel<float><<<total_ctas, FIN_THREADS, 0, st>>>(d_runs, d_base, nruns, d_t, measure);
+    }
+    return cudaGetLastError();
+  }
   if (fp64)
-    memint_kernel<double, CfgF64::T, CfgF64::NST, CfgF64::OPT>
+    memint_kernel<double, CfgF64::T, CfgF64::NST, CfgF64::OPT, false>
         <<<total_ctas, CfgF64::NT + 32, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure);
   else if (variant == 1)
-    memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT>
+    memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT, false>
         <<<total_ctas, CfgF32::NT + 32, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure);
   else
     memint_blk_kernel<CfgF32::NST><<<total_ctas, 288, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure);

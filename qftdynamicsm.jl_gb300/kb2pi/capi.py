@@ -50,11 +50,12 @@ class KbMeasScalars(C.Structure):
 
 class KbTuning(C.Structure):
     _fields_ = [("memint_variant", C.c_int32), ("sunset_grid", C.c_int32), ("batch_order", C.c_int32),
-                ("sunset_variant", C.c_int32)]
+                ("sunset_variant", C.c_int32), ("memint_split", C.c_int32), ("reserved", C.c_int32 * 3)]
 
     def as_dict(self):
         return {"memint_variant": self.memint_variant, "sunset_grid": self.sunset_grid,
-                "batch_order": self.batch_order, "sunset_variant": self.sunset_variant}
+                "batch_order": self.batch_order, "sunset_variant": self.sunset_variant,
+                "memint_split": self.memint_split}
 
 
 class KbError(RuntimeError):
@@ -296,7 +297,8 @@ class Handle:
         self._check(self.lib.kb_get_tuning(self.h, C.byref(out)))
         return out.as_dict()
 
-    def set_tuning(self, memint_variant=None, sunset_grid=None, batch_order=None, sunset_variant=None):
+    def set_tuning(self, memint_variant=None, sunset_grid=None, batch_order=None, sunset_variant=None,
+                   memint_split=None):
         cur = KbTuning()
         self._check(self.lib.kb_get_tuning(self.h, C.byref(cur)))
         if memint_variant is not None:
@@ -307,6 +309,8 @@ class Handle:
             cur.batch_order = int(batch_order)
         if sunset_variant is not None:
             cur.sunset_variant = int(sunset_variant)
+        if memint_split is not None:
+            cur.memint_split = int(memint_split)
         self._check(self.lib.kb_set_tuning(self.h, C.byref(cur)))
 
     def autotune(self, trials=3):

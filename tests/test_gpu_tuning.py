@@ -100,3 +100,63 @@ def test_batch_orders_are_bitwise_identical():
         h.close()
     for a, b in zip(out[0], out[1]):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("pexp", [1, 0, 4])
+def test_memint_split_matches_oracle_fp64(pexp):
+    """Split memory integrals (two half-triangle CTAs per chunk + finishing
+    kernel) against the FP64 oracle: 1e-10, the plain path's bound; the window
+    wraps so both halves and the ring edges are exercised."""
+    from kbtest_util import make_oracle
+
+    cfg = dict(Ns=8, M=23, N=4, lam=3.0, dt=0.1, mass2=1.0, pexp=pexp, T=1.5)
+    g = make_gpu(cfg, 0)
+    o = make_oracle(cfg)
+    _, k2, _ = g.orbits()
+    n0 = occupation(cfg, k2)
+    g.init(0, n0, 1.0)
+    o.init_occupation(n0, 1.0)
+    g.set_tuning(memint_split=1)
+    assert g.tuning()["memint_split"] == 1
+    for t in range(3, 63):
+        g.step(t)
+        o.step(t)
+        if t % 10 == 2:
+            mg, mo = g.measure(0, t), o.measure(t)
+            assert rel(mg["n"], mo["n"]) <= 1e-10
+            assert abs(mg["E"] - mo["E"]) <= 1e-10 * abs(mo["E"])
+            tp = max(g.window(0)[0], t - 15)
+            assert rel(g.get(0, 0, t, tp), o.F(t, tp)) <= 1e-10
+    g.close()
+    o.close()
+
+
+def test_memint_split_mixed_and_batched():
+    from kb2pi import capi
+
+    a = evolve(CFG, 1, 60, tuning={"memint_split": 0})
+    b = evolve(CFG, 1, 60, tuning={"memint_split": 1})
+    assert rel(a[0]["n"], b[0]["n"]) <= 1e-6
+    assert abs(a[0]["E"] - b[0]["E"]) <= 1e-6 * abs(a[0]["E"])
+    # a batched FP64 handle in split mode equals its single runs to rounding
+    cfgs = [dict(Ns=8, M=20, lam=2.0, T=1.0), dict(Ns=12, M=37, lam=4.0, T=2.0)]
+    ps = [capi.KbParams(Ns=c["Ns"], sdim=3, M=c["M"], N=4, pexp=1, precision=0, device=0, flags=0, dt=0.1,
+                        lam=c["lam"], mass2=1.0, mass=1.0) for c in cfgs]
+    hb = capi.Handle(ps)
+    hs = [capi.Handle([p]) for p in ps]
+    for r, c in enumerate(cfgs):
+        _, k2, _ = hb.orbits(r)
+        hb.init(r, occupation(dict(c), k2), 1.0)
+        hs[r].init(0, occupation(dict(c), k2), 1.0)
+    hb.set_tuning(memint_split=1, batch_order=1)
+    hb.steps(3, 50, 0)
+    for r, h in enumerate(hs):
+        h.steps(3, 50, 0)
+        x, y = hb.measure(r, 52), h.measure(0, 52)
+        assert rel(x["n"], y["n"]) <= 1e-10 and abs(x["E"] - y["E"]) <= 1e-10 * abs(y["E"])
+    for h in [hb] + hs:
+        h.close()
+    h = make_gpu(CFG, 1)
+    with pytest.raises(capi.KbError, match="memint_split"):
+        h.set_tuning(memint_variant=0, memint_split=1)
+    h.close()
