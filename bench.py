@@ -549,7 +549,16 @@ def run_ours(args):
     peak, peak_kind = read_peaks()
     achieved = alg / (mi_ms / 1000.0) / 1e9
     # the committed capture covers this workload only
-    traffic = read_traffic("traffic_bytes_per_launch") if (CFG["Ns"], CFG["M"]) == (64, 1000) else None
+    # memory-integral kernels of the chosen configuration; the committed capture
+    # covers the benchmark workload in each mode
+    split = bool(tuning.get("memint_split"))
+    if tuning.get("memint_variant") == 0:
+        mi_kernel, key = "memint_blk_kernel<3>", None
+    elif split:
+        mi_kernel, key = "memint_kernel<float,32,3,2,split> + memint_finish_kernel", "traffic_bytes_per_step_split"
+    else:
+        mi_kernel, key = "memint_kernel<float,32,3,2>", "traffic_bytes_per_launch"
+    traffic = read_traffic(key) if key and (CFG["Ns"], CFG["M"]) == (64, 1000) else None
     line = {
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -565,7 +574,7 @@ def run_ours(args):
         "tuning": tuning,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                     "kernel": "memint_kernel<float,32,3,2>", "algorithmic_bytes": alg},
+                     "kernel": mi_kernel, "algorithmic_bytes": alg},
         "clocks": clk.summary(),
         "e2e": {"value": e2e_val, "unit": "steps/s", "h2d_bytes_per_step": 4, "d2h_bytes_per_step": d2h,
                 "path": "kb_step + kb_measure through the C ABI, host buffers, wall clock"},
