@@ -166,29 +166,40 @@ struct TileIt {
 
 // issued by the producer warp: the F and rho tiles (each one contiguous block in
 // the tile-major history), Sigma_rho of the tile's rows and Sigma_rho, Sigma_F of
-// its columns, all into one stage
+// its columns, all into one stage. The consumers only read rows a in
+// [tmin, t-1], so a tile the window cuts is copied from its first to its last
+// such row: one copy of contiguous whole rows (the newest row block is partly
+// empty, the oldest diagonal tile starts at tmin). Cutting columns as well
+// (one copy per row) saves another 7 % of the bytes at Ns = 64 but costs more
+// time than it saves: the many small copies slow every CTA. The stage offsets
+// are those of the whole tile, so the consumers index it unchanged.
 template <typename TS, typename C>
 __device__ __forceinline__ void issue_tile(int stage, int I, int J, const RunDev &R, int c, TS *stages,
-                                           uint64_t *full) {
+                                           uint64_t *full, int tmin, int tlast) {
   const int lane = threadIdx.x & 31;
   uint64_t *bar = full + stage;
-  if (lane == 0) mbar_expect_tx(bar, C::TX_BYTES);
-  __syncwarp();
   TS *dst = stages + (size_t)stage * C::STAGE;
   const int sa0 = (I * C::T) % R.Malloc;  // Malloc is a multiple of T: rows stay contiguous
   const int sb0 = (J * C::T) % R.Malloc;
   const TS *hF = reinterpret_cast<const TS *>(R.hist_F);
   const TS *hR = reinterpret_cast<const TS *>(R.hist_r);
   if (lane == 0) {
-    const size_t off = hist_off(R.Malloc, C::T, c, sa0, sb0, 0);  // start of the tile
-    bulk_g2s(dst, hF + off, C::T * C::T * KC * sizeof(TS), bar);
-    bulk_g2s(dst + C::TILE, hR + off, C::T * C::T * KC * sizeof(TS), bar);
+    constexpr int T = C::T;
+    constexpr uint32_t ROWB = (uint32_t)(C::RS * sizeof(TS));
+    const size_t off = hist_off(R.Malloc, T, c, sa0, sb0, 0);  // start of the tile
+    const int rlo = max(0, tmin - I * T), rhi = min(T - 1, tlast - I * T);  // rows of the window
+    const uint32_t n = (uint32_t)(rhi - rlo + 1) * ROWB;
+    mbar_expect_tx(bar, 2 * n + 3 * C::XV * (uint32_t)sizeof(TS));
+    const size_t e = (size_t)rlo * C::RS;
+    bulk_g2s(dst + e, hF + off + e, n, bar);
+    bulk_g2s(dst + C::TILE + e, hR + off + e, n, bar);
     const TS *sr = reinterpret_cast<const TS *>(R.sig_r) + (size_t)c * R.Malloc * KC;
     const TS *sF = reinterpret_cast<const TS *>(R.sig_F) + (size_t)c * R.Malloc * KC;
     bulk_g2s(dst + 2 * C::TILE, sr + (size_t)sa0 * KC, C::XV * sizeof(TS), bar);
     bulk_g2s(dst + 2 * C::TILE + C::XV, sr + (size_t)sb0 * KC, C::XV * sizeof(TS), bar);
     bulk_g2s(dst + 2 * C::TILE + 2 * C::XV, sF + (size_t)sb0 * KC, C::XV * sizeof(TS), bar);
   }
+  __syncwarp();
 }
 
 __device__ __forceinline__ void consumer_sync(int nthreads) {
@@ -384,7 +395,7 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
         break;
       }
       if (*abort_flag) break;
-      issue_tile<TS, C>(stage, it.I, it.J, R, c, stages, full);
+      issue_tile<TS, C>(stage, it.I, it.J, R, c, stages, full, tmin, t - 1);
       if (lane == 0) *issued_count = n + 1;
     }
     __syncwarp();
@@ -784,7 +795,7 @@ memint_blk_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base,
         break;
       }
       if (*abort_flag) break;
-      issue_tile<float, C>(stage, it.I, it.J, R, c, stages, full);
+      issue_tile<float, C>(stage, it.I, it.J, R, c, stages, full, tmin, t - 1);
       if (lane == 0) *issued_count = n + 1;
     }
     __syncwarp();
