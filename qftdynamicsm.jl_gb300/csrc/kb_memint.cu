@@ -667,6 +667,8 @@ memint_finish_kernel(const RunDev *__restrict__ runs, const int *__restrict__ ba
   const double kk = (k < R.S) ? R.k2[k] : 0.0;
   const double om = (kk + M2) * R.dt2;
   double diag = 0.0;
+  // unrolled: the loads of several t' are in flight at once (the kernel is latency-bound otherwise)
+#pragma unroll 4
   for (int q = tid; q < (t - tmin) * KC; q += FIN_THREADS) {
     const int b = tmin + q / KC, sb = b % Ma;
     const size_t e = (size_t)sb * KC + j;
