@@ -53,8 +53,7 @@ struct SunGeom {
     P = H * (H + 1) / 2;
     P4 = rup4(P);
     S = H * (H + 1) * (H + 2) / 6;
-    const int e = H * P4, d = P * H4;
-    r1 = e > d ? e : d;
+    r1 = H * P4;  // E, then D (both [H][P4])
     if (S > r1) r1 = S;
     r2 = H * P4;
     if (S > r2) r2 = S;
@@ -62,6 +61,23 @@ struct SunGeom {
     r2 = rup4(r2);
   }
 };
+
+// shared memory of sunset_kernel without the expand table: cosine matrix,
+// one orbit buffer, the two pass regions (FP32 only), pass tables, pair list
+__host__ __device__ inline size_t sun_smem_base(bool fp64, int H) {
+  SunGeom g(H);
+  const size_t es = fp64 ? 8 : 4;
+  size_t elems = (size_t)g.H * g.H4 + rup4(g.S);
+  if (!fp64) elems += (size_t)g.r1 + g.r2;
+  return elems * es + (size_t)(g.H + 1 + g.P4 / 4 + 1) * sizeof(int) + (size_t)rup4(g.P) * sizeof(uint16_t) + 64;
+}
+// the expand table ([H][P4] orbit indices) is kept when it fits next to the
+// rest in the 227 KB a CTA may use
+constexpr size_t SUN_SMEM_CAP = 232448;
+__host__ __device__ inline bool sun_etab_fits(bool fp64, int H) {
+  SunGeom g(H);
+  return sun_smem_base(fp64, H) + (size_t)g.H * g.P4 * sizeof(uint16_t) <= SUN_SMEM_CAP;
+}
 
 // 4-wide vector load/store for float (float4) and double (2 x double2)
 __device__ __forceinline__ void ld4(const float *p, float v[4]) {
@@ -81,12 +97,16 @@ __device__ __forceinline__ void st4(double *p, const double v[4]) {
   *reinterpret_cast<double2 *>(p + 2) = make_double2(v[2], v[3]);
 }
 
+// orbit index of the sorted triple a <= b <= c in 32-bit arithmetic (c < 256
+// here: the pair list packs coordinates into bytes)
+__device__ __forceinline__ int orb3s(int a, int b, int c) { return c * (c + 1) * (c + 2) / 6 + tri2(b) + a; }
+
 // orbit index of (x, y, z) given y <= z
 __device__ __forceinline__ int orb_of(int x, int y, int z) {
   const int lo = min(x, y);
   const int mid = (x <= y) ? y : min(x, z);
   const int hi = max(x, z);
-  return orb3(lo, mid, hi);
+  return orb3s(lo, mid, hi);
 }
 
 template <typename TC>
@@ -97,17 +117,45 @@ struct SunCtx {
   const int *off3;      // [P4/4 + 1] item offsets of pass 3
   TC *R1, *R2, *bufF;
   SunGeom g;
+  const uint16_t *etab = nullptr;  // [H][P4]: orbit of E[x][p] (0 in the padding), when it fits
 };
 
 // expand: E[x][p] = in(orbit of (x, y_p, z_p)) for x < H, p < P
 template <typename TC, typename In>
 __device__ void sun_expand(const SunCtx<TC> &c, TC *E, In in) {
+  if (c.etab) {
+    const int n = c.g.H * c.g.P4;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) E[i] = in(c.etab[i]);
+    return;
+  }
   const int n = c.g.H * c.g.P;
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     const int x = i / c.g.P, p = i - x * c.g.P;
     const int y = c.pr[p] & 255, z = c.pr[p] >> 8;
     E[x * c.g.P4 + p] = in(orb_of(x, y, z));
   }
+}
+
+// orbit table of sun_expand in the layout of E
+__device__ void sun_build_etab(const SunGeom &g, const uint16_t *pr, uint16_t *etab) {
+  for (int i = threadIdx.x; i < g.H * g.P4; i += blockDim.x) {
+    const int x = i / g.P4, p = i - x * g.P4;
+    etab[i] = (p < g.P) ? (uint16_t)orb_of(x, pr[p] & 255, pr[p] >> 8) : (uint16_t)0;
+  }
+}
+
+// unroll of the pass loops (FP64 at 2: the 4 x 4 double tile fills the registers)
+template <typename TC>
+struct SunUnroll {
+  static constexpr int value = sizeof(TC) == 4 ? 4 : 2;
+};
+
+template <typename TC>
+__device__ __forceinline__ void fma4x4(TC acc[4][4], const TC a[4], const TC b[4]) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] += a[i] * b[j];
 }
 
 // pass 1: B[X][p] = sum_x CT[x][X] E[x][p]
@@ -119,14 +167,12 @@ __device__ void sun_pass1(const SunCtx<TC> &c, const TC *E, TC *B) {
     const int xb = it / npb, pb = it - xb * npb;
     const int X0 = 4 * xb, p0 = 4 * pb;
     TC acc[4][4] = {};
+#pragma unroll(SunUnroll<TC>::value)
     for (int x = 0; x < H; ++x) {
       TC cv[4], ev[4];
       ld4(c.CT + x * c.g.H4 + X0, cv);
       ld4(E + x * P4 + p0, ev);
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] += cv[i] * ev[j];
+      fma4x4(acc, cv, ev);
     }
 #pragma unroll
     for (int i = 0; i < 4; ++i)
@@ -134,7 +180,10 @@ __device__ void sun_pass1(const SunCtx<TC> &c, const TC *E, TC *B) {
   }
 }
 
-// pass 2: D[tri2(Y)+X][z] = sum_y CT[y][Y] B[X][(min(y,z), max(y,z))], Y >= X
+// pass 2: D[z][tri2(Y)+X] = sum_y CT[y][Y] B[X][(min(y,z), max(y,z))], Y >= X.
+// B[X] holds the pairs (y <= z) at tri2(z) + y; the y loop is split where the
+// four z of a thread's tile all lie above y (four rows of B, one entry each) or
+// all below it (four neighbouring entries of row y).
 template <typename TC>
 __device__ void sun_pass2(const SunCtx<TC> &c, const TC *B, TC *D) {
   const int H = c.g.H, H4 = c.g.H4, P4 = c.g.P4;
@@ -151,32 +200,56 @@ __device__ void sun_pass2(const SunCtx<TC> &c, const TC *B, TC *D) {
     const int yb = r / nzb, zb = r - yb * nzb;
     const int Y0 = 4 * (X / 4) + 4 * yb, z0 = 4 * zb;
     const TC *Bx = B + X * P4;
+    const TC *ct = c.CT + Y0;
+    int zc[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) zc[j] = min(z0 + j, H - 1);
     TC acc[4][4] = {};
-    for (int y = 0; y < H; ++y) {
-      TC cv[4], bv[4];
-      ld4(c.CT + y * H4 + Y0, cv);
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int z = min(z0 + j, H - 1);
-        bv[j] = (y <= z) ? Bx[tri2(z) + y] : Bx[tri2(y) + z];
+    const int ya = min(z0, H), yc = min(z0 + 4, H);
+    {  // y < z0 <= z
+      const TC *b0 = Bx + tri2(zc[0]), *b1 = Bx + tri2(zc[1]), *b2 = Bx + tri2(zc[2]), *b3 = Bx + tri2(zc[3]);
+#pragma unroll(SunUnroll<TC>::value)
+      for (int y = 0; y < ya; ++y) {
+        TC cv[4];
+        ld4(ct + y * H4, cv);
+        const TC bv[4] = {b0[y], b1[y], b2[y], b3[y]};
+        fma4x4(acc, cv, bv);
       }
+    }
+    for (int y = ya; y < yc; ++y) {  // the diagonal block
+      TC cv[4], bv[4];
+      ld4(ct + y * H4, cv);
 #pragma unroll
-      for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] += cv[i] * bv[j];
+      for (int j = 0; j < 4; ++j) bv[j] = (y <= zc[j]) ? Bx[tri2(zc[j]) + y] : Bx[tri2(y) + zc[j]];
+      fma4x4(acc, cv, bv);
+    }
+    {  // z <= z0 + 3 < y (only when z0 + 3 < H - 1, so no z is clamped)
+      const TC *by = Bx + tri2(yc) + z0;
+#pragma unroll(SunUnroll<TC>::value)
+      for (int y = yc; y < H; ++y) {
+        TC cv[4];
+        ld4(ct + y * H4, cv);
+        const TC bv[4] = {by[0], by[1], by[2], by[3]};
+        fma4x4(acc, cv, bv);
+        by += y + 1;
+      }
     }
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       const int Y = Y0 + i;
-      if (Y >= X && Y < H) st4(D + (tri2(Y) + X) * H4 + z0, acc[i]);
+      if (Y < X || Y >= H) continue;
+      const int q = tri2(Y) + X;
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if (z0 + j < H) D[(z0 + j) * P4 + q] = acc[i][j];
     }
   }
 }
 
-// pass 3: out(orbit(X,Y,Z), sum_z CT[z][Z] D[q][z]) for q = (X,Y), Z >= Y
+// pass 3: out(orbit(X,Y,Z), sum_z CT[z][Z] D[z][q]) for q = (X,Y), Z >= Y
 template <typename TC, typename Out>
 __device__ void sun_pass3(const SunCtx<TC> &c, const TC *D, Out out) {
-  const int H = c.g.H, H4 = c.g.H4, P = c.g.P;
+  const int H = c.g.H, H4 = c.g.H4, P = c.g.P, P4 = c.g.P4;
   const int nqb = c.g.P4 / 4;
   const int total = c.off3[nqb];
   for (int it = threadIdx.x; it < total; it += blockDim.x) {
@@ -190,18 +263,12 @@ __device__ void sun_pass3(const SunCtx<TC> &c, const TC *D, Out out) {
     const int Ymin = c.pr[min(q0, P - 1)] >> 8;
     const int Z0 = 4 * (Ymin / 4) + 4 * (it - c.off3[qb]);
     TC acc[4][4] = {};
-    int qrow[4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) qrow[i] = min(q0 + i, P - 1) * H4;
+#pragma unroll(SunUnroll<TC>::value)
     for (int z = 0; z < H; ++z) {
       TC cv[4], dv[4];
       ld4(c.CT + z * H4 + Z0, cv);
-#pragma unroll
-      for (int i = 0; i < 4; ++i) dv[i] = D[qrow[i] + z];
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] += dv[i] * cv[j];
+      ld4(D + z * P4 + q0, dv);
+      fma4x4(acc, dv, cv);
     }
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
@@ -211,7 +278,7 @@ __device__ void sun_pass3(const SunCtx<TC> &c, const TC *D, Out out) {
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const int Z = Z0 + j;
-        if (Z >= Y && Z < H) out(orb3(X, Y, Z), acc[i][j]);
+        if (Z >= Y && Z < H) out(orb3s(X, Y, Z), acc[i][j]);
       }
     }
   }
@@ -267,6 +334,7 @@ sunset_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
       int *off2 = reinterpret_cast<int *>(p);
       int *off3 = off2 + (g.H + 1);
       uint16_t *pr = reinterpret_cast<uint16_t *>(off3 + (g.P4 / 4 + 1));
+      uint16_t *etab = sun_etab_fits(sizeof(TC) == 8, g.H) ? pr + rup4(g.P) : nullptr;
       for (int i = threadIdx.x; i < g.H * g.H4; i += blockDim.x) {
         const int x = i / g.H4, X = i - x * g.H4;
         CT[i] = (X < g.H) ? (TC)R.Cm[X * g.H + x] : (TC)0;
@@ -287,20 +355,41 @@ sunset_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
           off3[qb + 1] = off3[qb] + (g.H4 / 4 - Ymin / 4);
         }
       }
+      if (etab) sun_build_etab(g, pr, etab);
       __syncthreads();
-      c = SunCtx<TC>{CT, pr, off2, off3, R1, R2, bufF, g};
+      c = SunCtx<TC>{CT, pr, off2, off3, R1, R2, bufF, g, etab};
     }
     const int S = c.g.S;
     const int slot = tp % R.Malloc;
     const size_t rowstride = (size_t)R.Malloc * KC;
-    const int r3 = (t - 1) % 3;
-    const double *stF = R.st_F + (size_t)r3 * R.nchunks * rowstride + (size_t)slot * KC;
-    const double *stR = R.st_r + (size_t)r3 * R.nchunks * rowstride + (size_t)slot * KC;
     auto gidx = [&](int o) { return (size_t)(o / KC) * rowstride + (o % KC); };
+    // row (t-1, t') of a history ring (the storage-type copy of the state row;
+    // chunks are Malloc^2 KC apart) into shared memory, orbit layout
+    const size_t hbase = hist_off(R.Malloc, R.T, 0, t - 1, tp, 0);
+    const size_t cstride = (size_t)R.Malloc * R.Malloc * KC;
+    auto stage = [&](const void *hist, TC *dst) {
+      const TS *h = reinterpret_cast<const TS *>(hist) + hbase;
+      constexpr int U = 4;
+      for (int o0 = threadIdx.x; o0 < S; o0 += U * blockDim.x) {
+        TS v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int o = o0 + u * blockDim.x;
+          v[u] = (o < S) ? h[(size_t)(o / KC) * cstride + (o % KC)] : (TS)0;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+          if (o0 + u * blockDim.x < S) dst[o0 + u * blockDim.x] = (TC)v[u];
+      }
+      __syncthreads();
+    };
 
-    // forward transforms of F(t-1,t') -> bufF and rho(t-1,t') -> R2 (orbit layout)
-    sun_transform<TC>(c, [&](int o) { return (TC)stF[gidx(o)]; }, [&](int o, TC v) { c.bufF[o] = v; });
-    sun_transform<TC>(c, [&](int o) { return (TC)stR[gidx(o)]; }, [&](int o, TC v) { c.R2[o] = v; });
+    // forward transforms of F(t-1,t') -> bufF and rho(t-1,t') -> R2 (orbit layout);
+    // each row is staged in the region the transform writes last
+    stage(R.hist_F, c.bufF);
+    sun_transform<TC>(c, [&](int o) { return c.bufF[o]; }, [&](int o, TC v) { c.bufF[o] = v; });
+    stage(R.hist_r, c.R2);
+    sun_transform<TC>(c, [&](int o) { return c.R2[o]; }, [&](int o, TC v) { c.R2[o] = v; });
 
     // pointwise sunset in position space (Evolution.jl:28-29, classical :114-115)
     const bool classical = (R.pexp == 2);
@@ -315,12 +404,12 @@ sunset_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
     // inverse transforms straight into the Sigma rings (scaled by ivol^3 * coefficient)
     TS *sigr = reinterpret_cast<TS *>(R.sig_r) + (size_t)slot * KC;
     TS *sigF = reinterpret_cast<TS *>(R.sig_F) + (size_t)slot * KC;
-    const double fr = R.fac_r, fF = R.fac_F;
+    const TC fr = (TC)R.fac_r, fF = (TC)R.fac_F;
     const TC *gr = c.R2;
     // expand reads R2 into R1 before pass 1 overwrites R2
-    sun_transform<TC>(c, [&](int o) { return gr[o]; }, [&](int o, TC v) { sigr[gidx(o)] = (TS)(fr * (double)v); });
+    sun_transform<TC>(c, [&](int o) { return gr[o]; }, [&](int o, TC v) { sigr[gidx(o)] = (TS)(fr * v); });
     const TC *gF = c.bufF;
-    sun_transform<TC>(c, [&](int o) { return gF[o]; }, [&](int o, TC v) { sigF[gidx(o)] = (TS)(fF * (double)v); });
+    sun_transform<TC>(c, [&](int o) { return gF[o]; }, [&](int o, TC v) { sigF[gidx(o)] = (TS)(fF * v); });
   }
 }
 
@@ -328,10 +417,7 @@ sunset_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
 
 size_t sunset_smem_bytes(bool fp64, int H) {
   SunGeom g(H);
-  const size_t es = fp64 ? sizeof(double) : sizeof(float);
-  size_t elems = (size_t)g.H * g.H4 + rup4(g.S);
-  if (!fp64) elems += (size_t)g.r1 + g.r2;
-  return elems * es + (size_t)(g.H + 1 + g.P4 / 4 + 1) * sizeof(int) + (size_t)g.P * sizeof(uint16_t) + 64;
+  return sun_smem_base(fp64, H) + (sun_etab_fits(fp64, H) ? (size_t)g.H * g.P4 * sizeof(uint16_t) : 0);
 }
 
 size_t sunset_scratch_elems(int H) {
