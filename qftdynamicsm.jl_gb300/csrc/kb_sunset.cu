@@ -55,7 +55,7 @@ struct SunGeom {
     S = H * (H + 1) * (H + 2) / 6;
     r1 = H * P4;  // E, then D (both [H][P4])
     if (S > r1) r1 = S;
-    r2 = H * P4;
+    r2 = H * P4 + 4;  // B: pass 2 reads up to 3 entries past the last row
     if (S > r2) r2 = S;
     r1 = rup4(r1);
     r2 = rup4(r2);
@@ -67,7 +67,7 @@ struct SunGeom {
 __host__ __device__ inline size_t sun_smem_base(bool fp64, int H) {
   SunGeom g(H);
   const size_t es = fp64 ? 8 : 4;
-  size_t elems = (size_t)g.H * g.H4 + rup4(g.S);
+  size_t elems = (size_t)g.H4 * g.H4 + rup4(g.S);
   if (!fp64) elems += (size_t)g.r1 + g.r2;
   return elems * es + (size_t)(g.H + 1 + g.P4 / 4 + 1) * sizeof(int) + (size_t)rup4(g.P) * sizeof(uint16_t) + 64;
 }
@@ -111,7 +111,7 @@ __device__ __forceinline__ int orb_of(int x, int y, int z) {
 
 template <typename TC>
 struct SunCtx {
-  const TC *CT;         // [H][H4]: CT[x][X] = C[X][x]
+  const TC *CT;         // [H4][H4]: CT[x][X] = C[X][x], zero where x or X >= H
   const uint16_t *pr;   // [P]: pair p -> (lo | hi << 8)
   const int *off2;      // [H+1] item offsets of pass 2
   const int *off3;      // [P4/4 + 1] item offsets of pass 3
@@ -181,9 +181,14 @@ __device__ void sun_pass1(const SunCtx<TC> &c, const TC *E, TC *B) {
 }
 
 // pass 2: D[z][tri2(Y)+X] = sum_y CT[y][Y] B[X][(min(y,z), max(y,z))], Y >= X.
-// B[X] holds the pairs (y <= z) at tri2(z) + y; the y loop is split where the
-// four z of a thread's tile all lie above y (four rows of B, one entry each) or
-// all below it (four neighbouring entries of row y).
+// B[X] holds the pairs (y <= z) at tri2(z) + y. Every thread walks y in blocks
+// of four and reads the 4 x 4 block of the symmetric B[X] at (y0.., z0..) as
+// four rows of four packed entries: rows y0 + k at columns z0.. when y0 >= z0,
+// rows z0 + k at columns y0.. (the transposed block) when y0 < z0; the block
+// is then picked entry by entry, so all lanes run the same instructions
+// whatever their z block. Rows past H - 1 are read as row H - 1 (their cosine
+// rows are zero); the entries picked from outside the triangle only reach
+// accumulators of z >= H, which are not stored.
 template <typename TC>
 __device__ void sun_pass2(const SunCtx<TC> &c, const TC *B, TC *D) {
   const int H = c.g.H, H4 = c.g.H4, P4 = c.g.P4;
@@ -196,52 +201,43 @@ __device__ void sun_pass2(const SunCtx<TC> &c, const TC *B, TC *D) {
       if (c.off2[mid] <= it) lo = mid; else hi = mid - 1;
     }
     const int X = lo;
+    const int nyb = nzb - X / 4;  // Y blocks of this X (Y >= 4 (X / 4))
     const int r = it - c.off2[X];
-    const int yb = r / nzb, zb = r - yb * nzb;
+    const int zb = r / nyb, yb = r - zb * nyb;  // neighbouring threads share z0
     const int Y0 = 4 * (X / 4) + 4 * yb, z0 = 4 * zb;
     const TC *Bx = B + X * P4;
-    const TC *ct = c.CT + Y0;
-    int zc[4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) zc[j] = min(z0 + j, H - 1);
     TC acc[4][4] = {};
-    const int ya = min(z0, H), yc = min(z0 + 4, H);
-    {  // y < z0 <= z
-      const TC *b0 = Bx + tri2(zc[0]), *b1 = Bx + tri2(zc[1]), *b2 = Bx + tri2(zc[2]), *b3 = Bx + tri2(zc[3]);
-#pragma unroll(SunUnroll<TC>::value)
-      for (int y = 0; y < ya; ++y) {
-        TC cv[4];
-        ld4(ct + y * H4, cv);
-        const TC bv[4] = {b0[y], b1[y], b2[y], b3[y]};
-        fma4x4(acc, cv, bv);
-      }
-    }
-    for (int y = ya; y < yc; ++y) {  // the diagonal block
-      TC cv[4], bv[4];
-      ld4(ct + y * H4, cv);
+    for (int y0 = 0; y0 < H4; y0 += 4) {
+      TC cv[4][4];  // cv[i][a] = C[Y0 + a][y0 + i]
 #pragma unroll
-      for (int j = 0; j < 4; ++j) bv[j] = (y <= zc[j]) ? Bx[tri2(zc[j]) + y] : Bx[tri2(y) + zc[j]];
-      fma4x4(acc, cv, bv);
-    }
-    {  // z <= z0 + 3 < y (only when z0 + 3 < H - 1, so no z is clamped)
-      const TC *by = Bx + tri2(yc) + z0;
-#pragma unroll(SunUnroll<TC>::value)
-      for (int y = yc; y < H; ++y) {
-        TC cv[4];
-        ld4(ct + y * H4, cv);
-        const TC bv[4] = {by[0], by[1], by[2], by[3]};
-        fma4x4(acc, cv, bv);
-        by += y + 1;
+      for (int i = 0; i < 4; ++i) ld4(c.CT + (y0 + i) * H4 + Y0, cv[i]);
+      const bool ge = y0 >= z0, gt = y0 > z0;
+      const int rb = ge ? y0 : z0, cb = ge ? z0 : y0;
+      TC L[4][4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const TC *row = Bx + tri2(min(rb + k, H - 1)) + cb;
+#pragma unroll
+        for (int m = 0; m < 4; ++m) L[k][m] = row[m];
       }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          // B(y0 + i, z0 + j): L[i][j] in the direct layout, L[j][i] in the transposed one
+          const TC v = (i == j) ? L[i][i] : ((j < i ? ge : gt) ? L[i][j] : L[j][i]);
+#pragma unroll
+          for (int a = 0; a < 4; ++a) acc[a][j] += cv[i][a] * v;
+        }
     }
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const int Y = Y0 + i;
+    for (int a = 0; a < 4; ++a) {
+      const int Y = Y0 + a;
       if (Y < X || Y >= H) continue;
       const int q = tri2(Y) + X;
 #pragma unroll
       for (int j = 0; j < 4; ++j)
-        if (z0 + j < H) D[(z0 + j) * P4 + q] = acc[i][j];
+        if (z0 + j < H) D[(z0 + j) * P4 + q] = acc[a][j];
     }
   }
 }
@@ -318,7 +314,7 @@ sunset_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
       SunGeom g(R.H);
       TC *p = reinterpret_cast<TC *>(smem_raw);
       TC *CT = p;
-      p += g.H * g.H4;
+      p += g.H4 * g.H4;
       TC *bufF = p;
       p += rup4(g.S);
       TC *R1, *R2;
@@ -335,9 +331,9 @@ sunset_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
       int *off3 = off2 + (g.H + 1);
       uint16_t *pr = reinterpret_cast<uint16_t *>(off3 + (g.P4 / 4 + 1));
       uint16_t *etab = sun_etab_fits(sizeof(TC) == 8, g.H) ? pr + rup4(g.P) : nullptr;
-      for (int i = threadIdx.x; i < g.H * g.H4; i += blockDim.x) {
+      for (int i = threadIdx.x; i < g.H4 * g.H4; i += blockDim.x) {
         const int x = i / g.H4, X = i - x * g.H4;
-        CT[i] = (X < g.H) ? (TC)R.Cm[X * g.H + x] : (TC)0;
+        CT[i] = (X < g.H && x < g.H) ? (TC)R.Cm[X * g.H + x] : (TC)0;
       }
       for (int z = threadIdx.x; z < g.H; z += blockDim.x)
         for (int y = 0; y <= z; ++y) pr[tri2(z) + y] = (uint16_t)(y | (z << 8));
@@ -492,9 +488,8 @@ constexpr int NOALLOC_MAX_CTAS = 160;
 
 constexpr size_t na_slot_elems(int H) {
   // the R1 + R2 regions of SunGeom for octant size H (pass intermediates)
-  return (size_t)rup4_c(std::max(std::max(H * rup4_c(H * (H + 1) / 2), (H * (H + 1) / 2) * rup4_c(H)),
-                                 H * (H + 1) * (H + 2) / 6)) +
-         (size_t)rup4_c(std::max(H * rup4_c(H * (H + 1) / 2), H * (H + 1) * (H + 2) / 6));
+  return (size_t)rup4_c(std::max(H * rup4_c(H * (H + 1) / 2), H * (H + 1) * (H + 2) / 6)) +
+         (size_t)rup4_c(std::max(H * rup4_c(H * (H + 1) / 2) + 4, H * (H + 1) * (H + 2) / 6));
 }
 constexpr size_t NOALLOC_SLOT_ELEMS = na_slot_elems(NOALLOC_MAX_NS / 2 + 1);
 
@@ -511,17 +506,17 @@ sunset_rows_noalloc_kernel(int Ns, double fac_r, double fac_F, int classical, in
   const int H = Ns / 2 + 1;
   SunGeom g(H);
   double *CT = reinterpret_cast<double *>(smem_raw);
-  double *bufF = CT + g.H * g.H4;
+  double *bufF = CT + g.H4 * g.H4;
   int *off2 = reinterpret_cast<int *>(bufF + rup4(g.S));
   int *off3 = off2 + (g.H + 1);
   uint16_t *pr = reinterpret_cast<uint16_t *>(off3 + (g.P4 / 4 + 1));
   double *R1 = scratch + (size_t)blockIdx.x * stride;
   double *R2 = R1 + g.r1;
   // cosine matrix of the even octant, C[X][x] = m(x) cos(2 pi x X / Ns), stored transposed
-  for (int i = threadIdx.x; i < g.H * g.H4; i += blockDim.x) {
+  for (int i = threadIdx.x; i < g.H4 * g.H4; i += blockDim.x) {
     const int x = i / g.H4, X = i - x * g.H4;
     const double m = (x == 0 || 2 * x == Ns) ? 1.0 : 2.0;
-    CT[i] = (X < g.H) ? m * cospi(2.0 * (double)((x * X) % Ns) / (double)Ns) : 0.0;
+    CT[i] = (X < g.H && x < g.H) ? m * cospi(2.0 * (double)((x * X) % Ns) / (double)Ns) : 0.0;
   }
   for (int z = threadIdx.x; z < g.H; z += blockDim.x)
     for (int y = 0; y <= z; ++y) pr[tri2(z) + y] = (uint16_t)(y | (z << 8));
@@ -624,7 +619,7 @@ extern "C" int kb_sunset_rows_noalloc(int32_t Ns, int32_t N, double lambda, int3
   const double fac_r = iv * iv * iv * (-(lambda * lambda) * (Nd + 2.0) / (6.0 * Nd * Nd));
   const double fac_F = iv * iv * iv * (-(lambda * lambda) * (Nd + 2.0) / (18.0 * Nd * Nd));
   SunGeom g(H);
-  const size_t smem = ((size_t)g.H * g.H4 + rup4(g.S)) * sizeof(double) +
+  const size_t smem = ((size_t)g.H4 * g.H4 + rup4(g.S)) * sizeof(double) +
                       (size_t)(g.H + 1 + g.P4 / 4 + 1) * sizeof(int) + (size_t)g.P * sizeof(uint16_t) + 64;
   sunset_rows_noalloc_kernel<<<grid, SUN_THREADS, smem, (cudaStream_t)stream>>>(
       Ns, fac_r, fac_F, pexp == KB_PEXP_NLO_CLASSICAL ? 1 : 0, nrows, F_rows, rho_rows, sigF_rows, sigr_rows,
@@ -662,7 +657,7 @@ sunset_adjoint_kernel(RunDev R, int t, const double *__restrict__ sbar_r, const 
   const int tmin = max(1, t - R.M + 1);
   SunGeom g(R.H);
   double *CT = reinterpret_cast<double *>(smem_raw);
-  double *bFx = CT + g.H * g.H4;      // Fx, then adjoint of Fx / deg
+  double *bFx = CT + g.H4 * g.H4;     // Fx, then adjoint of Fx / deg
   double *brx = bFx + rup4(g.S);      // rx, then adjoint of rx / deg
   double *bgr = brx + rup4(g.S);      // adjoint of g_r
   double *bgF = bgr + rup4(g.S);      // adjoint of g_F
@@ -672,9 +667,9 @@ sunset_adjoint_kernel(RunDev R, int t, const double *__restrict__ sbar_r, const 
   double *R1 = scratch + (size_t)blockIdx.x * stride;
   double *R2 = R1 + g.r1;
   __shared__ double red[SUN_THREADS / 32];
-  for (int i = threadIdx.x; i < g.H * g.H4; i += blockDim.x) {
+  for (int i = threadIdx.x; i < g.H4 * g.H4; i += blockDim.x) {
     const int x = i / g.H4, X = i - x * g.H4;
-    CT[i] = (X < g.H) ? R.Cm[X * g.H + x] : 0.0;
+    CT[i] = (X < g.H && x < g.H) ? R.Cm[X * g.H + x] : 0.0;
   }
   for (int z = threadIdx.x; z < g.H; z += blockDim.x)
     for (int y = 0; y <= z; ++y) pr[tri2(z) + y] = (uint16_t)(y | (z << 8));
@@ -757,7 +752,7 @@ sunset_adjoint_kernel(RunDev R, int t, const double *__restrict__ sbar_r, const 
 
 size_t sunset_adjoint_smem_bytes(int H) {
   SunGeom g(H);
-  return ((size_t)g.H * g.H4 + 4 * (size_t)rup4(g.S)) * sizeof(double) +
+  return ((size_t)g.H4 * g.H4 + 4 * (size_t)rup4(g.S)) * sizeof(double) +
          (size_t)(g.H + 1 + g.P4 / 4 + 1) * sizeof(int) + (size_t)g.P * sizeof(uint16_t) + 64;
 }
 
@@ -801,9 +796,9 @@ namespace {
 
 // cosine matrix and pass tables of one lattice size (as sunset_kernel builds them)
 __device__ void ninv_tables(const RunDev &R, const SunGeom &g, double *CT, uint16_t *pr, int *off2, int *off3) {
-  for (int i = threadIdx.x; i < g.H * g.H4; i += blockDim.x) {
+  for (int i = threadIdx.x; i < g.H4 * g.H4; i += blockDim.x) {
     const int x = i / g.H4, X = i - x * g.H4;
-    CT[i] = (X < g.H) ? R.Cm[X * g.H + x] : 0.0;
+    CT[i] = (X < g.H && x < g.H) ? R.Cm[X * g.H + x] : 0.0;
   }
   for (int z = threadIdx.x; z < g.H; z += blockDim.x)
     for (int y = 0; y <= z; ++y) pr[tri2(z) + y] = (uint16_t)(y | (z << 8));
@@ -827,7 +822,7 @@ __device__ void ninv_tables(const RunDev &R, const SunGeom &g, double *CT, uint1
 // shared memory: CT, NB orbit buffers, pass tables
 __host__ __device__ inline size_t ninv_rows_smem(int H, int NB) {
   SunGeom g(H);
-  return ((size_t)g.H * g.H4 + (size_t)NB * rup4(g.S)) * sizeof(double) +
+  return ((size_t)g.H4 * g.H4 + (size_t)NB * rup4(g.S)) * sizeof(double) +
          (size_t)(g.H + 1 + g.P4 / 4 + 1) * sizeof(int) + (size_t)g.P * sizeof(uint16_t) + 64;
 }
 
@@ -862,7 +857,7 @@ ninv_rows_kernel(const RunDev *__restrict__ runs, const int *__restrict__ sched,
       SunGeom g(R.H);
       double *p = reinterpret_cast<double *>(smem_raw);
       double *CT = p;
-      p += g.H * g.H4;
+      p += g.H4 * g.H4;
       for (int q = 0; q < (MODE == 0 ? 2 : 4); ++q) {
         buf[q] = p;
         p += rup4(g.S);
