@@ -79,6 +79,8 @@ __host__ __device__ inline bool sun_etab_fits(bool fp64, int H) {
   return sun_smem_base(fp64, H) + (size_t)g.H * g.P4 * sizeof(uint16_t) <= SUN_SMEM_CAP;
 }
 
+__device__ __forceinline__ void prefetch_l2(const void *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
 // 4-wide vector load/store for float (float4) and double (2 x double2)
 __device__ __forceinline__ void ld4(const float *p, float v[4]) {
   const float4 q = *reinterpret_cast<const float4 *>(p);
@@ -381,7 +383,10 @@ sunset_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
     };
 
     // forward transforms of F(t-1,t') -> bufF and rho(t-1,t') -> R2 (orbit layout);
-    // each row is staged in the region the transform writes last
+    // each row is staged in the region the transform writes last, the rho row
+    // fetched into L2 meanwhile
+    for (int q = threadIdx.x; q < R.nchunks; q += blockDim.x)
+      prefetch_l2(reinterpret_cast<const TS *>(R.hist_r) + hbase + q * cstride);
     stage(R.hist_F, c.bufF);
     sun_transform<TC>(c, [&](int o) { return c.bufF[o]; }, [&](int o, TC v) { c.bufF[o] = v; });
     stage(R.hist_r, c.R2);
@@ -397,15 +402,39 @@ sunset_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
     }
     __syncthreads();
 
-    // inverse transforms straight into the Sigma rings (scaled by ivol^3 * coefficient)
+    // the rows of the next item of this CTA go to L2 while the inverse transforms run
+    {
+      const int w2 = w + gridDim.x;
+      if (w2 < total) {
+        const RunDev &R2n = runs[run_at(base, nruns, w2)];
+        const int tp2 = max(1, t - R2n.M + 1) + (w2 - R2n.cta_base_sun);
+        if (pexp_sunset(R2n.pexp) && tp2 <= t - 1) {
+          const size_t b2 = hist_off(R2n.Malloc, R2n.T, 0, t - 1, tp2, 0) * sizeof(TS);
+          const size_t cs2 = (size_t)R2n.Malloc * R2n.Malloc * KC * sizeof(TS);
+          for (int q = threadIdx.x; q < R2n.nchunks; q += blockDim.x) {
+            prefetch_l2(reinterpret_cast<const char *>(R2n.hist_F) + b2 + q * cs2);
+            prefetch_l2(reinterpret_cast<const char *>(R2n.hist_r) + b2 + q * cs2);
+          }
+        }
+      }
+    }
+
+    // inverse transforms: pass 3 leaves the orbit values in R2 (free once pass 2
+    // has read B), then one coalesced sweep scales them into the Sigma rings
+    // (ivol^3 * coefficient); the next writer of R2 is behind a barrier
     TS *sigr = reinterpret_cast<TS *>(R.sig_r) + (size_t)slot * KC;
     TS *sigF = reinterpret_cast<TS *>(R.sig_F) + (size_t)slot * KC;
     const TC fr = (TC)R.fac_r, fF = (TC)R.fac_F;
+    auto flush = [&](TS *sig, TC f) {
+      for (int o = threadIdx.x; o < S; o += blockDim.x) sig[gidx(o)] = (TS)(f * c.R2[o]);
+    };
     const TC *gr = c.R2;
     // expand reads R2 into R1 before pass 1 overwrites R2
-    sun_transform<TC>(c, [&](int o) { return gr[o]; }, [&](int o, TC v) { sigr[gidx(o)] = (TS)(fr * v); });
+    sun_transform<TC>(c, [&](int o) { return gr[o]; }, [&](int o, TC v) { c.R2[o] = v; });
+    flush(sigr, fr);
     const TC *gF = c.bufF;
-    sun_transform<TC>(c, [&](int o) { return gF[o]; }, [&](int o, TC v) { sigF[gidx(o)] = (TS)(fF * v); });
+    sun_transform<TC>(c, [&](int o) { return gF[o]; }, [&](int o, TC v) { c.R2[o] = v; });
+    flush(sigF, fF);
   }
 }
 
