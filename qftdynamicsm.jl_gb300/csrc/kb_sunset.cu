@@ -223,7 +223,8 @@ __device__ void sun_pass2(const SunCtx<TC> &c, const TC *B, TC *D) {
         for (int m = 0; m < 4; ++m) L[k][m] = row[m];
       }
 #pragma unroll
-      for (int i = 0; i < 4; ++i)
+      for (int i = 0; i < 4; ++i) {
+        if (y0 + i >= H) break;  // the padded rows of the last block (same for all lanes)
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
           // B(y0 + i, z0 + j): L[i][j] in the direct layout, L[j][i] in the transposed one
@@ -231,6 +232,7 @@ __device__ void sun_pass2(const SunCtx<TC> &c, const TC *B, TC *D) {
 #pragma unroll
           for (int a = 0; a < 4; ++a) acc[a][j] += cv[i][a] * v;
         }
+      }
     }
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
