@@ -84,6 +84,72 @@ __device__ __forceinline__ void fence_proxy_async() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
+// ---------------------------------------------------------------------------
+// Tensor memory (TMEM) for the FP64 row accumulators of memint_kernel: one lane
+// per row-group thread, 2 x 32-bit columns per double. A warp reaches the 32
+// lanes 32 (warp mod 4) ..; the row group is warps 4..7 and the column group
+// warps 0..3, so the column-group thread with the same group index sits on the
+// same lane and reads that row's sum for its leapfrog. Each load and store
+// waits for itself (one asm block), so no register is read before it is valid.
+// ---------------------------------------------------------------------------
+constexpr uint32_t TMEM_COLS = 256;  // power of two in [32, 512]
+__device__ __forceinline__ void tmem_alloc(uint32_t *slot) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
+               "r"(TMEM_COLS)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(TMEM_COLS) : "memory");
+}
+__device__ __forceinline__ void tmem_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tmem_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// OPT doubles of this thread's lane at columns ta .. ta + 2 OPT - 1 (warp-collective)
+template <int OPT>
+struct TmemRow;
+template <>
+struct TmemRow<2> {
+  __device__ __forceinline__ static void ld(uint32_t ta, double v[2]) {
+    uint32_t w0, w1, w2, w3;
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(w0), "=r"(w1), "=r"(w2), "=r"(w3)
+        : "r"(ta)
+        : "memory");
+    v[0] = __hiloint2double((int)w1, (int)w0);
+    v[1] = __hiloint2double((int)w3, (int)w2);
+  }
+  __device__ __forceinline__ static void st(uint32_t ta, const double v[2]) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1, %2, %3, %4};\n\t"
+        "tcgen05.wait::st.sync.aligned;" ::"r"(ta),
+        "r"(__double2loint(v[0])), "r"(__double2hiint(v[0])), "r"(__double2loint(v[1])), "r"(__double2hiint(v[1]))
+        : "memory");
+  }
+};
+template <>
+struct TmemRow<1> {
+  __device__ __forceinline__ static void ld(uint32_t ta, double v[1]) {
+    uint32_t w0, w1;
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x2.b32 {%0, %1}, [%2];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(w0), "=r"(w1)
+        : "r"(ta)
+        : "memory");
+    v[0] = __hiloint2double((int)w1, (int)w0);
+  }
+  __device__ __forceinline__ static void st(uint32_t ta, const double v[1]) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x2.b32 [%0], {%1, %2};\n\t"
+        "tcgen05.wait::st.sync.aligned;" ::"r"(ta),
+        "r"(__double2loint(v[0])), "r"(__double2hiint(v[0]))
+        : "memory");
+  }
+};
+
 // OPT adjacent orbits per consumer thread: two FP32 values move with one 8-byte
 // shared-memory load and one packed fma.rn.f32x2; FP64 keeps one orbit per thread.
 template <typename TS, int OPT>
@@ -313,7 +379,8 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw + (size_t)NST * C::STAGE_BYTES);
   uint64_t *empty = full + NST;
   // misc: [0] hartreecont, [1] M^2, [2..2+KC) acc_F(t-1) per orbit, [10] abort flag,
-  // [11] tiles issued, [12] consumer abort flag, [16..16+(NG/32)*KC) diagonal partials
+  // [11] tiles issued, [12] consumer abort flag, [14] TMEM address,
+  // [16..16+(NG/32)*KC) diagonal partials
   double *misc = reinterpret_cast<double *>(empty + NST);  // 128 doubles
   volatile int *abort_flag = reinterpret_cast<volatile int *>(misc + 10);
   volatile int *issued_count = reinterpret_cast<volatile int *>(misc + 11);
@@ -321,6 +388,8 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   // consumers and they all meet at the named barrier after the tile loop
   volatile int *cabort = reinterpret_cast<volatile int *>(misc + 12);
   static_assert(16 + (C::NG / 32) * KC <= 128, "misc scratch too small");
+  static_assert(C::NG == 128, "one TMEM lane per row-group thread, column group in warps 0..3");
+  volatile uint32_t *tmem_slot = reinterpret_cast<volatile uint32_t *>(misc + 14);
 
   const int item = SPLIT ? (int)(blockIdx.x >> 1) : (int)blockIdx.x;
   const int half = SPLIT ? (int)(blockIdx.x & 1) : 0;
@@ -340,9 +409,13 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   const size_t rowstride = (size_t)Ma * KC;              // one row of one chunk
   const size_t st_row = (size_t)R.nchunks * rowstride;   // one state row (all chunks)
   // row sums of this chunk, [Malloc][KC]: entries (slot, j0..j0+OPT-1) are only
-  // ever written by row-group thread (slot mod T, jq), so they need no atomics;
-  // they live in a global scratch slot that stays in L2 (one per half in split mode).
+  // ever written by row-group thread (slot mod T, jq), so they need no atomics.
+  // They live in TMEM (Malloc/T slots x OPT doubles per lane) when they fit,
+  // else in a global scratch slot; a split CTA copies them there at the end
+  // (one buffer per half) for memint_finish_kernel.
   double *rowacc = R.rowacc + (size_t)half * R.nchunks * rowstride + (size_t)c * rowstride;
+  const bool use_tmem = (Ma / T) * OPT * 2 <= (int)TMEM_COLS;
+  if (use_tmem && warp == 0) tmem_alloc(const_cast<uint32_t *>(tmem_slot));
 
   // --- tadpole mass M^2(t-1) from the per-chunk sums of F(t-1,t-1) (fixed order)
   if (warp == 0) {
@@ -366,11 +439,21 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
     }
     fence_proxy_async();
   }
-  if (!producer && !colgrp)
+  if (!use_tmem && !producer && !colgrp)
     for (int s = loc; s < Ma; s += T)  // the slots this thread owns
       for (int o = 0; o < OPT; ++o) rowacc[(size_t)s * KC + j0 + o] = 0.0;
+  if (use_tmem) tmem_fence_before();
   __syncthreads();
-  const double hc = misc[0], M2 = misc[1];
+  if (use_tmem) tmem_fence_after();
+  const double M2 = misc[1];
+  const uint32_t tbase = use_tmem ? *tmem_slot : 0u;
+  const uint32_t tlane = ((uint32_t)(warp & 3) * 32u) << 16;  // this warp's TMEM lanes
+  // TMEM column of the row sums of slot s (s mod T is the thread's loc)
+  auto tcol = [&](int s) { return tbase + tlane + (uint32_t)((s / T) * OPT * 2); };
+  if (use_tmem && !producer && !colgrp) {
+    const double zero[OPT] = {};
+    for (int s = 0; s < Ma; s += T) TmemRow<OPT>::st(tcol(s), zero);
+  }
 
   const bool lo_only = pexp_lo(R.pexp);
   const int J0 = tmin / T, Jn = (t - 1) / T;
@@ -485,13 +568,18 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
           const int a = I * T + loc;
           const bool av = (a >= tmin) && (a <= t - 1);
           double *racc = rowacc + (size_t)(a % Ma) * KC + j0;
-          // the accumulator of this row was loaded during the previous tile; load the
-          // next tile's row now (tile order: (I+1, J), or (J+1, J+1) after the last row block)
           double prev[OPT];
-          for (int o = 0; o < OPT; ++o) prev[o] = pre[o];
-          const int an = (I < Jn ? (I + 1) : (J + 1)) * T + loc;
-          if (an != a && an >= tmin && an <= t - 1)  // an == a: the value stored below is the next one
-            for (int o = 0; o < OPT; ++o) pre[o] = rowacc[(size_t)(an % Ma) * KC + j0 + o];
+          int an = -1;
+          if (use_tmem) {
+            TmemRow<OPT>::ld(tcol((I * T) % Ma), prev);  // the same column for the whole warp
+          } else {
+            // the accumulator of this row was loaded during the previous tile; load the
+            // next tile's row now (tile order: (I+1, J), or (J+1, J+1) after the last row block)
+            for (int o = 0; o < OPT; ++o) prev[o] = pre[o];
+            an = (I < Jn ? (I + 1) : (J + 1)) * T + loc;
+            if (an != a && an >= tmin && an <= t - 1)  // an == a: the value stored below is the next one
+              for (int o = 0; o < OPT; ++o) pre[o] = rowacc[(size_t)(an % Ma) * KC + j0 + o];
+          }
           int lo = max(0, tmin - J * T), hi = min(T - 1, a - 1 - J * T);
           if (!av) hi = -1;
           V s0 = V::zero(), s1 = V::zero();
@@ -525,16 +613,23 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
           s0.add(s1);
           __syncwarp();
           if (lane == 0) mbar_arrive(empty + stage);
-          if (av)
+          if (use_tmem) {
+            double nv[OPT];
+            for (int o = 0; o < OPT; ++o) nv[o] = av ? prev[o] + s0.get(o) : prev[o];
+            TmemRow<OPT>::st(tcol((I * T) % Ma), nv);
+          } else if (av) {
             for (int o = 0; o < OPT; ++o) {
               const double v = prev[o] + s0.get(o);
               racc[o] = v;
               if (an == a) pre[o] = v;
             }
+          }
         }
       }
       // both groups: the row sums of column block J are final after its diagonal tile
+      if (use_tmem) tmem_fence_before();
       consumer_sync(C::NT);
+      if (use_tmem) tmem_fence_after();
       if (*cabort) {
         aborted = true;
         break;
@@ -548,7 +643,10 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
           }
         continue;
       }
-      // leapfrog for t' = b (evolve_r!/evolve_F!, Evolution.jl:890-915)
+      // leapfrog for t' = b (evolve_r!/evolve_F!, Evolution.jl:890-915); the row
+      // sums of row b come from the row-group thread on this thread's TMEM lane
+      double rowb[OPT];
+      if (use_tmem) TmemRow<OPT>::ld(tcol((J * T) % Ma), rowb);
       if (bvalid) {
         const int sb = b % Ma;
         const double wb = (b == tmin) ? 0.5 : 1.0;
@@ -570,7 +668,7 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
           const double om = (kk + M2) * R.dt2;  // setomega2values!: (kL2 + M^2) * dt^2
           const double xbr_d = lo_only ? 0.0 : wb * (double)sigr[j];
           const double xbF_d = lo_only ? 0.0 : wb * (double)sigF[j];
-          const double accF = colF[o] + rowacc[(size_t)sb * KC + j];
+          const double accF = colF[o] + (use_tmem ? rowb[o] : rowacc[(size_t)sb * KC + j]);
           const double accR = colR[o];
           const double F1 = F1row[(size_t)sb * KC + j];
           const double F2 = (b <= t - 2) ? F2row[(size_t)sb * KC + j] : F1row[(size_t)((t - 2) % Ma) * KC + j];
@@ -605,17 +703,33 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
       }
     }
   }
+  if (use_tmem) tmem_fence_before();
   __syncthreads();  // producer done issuing; consumers done with the triangle
+  if (use_tmem) tmem_fence_after();
   if (*abort_flag) {
-    // drain copies still in flight into this CTA's shared memory, then leave
+    // drain copies still in flight into this CTA's shared memory
     if (tid == 0)
       for (int q = 0; q < *issued_count; ++q)
         (void)mbar_wait_bounded(full + (q % NST), (uint32_t)((q / NST) & 1));
-    __syncthreads();
-    return;
+  } else {
+    if (SPLIT && use_tmem && !producer && !colgrp)  // this half's row sums, for memint_finish_kernel
+      for (int s = 0; s < Ma; s += T) {
+        double v[OPT];
+        TmemRow<OPT>::ld(tcol(s), v);
+        for (int o = 0; o < OPT; ++o) rowacc[(size_t)(s + loc) * KC + j0 + o] = v[o];
+      }
+    if (!SPLIT && tid < KC) memint_epilogue<TS>(R, c, t, tid, misc, C::NG / 32, M2, measure);
   }
-
-  if (!SPLIT && tid < KC) memint_epilogue<TS>(R, c, t, tid, misc, C::NG / 32, M2, measure);
+  if (use_tmem) {  // every path ends here: the allocating warp frees the TMEM
+    tmem_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+      tmem_fence_after();
+      tmem_dealloc(tbase);
+    }
+  } else {
+    __syncthreads();
+  }
 }
 
 // Second kernel of a split step: one CTA per chunk adds the column sums and
