@@ -410,11 +410,12 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   const size_t st_row = (size_t)R.nchunks * rowstride;   // one state row (all chunks)
   // row sums of this chunk, [Malloc][KC]: entries (slot, j0..j0+OPT-1) are only
   // ever written by row-group thread (slot mod T, jq), so they need no atomics.
-  // They live in TMEM (Malloc/T slots x OPT doubles per lane) when they fit,
-  // else in a global scratch slot; a split CTA copies them there at the end
-  // (one buffer per half) for memint_finish_kernel.
+  // With FP32 history they live in TMEM (Malloc/T slots x OPT doubles per lane)
+  // when they fit, else in a global scratch slot; a split CTA copies them there
+  // at the end (one buffer per half) for memint_finish_kernel. The FP64 kernel,
+  // bound by FP64 arithmetic, runs 1 % faster on the global scratch.
   double *rowacc = R.rowacc + (size_t)half * R.nchunks * rowstride + (size_t)c * rowstride;
-  const bool use_tmem = (Ma / T) * OPT * 2 <= (int)TMEM_COLS;
+  const bool use_tmem = sizeof(TS) == 4 && (Ma / T) * OPT * 2 <= (int)TMEM_COLS;
   if (use_tmem && warp == 0) tmem_alloc(const_cast<uint32_t *>(tmem_slot));
 
   // --- tadpole mass M^2(t-1) from the per-chunk sums of F(t-1,t-1) (fixed order)
