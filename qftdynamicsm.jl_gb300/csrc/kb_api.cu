@@ -35,6 +35,8 @@ struct Run {
   double *st_F = nullptr, *st_r = nullptr, *k2_d = nullptr, *deg_d = nullptr, *Cm_d = nullptr;
   double *tad = nullptr, *meas = nullptr, *epart = nullptr, *rowacc = nullptr, *colacc = nullptr;
   double *pi_r = nullptr, *pi_F = nullptr, *Ik = nullptr, *Jk = nullptr;  // 1/N NLO only
+  int *fin = nullptr;  // finishing kernel of a split step
+  double *fin_part = nullptr, *fin_prev = nullptr, *hcm2 = nullptr;
   size_t hist_elems = 0, st_elems = 0, sig_elems = 0;
   RunDev dev{};
 };
@@ -50,6 +52,7 @@ struct kb_handle {
   RunDev *d_runs = nullptr;
   int *d_base_sun = nullptr, *d_base_mi = nullptr;
   int total_sun = 0, total_mi = 0;
+  int fin_nb_max = 1;  // CTA slots per chunk of the finishing kernel (max over runs)
   int *d_t = nullptr, *d_err = nullptr;
   size_t smem_sun = 0, smem_mi = 0;
   int num_sms = 0, grid_sun = 0, grid_sun_max = 0;
@@ -162,7 +165,7 @@ size_t slot_off(const Run &R, int a) { return (size_t)(a % R.Malloc); }
 
 void free_run(Run &R) {
   void *ptrs[] = {R.hist_F, R.hist_r, R.sig_F, R.sig_r, R.st_F, R.st_r, R.k2_d, R.deg_d, R.Cm_d, R.tad, R.meas, R.epart,
-                  R.rowacc, R.colacc, R.pi_r, R.pi_F, R.Ik, R.Jk};
+                  R.rowacc, R.colacc, R.pi_r, R.pi_F, R.Ik, R.Jk, R.fin, R.fin_part, R.fin_prev, R.hcm2};
   for (void *q : ptrs)
     if (q) cudaFree(q);
 }
@@ -303,6 +306,10 @@ int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out) {
         {(void **)&R.meas, (size_t)5 * R.Spad * 8}, {(void **)&R.epart, (size_t)4 * R.nchunks * 8},
         {(void **)&R.rowacc, (size_t)2 * R.nchunks * R.Malloc * KC * 8},
         {(void **)&R.colacc, (size_t)2 * R.nchunks * R.Malloc * KC * 8},
+        {(void **)&R.fin, (size_t)R.nchunks * sizeof(int)},
+        {(void **)&R.fin_part, (size_t)R.nchunks * ((R.Malloc + kb::FIN_TP - 1) / kb::FIN_TP) * KC * 8},
+        {(void **)&R.fin_prev, (size_t)R.nchunks * KC * 8},
+        {(void **)&R.hcm2, (size_t)2 * 8},
     };
     std::vector<A> all(std::begin(al), std::end(al));
     if (R.p.pexp == KB_PEXP_NINV_NLO) {  // bubble rings and the resummed kernels of the window
@@ -363,6 +370,12 @@ int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out) {
     D.epart = R.epart;
     D.rowacc = R.rowacc;
     D.colacc = R.colacc;
+    D.fin = R.fin;
+    D.fin_nb = (R.Malloc + kb::FIN_TP - 1) / kb::FIN_TP;
+    D.fin_part = R.fin_part;
+    D.fin_prev = R.fin_prev;
+    D.hcm2 = R.hcm2;
+    h->fin_nb_max = std::max(h->fin_nb_max, D.fin_nb);
     D.pi_r = R.pi_r;
     D.pi_F = R.pi_F;
     D.Ik = R.Ik;
@@ -591,7 +604,7 @@ static int launch_step(kb_handle *h, int measure) {
     if (h->any_nlo || h->any_ninv) h->ev_pending.push_back({0, {e0, e1}});
   }
   KB_CUDA(h, kb::launch_memint(h->fp64, h->memint_variant, h->memint_split, h->d_runs, h->d_base_mi, (int)h->runs.size(),
-                               h->total_mi, h->d_t, h->d_err, measure, h->smem_mi, h->st));
+                               h->total_mi, h->fin_nb_max, h->d_t, h->d_err, measure, h->smem_mi, h->st));
   if (h->profiling) {
     KB_CUDA(h, cudaEventRecord(e2, h->st));
     h->ev_pending.push_back({1, {e1, e2}});
@@ -1137,7 +1150,7 @@ int kb_autotune(kb_handle *h, int32_t trials, kb_tuning *chosen, double *ms_per_
       if ((rc = launch_self_energies(h))) return rc;
       KB_CUDA(h, cudaEventRecord(e[1], h->st));
       KB_CUDA(h, kb::launch_memint(h->fp64, h->memint_variant, h->memint_split, h->d_runs, h->d_base_mi, (int)h->runs.size(),
-                                   h->total_mi, h->d_t, h->d_err, 1, h->smem_mi, h->st));
+                                   h->total_mi, h->fin_nb_max, h->d_t, h->d_err, 1, h->smem_mi, h->st));
       KB_CUDA(h, cudaEventRecord(e[2], h->st));
       KB_CUDA(h, cudaEventSynchronize(e[2]));
       float a = 0, b = 0;

@@ -19,6 +19,8 @@
 //   rowacc          [2][nchunks][Malloc][KC]  double: row sums of the memory integrals
 //                                              (the second half only in split mode)
 //   colacc          [2][nchunks][Malloc][KC]  double: column sums (F, rho) of a split step
+//   fin, fin_part, fin_prev, hcm2             partial sums and arrival counts of the
+//                                              finishing kernel of a split step
 //   sunset scratch  [grid][R1 + R2]           double: FP64 cosine-transform intermediates
 #pragma once
 #include <cstdint>
@@ -56,6 +58,13 @@ struct RunDev {
   double *pi_r, *pi_F, *Ik, *Jk;
   double lam;       // lambda
   double ninv_fac;  // -lambda / (3 N) * ivol^2
+  // finishing kernel of a split step (memint_finish_kernel): FIN_TP t' per CTA
+  int *fin;          // [nchunks] CTAs of the chunk done this step (0 between steps)
+  int fin_nb;        // CTA slots per chunk: ceil(Malloc / FIN_TP)
+  int pad2;
+  double *fin_part;  // [nchunks][fin_nb][KC] per-CTA sums of acc_F(t) terms
+  double *fin_prev;  // [nchunks][KC] acc_F(t-1)
+  double *hcm2;      // [2] hartreecont and M^2(t-1) of the step
 };
 
 // perturbative expansions (kb2pi.h): 0 LambdaLO, 1 LambdaNLO, 2 LambdaNLOclassical,
@@ -96,7 +105,9 @@ int sunset_grid(bool fp64, int num_sms, int total_rows);
 int sunset_max_ctas_per_sm(bool fp64, int variant, size_t smem);
 cudaError_t configure_sunset(bool fp64, size_t smem);
 cudaError_t launch_memint(bool fp64, int variant, int split, const RunDev *d_runs, const int *d_base, int nruns,
-                          int total_ctas, const int *d_t, int *d_err, int measure, size_t smem, cudaStream_t st);
+                          int total_ctas, int fin_nb_max, const int *d_t, int *d_err, int measure, size_t smem,
+                          cudaStream_t st);
+constexpr int FIN_TP = 128;  // t' per CTA of the finishing kernel
 size_t memint_smem_bytes(bool fp64, int Malloc, int variant);
 cudaError_t configure_memint(bool fp64, size_t smem);
 int memint_tile(bool fp64);

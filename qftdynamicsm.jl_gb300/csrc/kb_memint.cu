@@ -293,8 +293,9 @@ __device__ void memint_epilogue(const RunDev &R, int c, int t, int tid, const do
   const int kd = c * KC + jj;
   const double kd2 = (kd < R.S) ? R.k2[kd] : 0.0;
   const double omd = (kd2 + M2) * R.dt2;
-  const double Ft1 = FNrow[(size_t)((t - 1) % Ma) * KC + jj];  // F(t, t-1)
-  const double Ft2 = FNrow[(size_t)((t - 2) % Ma) * KC + jj];  // F(t, t-2)
+  // F(t, t-1), F(t, t-2): written in this launch, possibly by another CTA of the chunk
+  const double Ft1 = __ldcg(FNrow + (size_t)((t - 1) % Ma) * KC + jj);
+  const double Ft2 = __ldcg(FNrow + (size_t)((t - 2) % Ma) * KC + jj);
   const double Ftt = (2.0 - omd) * Ft1 - Ft2 - accd * R.dt3;
   FNrow[(size_t)(t % Ma) * KC + jj] = Ftt;
   RNrow[(size_t)(t % Ma) * KC + jj] = 0.0;
@@ -447,6 +448,10 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   __syncthreads();
   if (use_tmem) tmem_fence_after();
   const double M2 = misc[1];
+  if (SPLIT && c == 0 && half == 0 && tid == 0) {  // for memint_finish_kernel
+    R.hcm2[0] = misc[0];
+    R.hcm2[1] = misc[1];
+  }
   const uint32_t tbase = use_tmem ? *tmem_slot : 0u;
   const uint32_t tlane = ((uint32_t)(warp & 3) * 32u) << 16;  // this warp's TMEM lanes
   // TMEM column of the row sums of slot s (s mod T is the thread's loc)
@@ -733,83 +738,120 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   }
 }
 
-// Second kernel of a split step: one CTA per chunk adds the column sums and
-// the two halves' row sums, runs the leapfrog of every t' of the window (the
-// same arithmetic as memint_kernel's), then the diagonal and measurement.
+// Second kernel of a split step: CTA (chunk, k) takes the FIN_TP t' from tmin +
+// k FIN_TP on, FIN_IT (t', orbit) items per thread with all their loads issued
+// before any arithmetic. It adds the column sums and the two halves' row sums,
+// runs the leapfrog (the same arithmetic as memint_kernel's) and stores its
+// per-orbit sums of the acc_F(t) terms; the CTA of the chunk that arrives last
+// adds those in CTA order and runs the diagonal and measurement (no CTA waits
+// for another).
 constexpr int FIN_THREADS = 256;
+constexpr int FIN_IT = FIN_TP * KC / FIN_THREADS;
+static_assert(FIN_IT * FIN_THREADS == FIN_TP * KC, "whole items per thread");
 
 template <typename TS>
-__global__ void __launch_bounds__(FIN_THREADS)
-memint_finish_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int nruns,
+__global__ void __launch_bounds__(FIN_THREADS, 2)
+memint_finish_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int nruns, int nb_max,
                      const int *__restrict__ d_t, int measure) {
-  __shared__ double misc[16 + (FIN_THREADS / 32) * KC];
-  const int r = run_at(base, nruns, blockIdx.x);
+  __shared__ double red[FIN_THREADS / 32][KC];
+  __shared__ double misc[16 + KC];
+  __shared__ int is_last;
+  const int ci = blockIdx.x / nb_max, blk = blockIdx.x - ci * nb_max;
+  const int r = run_at(base, nruns, ci);
   const RunDev &R = runs[r];
-  const int c = blockIdx.x - R.cta_base_mi;
+  const int c = ci - R.cta_base_mi;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int t = *d_t;
   const int Ma = R.Malloc, T = R.T;
   const int tmin = max(1, t - R.M + 1);
+  const int nq = (t - tmin) * KC;
+  const int nact = (nq + FIN_TP * KC - 1) / (FIN_TP * KC);  // CTAs of this chunk with work (<= fin_nb)
+  if (blk >= nact) return;
   const size_t rowstride = (size_t)Ma * KC, st_row = (size_t)R.nchunks * rowstride, cs = (size_t)c * rowstride;
-  if (warp == 0) {
-    const double *tad = R.tad + (size_t)((t - 1) & 1) * R.nchunks;
-    double s = 0.0;
-    for (int q = lane; q < R.nchunks; q += 32) s += tad[q];
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) {
-      misc[0] = s;
-      misc[1] = s * R.pref_ivol + R.mass2;
-    }
-  }
-  if (tid < KC) misc[2 + tid] = 0.0;
-  __syncthreads();
-  const double M2 = misc[1], dt3 = R.dt3;
+  const size_t half2 = (size_t)R.nchunks * rowstride;
+  const double M2 = R.hcm2[1];
   const bool lo_only = pexp_lo(R.pexp);
-  const double *colF = R.colacc + cs, *colR = R.colacc + (size_t)R.nchunks * rowstride + cs;
-  const double *rowA = R.rowacc + cs, *rowB = R.rowacc + (size_t)R.nchunks * rowstride + cs;
-  const TS *sigr = reinterpret_cast<const TS *>(R.sig_r) + cs;
-  const TS *sigF = reinterpret_cast<const TS *>(R.sig_F) + cs;
-  const double *F1row = R.st_F + (size_t)((t - 1) % 3) * st_row + cs;
-  const double *F2row = R.st_F + (size_t)((t - 2) % 3) * st_row + cs;
-  const double *R1row = R.st_r + (size_t)((t - 1) % 3) * st_row + cs;
-  const double *R2row = R.st_r + (size_t)((t - 2) % 3) * st_row + cs;
-  double *FNrow = R.st_F + (size_t)(t % 3) * st_row + cs;
-  double *RNrow = R.st_r + (size_t)(t % 3) * st_row + cs;
-  TS *hF = reinterpret_cast<TS *>(R.hist_F);
-  TS *hR = reinterpret_cast<TS *>(R.hist_r);
-  const int j = tid % KC;  // FIN_THREADS is a multiple of KC: each thread keeps one orbit
+  const int j = tid % KC;  // FIN_THREADS is a multiple of KC: one orbit per thread
   const int k = c * KC + j;
-  const double kk = (k < R.S) ? R.k2[k] : 0.0;
-  const double om = (kk + M2) * R.dt2;
-  double diag = 0.0;
-  // unrolled: the loads of several t' are in flight at once (the kernel is latency-bound otherwise)
-#pragma unroll 4
-  for (int q = tid; q < (t - tmin) * KC; q += FIN_THREADS) {
-    const int b = tmin + q / KC, sb = b % Ma;
-    const size_t e = (size_t)sb * KC + j;
-    const double wb = (b == tmin) ? 0.5 : 1.0;
-    const double xbr_d = lo_only ? 0.0 : wb * (double)sigr[e];
-    const double xbF_d = lo_only ? 0.0 : wb * (double)sigF[e];
-    const double accF = colF[e] + (rowA[e] + rowB[e]);
-    const double accR = colR[e];
-    const double F1 = F1row[e];
-    const double F2 = (b <= t - 2) ? F2row[e] : F1row[(size_t)((t - 2) % Ma) * KC + j];
-    const double Fn = (2.0 - om) * F1 - F2 - accF * dt3;
-    const double rn = (b == t - 1) ? R.dt : (2.0 - om) * R1row[e] - R2row[e] - accR * dt3;
-    FNrow[e] = Fn;
-    RNrow[e] = rn;
-    const size_t ho = hist_off(Ma, T, c, t, b, j);
-    hF[ho] = (TS)Fn;
-    hR[ho] = (TS)rn;
-    diag += xbr_d * Fn + xbF_d * rn;
-    if (b == t - 1) misc[2 + j] = accF;
+  const double om = (((k < R.S) ? R.k2[k] : 0.0) + M2) * R.dt2;
+  const double *F1 = R.st_F + (size_t)((t - 1) % 3) * st_row, *F2 = R.st_F + (size_t)((t - 2) % 3) * st_row;
+  const double *R1 = R.st_r + (size_t)((t - 1) % 3) * st_row, *R2 = R.st_r + (size_t)((t - 2) % 3) * st_row;
+  const TS *sr = reinterpret_cast<const TS *>(R.sig_r), *sf = reinterpret_cast<const TS *>(R.sig_F);
+  // GB300 runs FP64 at about 1/64 of the FP32 rate and this kernel is bound by
+  // it: the leapfrog is written as FMAs, and the acc_F(t) terms x * F(t,t') are
+  // formed in the history's type from the values stored anyway (up to FIN_IT
+  // terms per thread, as the memory integrals form theirs per tile) and summed
+  // in FP64 from there on.
+  const double c2 = 2.0 - om, dt3 = R.dt3;
+  TS xr[FIN_IT], xf[FIN_IT];
+  double aF[FIN_IT], aR[FIN_IT], f1[FIN_IT], f2[FIN_IT], r1[FIN_IT], r2[FIN_IT];
+#pragma unroll
+  for (int u = 0; u < FIN_IT; ++u) {
+    const int q = blk * FIN_TP * KC + u * FIN_THREADS + tid;
+    const int b = tmin + min(q, nq - 1) / KC;  // items past the window repeat the last one (not stored)
+    const size_t e = cs + (size_t)(b % Ma) * KC + j;
+    xr[u] = lo_only ? (TS)0 : sr[e];
+    xf[u] = lo_only ? (TS)0 : sf[e];
+    aF[u] = R.colacc[e] + (R.rowacc[e] + R.rowacc[half2 + e]);
+    aR[u] = R.colacc[half2 + e];
+    f1[u] = F1[e];
+    f2[u] = (b <= t - 2) ? F2[e] : F1[cs + (size_t)((t - 2) % Ma) * KC + j];
+    r1[u] = R1[e];
+    r2[u] = R2[e];
   }
-  // partial sums of acc_F(t) per orbit: lanes l, l^8, l^16, l^24 share an orbit
-  diag += __shfl_xor_sync(0xffffffffu, diag, 8);
-  diag += __shfl_xor_sync(0xffffffffu, diag, 16);
-  if (lane < KC) misc[16 + warp * KC + lane] = diag;
+  TS dp = (TS)0;
+  bool wrote_shared = false;  // stores the last CTA reads: acc_F(t-1), F(t,t-1), F(t,t-2)
+#pragma unroll
+  for (int u = 0; u < FIN_IT; ++u) {
+    const int q = blk * FIN_TP * KC + u * FIN_THREADS + tid;
+    if (q >= nq) break;
+    const int b = tmin + q / KC;
+    const size_t e = cs + (size_t)(b % Ma) * KC + j;
+    const double Fn = fma(c2, f1[u], -fma(aF[u], dt3, f2[u]));
+    const double rn = (b == t - 1) ? R.dt : fma(c2, r1[u], -fma(aR[u], dt3, r2[u]));
+    R.st_F[(size_t)(t % 3) * st_row + e] = Fn;
+    R.st_r[(size_t)(t % 3) * st_row + e] = rn;
+    const TS Fs = (TS)Fn, rs = (TS)rn;
+    const size_t ho = hist_off(Ma, T, c, t, b, j);
+    reinterpret_cast<TS *>(R.hist_F)[ho] = Fs;
+    reinterpret_cast<TS *>(R.hist_r)[ho] = rs;
+    const TS wb = (b == tmin) ? (TS)0.5 : (TS)1;
+    dp += (wb * xr[u]) * Fs + (wb * xf[u]) * rs;
+    if (b == t - 1) R.fin_prev[(size_t)c * KC + j] = aF[u];
+    if (b >= t - 2) wrote_shared = true;
+  }
+  double d = (double)dp;
+  // per-orbit sums over this CTA's t' in a fixed order: lanes l, l^8, l^16, l^24 share an orbit
+  d += __shfl_xor_sync(0xffffffffu, d, 8);
+  d += __shfl_xor_sync(0xffffffffu, d, 16);
+  if (lane < KC) red[warp][lane] = d;
   __syncthreads();
-  if (tid < KC) memint_epilogue<TS>(R, c, t, tid, misc, FIN_THREADS / 32, M2, measure);
+  if (tid < KC) {
+    double s = 0.0;
+    for (int w = 0; w < FIN_THREADS / 32; ++w) s += red[w][tid];
+    R.fin_part[((size_t)c * R.fin_nb + blk) * KC + tid] = s;
+    wrote_shared = true;
+  }
+  // arrival: the stores the last CTA reads are published before the count moves
+  if (wrote_shared) __threadfence();
+  __syncthreads();
+  if (tid == 0) {
+    const int old = atomicAdd(R.fin + c, 1);
+    is_last = (old == nact - 1);
+    if (is_last) R.fin[c] = 0;  // all CTAs of the chunk are in: reset for the next step
+  }
+  __syncthreads();
+  if (!is_last) return;
+  __threadfence();
+  if (tid < KC) {
+    double s = 0.0;
+    for (int k2 = 0; k2 < nact; ++k2) s += __ldcg(R.fin_part + ((size_t)c * R.fin_nb + k2) * KC + tid);
+    misc[16 + tid] = s;
+    misc[2 + tid] = __ldcg(R.fin_prev + (size_t)c * KC + tid);
+  }
+  if (tid == 0) misc[0] = R.hcm2[0];
+  __syncthreads();
+  if (tid < KC) memint_epilogue<TS>(R, c, t, tid, misc, 1, M2, measure);
 }
 
 // ---------------------------------------------------------------------------
@@ -1307,16 +1349,19 @@ cudaError_t configure_memint(bool fp64, size_t smem) {
 }
 
 cudaError_t launch_memint(bool fp64, int variant, int split, const RunDev *d_runs, const int *d_base, int nruns,
-                          int total_ctas, const int *d_t, int *d_err, int measure, size_t smem, cudaStream_t st) {
+                          int total_ctas, int fin_nb_max, const int *d_t, int *d_err, int measure, size_t smem,
+                          cudaStream_t st) {
   if (split && (fp64 || variant == 1)) {  // two half-triangle CTAs per chunk, then the finishing kernel
     if (fp64) {
       memint_kernel<double, CfgF64::T, CfgF64::NST, CfgF64::OPT, true>
           <<<2 * total_ctas, CfgF64::NT + 32, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure);
-      memint_finish_kernel<double><<<total_ctas, FIN_THREADS, 0, st>>>(d_runs, d_base, nruns, d_t, measure);
+      memint_finish_kernel<double>
+          <<<total_ctas * fin_nb_max, FIN_THREADS, 0, st>>>(d_runs, d_base, nruns, fin_nb_max, d_t, measure);
     } else {
       memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT, true>
           <<<2 * total_ctas, CfgF32::NT + 32, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure);
-      memint_finish_kernel<float><<<total_ctas, FIN_THREADS, 0, st>>>(d_runs, d_base, nruns, d_t, measure);
+      memint_finish_kernel<float>
+          <<<total_ctas * fin_nb_max, FIN_THREADS, 0, st>>>(d_runs, d_base, nruns, fin_nb_max, d_t, measure);
     }
     return cudaGetLastError();
   }
