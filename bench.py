@@ -211,6 +211,31 @@ def read_peaks():
         return 6800.0, "fallback"
 
 
+def sunset_flops(Ns, S, rows):
+    """Useful FP32 flops of the sunset per step: per t' row, four orbit cosine
+    transforms of 2 H^2 P + S H multiply-adds each (H = Ns/2+1, P = H(H+1)/2)."""
+    H = Ns // 2 + 1
+    P = H * (H + 1) // 2
+    return 2.0 * 4 * (2 * H * H * P + S * H) * rows
+
+
+def fp32_fma_peak_tflops(device):
+    """Nominal FP32 FMA rate: SMs x 128 lanes x 2 flops x maximum SM clock."""
+    mhz = 2070.0
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            mhz = float(json.load(f).get("sm_max_mhz", mhz))
+    except Exception:
+        pass
+    try:
+        import torch
+
+        nsm = torch.cuda.get_device_properties(device).multi_processor_count
+    except Exception:
+        nsm = 152
+    return nsm * 128 * 2 * mhz * 1e6 / 1e12
+
+
 def read_traffic(key):
     """Per-launch DRAM bytes of the memory-integral kernel from the committed ncu summary."""
     path = os.path.join(ROOT, "profiles", "memint_mixed_ns64_m1000.md")
@@ -559,6 +584,7 @@ def run_ours(args):
     else:
         mi_kernel, key = "memint_kernel<float,32,3,2>", "traffic_bytes_per_launch"
     traffic = read_traffic(key) if key and (CFG["Ns"], CFG["M"]) == (64, 1000) else None
+    fp32_peak = fp32_fma_peak_tflops(local)
     line = {
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -572,6 +598,12 @@ def run_ours(args):
         "graph_ms_per_step": gms / args.steps,
         "kernels_ms": {"memint": mi_ms, "sunset": sun_ms},
         "tuning": tuning,
+        "sunset": {"bound": "FP32 CUDA cores (shared-memory operand traffic and barriers between passes)",
+                   "useful_gflop_per_step": sunset_flops(CFG["Ns"], S, M - 1) / 1e9,
+                   "achieved_tflops": sunset_flops(CFG["Ns"], S, M - 1) / (sun_ms / 1000.0) / 1e12,
+                   "fp32_fma_peak_tflops": fp32_peak,
+                   "frac": sunset_flops(CFG["Ns"], S, M - 1) / (sun_ms / 1000.0) / 1e12 / fp32_peak,
+                   "peak_kind": "nominal (SMs x 128 x 2 x max SM clock)"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                      "kernel": mi_kernel, "algorithmic_bytes": alg},
