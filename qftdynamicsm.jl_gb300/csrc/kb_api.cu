@@ -10,8 +10,12 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
+
+#include <cuda.h>  // CUtensorMap and its enums (the encoder comes from the runtime's driver entry point)
+#include <cudaTypedefs.h>
 
 #include "../../include/kb2pi.h"
 #include "kb_internal.cuh"
@@ -37,6 +41,7 @@ struct Run {
   double *pi_r = nullptr, *pi_F = nullptr, *Ik = nullptr, *Jk = nullptr;  // 1/N NLO only
   int *fin = nullptr;  // finishing kernel of a split step
   double *fin_part = nullptr, *fin_prev = nullptr, *hcm2 = nullptr;
+  void *tmap = nullptr;  // two CUtensorMap of the history rings
   size_t hist_elems = 0, st_elems = 0, sig_elems = 0;
   RunDev dev{};
 };
@@ -165,12 +170,62 @@ size_t slot_off(const Run &R, int a) { return (size_t)(a % R.Malloc); }
 
 void free_run(Run &R) {
   void *ptrs[] = {R.hist_F, R.hist_r, R.sig_F, R.sig_r, R.st_F, R.st_r, R.k2_d, R.deg_d, R.Cm_d, R.tad, R.meas, R.epart,
-                  R.rowacc, R.colacc, R.pi_r, R.pi_F, R.Ik, R.Jk, R.fin, R.fin_part, R.fin_prev, R.hcm2};
+                  R.rowacc, R.colacc, R.pi_r, R.pi_F, R.Ik, R.Jk, R.fin, R.fin_part, R.fin_prev, R.hcm2, R.tmap};
   for (void *q : ptrs)
     if (q) cudaFree(q);
 }
 
 int tmin_of(const Run &R, int t) { return std::max(1, t - R.p.M + 1); }
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link to
+// the driver library); null when the driver does not provide it
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    else
+      cudaGetLastError();
+  });
+  return fn;
+}
+
+// Tensor maps of the two history rings as [tiles][T rows][T*KC] (tile-major
+// layout: every T x T x KC tile is contiguous, rows RS apart); box = one tile.
+// Returns a device copy of the two maps, or null (the kernels then use plain
+// bulk copies).
+void *make_history_maps(const Run &R) {
+  auto enc = tensor_map_encoder();
+  if (!enc) return nullptr;
+  alignas(64) CUtensorMap maps[2];
+  const cuuint64_t inner = (cuuint64_t)R.T * KC;
+  const cuuint64_t dims[3] = {inner, (cuuint64_t)R.T,
+                              (cuuint64_t)R.nchunks * (R.Malloc / R.T) * (R.Malloc / R.T)};
+  const cuuint64_t strides[2] = {inner * R.esz, inner * R.T * R.esz};
+  const cuuint32_t box[3] = {(cuuint32_t)inner, (cuuint32_t)R.T, 1}, estr[3] = {1, 1, 1};
+  const CUtensorMapDataType dt = R.esz == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+  void *bases[2] = {R.hist_F, R.hist_r};
+  for (int f = 0; f < 2; ++f)
+    if (enc(&maps[f], dt, 3, bases[f], dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) !=
+        CUDA_SUCCESS)
+      return nullptr;
+  void *d = nullptr;
+  if (cudaMalloc(&d, sizeof maps) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (cudaMemcpy(d, maps, sizeof maps, cudaMemcpyHostToDevice) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(d);
+    return nullptr;
+  }
+  return d;
+}
 
 // host <-> device copies of one (a, b) element column: S values spread over
 // chunks (KC contiguous per chunk)
@@ -375,6 +430,8 @@ int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out) {
     D.fin_part = R.fin_part;
     D.fin_prev = R.fin_prev;
     D.hcm2 = R.hcm2;
+    R.tmap = make_history_maps(R);
+    D.tmap = R.tmap;
     h->fin_nb_max = std::max(h->fin_nb_max, D.fin_nb);
     D.pi_r = R.pi_r;
     D.pi_F = R.pi_F;

@@ -65,6 +65,9 @@ struct RunDev {
   double *fin_part;  // [nchunks][fin_nb][KC] per-CTA sums of acc_F(t) terms
   double *fin_prev;  // [nchunks][KC] acc_F(t-1)
   double *hcm2;      // [2] hartreecont and M^2(t-1) of the step
+  // tensor maps (CUtensorMap, 64-byte aligned, device memory) of hist_F and hist_r
+  // as [tiles][T rows][T KC]: a tile is one box; null when the driver has none
+  const void *tmap;
 };
 
 // perturbative expansions (kb2pi.h): 0 LambdaLO, 1 LambdaNLO, 2 LambdaNLOclassical,

@@ -83,6 +83,14 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
 __device__ __forceinline__ void fence_proxy_async() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
+// tiled TMA load of one box of a 3D tensor map (x innermost, in elements)
+__device__ __forceinline__ void tma_load_3d(void *dst, const void *tmap, int x, int y, int z, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(smem_u32(dst)),
+      "l"(tmap), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
 
 // ---------------------------------------------------------------------------
 // Tensor memory (TMEM) for the FP64 row accumulators of memint_kernel: one lane
@@ -239,9 +247,23 @@ struct TileIt {
 // (one copy per row) saves another 7 % of the bytes at Ns = 64 but costs more
 // time than it saves: the many small copies slow every CTA. The stage offsets
 // are those of the whole tile, so the consumers index it unchanged.
+// Box of tile (I, J) fetched through the tensor maps: the tile's size, from row
+// r0 and column position x0 (in elements). Rows past t-1 (newest row block) or
+// before tmin (oldest diagonal tile) and the columns before tmin (oldest column
+// block, to the 4-column group of the XOR swizzle) fall outside the tile and are
+// filled with zeros instead of read. The box lands at the start of the stage,
+// so tile element (row, pos) sits at (row - r0) RS + pos - x0 there.
+template <typename C>
+__device__ __forceinline__ void tile_box(int I, int J, int tmin, int tlast, int &r0, int &x0) {
+  constexpr int T = C::T;
+  const int rlo = max(0, tmin - I * T), rhi = min(T - 1, tlast - I * T);
+  r0 = (rhi < T - 1) ? rhi - (T - 1) : rlo;
+  x0 = (J == tmin / T) ? ((tmin - J * T) & ~3) * KC : 0;
+}
+
 template <typename TS, typename C>
 __device__ __forceinline__ void issue_tile(int stage, int I, int J, const RunDev &R, int c, TS *stages,
-                                           uint64_t *full, int tmin, int tlast) {
+                                           uint64_t *full, int tmin, int tlast, bool use_tmap) {
   const int lane = threadIdx.x & 31;
   uint64_t *bar = full + stage;
   TS *dst = stages + (size_t)stage * C::STAGE;
@@ -251,14 +273,25 @@ __device__ __forceinline__ void issue_tile(int stage, int I, int J, const RunDev
   const TS *hR = reinterpret_cast<const TS *>(R.hist_r);
   if (lane == 0) {
     constexpr int T = C::T;
-    constexpr uint32_t ROWB = (uint32_t)(C::RS * sizeof(TS));
-    const size_t off = hist_off(R.Malloc, T, c, sa0, sb0, 0);  // start of the tile
-    const int rlo = max(0, tmin - I * T), rhi = min(T - 1, tlast - I * T);  // rows of the window
-    const uint32_t n = (uint32_t)(rhi - rlo + 1) * ROWB;
-    mbar_expect_tx(bar, 2 * n + 3 * C::XV * (uint32_t)sizeof(TS));
-    const size_t e = (size_t)rlo * C::RS;
-    bulk_g2s(dst + e, hF + off + e, n, bar);
-    bulk_g2s(dst + C::TILE + e, hR + off + e, n, bar);
+    if (use_tmap) {
+      int r0, x0;
+      tile_box<C>(I, J, tmin, tlast, r0, x0);
+      const int nb = R.Malloc / T;
+      const int tile = (c * nb + sa0 / T) * nb + sb0 / T;
+      mbar_expect_tx(bar, 2 * C::TILE * (uint32_t)sizeof(TS) + 3 * C::XV * (uint32_t)sizeof(TS));
+      const char *tm = reinterpret_cast<const char *>(R.tmap);
+      tma_load_3d(dst, tm, x0, r0, tile, bar);
+      tma_load_3d(dst + C::TILE, tm + 128, x0, r0, tile, bar);
+    } else {
+      constexpr uint32_t ROWB = (uint32_t)(C::RS * sizeof(TS));
+      const size_t off = hist_off(R.Malloc, T, c, sa0, sb0, 0);  // start of the tile
+      const int rlo = max(0, tmin - I * T), rhi = min(T - 1, tlast - I * T);  // rows of the window
+      const uint32_t n = (uint32_t)(rhi - rlo + 1) * ROWB;
+      mbar_expect_tx(bar, 2 * n + 3 * C::XV * (uint32_t)sizeof(TS));
+      const size_t e = (size_t)rlo * C::RS;
+      bulk_g2s(dst + e, hF + off + e, n, bar);
+      bulk_g2s(dst + C::TILE + e, hR + off + e, n, bar);
+    }
     const TS *sr = reinterpret_cast<const TS *>(R.sig_r) + (size_t)c * R.Malloc * KC;
     const TS *sF = reinterpret_cast<const TS *>(R.sig_F) + (size_t)c * R.Malloc * KC;
     bulk_g2s(dst + 2 * C::TILE, sr + (size_t)sa0 * KC, C::XV * sizeof(TS), bar);
@@ -417,6 +450,7 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   // bound by FP64 arithmetic, runs 1 % faster on the global scratch.
   double *rowacc = R.rowacc + (size_t)half * R.nchunks * rowstride + (size_t)c * rowstride;
   const bool use_tmem = sizeof(TS) == 4 && (Ma / T) * OPT * 2 <= (int)TMEM_COLS;
+  const bool use_tmap = R.tmap != nullptr;
   if (use_tmem && warp == 0) tmem_alloc(const_cast<uint32_t *>(tmem_slot));
 
   // --- tadpole mass M^2(t-1) from the per-chunk sums of F(t-1,t-1) (fixed order)
@@ -484,7 +518,7 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
         break;
       }
       if (*abort_flag) break;
-      issue_tile<TS, C>(stage, it.I, it.J, R, c, stages, full, tmin, t - 1);
+      issue_tile<TS, C>(stage, it.I, it.J, R, c, stages, full, tmin, t - 1, use_tmap);
       if (lane == 0) *issued_count = n + 1;
     }
     __syncwarp();
@@ -525,9 +559,12 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
           aborted = true;
           break;
         }
-        const TS *tF = stages + (size_t)stage * C::STAGE;
+        const TS *sbase = stages + (size_t)stage * C::STAGE;
+        int r0 = 0, x0 = 0;  // origin of the tensor-map box in the tile (see tile_box)
+        if (use_tmap) tile_box<C>(I, J, tmin, t - 1, r0, x0);
+        const TS *tF = sbase - ((ptrdiff_t)r0 * C::RS + x0);
         const TS *tR = tF + C::TILE;
-        const TS *xr_row = tF + 2 * C::TILE;
+        const TS *xr_row = sbase + 2 * C::TILE;
         const TS *xr_col = xr_row + C::XV;
         const TS *xF_col = xr_col + C::XV;
         if (colgrp) {
@@ -954,7 +991,7 @@ memint_blk_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base,
         break;
       }
       if (*abort_flag) break;
-      issue_tile<float, C>(stage, it.I, it.J, R, c, stages, full, tmin, t - 1);
+      issue_tile<float, C>(stage, it.I, it.J, R, c, stages, full, tmin, t - 1, false);
       if (lane == 0) *issued_count = n + 1;
     }
     __syncwarp();
