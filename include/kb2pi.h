@@ -121,6 +121,17 @@ int kb_expand(kb_handle *h);
  * F = F(t-1,t-1), ddF, n, omega, c. */
 int kb_measure(kb_handle *h, int32_t run, int32_t t, kb_meas_scalars *s, double *F, double *ddF,
                double *n, double *omega, double *c);
+/* Pipelined kb_measure for a time loop that issues step t+1 before it reads
+ * step t (evolve!/measure! of G_Simulation.jl:11-30 with the measurement one
+ * step behind): kb_measure_enqueue(h, run, t), right after kb_step(h, t), queues
+ * a copy of step t's measurement into one of two pinned host slots (t mod 2)
+ * and returns at once; kb_measure_take(h, run, t, ...) waits for that copy only
+ * and fills the outputs of kb_measure. A slot holds one step: take step t
+ * before enqueuing step t+2. Device error flags travel with the copy and fail
+ * the take as kb_sync would. */
+int kb_measure_enqueue(kb_handle *h, int32_t run, int32_t t);
+int kb_measure_take(kb_handle *h, int32_t run, int32_t t, kb_meas_scalars *s, double *F, double *ddF,
+                    double *n, double *omega, double *c);
 /* Traces of createMeasurement at lattice site 1 (TwoPIScalar_Measurement.jl:89-96):
  * SigF/Sigr at (t-1, tp) for tp = t-1 down to tmin; Fonet/ronet = F/rho(tmin, tp)
  * for tp = tmin .. t-1. Each has t - tmin entries. */

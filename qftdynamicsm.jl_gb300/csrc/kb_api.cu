@@ -58,6 +58,15 @@ struct kb_handle {
   int *d_base_sun = nullptr, *d_base_mi = nullptr;
   int total_sun = 0, total_mi = 0;
   int fin_nb_max = 1;  // CTA slots per chunk of the finishing kernel (max over runs)
+  // pipelined measurement (kb_measure_enqueue / kb_measure_take): two pinned
+  // host slots holding meas [5][Spad], epart [nchunks][4] and the device error
+  // flags of one measured step, by t mod 2
+  struct MeasSlot {
+    double *host = nullptr;
+    size_t cap = 0;  // doubles
+    int run = -1, t = -1;
+    cudaEvent_t ev = nullptr;
+  } mslot[2];
   int *d_t = nullptr, *d_err = nullptr;
   size_t smem_sun = 0, smem_mi = 0;
   int num_sms = 0, grid_sun = 0, grid_sun_max = 0;
@@ -510,6 +519,10 @@ void kb_destroy(kb_handle *h) {
   if (h->d_rec_off) cudaFree(h->d_rec_off);
   if (h->d_rec) cudaFree(h->d_rec);
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
+  for (auto &m : h->mslot) {
+    if (m.ev) cudaEventDestroy(m.ev);
+    if (m.host) cudaFreeHost(m.host);
+  }
   for (auto &R : h->runs) free_run(R);
   void *ptrs[] = {h->d_runs, h->d_base_sun, h->d_base_mi, h->d_t, h->d_err, h->sun_scratch};
   for (void *q : ptrs)
@@ -690,11 +703,8 @@ int kb_expand(kb_handle *h) {
   return KB_OK;
 }
 
-static int collect_scalars(kb_handle *h, int run, int t, kb_meas_scalars *s) {
-  Run &R = h->runs[run];
-  std::vector<double> ep((size_t)4 * R.nchunks);
-  KB_CUDA(h, cudaMemcpyAsync(ep.data(), R.epart, ep.size() * 8, cudaMemcpyDeviceToHost, h->st));
-  KB_CUDA(h, cudaStreamSynchronize(h->st));
+// energies of step t from the per-chunk partials ep [nchunks][4]
+static void scalars_from(const Run &R, int t, const double *ep, kb_meas_scalars *s) {
   double ek = 0, epo = 0, em = 0;
   for (int c = 0; c < R.nchunks; ++c) {
     ek += ep[(size_t)c * 4 + 0];
@@ -707,6 +717,14 @@ static int collect_scalars(kb_handle *h, int run, int t, kb_meas_scalars *s) {
   s->E_mem = (t == 2) ? 0.0 : em;
   s->E = s->E_kin + s->E_pot + s->E_mem;
   s->M2 = ep[3];
+}
+
+static int collect_scalars(kb_handle *h, int run, int t, kb_meas_scalars *s) {
+  Run &R = h->runs[run];
+  std::vector<double> ep((size_t)4 * R.nchunks);
+  KB_CUDA(h, cudaMemcpyAsync(ep.data(), R.epart, ep.size() * 8, cudaMemcpyDeviceToHost, h->st));
+  KB_CUDA(h, cudaStreamSynchronize(h->st));
+  scalars_from(R, t, ep.data(), s);
   return KB_OK;
 }
 
@@ -725,6 +743,63 @@ int kb_measure(kb_handle *h, int32_t run, int32_t t, kb_meas_scalars *s, double 
   rc = collect_scalars(h, run, t, s ? s : &tmp);
   if (rc) return rc;
   if (s && !std::isfinite(s->E)) return fail(h, KB_ERR_NAN, "non-finite energy at t=%d", t);
+  return KB_OK;
+}
+
+int kb_measure_enqueue(kb_handle *h, int32_t run, int32_t t) {
+  if (!h || run < 0 || run >= (int)h->runs.size()) return KB_ERR_PARAM;
+  if (t != h->t_cur || h->t_cur < 2)
+    return fail(h, KB_ERR_PARAM, "kb_measure_enqueue(%d): only the last evolved step %d can be measured", t, h->t_cur);
+  cudaSetDevice(h->device);
+  Run &R = h->runs[run];
+  auto &m = h->mslot[t & 1];
+  const size_t nm = (size_t)5 * R.Spad, ne = (size_t)4 * R.nchunks, need = nm + ne + 1;
+  if (!m.ev) KB_CUDA(h, cudaEventCreateWithFlags(&m.ev, cudaEventDisableTiming));
+  if (m.cap < need) {
+    if (m.host) {
+      KB_CUDA(h, cudaEventSynchronize(m.ev));  // a copy into the old buffer may be in flight
+      cudaFreeHost(m.host);
+      m.host = nullptr;
+      m.cap = 0;
+    }
+    KB_CUDA(h, cudaHostAlloc((void **)&m.host, need * sizeof(double), cudaHostAllocDefault));
+    m.cap = need;
+  }
+  // behind step t's kernels on the handle's stream; step t+1's run after them
+  KB_CUDA(h, cudaMemcpyAsync(m.host, R.meas, nm * 8, cudaMemcpyDeviceToHost, h->st));
+  KB_CUDA(h, cudaMemcpyAsync(m.host + nm, R.epart, ne * 8, cudaMemcpyDeviceToHost, h->st));
+  KB_CUDA(h, cudaMemcpyAsync(m.host + nm + ne, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  KB_CUDA(h, cudaEventRecord(m.ev, h->st));
+  m.run = run;
+  m.t = t;
+  return KB_OK;
+}
+
+int kb_measure_take(kb_handle *h, int32_t run, int32_t t, kb_meas_scalars *s, double *F, double *ddF, double *n,
+                    double *omega, double *c) {
+  if (!h || run < 0 || run >= (int)h->runs.size()) return KB_ERR_PARAM;
+  auto &m = h->mslot[t & 1];
+  if (m.t != t || m.run != run)
+    return fail(h, KB_ERR_PARAM, "kb_measure_take(%d): no measurement of step %d of run %d is queued", t, t, run);
+  cudaSetDevice(h->device);
+  KB_CUDA(h, cudaEventSynchronize(m.ev));
+  m.t = -1;  // taken
+  Run &R = h->runs[run];
+  const size_t nm = (size_t)5 * R.Spad, ne = (size_t)4 * R.nchunks;
+  int e = 0;
+  std::memcpy(&e, m.host + nm + ne, sizeof(int));
+  if (e) {
+    cudaMemset(h->d_err, 0, sizeof(int));
+    if (e & kb::DEVERR_TIMEOUT) return fail(h, KB_ERR_TIMEOUT, "a bounded device wait expired (kernel returned early)");
+    return fail(h, KB_ERR_CUDA, "device error flags 0x%x", e);
+  }
+  double *outs[5] = {F, ddF, n, omega, c};
+  for (int q = 0; q < 5; ++q)
+    if (outs[q]) std::memcpy(outs[q], m.host + (size_t)q * R.Spad, (size_t)R.S * 8);
+  kb_meas_scalars tmp;
+  kb_meas_scalars *sp = s ? s : &tmp;
+  scalars_from(R, t, m.host + nm, sp);
+  if (!std::isfinite(sp->E)) return fail(h, KB_ERR_NAN, "non-finite energy at t=%d", t);
   return KB_OK;
 }
 

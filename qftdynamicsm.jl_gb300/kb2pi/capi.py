@@ -26,6 +26,7 @@ KB_PREC_FP64, KB_PREC_MIXED = 0, 1
 EXPORTS = [
     "kb_create", "kb_create_batch", "kb_destroy", "kb_last_error", "kb_num_orbits", "kb_get_orbits",
     "kb_site_orbits", "kb_init", "kb_init_rows", "kb_step", "kb_steps", "kb_expand", "kb_measure",
+    "kb_measure_enqueue", "kb_measure_take",
     "kb_get_traces", "kb_get", "kb_set", "kb_self_energies", "kb_get_sigma", "kb_window",
     "kb_checkpoint_size", "kb_checkpoint_save", "kb_checkpoint_restore", "kb_sync",
     "kb_get_stream", "kb_profile", "kb_profile_read", "kb_steps_recorded", "kb_get_tuning", "kb_set_tuning", "kb_autotune",
@@ -95,6 +96,8 @@ def load_library(path: str | None = None):
             "kb_steps": (C.c_int, [vp, i32, i32, i32, P(KbMeasScalars), i32]),
             "kb_expand": (C.c_int, [vp]),
             "kb_measure": (C.c_int, [vp, i32, i32, P(KbMeasScalars), dp, dp, dp, dp, dp]),
+            "kb_measure_enqueue": (C.c_int, [vp, i32, i32]),
+            "kb_measure_take": (C.c_int, [vp, i32, i32, P(KbMeasScalars), dp, dp, dp, dp, dp]),
             "kb_get_traces": (C.c_int, [vp, i32, dp, dp, dp, dp]),
             "kb_get": (C.c_int, [vp, i32, i32, i32, i32, dp]),
             "kb_set": (C.c_int, [vp, i32, i32, i32, i32, dp]),
@@ -231,6 +234,21 @@ class Handle:
         arrs = {k: np.zeros(S) for k in ("F", "ddF", "n", "omega", "c")} if arrays else {}
         self._check(self.lib.kb_measure(self.h, run, int(t), C.byref(s), *[dptr(arrs.get(k)) for k in
                                                                             ("F", "ddF", "n", "omega", "c")]))
+        out = s.as_dict()
+        out.update(arrs)
+        return out
+
+    def measure_enqueue(self, run, t):
+        """Queue step t's measurement (t = the last evolved step) without waiting."""
+        self._check(self.lib.kb_measure_enqueue(self.h, run, int(t)))
+
+    def measure_take(self, run, t, arrays=True):
+        """The measurement queued by measure_enqueue(run, t): same dict as measure()."""
+        S = self.S[run]
+        s = KbMeasScalars()
+        arrs = {k: np.zeros(S) for k in ("F", "ddF", "n", "omega", "c")} if arrays else {}
+        self._check(self.lib.kb_measure_take(self.h, run, int(t), C.byref(s),
+                                             *[dptr(arrs.get(k)) for k in ("F", "ddF", "n", "omega", "c")]))
         out = s.as_dict()
         out.update(arrs)
         return out

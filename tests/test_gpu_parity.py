@@ -411,6 +411,43 @@ def test_device_measurement_stream(precision, tmp_path):
         assert m1["E"] == m2["E"] and np.array_equal(m1["n"], m2["n"])
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_pipelined_measurement(precision):
+    """kb_measure_enqueue / kb_measure_take with the next step issued before the
+    take equal kb_measure after each step, bitwise; a take of a step that was
+    not queued (or was taken already) and an enqueue of an old step fail."""
+    from kb2pi import capi
+
+    cfg = dict(Ns=10, M=12, N=4, lam=3.0, dt=0.1, pexp=1, T=1.5)
+    a = make_gpu(cfg, precision)
+    b = make_gpu(cfg, precision)
+    _, k2, _ = a.orbits()
+    n0 = occupation(cfg, k2)
+    a.init(0, n0, 1.0)
+    b.init(0, n0, 1.0)
+    ref, got = {}, {}
+    a.step(3)
+    a.measure_enqueue(0, 3)
+    for t in range(3, 30):
+        b.step(t)
+        ref[t] = b.measure(0, t)
+        if t + 1 < 30:
+            a.step(t + 1)
+            a.measure_enqueue(0, t + 1)
+        got[t] = a.measure_take(0, t)
+    for t in ref:
+        for k in ("time", "E", "E_pot", "E_kin", "E_mem", "M2"):
+            assert got[t][k] == ref[t][k], (t, k)
+        for k in ("F", "ddF", "n", "omega", "c"):
+            assert np.array_equal(got[t][k], ref[t][k]), (t, k)
+    with pytest.raises(capi.KbError):
+        a.measure_take(0, 29)  # taken already
+    with pytest.raises(capi.KbError):
+        a.measure_enqueue(0, 28)  # not the last evolved step
+    a.close()
+    b.close()
+
+
 # --- 1/N expansion (NinverseLO, NinverseNLO) -----------------------------------
 
 @pytest.mark.parametrize("cfg,steps", [
