@@ -129,6 +129,23 @@ function createMeasurement(t::Int64, model::TwoPIScalarPhi4, simdata::TwoPIScala
     return meas
 end
 
+# Pipelined measurement for a driver loop that evolves step t+1 before it reads
+# step t: call measure_enqueue(simdata, t) right after evolve!(..., t), and
+# measure_take(simdata, t) (scalars and per-orbit arrays, as kb_measure) once
+# step t+1 has been issued.
+measure_enqueue(simdata::TwoPIScalarSimDataGPUkb, t) =
+    kbcheck(ccall((:kb_measure_enqueue, libkb2pi), Cint, (Ptr{Cvoid}, Int32, Int32), simdata.h, 0, t), simdata.h)
+
+function measure_take(simdata::TwoPIScalarSimDataGPUkb, t)
+    S = simdata.S
+    s = Ref(KbMeasScalars())
+    F = zeros(S); ddF = zeros(S); n = zeros(S); omega = zeros(S); c = zeros(S)
+    kbcheck(ccall((:kb_measure_take, libkb2pi), Cint,
+                  (Ptr{Cvoid}, Int32, Int32, Ref{KbMeasScalars}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
+                   Ptr{Float64}), simdata.h, 0, t, s, F, ddF, n, omega, c), simdata.h)
+    return s[], F, ddF, n, omega, c
+end
+
 # occupation per orbit with lev2 = k2 (getparticlenr, TwoPIScalar_Initialization.jl:133-203)
 getparticlenr_orbit(init::TwoPIScalarParticle, disc, k2) = init.n
 getparticlenr_orbit(init::TwoPIScalarThermal, disc, k2) = 1 / (exp(sqrt(k2 + disc.Mass^2) / (init.T * disc.Mass)) - 1)
