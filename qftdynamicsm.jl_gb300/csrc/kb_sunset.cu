@@ -47,12 +47,22 @@ constexpr int rup4_c(int v) { return (v + 3) & ~3; }
 struct SunGeom {
   int H, H4, P, P4, S;
   int r1, r2;  // region sizes in elements
+  // pass 1 folded by C[X][h-x] = (-1)^X C[X][x] (h = Ns/2 = H-1): npair pairs
+  // x < h-x, a middle x = h/2 when h is even; ne even and no odd outputs X
+  int npair, mid, ne, no, ne4, no4, cf;  // cf: elements of the two folded matrices
   __host__ __device__ SunGeom(int H_) {
     H = H_;
     H4 = rup4(H);
     P = H * (H + 1) / 2;
     P4 = rup4(P);
     S = H * (H + 1) * (H + 2) / 6;
+    npair = H / 2;  // (h + 1) / 2
+    mid = (H - 1) % 2 == 0;
+    ne = npair + mid;
+    no = H - ne;
+    ne4 = rup4(ne);
+    no4 = rup4(no);
+    cf = rup4(ne * ne4 + no * no4);
     r1 = H * P4;  // E, then D (both [H][P4])
     if (S > r1) r1 = S;
     r2 = H * P4 + 4;  // B: pass 2 reads up to 3 entries past the last row
@@ -67,7 +77,7 @@ struct SunGeom {
 __host__ __device__ inline size_t sun_smem_base(bool fp64, int H) {
   SunGeom g(H);
   const size_t es = fp64 ? 8 : 4;
-  size_t elems = (size_t)g.H4 * g.H4 + rup4(g.S);
+  size_t elems = (size_t)g.H4 * g.H4 + g.cf + rup4(g.S);
   if (!fp64) elems += (size_t)g.r1 + g.r2;
   return elems * es + (size_t)(g.H + 1 + g.P4 / 4 + 1) * sizeof(int) + (size_t)rup4(g.P) * sizeof(uint16_t) + 64;
 }
@@ -113,7 +123,8 @@ __device__ __forceinline__ int orb_of(int x, int y, int z) {
 
 template <typename TC>
 struct SunCtx {
-  const TC *CT;         // [H4][H4]: CT[x][X] = C[X][x], zero where x or X >= H
+  const TC *CT;         // [H4][H4]: CT[x][X] = C[X][x], zero where x or X >= H; followed by CF:
+                        // [ne][ne4] C[2j][k] (even X = 2j), then [no][no4] C[2j+1][k] (odd X)
   const uint16_t *pr;   // [P]: pair p -> (lo | hi << 8)
   const int *off2;      // [H+1] item offsets of pass 2
   const int *off3;      // [P4/4 + 1] item offsets of pass 3
@@ -146,6 +157,20 @@ __device__ void sun_build_etab(const SunGeom &g, const uint16_t *pr, uint16_t *e
   }
 }
 
+// folded cosine matrices of pass 1 at CF = CT + H4^2, from cm(X, x) = C[X][x]
+template <typename TC, typename Cm>
+__device__ void sun_build_cf(const SunGeom &g, TC *CF, Cm cm) {
+  for (int i = threadIdx.x; i < g.ne * g.ne4; i += blockDim.x) {
+    const int k = i / g.ne4, j = i - k * g.ne4;
+    CF[i] = (j < g.ne) ? (TC)cm(2 * j, k) : (TC)0;
+  }
+  TC *CFo = CF + g.ne * g.ne4;
+  for (int i = threadIdx.x; i < g.no * g.no4; i += blockDim.x) {
+    const int k = i / g.no4, j = i - k * g.no4;
+    CFo[i] = (j < g.no) ? (TC)cm(2 * j + 1, k) : (TC)0;
+  }
+}
+
 // unroll of the pass loops (FP64 at 2: the 4 x 4 double tile fills the registers)
 template <typename TC>
 struct SunUnroll {
@@ -160,25 +185,42 @@ __device__ __forceinline__ void fma4x4(TC acc[4][4], const TC a[4], const TC b[4
     for (int j = 0; j < 4; ++j) acc[i][j] += a[i] * b[j];
 }
 
-// pass 1: B[X][p] = sum_x CT[x][X] E[x][p]
+// pass 1: B[X][p] = sum_x C[X][x] E[x][p], folded: with C[X][h-x] = (-1)^X C[X][x]
+// (h = H - 1), B[2j] = sum_{k<npair} C[2j][k] (E[k] + E[h-k]) (+ C[2j][h/2] E[h/2])
+// and B[2j+1] = sum_{k<npair} C[2j+1][k] (E[k] - E[h-k]): half the multiply-adds
 template <typename TC>
 __device__ void sun_pass1(const SunCtx<TC> &c, const TC *E, TC *B) {
-  const int H = c.g.H, P4 = c.g.P4;
-  const int nxb = c.g.H4 / 4, npb = P4 / 4;
-  for (int it = threadIdx.x; it < nxb * npb; it += blockDim.x) {
-    const int xb = it / npb, pb = it - xb * npb;
-    const int X0 = 4 * xb, p0 = 4 * pb;
+  const int P4 = c.g.P4, h = c.g.H - 1, npair = c.g.npair;
+  const int npb = P4 / 4, nbe = c.g.ne4 / 4, nbo = c.g.no4 / 4;
+  const TC *CF = c.CT + c.g.H4 * c.g.H4;
+  for (int it = threadIdx.x; it < (nbe + nbo) * npb; it += blockDim.x) {
+    const int jq = it / npb, pb = it - jq * npb;
+    const int odd = jq >= nbe ? 1 : 0;
+    const int j0 = 4 * (odd ? jq - nbe : jq), p0 = 4 * pb;
+    const int stride = odd ? c.g.no4 : c.g.ne4;
+    const TC *cf = CF + (odd ? c.g.ne * c.g.ne4 : 0) + j0;
+    const TC sg = odd ? (TC)-1 : (TC)1;
     TC acc[4][4] = {};
-#pragma unroll(SunUnroll<TC>::value)
-    for (int x = 0; x < H; ++x) {
-      TC cv[4], ev[4];
-      ld4(c.CT + x * c.g.H4 + X0, cv);
-      ld4(E + x * P4 + p0, ev);
+#pragma unroll 2
+    for (int k = 0; k < npair; ++k) {
+      TC cv[4], ea[4], eb[4], ev[4];
+      ld4(cf + k * stride, cv);
+      ld4(E + k * P4 + p0, ea);
+      ld4(E + (h - k) * P4 + p0, eb);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) ev[q] = ea[q] + sg * eb[q];
       fma4x4(acc, cv, ev);
     }
+    if (!odd && c.g.mid) {  // x = h/2: coefficient row npair of the even matrix
+      TC cv[4], ev[4];
+      ld4(cf + npair * stride, cv);
+      ld4(E + (h / 2) * P4 + p0, ev);
+      fma4x4(acc, cv, ev);
+    }
+    const int nrow = odd ? c.g.no : c.g.ne;
 #pragma unroll
     for (int i = 0; i < 4; ++i)
-      if (X0 + i < H) st4(B + (X0 + i) * P4 + p0, acc[i]);
+      if (j0 + i < nrow) st4(B + (2 * (j0 + i) + odd) * P4 + p0, acc[i]);
   }
 }
 
@@ -318,7 +360,7 @@ sunset_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
       SunGeom g(R.H);
       TC *p = reinterpret_cast<TC *>(smem_raw);
       TC *CT = p;
-      p += g.H4 * g.H4;
+      p += g.H4 * g.H4 + g.cf;
       TC *bufF = p;
       p += rup4(g.S);
       TC *R1, *R2;
@@ -356,6 +398,7 @@ sunset_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
         }
       }
       if (etab) sun_build_etab(g, pr, etab);
+      sun_build_cf(g, CT + g.H4 * g.H4, [&](int X, int x) { return R.Cm[X * g.H + x]; });
       __syncthreads();
       c = SunCtx<TC>{CT, pr, off2, off3, R1, R2, bufF, g, etab};
     }
@@ -537,7 +580,7 @@ sunset_rows_noalloc_kernel(int Ns, double fac_r, double fac_F, int classical, in
   const int H = Ns / 2 + 1;
   SunGeom g(H);
   double *CT = reinterpret_cast<double *>(smem_raw);
-  double *bufF = CT + g.H4 * g.H4;
+  double *bufF = CT + g.H4 * g.H4 + g.cf;
   int *off2 = reinterpret_cast<int *>(bufF + rup4(g.S));
   int *off3 = off2 + (g.H + 1);
   uint16_t *pr = reinterpret_cast<uint16_t *>(off3 + (g.P4 / 4 + 1));
@@ -549,6 +592,10 @@ sunset_rows_noalloc_kernel(int Ns, double fac_r, double fac_F, int classical, in
     const double m = (x == 0 || 2 * x == Ns) ? 1.0 : 2.0;
     CT[i] = (X < g.H && x < g.H) ? m * cospi(2.0 * (double)((x * X) % Ns) / (double)Ns) : 0.0;
   }
+  sun_build_cf(g, CT + g.H4 * g.H4, [&](int X, int x) {
+    const double m = (x == 0 || 2 * x == Ns) ? 1.0 : 2.0;
+    return m * cospi(2.0 * (double)((x * X) % Ns) / (double)Ns);
+  });
   for (int z = threadIdx.x; z < g.H; z += blockDim.x)
     for (int y = 0; y <= z; ++y) pr[tri2(z) + y] = (uint16_t)(y | (z << 8));
   if (threadIdx.x == 0) {
@@ -650,7 +697,7 @@ extern "C" int kb_sunset_rows_noalloc(int32_t Ns, int32_t N, double lambda, int3
   const double fac_r = iv * iv * iv * (-(lambda * lambda) * (Nd + 2.0) / (6.0 * Nd * Nd));
   const double fac_F = iv * iv * iv * (-(lambda * lambda) * (Nd + 2.0) / (18.0 * Nd * Nd));
   SunGeom g(H);
-  const size_t smem = ((size_t)g.H4 * g.H4 + rup4(g.S)) * sizeof(double) +
+  const size_t smem = ((size_t)g.H4 * g.H4 + g.cf + rup4(g.S)) * sizeof(double) +
                       (size_t)(g.H + 1 + g.P4 / 4 + 1) * sizeof(int) + (size_t)g.P * sizeof(uint16_t) + 64;
   sunset_rows_noalloc_kernel<<<grid, SUN_THREADS, smem, (cudaStream_t)stream>>>(
       Ns, fac_r, fac_F, pexp == KB_PEXP_NLO_CLASSICAL ? 1 : 0, nrows, F_rows, rho_rows, sigF_rows, sigr_rows,
@@ -688,7 +735,7 @@ sunset_adjoint_kernel(RunDev R, int t, const double *__restrict__ sbar_r, const 
   const int tmin = max(1, t - R.M + 1);
   SunGeom g(R.H);
   double *CT = reinterpret_cast<double *>(smem_raw);
-  double *bFx = CT + g.H4 * g.H4;     // Fx, then adjoint of Fx / deg
+  double *bFx = CT + g.H4 * g.H4 + g.cf;  // Fx, then adjoint of Fx / deg
   double *brx = bFx + rup4(g.S);      // rx, then adjoint of rx / deg
   double *bgr = brx + rup4(g.S);      // adjoint of g_r
   double *bgF = bgr + rup4(g.S);      // adjoint of g_F
@@ -702,6 +749,7 @@ sunset_adjoint_kernel(RunDev R, int t, const double *__restrict__ sbar_r, const 
     const int x = i / g.H4, X = i - x * g.H4;
     CT[i] = (X < g.H && x < g.H) ? R.Cm[X * g.H + x] : 0.0;
   }
+  sun_build_cf(g, CT + g.H4 * g.H4, [&](int X, int x) { return R.Cm[X * g.H + x]; });
   for (int z = threadIdx.x; z < g.H; z += blockDim.x)
     for (int y = 0; y <= z; ++y) pr[tri2(z) + y] = (uint16_t)(y | (z << 8));
   if (threadIdx.x == 0) {
@@ -783,7 +831,7 @@ sunset_adjoint_kernel(RunDev R, int t, const double *__restrict__ sbar_r, const 
 
 size_t sunset_adjoint_smem_bytes(int H) {
   SunGeom g(H);
-  return ((size_t)g.H4 * g.H4 + 4 * (size_t)rup4(g.S)) * sizeof(double) +
+  return ((size_t)g.H4 * g.H4 + g.cf + 4 * (size_t)rup4(g.S)) * sizeof(double) +
          (size_t)(g.H + 1 + g.P4 / 4 + 1) * sizeof(int) + (size_t)g.P * sizeof(uint16_t) + 64;
 }
 
@@ -831,6 +879,7 @@ __device__ void ninv_tables(const RunDev &R, const SunGeom &g, double *CT, uint1
     const int x = i / g.H4, X = i - x * g.H4;
     CT[i] = (X < g.H && x < g.H) ? R.Cm[X * g.H + x] : 0.0;
   }
+  sun_build_cf(g, CT + g.H4 * g.H4, [&](int X, int x) { return R.Cm[X * g.H + x]; });
   for (int z = threadIdx.x; z < g.H; z += blockDim.x)
     for (int y = 0; y <= z; ++y) pr[tri2(z) + y] = (uint16_t)(y | (z << 8));
   if (threadIdx.x == 0) {
@@ -853,7 +902,7 @@ __device__ void ninv_tables(const RunDev &R, const SunGeom &g, double *CT, uint1
 // shared memory: CT, NB orbit buffers, pass tables
 __host__ __device__ inline size_t ninv_rows_smem(int H, int NB) {
   SunGeom g(H);
-  return ((size_t)g.H4 * g.H4 + (size_t)NB * rup4(g.S)) * sizeof(double) +
+  return ((size_t)g.H4 * g.H4 + g.cf + (size_t)NB * rup4(g.S)) * sizeof(double) +
          (size_t)(g.H + 1 + g.P4 / 4 + 1) * sizeof(int) + (size_t)g.P * sizeof(uint16_t) + 64;
 }
 
@@ -888,7 +937,7 @@ ninv_rows_kernel(const RunDev *__restrict__ runs, const int *__restrict__ sched,
       SunGeom g(R.H);
       double *p = reinterpret_cast<double *>(smem_raw);
       double *CT = p;
-      p += g.H4 * g.H4;
+      p += g.H4 * g.H4 + g.cf;
       for (int q = 0; q < (MODE == 0 ? 2 : 4); ++q) {
         buf[q] = p;
         p += rup4(g.S);
