@@ -72,6 +72,12 @@ struct SunGeom {
   }
 };
 
+// pass 3 items of a block of four pairs whose smallest Y is Ymin: blocks of four
+// even outputs Z = 2j >= Ymin, then blocks of four odd outputs Z = 2j+1 >= Ymin
+__host__ __device__ inline int sun_items3(const SunGeom &g, int Ymin) {
+  return (g.ne4 / 4 - ((Ymin + 1) / 2) / 4) + (g.no4 / 4 - (Ymin / 2) / 4);
+}
+
 // shared memory of sunset_kernel without the expand table: cosine matrix,
 // one orbit buffer, the two pass regions (FP32 only), pass tables, pair list
 __host__ __device__ inline size_t sun_smem_base(bool fp64, int H) {
@@ -288,12 +294,15 @@ __device__ void sun_pass2(const SunCtx<TC> &c, const TC *B, TC *D) {
   }
 }
 
-// pass 3: out(orbit(X,Y,Z), sum_z CT[z][Z] D[z][q]) for q = (X,Y), Z >= Y
+// pass 3: out(orbit(X,Y,Z), sum_z C[Z][z] D[z][q]) for q = (X,Y), Z >= Y, folded
+// as pass 1: even Z = 2j from D[k] + D[h-k] (and the middle row), odd Z = 2j+1
+// from D[k] - D[h-k]; an item is four pairs by four outputs of one parity
 template <typename TC, typename Out>
 __device__ void sun_pass3(const SunCtx<TC> &c, const TC *D, Out out) {
-  const int H = c.g.H, H4 = c.g.H4, P = c.g.P, P4 = c.g.P4;
+  const int H = c.g.H, P = c.g.P, P4 = c.g.P4, h = H - 1, npair = c.g.npair;
   const int nqb = c.g.P4 / 4;
   const int total = c.off3[nqb];
+  const TC *CF = c.CT + c.g.H4 * c.g.H4;
   for (int it = threadIdx.x; it < total; it += blockDim.x) {
     int lo = 0, hi = nqb - 1;
     while (lo < hi) {
@@ -303,13 +312,28 @@ __device__ void sun_pass3(const SunCtx<TC> &c, const TC *D, Out out) {
     const int qb = lo;
     const int q0 = 4 * qb;
     const int Ymin = c.pr[min(q0, P - 1)] >> 8;
-    const int Z0 = 4 * (Ymin / 4) + 4 * (it - c.off3[qb]);
+    const int r = it - c.off3[qb];
+    const int jbe = ((Ymin + 1) / 2) / 4, ne_items = c.g.ne4 / 4 - jbe;
+    const int odd = r >= ne_items ? 1 : 0;
+    const int j0 = odd ? 4 * ((Ymin / 2) / 4 + (r - ne_items)) : 4 * (jbe + r);
+    const int stride = odd ? c.g.no4 : c.g.ne4;
+    const TC *cf = CF + (odd ? c.g.ne * c.g.ne4 : 0) + j0;
+    const TC sg = odd ? (TC)-1 : (TC)1;
     TC acc[4][4] = {};
-#pragma unroll(SunUnroll<TC>::value)
-    for (int z = 0; z < H; ++z) {
+#pragma unroll 2
+    for (int k = 0; k < npair; ++k) {
+      TC cv[4], da[4], db[4], dv[4];
+      ld4(cf + k * stride, cv);
+      ld4(D + k * P4 + q0, da);
+      ld4(D + (h - k) * P4 + q0, db);
+#pragma unroll
+      for (int i = 0; i < 4; ++i) dv[i] = da[i] + sg * db[i];
+      fma4x4(acc, dv, cv);
+    }
+    if (!odd && c.g.mid) {  // z = h/2: coefficient row npair of the even matrix
       TC cv[4], dv[4];
-      ld4(c.CT + z * H4 + Z0, cv);
-      ld4(D + z * P4 + q0, dv);
+      ld4(cf + npair * stride, cv);
+      ld4(D + (h / 2) * P4 + q0, dv);
       fma4x4(acc, dv, cv);
     }
 #pragma unroll
@@ -318,9 +342,9 @@ __device__ void sun_pass3(const SunCtx<TC> &c, const TC *D, Out out) {
       if (q >= P) continue;
       const int X = c.pr[q] & 255, Y = c.pr[q] >> 8;
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int Z = Z0 + j;
-        if (Z >= Y && Z < H) out(orb3s(X, Y, Z), acc[i][j]);
+      for (int jj = 0; jj < 4; ++jj) {
+        const int Z = 2 * (j0 + jj) + odd;
+        if (Z >= Y && Z < H) out(orb3s(X, Y, Z), acc[i][jj]);
       }
     }
   }
@@ -394,7 +418,7 @@ sunset_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
         off3[0] = 0;
         for (int qb = 0; qb < nqb; ++qb) {
           const int Ymin = pr[min(4 * qb, g.P - 1)] >> 8;
-          off3[qb + 1] = off3[qb] + (g.H4 / 4 - Ymin / 4);
+          off3[qb + 1] = off3[qb] + sun_items3(g, Ymin);
         }
       }
       if (etab) sun_build_etab(g, pr, etab);
@@ -609,7 +633,7 @@ sunset_rows_noalloc_kernel(int Ns, double fac_r, double fac_F, int classical, in
     off3[0] = 0;
     for (int qb = 0; qb < nqb; ++qb) {
       const int Ymin = pr[min(4 * qb, g.P - 1)] >> 8;
-      off3[qb + 1] = off3[qb] + (g.H4 / 4 - Ymin / 4);
+      off3[qb + 1] = off3[qb] + sun_items3(g, Ymin);
     }
   }
   __syncthreads();
@@ -763,7 +787,7 @@ sunset_adjoint_kernel(RunDev R, int t, const double *__restrict__ sbar_r, const 
     off3[0] = 0;
     for (int qb = 0; qb < nqb; ++qb) {
       const int Ymin = pr[min(4 * qb, g.P - 1)] >> 8;
-      off3[qb + 1] = off3[qb] + (g.H4 / 4 - Ymin / 4);
+      off3[qb + 1] = off3[qb] + sun_items3(g, Ymin);
     }
   }
   __syncthreads();
@@ -893,7 +917,7 @@ __device__ void ninv_tables(const RunDev &R, const SunGeom &g, double *CT, uint1
     off3[0] = 0;
     for (int qb = 0; qb < nqb; ++qb) {
       const int Ymin = pr[min(4 * qb, g.P - 1)] >> 8;
-      off3[qb + 1] = off3[qb] + (g.H4 / 4 - Ymin / 4);
+      off3[qb + 1] = off3[qb] + sun_items3(g, Ymin);
     }
   }
   __syncthreads();
