@@ -617,7 +617,8 @@ def run_ours(args):
         "e2e": {"value": e2e_val, "unit": "steps/s", "h2d_bytes_per_step": 4, "d2h_bytes_per_step": d2h,
                 "path": "kb_step + kb_measure_enqueue/kb_measure_take (one step behind) through the C ABI, "
                         "host buffers, wall clock"},
-        "gpu_launches": 3 * args.steps,
+        # per timed step: set_t_kernel, sunset_kernel, memint_kernel (+ memint_finish_kernel when split)
+        "gpu_launches": (4 if split else 3) * args.steps,
         "fp64_plain": fp64,
         "speedup_mixed_vs_fp64": (value / fp64["steps_per_s"]) if fp64 else None,
     }
