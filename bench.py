@@ -342,7 +342,9 @@ def run_batched(args):
             "data": f"synthetic: thermal states, per-run draws seeded with {args.seed}",
             "config": {"workload": "64 runs, Ns in {16,24,32,48}, lambda U[0.5,8], T U[0.5,3], M U{100..500}, "
                                    "dt=0.05, steps 478..500 of 500", "runs": runs},
-            "clocks": clk.summary(), "gpu_launches": 3 * args.steps, "tuning": tuning,
+            # per graph step: advance_t_kernel, sunset_kernel, memint_kernel (+ memint_finish_kernel when split)
+            "clocks": clk.summary(), "gpu_launches": (3 + bool(tuning.get("memint_split"))) * args.steps,
+            "tuning": tuning,
             "kernels_ms": {"memint": prof["memint"][0] / max(1, prof["memint"][1]),
                            "sunset": prof["sunset"][0] / max(1, prof["sunset"][1])}}
     print(json.dumps(line), flush=True)
@@ -463,7 +465,9 @@ def run_ninverse(args):
             "config": {"workload": f"NinverseNLO, Ns={Ns}, N=4, lambda=4, dt=0.05, M={M}, full window"},
             "kernels_ms": {"self_energies": prof["sunset"][0] / max(1, prof["sunset"][1]),
                            "memint": prof["memint"][0] / max(1, prof["memint"][1])},
-            "E": m["E"], "tuning": tuning, "clocks": clk.summary(), "gpu_launches": 5 * args.steps}
+            # per step: set_t_kernel, the three 1/N kernels, memint_kernel (+ memint_finish_kernel when split)
+            "E": m["E"], "tuning": tuning, "clocks": clk.summary(),
+            "gpu_launches": (5 + bool(tuning.get("memint_split"))) * args.steps}
     print(json.dumps(line), flush=True)
     return 0
 
