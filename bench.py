@@ -608,7 +608,8 @@ def run_ours(args):
         "graph_ms_per_step": gms / args.steps,
         "kernels_ms": {"memint": mi_ms, "sunset": sun_ms},
         "tuning": tuning,
-        "sunset": {"bound": "FP32 CUDA cores (shared-memory operand traffic and barriers between passes)",
+        "sunset": {"bound": "FP32 CUDA cores (shared-memory operand traffic and barriers between passes); "
+                            "flops counted as the direct cosine transforms (passes 1 and 3 run folded)",
                    "useful_gflop_per_step": sunset_flops(CFG["Ns"], S, M - 1) / 1e9,
                    "achieved_tflops": sunset_flops(CFG["Ns"], S, M - 1) / (sun_ms / 1000.0) / 1e12,
                    "fp32_fma_peak_tflops": fp32_peak,
