@@ -199,8 +199,9 @@ typedef struct kb_tuning {
                            * their shared memory fits); KB_PREC_FP64: 0 */
   int32_t memint_split;   /* 1: each chunk's triangle of history tiles is streamed by two CTAs (equal
                            * halves by column blocks), then a finishing kernel adds their sums and runs
-                           * the leapfrog; 0: one CTA per chunk. Needs memint_variant 1 in
-                           * KB_PREC_MIXED */
+                           * the leapfrog; 2: the same for the chunks past the last whole wave of one
+                           * CTA per SM only (the others as 0); 0: one CTA per chunk. 1 and 2 need
+                           * memint_variant 1 in KB_PREC_MIXED */
   int32_t reserved[3];
 } kb_tuning;
 int kb_get_tuning(const kb_handle *h, kb_tuning *out);

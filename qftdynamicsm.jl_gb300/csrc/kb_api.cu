@@ -71,7 +71,8 @@ struct kb_handle {
   size_t smem_sun = 0, smem_mi = 0;
   int num_sms = 0, grid_sun = 0, grid_sun_max = 0;
   int memint_variant = 0;         // FP32 consumer layout of the memory-integral kernel
-  int memint_split = 0;           // 1: two half-triangle CTAs per chunk and a finishing kernel
+  int memint_split = 0;           // 1: two half-triangle CTAs per chunk and a finishing kernel;
+                                  // 2: the same for the chunks past the last whole wave only
   int batch_order = 0;            // order of the runs' CTA ranges in the batched grids
   int sunset_variant = 0;         // FP32 sunset: 0 1024 threads per CTA, 1 512 threads (2 CTAs per SM)
   void *sun_scratch = nullptr;    // FP64 cosine-transform intermediates, one slot per CTA
@@ -644,6 +645,13 @@ static cudaEvent_t next_event(kb_handle *h) {
 
 // Sigma(t-1, .) of every run: the sunset (lambda expansion) and/or the 1/N
 // kernels; each kernel skips the runs of the other expansion.
+// chunks streamed whole by one CTA before the split ones (memint_split 2: the
+// whole waves of one CTA per SM; 1: none)
+static int memint_nwhole(const kb_handle *h) {
+  if (h->memint_split != 2) return 0;
+  return (h->total_mi / h->num_sms) * h->num_sms;
+}
+
 static int launch_self_energies(kb_handle *h) {
   if (h->any_nlo)
     KB_CUDA(h, kb::launch_sunset(h->fp64, h->sunset_variant, h->d_runs, h->d_base_sun, (int)h->runs.size(),
@@ -673,7 +681,8 @@ static int launch_step(kb_handle *h, int measure) {
     KB_CUDA(h, cudaEventRecord(e1, h->st));
     if (h->any_nlo || h->any_ninv) h->ev_pending.push_back({0, {e0, e1}});
   }
-  KB_CUDA(h, kb::launch_memint(h->fp64, h->memint_variant, h->memint_split, h->d_runs, h->d_base_mi, (int)h->runs.size(),
+  KB_CUDA(h, kb::launch_memint(h->fp64, h->memint_variant, h->memint_split, memint_nwhole(h), h->d_runs, h->d_base_mi,
+                                   (int)h->runs.size(),
                                h->total_mi, h->fin_nb_max, h->d_t, h->d_err, measure, h->smem_mi, h->st));
   if (h->profiling) {
     KB_CUDA(h, cudaEventRecord(e2, h->st));
@@ -1236,8 +1245,8 @@ int kb_set_tuning(kb_handle *h, const kb_tuning *in) {
   if (in->sunset_grid != 0 &&
       in->sunset_grid > h->num_sms * kb::sunset_max_ctas_per_sm(h->fp64, in->sunset_variant, h->smem_sun) * 4)
     return fail(h, KB_ERR_PARAM, "sunset_grid=%d: too large for this variant", in->sunset_grid);
-  if (in->memint_split < 0 || in->memint_split > 1 || (in->memint_split && !h->fp64 && in->memint_variant != 1))
-    return fail(h, KB_ERR_PARAM, "memint_split=%d: 0 or 1, and 1 only with memint_variant 1 in KB_PREC_MIXED",
+  if (in->memint_split < 0 || in->memint_split > 2 || (in->memint_split && !h->fp64 && in->memint_variant != 1))
+    return fail(h, KB_ERR_PARAM, "memint_split=%d: 0, 1 or 2, and 1, 2 only with memint_variant 1 in KB_PREC_MIXED",
                 in->memint_split);
   if (in->batch_order < 0 || in->batch_order > 1)
     return fail(h, KB_ERR_PARAM, "batch_order=%d: 0 (runs in order) or 1 (costliest first)", in->batch_order);
@@ -1281,7 +1290,8 @@ int kb_autotune(kb_handle *h, int32_t trials, kb_tuning *chosen, double *ms_per_
       KB_CUDA(h, cudaEventRecord(e[0], h->st));
       if ((rc = launch_self_energies(h))) return rc;
       KB_CUDA(h, cudaEventRecord(e[1], h->st));
-      KB_CUDA(h, kb::launch_memint(h->fp64, h->memint_variant, h->memint_split, h->d_runs, h->d_base_mi, (int)h->runs.size(),
+      KB_CUDA(h, kb::launch_memint(h->fp64, h->memint_variant, h->memint_split, memint_nwhole(h), h->d_runs, h->d_base_mi,
+                                   (int)h->runs.size(),
                                    h->total_mi, h->fin_nb_max, h->d_t, h->d_err, 1, h->smem_mi, h->st));
       KB_CUDA(h, cudaEventRecord(e[2], h->st));
       KB_CUDA(h, cudaEventSynchronize(e[2]));
@@ -1312,6 +1322,7 @@ int kb_autotune(kb_handle *h, int32_t trials, kb_tuning *chosen, double *ms_per_
   const int norder = h->runs.size() > 1 ? 2 : 1;
   const int v0 = h->fp64 ? 0 : 1;  // default memint variant first
   std::vector<std::pair<int, int>> mi_cands = {{v0, 1}};  // (variant, split) after (v0, 0)
+  if (h->total_mi > h->num_sms && h->total_mi % h->num_sms) mi_cands.push_back({v0, 2});
   if (!h->fp64) mi_cands.push_back({0, 0});
   int best_o = h->batch_order, best_v = v0, best_split = 0;
   std::pair<int, int> best_sc = sun_cands[0];

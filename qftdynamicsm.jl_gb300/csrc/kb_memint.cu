@@ -412,15 +412,16 @@ __host__ __device__ inline int split_block(int J0, int Jn) {
 // releases the stage through the empty mbarrier. Once per column block both
 // groups meet at a named barrier: the row sums of that block are complete and
 // the column group runs its leapfrog.
-// SPLIT: CTA 2k + h streams half h of chunk k's triangle, keeps its row sums in
-// row buffer h and stores the column sums of its column blocks instead of
-// running the leapfrog; memint_finish_kernel completes the step. Two CTAs per
-// chunk fill the partial last wave of a large grid and double the CTAs of a
-// small one.
+// SPLIT: the first nwhole CTAs take whole chunks as above; after them CTA
+// nwhole + 2k + h streams half h of chunk nwhole + k's triangle, keeps its row
+// sums in row buffer h and stores the column sums of its column blocks instead
+// of running the leapfrog; memint_finish_kernel completes those chunks. Split
+// chunks fill the partial last wave of a large grid (nwhole = whole waves) or
+// double the CTAs of a small one (nwhole = 0).
 template <typename TS, int T, int NST, int OPT, bool SPLIT>
 __global__ void __launch_bounds__(2 * T * (KC / OPT) + 32)
 memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int nruns,
-              const int *__restrict__ d_t, int *__restrict__ d_err, int measure) {
+              const int *__restrict__ d_t, int *__restrict__ d_err, int measure, int nwhole) {
   using C = Cfg<TS, T, NST, OPT>;
   using V = Vec<TS, OPT>;
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -440,8 +441,9 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   static_assert(C::NG == 128, "one TMEM lane per row-group thread, column group in warps 0..3");
   volatile uint32_t *tmem_slot = reinterpret_cast<volatile uint32_t *>(misc + 14);
 
-  const int item = SPLIT ? (int)(blockIdx.x >> 1) : (int)blockIdx.x;
-  const int half = SPLIT ? (int)(blockIdx.x & 1) : 0;
+  const bool split = SPLIT && (int)blockIdx.x >= nwhole;
+  const int item = split ? nwhole + (((int)blockIdx.x - nwhole) >> 1) : (int)blockIdx.x;
+  const int half = split ? (((int)blockIdx.x - nwhole) & 1) : 0;
   const int r = run_at(base, nruns, item);
   const RunDev &R = runs[r];
   const int c = item - R.cta_base_mi;  // chunk
@@ -512,9 +514,9 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   const bool lo_only = pexp_lo(R.pexp);
   const int J0 = tmin / T, Jn = (t - 1) / T;
   // column blocks of this CTA: all of them, or one half of the triangle
-  const int Js = SPLIT ? split_block(J0, Jn) : J0;
-  const int Jlo = (SPLIT && half == 1) ? Js : J0;
-  const int Jhi = (SPLIT && half == 0) ? Js - 1 : Jn;
+  const int Js = split ? split_block(J0, Jn) : J0;
+  const int Jlo = (split && half == 1) ? Js : J0;
+  const int Jhi = (split && half == 0) ? Js - 1 : Jn;
   int ntiles = 0;
   if (!lo_only)
     for (int J = Jlo; J <= Jhi; ++J) ntiles += Jn - J + 1;
@@ -692,7 +694,7 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
         break;
       }
 
-      if (SPLIT) {  // column sums of this block, for memint_finish_kernel
+      if (split) {  // column sums of this block, for memint_finish_kernel
         if (bvalid)
           for (int o = 0; o < OPT; ++o) {
             R.colacc[(size_t)c * rowstride + (size_t)(b % Ma) * KC + j0 + o] = colF[o];
@@ -749,7 +751,7 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
         if (b == t - 1) has_emem = true;
       }
     }
-    if (!SPLIT && !aborted && colgrp) {
+    if (!split && !aborted && colgrp) {
       // partial sums of acc_F(t) over this warp's columns (lanes sharing jq)
       for (int o = 0; o < OPT; ++o) {
         double v = diag[o];
@@ -769,13 +771,13 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
       for (int q = 0; q < *issued_count; ++q)
         (void)mbar_wait_bounded(full + (q % NST), (uint32_t)((q / NST) & 1));
   } else {
-    if (SPLIT && use_tmem && !producer && !colgrp)  // this half's row sums, for memint_finish_kernel
+    if (split && use_tmem && !producer && !colgrp)  // this half's row sums, for memint_finish_kernel
       for (int s = 0; s < Ma; s += T) {
         double v[OPT];
         TmemRow<OPT>::ld(tcol(s), v);
         for (int o = 0; o < OPT; ++o) rowacc[(size_t)(s + loc) * KC + j0 + o] = v[o];
       }
-    if (!SPLIT && tid < KC) memint_epilogue<TS>(R, c, t, tid, misc, C::NG / 32, M2, measure);
+    if (!split && tid < KC) memint_epilogue<TS>(R, c, t, tid, misc, C::NG / 32, M2, measure);
   }
   if (use_tmem) {  // every path ends here: the allocating warp frees the TMEM
     tmem_fence_before();
@@ -803,11 +805,11 @@ static_assert(FIN_IT * FIN_THREADS == FIN_TP * KC, "whole items per thread");
 template <typename TS>
 __global__ void __launch_bounds__(FIN_THREADS, 2)
 memint_finish_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int nruns, int nb_max,
-                     const int *__restrict__ d_t, int measure) {
+                     int nwhole, const int *__restrict__ d_t, int measure) {
   __shared__ double red[FIN_THREADS / 32][KC];
   __shared__ double misc[16 + KC];
   __shared__ int is_last;
-  const int ci = blockIdx.x / nb_max, blk = blockIdx.x - ci * nb_max;
+  const int ci = nwhole + (int)blockIdx.x / nb_max, blk = (int)blockIdx.x % nb_max;
   const int r = run_at(base, nruns, ci);
   const RunDev &R = runs[r];
   const int c = ci - R.cta_base_mi;
@@ -1398,29 +1400,34 @@ cudaError_t configure_memint(bool fp64, size_t smem) {
                               (int)smem);
 }
 
-cudaError_t launch_memint(bool fp64, int variant, int split, const RunDev *d_runs, const int *d_base, int nruns,
-                          int total_ctas, int fin_nb_max, const int *d_t, int *d_err, int measure, size_t smem,
-                          cudaStream_t st) {
-  if (split && (fp64 || variant == 1)) {  // two half-triangle CTAs per chunk, then the finishing kernel
+cudaError_t launch_memint(bool fp64, int variant, int split, int nwhole, const RunDev *d_runs, const int *d_base,
+                          int nruns, int total_ctas, int fin_nb_max, const int *d_t, int *d_err, int measure,
+                          size_t smem, cudaStream_t st) {
+  // split: the chunks from nwhole on are streamed by two half-triangle CTAs each
+  // and completed by the finishing kernel
+  const int nsplit = total_ctas - nwhole;
+  if (split && nsplit > 0 && (fp64 || variant == 1)) {
     if (fp64) {
-      memint_kernel<double, CfgF64::T, CfgF64::NST, CfgF64::OPT, true>
-          <<<2 * total_ctas, CfgF64::NT + 32, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure);
-      memint_finish_kernel<double>
-          <<<total_ctas * fin_nb_max, FIN_THREADS, 0, st>>>(d_runs, d_base, nruns, fin_nb_max, d_t, measure);
+      memint_kernel<double, CfgF64::T, CfgF64::NST, CfgF64::OPT, true><<<nwhole + 2 * nsplit, CfgF64::NT + 32, smem,
+                                                                         st>>>(d_runs, d_base, nruns, d_t, d_err,
+                                                                               measure, nwhole);
+      memint_finish_kernel<double><<<nsplit * fin_nb_max, FIN_THREADS, 0, st>>>(d_runs, d_base, nruns, fin_nb_max,
+                                                                                nwhole, d_t, measure);
     } else {
-      memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT, true>
-          <<<2 * total_ctas, CfgF32::NT + 32, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure);
-      memint_finish_kernel<float>
-          <<<total_ctas * fin_nb_max, FIN_THREADS, 0, st>>>(d_runs, d_base, nruns, fin_nb_max, d_t, measure);
+      memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT, true><<<nwhole + 2 * nsplit, CfgF32::NT + 32, smem,
+                                                                        st>>>(d_runs, d_base, nruns, d_t, d_err,
+                                                                              measure, nwhole);
+      memint_finish_kernel<float><<<nsplit * fin_nb_max, FIN_THREADS, 0, st>>>(d_runs, d_base, nruns, fin_nb_max,
+                                                                               nwhole, d_t, measure);
     }
     return cudaGetLastError();
   }
   if (fp64)
     memint_kernel<double, CfgF64::T, CfgF64::NST, CfgF64::OPT, false>
-        <<<total_ctas, CfgF64::NT + 32, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure);
+        <<<total_ctas, CfgF64::NT + 32, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, total_ctas);
   else if (variant == 1)
     memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT, false>
-        <<<total_ctas, CfgF32::NT + 32, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure);
+        <<<total_ctas, CfgF32::NT + 32, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, total_ctas);
   else
     memint_blk_kernel<CfgF32::NST><<<total_ctas, 288, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure);
   return cudaGetLastError();

@@ -160,3 +160,34 @@ def test_memint_split_mixed_and_batched():
     with pytest.raises(capi.KbError, match="memint_split"):
         h.set_tuning(memint_variant=0, memint_split=1)
     h.close()
+
+
+@pytest.mark.parametrize("precision,tol", [(0, 1e-10), (1, 1e-6)])
+def test_memint_tail_split_matches_whole(precision, tol):
+    """memint_split 2 at Ns=40 (222 chunks): the chunks of the whole waves of one
+    CTA per SM stream whole, the rest split in two and the finishing kernel
+    completes them; F, rho, n and E agree with the whole-chunk kernel (FP64 to
+    1e-10, mixed to 1e-6) with the window wrapped."""
+    cfg = dict(Ns=40, M=20, N=4, lam=3.0, dt=0.1, pexp=1, T=1.5)
+    hs = []
+    for split in (0, 2):
+        h = make_gpu(cfg, precision)
+        _, k2, _ = h.orbits()
+        h.init(0, occupation(cfg, k2), 1.0)
+        if precision == 1:
+            h.set_tuning(memint_variant=1, memint_split=split)
+        else:
+            h.set_tuning(memint_split=split)
+        assert h.tuning()["memint_split"] == split
+        h.steps(3, 30, 0)
+        hs.append(h)
+    a, b = hs
+    ma, mb = a.measure(0, 32), b.measure(0, 32)
+    assert rel(mb["n"], ma["n"]) <= tol
+    assert abs(mb["E"] - ma["E"]) <= tol * abs(ma["E"])
+    for tp in (13, 20, 31, 32):
+        assert rel(b.get(0, 0, 32, tp), a.get(0, 0, 32, tp)) <= tol
+        assert rel(b.get(0, 1, 32, tp), a.get(0, 1, 32, tp)) <= tol
+    for h in hs:
+        h.close()
+
