@@ -202,7 +202,9 @@ typedef struct kb_tuning {
                            * the leapfrog; 2: the same for the chunks past the last whole wave of one
                            * CTA per SM only (the others as 0); 0: one CTA per chunk. 1 and 2 need
                            * memint_variant 1 in KB_PREC_MIXED */
-  int32_t reserved[3];
+  int32_t memint_bulk;    /* 1: history tiles by plain bulk copies of whole rows instead of tensor-map
+                           * boxes (the path taken when the driver has no tensor-map encoder); 0 */
+  int32_t reserved[2];
 } kb_tuning;
 int kb_get_tuning(const kb_handle *h, kb_tuning *out);
 int kb_set_tuning(kb_handle *h, const kb_tuning *in);

@@ -421,7 +421,7 @@ __host__ __device__ inline int split_block(int J0, int Jn) {
 template <typename TS, int T, int NST, int OPT, bool SPLIT>
 __global__ void __launch_bounds__(2 * T * (KC / OPT) + 32)
 memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int nruns,
-              const int *__restrict__ d_t, int *__restrict__ d_err, int measure, int nwhole) {
+              const int *__restrict__ d_t, int *__restrict__ d_err, int measure, int nwhole, int use_maps) {
   using C = Cfg<TS, T, NST, OPT>;
   using V = Vec<TS, OPT>;
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -467,7 +467,7 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   // bound by FP64 arithmetic, runs 1 % faster on the global scratch.
   double *rowacc = R.rowacc + (size_t)half * R.nchunks * rowstride + (size_t)c * rowstride;
   const bool use_tmem = sizeof(TS) == 4 && (Ma / T) * OPT * 2 <= (int)TMEM_COLS;
-  const bool use_tmap = R.tmap != nullptr;
+  const bool use_tmap = use_maps && R.tmap != nullptr;
   if (use_tmem && warp == 0) tmem_alloc(const_cast<uint32_t *>(tmem_slot));
 
   // --- tadpole mass M^2(t-1) from the per-chunk sums of F(t-1,t-1) (fixed order)
@@ -1401,8 +1401,8 @@ cudaError_t configure_memint(bool fp64, size_t smem) {
 }
 
 cudaError_t launch_memint(bool fp64, int variant, int split, int nwhole, const RunDev *d_runs, const int *d_base,
-                          int nruns, int total_ctas, int fin_nb_max, const int *d_t, int *d_err, int measure,
-                          size_t smem, cudaStream_t st) {
+                          int nruns, int total_ctas, int fin_nb_max, int use_maps, const int *d_t, int *d_err,
+                          int measure, size_t smem, cudaStream_t st) {
   // split: the chunks from nwhole on are streamed by two half-triangle CTAs each
   // and completed by the finishing kernel
   const int nsplit = total_ctas - nwhole;
@@ -1410,13 +1410,13 @@ cudaError_t launch_memint(bool fp64, int variant, int split, int nwhole, const R
     if (fp64) {
       memint_kernel<double, CfgF64::T, CfgF64::NST, CfgF64::OPT, true><<<nwhole + 2 * nsplit, CfgF64::NT + 32, smem,
                                                                          st>>>(d_runs, d_base, nruns, d_t, d_err,
-                                                                               measure, nwhole);
+                                                                               measure, nwhole, use_maps);
       memint_finish_kernel<double><<<nsplit * fin_nb_max, FIN_THREADS, 0, st>>>(d_runs, d_base, nruns, fin_nb_max,
                                                                                 nwhole, d_t, measure);
     } else {
       memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT, true><<<nwhole + 2 * nsplit, CfgF32::NT + 32, smem,
                                                                         st>>>(d_runs, d_base, nruns, d_t, d_err,
-                                                                              measure, nwhole);
+                                                                              measure, nwhole, use_maps);
       memint_finish_kernel<float><<<nsplit * fin_nb_max, FIN_THREADS, 0, st>>>(d_runs, d_base, nruns, fin_nb_max,
                                                                                nwhole, d_t, measure);
     }
@@ -1424,10 +1424,10 @@ cudaError_t launch_memint(bool fp64, int variant, int split, int nwhole, const R
   }
   if (fp64)
     memint_kernel<double, CfgF64::T, CfgF64::NST, CfgF64::OPT, false>
-        <<<total_ctas, CfgF64::NT + 32, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, total_ctas);
+        <<<total_ctas, CfgF64::NT + 32, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, total_ctas, use_maps);
   else if (variant == 1)
     memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT, false>
-        <<<total_ctas, CfgF32::NT + 32, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, total_ctas);
+        <<<total_ctas, CfgF32::NT + 32, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, total_ctas, use_maps);
   else
     memint_blk_kernel<CfgF32::NST><<<total_ctas, 288, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure);
   return cudaGetLastError();

@@ -191,3 +191,28 @@ def test_memint_tail_split_matches_whole(precision, tol):
     for h in hs:
         h.close()
 
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_memint_bulk_copies_match_tensor_maps(precision):
+    """History tiles by plain bulk copies (memint_bulk 1, the path without a
+    tensor-map encoder) give the same F, rho, n and E as the tensor-map boxes,
+    bitwise: both deliver the same bytes in the same stage layout."""
+    cfg = dict(Ns=12, M=40, N=4, lam=3.0, dt=0.1, pexp=1, T=1.5)
+    hs = []
+    for bulk in (0, 1):
+        h = make_gpu(cfg, precision)
+        _, k2, _ = h.orbits()
+        h.init(0, occupation(cfg, k2), 1.0)
+        h.set_tuning(memint_bulk=bulk)
+        assert h.tuning()["memint_bulk"] == bulk
+        h.steps(3, 70, 0)
+        hs.append(h)
+    a, b = hs
+    ma, mb = a.measure(0, 72), b.measure(0, 72)
+    assert ma["E"] == mb["E"] and np.array_equal(ma["n"], mb["n"])
+    for tp in (33, 50, 72):
+        assert np.array_equal(a.get(0, 0, 72, tp), b.get(0, 0, 72, tp))
+        assert np.array_equal(a.get(0, 1, 72, tp), b.get(0, 1, 72, tp))
+    for h in hs:
+        h.close()
+
