@@ -14,19 +14,21 @@
 // passes keep the symmetry that survives them:
 //   expand  E[x][p]   = f(x, y_p, z_p)                      p = (y <= z) pair
 //   pass 1  B[X][p]   = sum_x C[X][x] E[x][p]                (symmetric in y,z)
-//   pass 2  D[q][z]   = sum_y C[Y][y] B[X][(y,z)]            q = (X <= Y) pair
-//   pass 3  P(X,Y,Z)  = sum_z C[Z][z] D[(X,Y)][z]            X <= Y <= Z: an orbit
+//   pass 2  D[z][q]   = sum_y C[Y][y] B[X][(y,z)]            q = (X <= Y) pair
+//   pass 3  P(X,Y,Z)  = sum_z C[Z][z] D[z][(X,Y)]            X <= Y <= Z: an orbit
 // Each pass is a small dense GEMM; every thread computes a 4 x 4 register
-// tile, loading four cosine coefficients with one 16-byte load per k. At
-// Ns = 64 a transform costs about 2 M multiply-adds (four per t') instead of
-// the four 262144-point FFTs of the reference.
+// tile. Passes 1 and 3 are folded by the parity of the cosine matrix,
+// C[X][h-x] = (-1)^X C[X][x] (h = Ns/2), so they contract over about half of
+// x (z); pass 2 contracts over y, one index of the symmetric pair storage,
+// and is not. At Ns = 64 a transform costs about 1.4 M multiply-adds (four per
+// t') instead of the four 262144-point FFTs of the reference.
 //
-// Intermediates E/D and B live in two regions R1, R2 of H*P values: in shared
-// memory for FP32, in a per-CTA global scratch slot for FP64 (whose regions
-// do not fit next to each other in 227 KB). The grid is persistent: CTA b
-// handles the t' rows b, b + gridDim, ... of all runs of the batch, so the
-// same launch serves every step of a CUDA graph (rows outside the window are
-// skipped).
+// Intermediates E/D and B live in two regions R1, R2 of about H*P values: in
+// shared memory for FP32, in a per-CTA global scratch slot for FP64 (whose
+// regions do not fit next to each other in 227 KB). The grid is persistent:
+// CTA b handles the t' rows b, b + gridDim, ... of all runs of the batch, so
+// the same launch serves every step of a CUDA graph (rows outside the window
+// are skipped).
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
