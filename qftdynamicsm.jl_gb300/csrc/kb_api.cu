@@ -1,9 +1,10 @@
 // kb_api.cu -- host side of libkb2pi: the C ABI declared in include/kb2pi.h.
 //
 // Owns the device memory of one or more runs, orchestrates one KB step as
-// two kernel launches (sunset, memory integral + leapfrog), captures multi-step
-// sequences in a CUDA graph, and exposes host views of the history for the
-// reference's measure!/getindex. No computation of the step happens on the
+// two kernel launches (sunset, memory integral + leapfrog; a third, the
+// finishing kernel, in split mode), captures multi-step sequences in a CUDA
+// graph, and exposes host views of the history for the reference's
+// measure!/getindex. No computation of the step happens on the
 // host; without a CUDA device every entry point fails with KB_ERR_NODEV.
 #include <algorithm>
 #include <cmath>
