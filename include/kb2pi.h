@@ -204,7 +204,10 @@ typedef struct kb_tuning {
                            * memint_variant 1 in KB_PREC_MIXED */
   int32_t memint_bulk;    /* 1: history tiles by plain bulk copies of whole rows instead of tensor-map
                            * boxes (the path taken when the driver has no tensor-map encoder); 0 */
-  int32_t reserved[2];
+  int32_t test_no_tiles;  /* test hook, 0 in use: 1 makes the memory-integral producer issue no tiles,
+                           * so every consumer's bounded wait runs out (about 2 s) and the step ends
+                           * with KB_ERR_TIMEOUT at the next kb_sync, the device still usable */
+  int32_t reserved[1];
 } kb_tuning;
 int kb_get_tuning(const kb_handle *h, kb_tuning *out);
 int kb_set_tuning(kb_handle *h, const kb_tuning *in);

@@ -73,6 +73,7 @@ struct kb_handle {
   int num_sms = 0, grid_sun = 0, grid_sun_max = 0;
   int memint_variant = 0;         // FP32 consumer layout of the memory-integral kernel
   int memint_bulk = 0;            // 1: history tiles by bulk copies instead of tensor-map boxes
+  int test_no_tiles = 0;          // test hook: the memint producer issues no tiles (waits run out)
   int memint_split = 0;           // 1: two half-triangle CTAs per chunk and a finishing kernel;
                                   // 2: the same for the chunks past the last whole wave only
   int batch_order = 0;            // order of the runs' CTA ranges in the batched grids
@@ -685,7 +686,7 @@ static int launch_step(kb_handle *h, int measure) {
   }
   KB_CUDA(h, kb::launch_memint(h->fp64, h->memint_variant, h->memint_split, memint_nwhole(h), h->d_runs, h->d_base_mi,
                                    (int)h->runs.size(),
-                               h->total_mi, h->fin_nb_max, !h->memint_bulk, h->d_t, h->d_err, measure, h->smem_mi, h->st));
+                               h->total_mi, h->fin_nb_max, !h->memint_bulk + 2 * h->test_no_tiles, h->d_t, h->d_err, measure, h->smem_mi, h->st));
   if (h->profiling) {
     KB_CUDA(h, cudaEventRecord(e2, h->st));
     h->ev_pending.push_back({1, {e1, e2}});
@@ -1232,6 +1233,7 @@ int kb_get_tuning(const kb_handle *h, kb_tuning *out) {
   out->sunset_variant = h->sunset_variant;
   out->memint_split = h->memint_split;
   out->memint_bulk = h->memint_bulk;
+  out->test_no_tiles = h->test_no_tiles;
   return KB_OK;
 }
 
@@ -1255,6 +1257,8 @@ int kb_set_tuning(kb_handle *h, const kb_tuning *in) {
     return fail(h, KB_ERR_PARAM, "batch_order=%d: 0 (runs in order) or 1 (costliest first)", in->batch_order);
   if (in->memint_bulk < 0 || in->memint_bulk > 1)
     return fail(h, KB_ERR_PARAM, "memint_bulk=%d: 0 (tensor-map boxes) or 1 (bulk copies)", in->memint_bulk);
+  if (in->test_no_tiles < 0 || in->test_no_tiles > 1)
+    return fail(h, KB_ERR_PARAM, "test_no_tiles=%d: 0 or 1", in->test_no_tiles);
   cudaSetDevice(h->device);
   int rc = kb_sync(h);
   if (rc) return rc;
@@ -1263,6 +1267,7 @@ int kb_set_tuning(kb_handle *h, const kb_tuning *in) {
   h->memint_variant = in->memint_variant;
   h->memint_split = in->memint_split;
   h->memint_bulk = in->memint_bulk;
+  h->test_no_tiles = in->test_no_tiles;
   h->sunset_variant = in->sunset_variant;
   h->grid_sun = g;
   if (h->graph) {  // captured with the old configuration
@@ -1298,7 +1303,7 @@ int kb_autotune(kb_handle *h, int32_t trials, kb_tuning *chosen, double *ms_per_
       KB_CUDA(h, cudaEventRecord(e[1], h->st));
       KB_CUDA(h, kb::launch_memint(h->fp64, h->memint_variant, h->memint_split, memint_nwhole(h), h->d_runs, h->d_base_mi,
                                    (int)h->runs.size(),
-                                   h->total_mi, h->fin_nb_max, !h->memint_bulk, h->d_t, h->d_err, 1, h->smem_mi, h->st));
+                                   h->total_mi, h->fin_nb_max, !h->memint_bulk + 2 * h->test_no_tiles, h->d_t, h->d_err, 1, h->smem_mi, h->st));
       KB_CUDA(h, cudaEventRecord(e[2], h->st));
       KB_CUDA(h, cudaEventSynchronize(e[2]));
       float a = 0, b = 0;

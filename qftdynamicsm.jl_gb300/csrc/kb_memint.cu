@@ -469,7 +469,8 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   // bound by FP64 arithmetic, runs 1 % faster on the global scratch.
   double *rowacc = R.rowacc + (size_t)half * R.nchunks * rowstride + (size_t)c * rowstride;
   const bool use_tmem = sizeof(TS) == 4 && (Ma / T) * OPT * 2 <= (int)TMEM_COLS;
-  const bool use_tmap = use_maps && R.tmap != nullptr;
+  const bool use_tmap = (use_maps & 1) && R.tmap != nullptr;
+  const bool no_tiles = (use_maps & 2) != 0;  // test hook: nothing is issued, the consumers' waits run out
   if (use_tmem && warp == 0) tmem_alloc(const_cast<uint32_t *>(tmem_slot));
 
   // --- tadpole mass M^2(t-1) from the per-chunk sums of F(t-1,t-1) (fixed order)
@@ -535,7 +536,7 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
         }
         break;
       }
-      if (*abort_flag) break;
+      if (*abort_flag || no_tiles) break;
       issue_tile<TS, C>(stage, it.I, it.J, R, c, stages, full, tmin, t - 1, use_tmap);
       if (lane == 0) *issued_count = n + 1;
     }
@@ -1402,6 +1403,8 @@ cudaError_t configure_memint(bool fp64, size_t smem) {
                               (int)smem);
 }
 
+// use_maps: bit 0 tensor-map boxes (else bulk copies), bit 1 the test hook that
+// issues no tiles (memint_kernel only)
 cudaError_t launch_memint(bool fp64, int variant, int split, int nwhole, const RunDev *d_runs, const int *d_base,
                           int nruns, int total_ctas, int fin_nb_max, int use_maps, const int *d_t, int *d_err,
                           int measure, size_t smem, cudaStream_t st) {

@@ -3,6 +3,8 @@ configuration computes the same step. Sunset grids are bitwise identical (one
 CTA per row whatever the grid); the two FP32 memory-integral variants differ
 only in the order of FP32 tile partial sums; the autotuner re-runs the last
 step and leaves the state as a plain run would."""
+import time
+
 import numpy as np
 import pytest
 
@@ -215,4 +217,35 @@ def test_memint_bulk_copies_match_tensor_maps(precision):
         assert np.array_equal(a.get(0, 1, 72, tp), b.get(0, 1, 72, tp))
     for h in hs:
         h.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_bounded_wait_runs_out_and_is_reported(precision):
+    """Failure detection without a GPU fault: with the test hook the memory-
+    integral producer issues no tiles, so every consumer's bounded wait runs out
+    (about 2 s), the kernel sets its error bit, frees its tensor memory and
+    returns; kb_sync reports KB_ERR_TIMEOUT once and the device keeps working
+    (a new handle evolves and measures)."""
+    from kb2pi import capi
+
+    cfg = dict(Ns=6, M=8, N=4, lam=2.0, dt=0.1, pexp=1, T=1.5)
+    h = make_gpu(cfg, precision)
+    _, k2, _ = h.orbits()
+    h.init(0, occupation(cfg, k2), 1.0)
+    h.steps(3, 5, 0)
+    h.sync()
+    h.set_tuning(test_no_tiles=1)
+    t0 = time.time()
+    h.step(8)
+    with pytest.raises(capi.KbError, match="KB_ERR_TIMEOUT"):
+        h.sync()
+    assert time.time() - t0 < 60
+    h.set_tuning(test_no_tiles=0)  # synchronises: the error was reported once and cleared
+    h.close()
+    g = make_gpu(cfg, precision)
+    g.init(0, occupation(cfg, k2), 1.0)
+    g.steps(3, 20, 0)
+    m = g.measure(0, 22)
+    assert np.isfinite(m["E"]) and np.all(np.isfinite(m["n"]))
+    g.close()
 
