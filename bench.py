@@ -1,5 +1,5 @@
 #!/usr/bin/env python
-"""Benchmark of the GB300 2PI Kadanoff-Baym step (metric of BASELINE: KB steps/s).
+"""Benchmark of the GB300 2PI Kadanoff-Baym step (headline metric: KB steps/s).
 
 Workload (N=1): the Ns=64 lattice, O(N=4), lambda=2, m=1, dt=0.05, memory
 window M=1000, tsunami initial state (the large configuration of the

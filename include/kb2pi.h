@@ -203,7 +203,7 @@ typedef struct kb_tuning {
                            * CTA per SM only (the others as 0); 0: one CTA per chunk. 1 and 2 need
                            * memint_variant 1 in KB_PREC_MIXED */
   int32_t memint_bulk;    /* 1: history tiles by plain bulk copies of whole rows instead of tensor-map
-                           * boxes (the path taken when the driver has no tensor-map encoder); 0 */
+                           * boxes (the path taken when the CUDA driver has no tensor-map encoder); 0 */
   int32_t test_no_tiles;  /* test hook, 0 in use: 1 makes the memory-integral producer issue no tiles,
                            * so every consumer's bounded wait runs out (about 2 s) and the step ends
                            * with KB_ERR_TIMEOUT at the next kb_sync, the device still usable */

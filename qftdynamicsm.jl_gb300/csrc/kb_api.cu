@@ -191,7 +191,7 @@ void free_run(Run &R) {
 int tmin_of(const Run &R, int t) { return std::max(1, t - R.p.M + 1); }
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no link to
-// the driver library); null when the driver does not provide it
+// the CUDA driver library); null when the CUDA driver does not provide it
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
   static std::once_flag once;
