@@ -805,8 +805,13 @@ constexpr int FIN_THREADS = 256;
 constexpr int FIN_IT = FIN_TP * KC / FIN_THREADS;
 static_assert(FIN_IT * FIN_THREADS == FIN_TP * KC, "whole items per thread");
 
+// FP32 history: four CTAs per SM (64 registers, about 120 bytes of spills), which
+// overlaps more of the loads with the FP64 arithmetic. Memory integrals per
+// Ns = 64, M = 1000 step: 4.077 against 4.099 ms with two CTAs per SM (128
+// registers); on another GB300, 4.046 against 4.092 ms for 512-thread CTAs
+// with two items per thread, two CTAs per SM
 template <typename TS>
-__global__ void __launch_bounds__(FIN_THREADS, 2)
+__global__ void __launch_bounds__(FIN_THREADS, sizeof(TS) == 4 ? 4 : 2)
 memint_finish_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int nruns, int nb_max,
                      int nwhole, const int *__restrict__ d_t, int measure) {
   __shared__ double red[FIN_THREADS / 32][KC];
