@@ -589,6 +589,11 @@ def run_ours(args):
     split = bool(tuning.get("memint_split"))
     if tuning.get("memint_variant") == 0:
         mi_kernel, key = "memint_blk_kernel<3>", None
+    elif tuning.get("memint_variant") == 2 and tuning.get("memint_split") == 2:
+        mi_kernel, key = ("memint_kernel<float,32,3,2,split,leapfrog warps> (whole waves whole, the rest split) + "
+                          "memint_finish_kernel", "traffic_bytes_per_step_tail_lfw")
+    elif tuning.get("memint_variant") == 2:
+        mi_kernel, key = "memint_kernel<float,32,3,2,whole,leapfrog warps>", "traffic_bytes_per_launch_lfw"
     elif tuning.get("memint_split") == 2:
         mi_kernel, key = ("memint_kernel<float,32,3,2,split> (whole waves whole, the rest split) + "
                           "memint_finish_kernel", "traffic_bytes_per_step_tail")

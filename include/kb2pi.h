@@ -192,7 +192,8 @@ int kb_profile_read(kb_handle *h, double *ms, int64_t *launches);
  * variant only changes the order of the FP32 tile partial sums (KB_PREC_MIXED). */
 typedef struct kb_tuning {
   int32_t memint_variant; /* KB_PREC_MIXED: 1 column/row consumer groups (default), 0 register-blocked
-                           * consumers; KB_PREC_FP64: 0 (one kernel) */
+                           * consumers, 2 as 1 with four more warps that run the leapfrog of whole
+                           * chunks while the consumers stream; KB_PREC_FP64: 0 (one kernel) */
   int32_t sunset_grid;    /* CTAs of the persistent sunset kernel; 0 = one per SM */
   int32_t batch_order;    /* batched handles: 0 runs in order, 1 costliest runs first in both grids */
   int32_t sunset_variant; /* KB_PREC_MIXED: 0 1024 threads per CTA, 1 512 threads (two CTAs per SM where
@@ -201,7 +202,7 @@ typedef struct kb_tuning {
                            * halves by column blocks), then a finishing kernel adds their sums and runs
                            * the leapfrog; 2: the same for the chunks past the last whole wave of one
                            * CTA per SM only (the others as 0); 0: one CTA per chunk. 1 and 2 need
-                           * memint_variant 1 in KB_PREC_MIXED */
+                           * memint_variant 1 or 2 in KB_PREC_MIXED */
   int32_t memint_bulk;    /* 1: history tiles by plain bulk copies of whole rows instead of tensor-map
                            * boxes (the path taken when the CUDA driver has no tensor-map encoder); 0 */
   int32_t test_no_tiles;  /* test hook, 0 in use: 1 makes the memory-integral producer issue no tiles,

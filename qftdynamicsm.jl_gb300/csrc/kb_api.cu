@@ -338,7 +338,8 @@ int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out) {
     R.Malloc = ((R.p.M + (R.p.flags & 0xffff) + T - 1) / T) * T;  // extra slots for kb_adjoint
     R.esz = h->fp64 ? 8 : 4;
     smem_sun = std::max(smem_sun, kb::sunset_smem_bytes(h->fp64, R.H));
-    smem_mi = std::max({smem_mi, kb::memint_smem_bytes(h->fp64, R.Malloc, 0), kb::memint_smem_bytes(h->fp64, R.Malloc, 1)});
+    smem_mi = std::max({smem_mi, kb::memint_smem_bytes(h->fp64, R.Malloc, 0), kb::memint_smem_bytes(h->fp64, R.Malloc, 1),
+                        kb::memint_smem_bytes(h->fp64, R.Malloc, 2)});
     base_sun += R.p.M;
     base_mi += R.nchunks;
     if (kb::pexp_sunset(R.p.pexp)) h->any_nlo = true;
@@ -1239,8 +1240,8 @@ int kb_get_tuning(const kb_handle *h, kb_tuning *out) {
 
 int kb_set_tuning(kb_handle *h, const kb_tuning *in) {
   if (!h || !in) return KB_ERR_PARAM;
-  if (in->memint_variant < 0 || in->memint_variant > 1 || (h->fp64 && in->memint_variant != 0))
-    return fail(h, KB_ERR_PARAM, "memint_variant=%d: 0 or 1, and 0 for KB_PREC_FP64", in->memint_variant);
+  if (in->memint_variant < 0 || in->memint_variant > 2 || (h->fp64 && in->memint_variant != 0))
+    return fail(h, KB_ERR_PARAM, "memint_variant=%d: 0, 1 or 2, and 0 for KB_PREC_FP64", in->memint_variant);
   const int g = in->sunset_grid == 0 ? kb::sunset_grid(h->fp64, h->num_sms, h->total_sun) : in->sunset_grid;
   if (g < 1 || g > h->grid_sun_max)
     return fail(h, KB_ERR_PARAM, "sunset_grid=%d: at most %d CTAs fit on this device", in->sunset_grid,
@@ -1250,8 +1251,8 @@ int kb_set_tuning(kb_handle *h, const kb_tuning *in) {
   if (in->sunset_grid != 0 &&
       in->sunset_grid > h->num_sms * kb::sunset_max_ctas_per_sm(h->fp64, in->sunset_variant, h->smem_sun) * 4)
     return fail(h, KB_ERR_PARAM, "sunset_grid=%d: too large for this variant", in->sunset_grid);
-  if (in->memint_split < 0 || in->memint_split > 2 || (in->memint_split && !h->fp64 && in->memint_variant != 1))
-    return fail(h, KB_ERR_PARAM, "memint_split=%d: 0, 1 or 2, and 1, 2 only with memint_variant 1 in KB_PREC_MIXED",
+  if (in->memint_split < 0 || in->memint_split > 2 || (in->memint_split && !h->fp64 && in->memint_variant == 0))
+    return fail(h, KB_ERR_PARAM, "memint_split=%d: 0, 1 or 2, and 1, 2 only with memint_variant 1 or 2 in KB_PREC_MIXED",
                 in->memint_split);
   if (in->batch_order < 0 || in->batch_order > 1)
     return fail(h, KB_ERR_PARAM, "batch_order=%d: 0 (runs in order) or 1 (costliest first)", in->batch_order);
@@ -1334,7 +1335,12 @@ int kb_autotune(kb_handle *h, int32_t trials, kb_tuning *chosen, double *ms_per_
   const int v0 = h->fp64 ? 0 : 1;  // default memint variant first
   std::vector<std::pair<int, int>> mi_cands = {{v0, 1}};  // (variant, split) after (v0, 0)
   if (h->total_mi > h->num_sms && h->total_mi % h->num_sms) mi_cands.push_back({v0, 2});
-  if (!h->fp64) mi_cands.push_back({0, 0});
+  if (!h->fp64) {
+    mi_cands.push_back({0, 0});
+    // whole chunks with their leapfrog on the leapfrog warps: alone, or for the whole waves
+    mi_cands.push_back({2, 0});
+    if (h->total_mi > h->num_sms && h->total_mi % h->num_sms) mi_cands.push_back({2, 2});
+  }
   int best_o = h->batch_order, best_v = v0, best_split = 0;
   std::pair<int, int> best_sc = sun_cands[0];
   float best_total = 1e30f, best_s_all = 0, best_m_all = 0;

@@ -390,6 +390,78 @@ __device__ void memint_epilogue(const RunDev &R, int c, int t, int tid, const do
   }
 }
 
+// leapfrog of column b (t' = b) for orbits j0 .. j0+OPT-1 of chunk c
+// (evolve_r!/evolve_F!, Evolution.jl:890-915) from the column sums colF, colR
+// and the row sums rowb of row b; adds the column's acc_F(t) terms to diag and
+// keeps acc_F(t-1) in emem (b = t-1)
+template <typename TS, int OPT>
+__device__ __forceinline__ void leapfrog_column(const RunDev &R, int c, int t, int tmin, int b, int j0, double M2,
+                                                bool lo_only, const double *colF, const double *colR,
+                                                const double *rowb, double *diag, double *emem, bool &has_emem) {
+  const int Ma = R.Malloc;
+  const size_t rowstride = (size_t)Ma * KC, st_row = (size_t)R.nchunks * rowstride;
+  const double dt3 = R.dt3;
+  const int sb = b % Ma;
+  const double wb = (b == tmin) ? 0.5 : 1.0;
+  const TS *sigr = reinterpret_cast<const TS *>(R.sig_r) + (size_t)c * rowstride + (size_t)sb * KC;
+  const TS *sigF = reinterpret_cast<const TS *>(R.sig_F) + (size_t)c * rowstride + (size_t)sb * KC;
+  const size_t cs = (size_t)c * rowstride;
+  const double *F1row = R.st_F + (size_t)((t - 1) % 3) * st_row + cs;
+  const double *F2row = R.st_F + (size_t)((t - 2) % 3) * st_row + cs;
+  const double *R1row = R.st_r + (size_t)((t - 1) % 3) * st_row + cs;
+  const double *R2row = R.st_r + (size_t)((t - 2) % 3) * st_row + cs;
+  double *FNrow = R.st_F + (size_t)(t % 3) * st_row + cs;
+  double *RNrow = R.st_r + (size_t)(t % 3) * st_row + cs;
+  TS *hF = reinterpret_cast<TS *>(R.hist_F);
+  TS *hR = reinterpret_cast<TS *>(R.hist_r);
+  for (int o = 0; o < OPT; ++o) {
+    const int j = j0 + o;
+    const int k = c * KC + j;
+    const double kk = (k < R.S) ? R.k2[k] : 0.0;
+    const double om = (kk + M2) * R.dt2;  // setomega2values!: (kL2 + M^2) * dt^2
+    const double xbr_d = lo_only ? 0.0 : wb * (double)sigr[j];
+    const double xbF_d = lo_only ? 0.0 : wb * (double)sigF[j];
+    const double accF = colF[o] + rowb[o];
+    const double accR = colR[o];
+    const double F1 = F1row[(size_t)sb * KC + j];
+    const double F2 = (b <= t - 2) ? F2row[(size_t)sb * KC + j] : F1row[(size_t)((t - 2) % Ma) * KC + j];
+    const double Fn = (2.0 - om) * F1 - F2 - accF * dt3;
+    double rn;
+    if (b == t - 1) {
+      rn = R.dt;  // phi-pi commutator rho(t, t-1) = dt
+    } else {
+      const double r1 = R1row[(size_t)sb * KC + j];
+      const double r2 = R2row[(size_t)sb * KC + j];
+      rn = (2.0 - om) * r1 - r2 - accR * dt3;
+    }
+    FNrow[(size_t)sb * KC + j] = Fn;
+    RNrow[(size_t)sb * KC + j] = rn;
+    const size_t ho = hist_off(Ma, R.T, c, t, b, j);
+    hF[ho] = (TS)Fn;
+    hR[ho] = (TS)rn;
+    diag[o] += xbr_d * Fn + xbF_d * rn;
+    if (b == t - 1) emem[o] = accF;
+  }
+  if (b == t - 1) has_emem = true;
+}
+
+// wait of a leapfrog warp on a hand-off barrier: false when the consumers
+// abort the chunk or after ~2 s
+__device__ bool lf_wait(uint64_t *bar, uint32_t parity, volatile int *cabort) {
+  const uint64_t t0 = globaltimer_ns();
+  for (uint32_t it = 0; it < (1u << 30); ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (*cabort) return false;
+    if ((it & 255u) == 0 && globaltimer_ns() - t0 > 2000000000ull) return false;
+  }
+  return false;
+}
+
+// hand-off stage of the leapfrog warps: two buffers of (colF, colR) x OPT per
+// column-group thread (128 threads x 2 orbits)
+constexpr size_t LF_STAGE_BYTES = 2 * 128 * 2 * 2 * sizeof(double);
+static_assert(LF_STAGE_BYTES <= 8 * 32 * KC * sizeof(double), "the stage fits where memint_blk_kernel keeps its column buffer");
+
 // Split mode: the triangle of a chunk is cut between column blocks into two
 // halves with (nearly) equal tile counts; half 0 takes blocks [J0, Js), half 1
 // blocks [Js, Jn]. Both kernels of the split step compute Js the same way.
@@ -420,8 +492,14 @@ __host__ __device__ inline int split_block(int J0, int Jn) {
 // of running the leapfrog; memint_finish_kernel completes those chunks. Split
 // chunks fill the partial last wave of a large grid (nwhole = whole waves) or
 // double the CTAs of a small one (nwhole = 0).
-template <typename TS, int T, int NST, int OPT, bool SPLIT>
-__global__ void __launch_bounds__(2 * T * (KC / OPT) + 32)
+// LFW (FP32 history): four more warps run the leapfrog of a whole chunk's column
+// blocks. The column group hands each block's column sums over through a
+// double-buffered shared-memory stage (lf_full / lf_empty mbarriers) and goes on
+// streaming; leapfrog warp q reads the row sums from TMEM quadrant q, the lanes
+// the column group's warp q reads, and takes over that warp's columns and
+// orbits, so the arithmetic and its order are the column group's.
+template <typename TS, int T, int NST, int OPT, bool SPLIT, bool LFW = false>
+__global__ void __launch_bounds__(2 * T * (KC / OPT) + 32 + (LFW ? T * (KC / OPT) : 0))
 memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int nruns,
               const int *__restrict__ d_t, int *__restrict__ d_err, int measure, int nwhole, int use_maps) {
   using C = Cfg<TS, T, NST, OPT>;
@@ -442,6 +520,11 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   static_assert(16 + (C::NG / 32) * KC <= 128, "misc scratch too small");
   static_assert(C::NG == 128, "one TMEM lane per row-group thread, column group in warps 0..3");
   volatile uint32_t *tmem_slot = reinterpret_cast<volatile uint32_t *>(misc + 14);
+  // LFW: [120..122) lf_full, [122..124) lf_empty mbarriers; the hand-off stage
+  // (two buffers of colF, colR per column-group thread) after the fixed region
+  uint64_t *lf_full = reinterpret_cast<uint64_t *>(misc + 120);
+  uint64_t *lf_empty = lf_full + 2;
+  double *lf_stage = reinterpret_cast<double *>(smem_raw + smem_fixed_bytes<C>());
 
   const bool split = SPLIT && (int)blockIdx.x >= nwhole;
   const int item = split ? nwhole + (((int)blockIdx.x - nwhole) >> 1) : (int)blockIdx.x;
@@ -450,8 +533,10 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   const RunDev &R = runs[r];
   const int c = item - R.cta_base_mi;  // chunk
   const int tid = threadIdx.x;
-  const bool producer = tid >= C::NT;
+  const bool producer = tid >= C::NT && tid < C::NT + 32;
+  const bool lfwarp = LFW && tid >= C::NT + 32;  // leapfrog warps
   const bool colgrp = tid < C::NG;
+  const bool rowgrp = tid >= C::NG && tid < C::NT;
   const int gtid = colgrp ? tid : tid - C::NG;  // index inside the group
   const int jq = gtid % C::NJ, loc = gtid / C::NJ;  // orbit group; column (col group) or row (row group)
   const int j0 = jq * OPT;                          // first orbit of this thread in the chunk
@@ -460,7 +545,6 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   const int M = R.M, Ma = R.Malloc;
   const int tmin = max(1, t - M + 1);
   const size_t rowstride = (size_t)Ma * KC;              // one row of one chunk
-  const size_t st_row = (size_t)R.nchunks * rowstride;   // one state row (all chunks)
   // row sums of this chunk, [Malloc][KC]: entries (slot, j0..j0+OPT-1) are only
   // ever written by row-group thread (slot mod T, jq), so they need no atomics.
   // With FP32 history they live in TMEM (Malloc/T slots x OPT doubles per lane)
@@ -492,9 +576,14 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
       mbar_init(full + q, 1);
       mbar_init(empty + q, C::NW);  // one arrival per consumer warp
     }
+    if (LFW)
+      for (int q = 0; q < 2; ++q) {
+        mbar_init(lf_full + q, C::NG / 32);   // column-group warps
+        mbar_init(lf_empty + q, C::NG / 32);  // leapfrog warps
+      }
     fence_proxy_async();
   }
-  if (!use_tmem && !producer && !colgrp)
+  if (!use_tmem && rowgrp)
     for (int s = loc; s < Ma; s += T)  // the slots this thread owns
       for (int o = 0; o < OPT; ++o) rowacc[(size_t)s * KC + j0 + o] = 0.0;
   if (use_tmem) tmem_fence_before();
@@ -509,10 +598,12 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   const uint32_t tlane = ((uint32_t)(warp & 3) * 32u) << 16;  // this warp's TMEM lanes
   // TMEM column of the row sums of slot s (s mod T is the thread's loc)
   auto tcol = [&](int s) { return tbase + tlane + (uint32_t)((s / T) * OPT * 2); };
-  if (use_tmem && !producer && !colgrp) {
+  if (use_tmem && rowgrp) {
     const double zero[OPT] = {};
     for (int s = 0; s < Ma; s += T) TmemRow<OPT>::st(tcol(s), zero);
   }
+  // whole chunks of an LFW kernel leave their leapfrog to the leapfrog warps
+  const bool lf_on = LFW && !split;
 
   const bool lo_only = pexp_lo(R.pexp);
   const int J0 = tmin / T, Jn = (t - 1) / T;
@@ -541,9 +632,52 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
       if (lane == 0) *issued_count = n + 1;
     }
     __syncwarp();
+  } else if (lfwarp) {
+    // ---------------- leapfrog warps (whole chunks of an LFW kernel)
+    if (lf_on) {
+      const int lq = warp & 3;         // TMEM quadrant of this warp
+      const int lg = lq * 32 + lane;   // the column-group thread whose columns and orbits this lane takes
+      const int lj0 = (lg % C::NJ) * OPT, lloc = lg / C::NJ;
+      double diag[OPT], emem[OPT];
+      for (int o = 0; o < OPT; ++o) diag[o] = emem[o] = 0.0;
+      bool has_emem = false, ok = true;
+      for (int J = Jlo; J <= Jhi; ++J) {
+        const int slot = (J - Jlo) & 1, use = (J - Jlo) >> 1;
+        ok = __all_sync(0xffffffffu, lf_wait(lf_full + slot, (uint32_t)(use & 1), cabort));
+        if (!ok) break;
+        if (use_tmem) tmem_fence_after();
+        const double *stg = lf_stage + ((size_t)slot * C::NG + lg) * 2 * OPT;
+        double colF[OPT], colR[OPT], rowb[OPT];
+        for (int o = 0; o < OPT; ++o) {
+          colF[o] = stg[o];
+          colR[o] = stg[OPT + o];
+        }
+        if (use_tmem) TmemRow<OPT>::ld(tcol((J * T) % Ma), rowb);
+        __syncwarp();
+        if (lane == 0) mbar_arrive(lf_empty + slot);
+        const int b = J * T + lloc;
+        if (b >= tmin && b <= t - 1) {
+          if (!use_tmem)
+            for (int o = 0; o < OPT; ++o) rowb[o] = rowacc[(size_t)(b % Ma) * KC + lj0 + o];
+          leapfrog_column<TS, OPT>(R, c, t, tmin, b, lj0, M2, lo_only, colF, colR, rowb, diag, emem, has_emem);
+        }
+      }
+      if (ok) {
+        // partial sums of acc_F(t) as the column group's warp lq would form them
+        for (int o = 0; o < OPT; ++o) {
+          double v = diag[o];
+#pragma unroll
+          for (int off = 16; off >= C::NJ; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+          if (lane < C::NJ) misc[16 + lq * KC + lj0 + o] = v;
+          if (has_emem) misc[2 + lj0 + o] = emem[o];
+        }
+      } else if (lane == 0) {
+        *abort_flag = 1;
+        atomicOr(d_err, DEVERR_TIMEOUT);
+      }
+    }
   } else {
     // ---------------- consumers
-    const double dt3 = R.dt3;
     double diag[OPT];  // acc_F(t) for the diagonal, partial over this thread's columns
     double emem[OPT];  // acc_F(t-1), kept by the thread of column t-1
     for (int o = 0; o < OPT; ++o) diag[o] = emem[o] = 0.0;
@@ -705,56 +839,38 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
           }
         continue;
       }
-      // leapfrog for t' = b (evolve_r!/evolve_F!, Evolution.jl:890-915); the row
-      // sums of row b come from the row-group thread on this thread's TMEM lane
+      if (lf_on) {  // column sums of this block to the leapfrog warps
+        if (colgrp) {
+          const int slot = (J - Jlo) & 1, use = (J - Jlo) >> 1;
+          // the buffer's previous block must have been read; a wait that runs out
+          // aborts the chunk at the next tile wait of every consumer
+          if (use > 0 && !mbar_wait_bounded(lf_empty + slot, (uint32_t)((use - 1) & 1))) {
+            *abort_flag = 1;
+            *cabort = 1;
+            atomicOr(d_err, DEVERR_TIMEOUT);
+            continue;
+          }
+          double *stg = lf_stage + ((size_t)slot * C::NG + gtid) * 2 * OPT;
+          for (int o = 0; o < OPT; ++o) {
+            stg[o] = colF[o];
+            stg[OPT + o] = colR[o];
+          }
+          __syncwarp();
+          if (lane == 0) mbar_arrive(lf_full + slot);
+        }
+        continue;
+      }
+      // leapfrog for t' = b; the row sums of row b come from the row-group thread
+      // on this thread's TMEM lane
       double rowb[OPT];
       if (use_tmem) TmemRow<OPT>::ld(tcol((J * T) % Ma), rowb);
       if (bvalid) {
-        const int sb = b % Ma;
-        const double wb = (b == tmin) ? 0.5 : 1.0;
-        const TS *sigr = reinterpret_cast<const TS *>(R.sig_r) + (size_t)c * rowstride + (size_t)sb * KC;
-        const TS *sigF = reinterpret_cast<const TS *>(R.sig_F) + (size_t)c * rowstride + (size_t)sb * KC;
-        const size_t cs = (size_t)c * rowstride;
-        const double *F1row = R.st_F + (size_t)((t - 1) % 3) * st_row + cs;
-        const double *F2row = R.st_F + (size_t)((t - 2) % 3) * st_row + cs;
-        const double *R1row = R.st_r + (size_t)((t - 1) % 3) * st_row + cs;
-        const double *R2row = R.st_r + (size_t)((t - 2) % 3) * st_row + cs;
-        double *FNrow = R.st_F + (size_t)(t % 3) * st_row + cs;
-        double *RNrow = R.st_r + (size_t)(t % 3) * st_row + cs;
-        TS *hF = reinterpret_cast<TS *>(R.hist_F);
-        TS *hR = reinterpret_cast<TS *>(R.hist_r);
-        for (int o = 0; o < OPT; ++o) {
-          const int j = j0 + o;
-          const int k = c * KC + j;
-          const double kk = (k < R.S) ? R.k2[k] : 0.0;
-          const double om = (kk + M2) * R.dt2;  // setomega2values!: (kL2 + M^2) * dt^2
-          const double xbr_d = lo_only ? 0.0 : wb * (double)sigr[j];
-          const double xbF_d = lo_only ? 0.0 : wb * (double)sigF[j];
-          const double accF = colF[o] + (use_tmem ? rowb[o] : rowacc[(size_t)sb * KC + j]);
-          const double accR = colR[o];
-          const double F1 = F1row[(size_t)sb * KC + j];
-          const double F2 = (b <= t - 2) ? F2row[(size_t)sb * KC + j] : F1row[(size_t)((t - 2) % Ma) * KC + j];
-          const double Fn = (2.0 - om) * F1 - F2 - accF * dt3;
-          double rn;
-          if (b == t - 1) {
-            rn = R.dt;  // phi-pi commutator rho(t, t-1) = dt
-          } else {
-            const double r1 = R1row[(size_t)sb * KC + j];
-            const double r2 = R2row[(size_t)sb * KC + j];
-            rn = (2.0 - om) * r1 - r2 - accR * dt3;
-          }
-          FNrow[(size_t)sb * KC + j] = Fn;
-          RNrow[(size_t)sb * KC + j] = rn;
-          const size_t ho = hist_off(Ma, T, c, t, b, j);
-          hF[ho] = (TS)Fn;
-          hR[ho] = (TS)rn;
-          diag[o] += xbr_d * Fn + xbF_d * rn;
-          if (b == t - 1) emem[o] = accF;
-        }
-        if (b == t - 1) has_emem = true;
+        if (!use_tmem)
+          for (int o = 0; o < OPT; ++o) rowb[o] = rowacc[(size_t)(b % Ma) * KC + j0 + o];
+        leapfrog_column<TS, OPT>(R, c, t, tmin, b, j0, M2, lo_only, colF, colR, rowb, diag, emem, has_emem);
       }
     }
-    if (!split && !aborted && colgrp) {
+    if (!split && !lf_on && !aborted && colgrp) {
       // partial sums of acc_F(t) over this warp's columns (lanes sharing jq)
       for (int o = 0; o < OPT; ++o) {
         double v = diag[o];
@@ -774,7 +890,7 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
       for (int q = 0; q < *issued_count; ++q)
         (void)mbar_wait_bounded(full + (q % NST), (uint32_t)((q / NST) & 1));
   } else {
-    if (split && use_tmem && !producer && !colgrp)  // this half's row sums, for memint_finish_kernel
+    if (split && use_tmem && rowgrp)  // this half's row sums, for memint_finish_kernel
       for (int s = 0; s < Ma; s += T) {
         double v[OPT];
         TmemRow<OPT>::ld(tcol(s), v);
@@ -1387,7 +1503,9 @@ int memint_tile(bool fp64) { return fp64 ? CfgF64::T : CfgF32::T; }
 size_t memint_smem_bytes(bool fp64, int Malloc, int variant) {
   (void)Malloc;
   if (fp64) return smem_fixed_bytes<CfgF64>();
-  return variant == 1 ? smem_fixed_bytes<CfgF32>() : smem_fixed_bytes<CfgF32>() + BLK_COLBUF_BYTES;
+  return variant == 1   ? smem_fixed_bytes<CfgF32>()
+         : variant == 2 ? smem_fixed_bytes<CfgF32>() + LF_STAGE_BYTES
+                        : smem_fixed_bytes<CfgF32>() + BLK_COLBUF_BYTES;
 }
 
 cudaError_t configure_memint(bool fp64, size_t smem) {
@@ -1404,6 +1522,12 @@ cudaError_t configure_memint(bool fp64, size_t smem) {
   e = cudaFuncSetAttribute(memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT, true>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT, false, true>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT, true, true>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
   return cudaFuncSetAttribute(memint_blk_kernel<CfgF32::NST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)smem);
 }
@@ -1416,6 +1540,19 @@ cudaError_t launch_memint(bool fp64, int variant, int split, int nwhole, const R
   // split: the chunks from nwhole on are streamed by two half-triangle CTAs each
   // and completed by the finishing kernel
   const int nsplit = total_ctas - nwhole;
+  constexpr int NTHR_LF = CfgF32::NT + 32 + CfgF32::NG;  // consumers, producer, leapfrog warps
+  if (!fp64 && variant == 2) {  // leapfrog warps for the whole chunks
+    if (split && nsplit > 0) {
+      memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT, true, true>
+          <<<nwhole + 2 * nsplit, NTHR_LF, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, nwhole, use_maps);
+      memint_finish_kernel<float><<<nsplit * fin_nb_max, FIN_THREADS, 0, st>>>(d_runs, d_base, nruns, fin_nb_max,
+                                                                               nwhole, d_t, measure);
+    } else {
+      memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT, false, true>
+          <<<total_ctas, NTHR_LF, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, total_ctas, use_maps);
+    }
+    return cudaGetLastError();
+  }
   if (split && nsplit > 0 && (fp64 || variant == 1)) {
     if (fp64) {
       memint_kernel<double, CfgF64::T, CfgF64::NST, CfgF64::OPT, true><<<nwhole + 2 * nsplit, CfgF64::NT + 32, smem,

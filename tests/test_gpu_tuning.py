@@ -194,6 +194,59 @@ def test_memint_tail_split_matches_whole(precision, tol):
         h.close()
 
 
+@pytest.mark.parametrize("cfg,split", [
+    (dict(Ns=40, M=20, N=4, lam=3.0, dt=0.1, pexp=1, T=1.5), 0),   # 222 chunks, window wrapped
+    (dict(Ns=40, M=20, N=4, lam=3.0, dt=0.1, pexp=1, T=1.5), 2),   # whole waves with leapfrog warps, tail split
+    (dict(Ns=12, M=40, N=4, lam=3.0, dt=0.1, pexp=2, T=1.5), 0),   # classical sunset, one partial wave
+    (dict(Ns=10, M=30, N=4, lam=3.0, dt=0.1, pexp=0, T=1.5), 0),   # LO: no memory integral, leapfrog only
+])
+def test_leapfrog_warps_are_bitwise_identical(cfg, split):
+    """memint_variant 2 (whole chunks hand each column block's sums to four
+    leapfrog warps) runs the same leapfrog arithmetic in the same order as the
+    column group of variant 1: F, rho, n and E agree bitwise."""
+    hs = []
+    for variant in (1, 2):
+        h = make_gpu(cfg, 1)
+        _, k2, _ = h.orbits()
+        h.init(0, occupation(cfg, k2), 1.0)
+        h.set_tuning(memint_variant=variant, memint_split=split)
+        assert h.tuning()["memint_variant"] == variant
+        h.steps(3, 30, 0)
+        for t in range(33, 36):  # single steps after the graph-captured ones
+            h.step(t)
+        hs.append(h)
+    a, b = hs
+    ma, mb = a.measure(0, 35), b.measure(0, 35)
+    assert ma["E"] == mb["E"] and np.array_equal(ma["n"], mb["n"])
+    tmin, _ = a.window(0)
+    for tp in sorted({tmin, (tmin + 35) // 2, 34, 35}):
+        assert np.array_equal(a.get(0, 0, 35, tp), b.get(0, 0, 35, tp))
+        assert np.array_equal(a.get(0, 1, 35, tp), b.get(0, 1, 35, tp))
+    for h in hs:
+        h.close()
+
+
+def test_leapfrog_warps_batched_runs():
+    """Batched uneven runs with the leapfrog warps: bitwise equal to variant 1."""
+    from kb2pi import capi
+
+    cfgs = [dict(Ns=8, M=20, lam=2.0, T=1.0), dict(Ns=16, M=45, lam=4.0, T=2.0), dict(Ns=12, M=33, lam=1.0, T=0.7)]
+    out = []
+    for variant in (1, 2):
+        ps = [capi.KbParams(Ns=c["Ns"], sdim=3, M=c["M"], N=4, pexp=1, precision=1, device=0, flags=0, dt=0.1,
+                            lam=c["lam"], mass2=1.0, mass=1.0) for c in cfgs]
+        h = capi.Handle(ps)
+        for r, c in enumerate(cfgs):
+            _, k2, _ = h.orbits(r)
+            h.init(r, occupation(dict(c), k2), 1.0)
+        h.set_tuning(memint_variant=variant)
+        h.steps(3, 60, 0)
+        out.append([h.measure(r, 62) for r in range(3)])
+        h.close()
+    for a, b in zip(out[0], out[1]):
+        assert a["E"] == b["E"] and np.array_equal(a["n"], b["n"])
+
+
 @pytest.mark.parametrize("precision", [0, 1])
 def test_memint_bulk_copies_match_tensor_maps(precision):
     """History tiles by plain bulk copies (memint_bulk 1, the path without a
@@ -219,8 +272,8 @@ def test_memint_bulk_copies_match_tensor_maps(precision):
         h.close()
 
 
-@pytest.mark.parametrize("precision", [0, 1])
-def test_bounded_wait_runs_out_and_is_reported(precision):
+@pytest.mark.parametrize("precision,variant", [(0, None), (1, None), (1, 2)])
+def test_bounded_wait_runs_out_and_is_reported(precision, variant):
     """Failure detection without a GPU fault: with the test hook the memory-
     integral producer issues no tiles, so every consumer's bounded wait runs out
     (about 2 s), the kernel sets its error bit, frees its tensor memory and
@@ -232,6 +285,8 @@ def test_bounded_wait_runs_out_and_is_reported(precision):
     h = make_gpu(cfg, precision)
     _, k2, _ = h.orbits()
     h.init(0, occupation(cfg, k2), 1.0)
+    if variant is not None:  # the leapfrog warps leave their hand-off wait when the consumers abort
+        h.set_tuning(memint_variant=variant)
     h.steps(3, 5, 0)
     h.sync()
     h.set_tuning(test_no_tiles=1)
