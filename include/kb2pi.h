@@ -191,8 +191,8 @@ int kb_profile_read(kb_handle *h, double *ms, int64_t *launches);
  * (it has no tunables). Every choice computes the same step; the memory-integral
  * variant only changes the order of the FP32 tile partial sums (KB_PREC_MIXED). */
 typedef struct kb_tuning {
-  int32_t memint_variant; /* KB_PREC_MIXED: 1 column/row consumer groups (default), 0 register-blocked
-                           * consumers, 2 as 1 with four more warps that run the leapfrog of whole
+  int32_t memint_variant; /* KB_PREC_MIXED: 1 column/row consumer groups, 0 register-blocked consumers,
+                           * 2 (default) as 1 with four more warps that run the leapfrog of whole
                            * chunks while the consumers stream; KB_PREC_FP64: 0 (one kernel) */
   int32_t sunset_grid;    /* CTAs of the persistent sunset kernel; 0 = one per SM */
   int32_t batch_order;    /* batched handles: 0 runs in order, 1 costliest runs first in both grids */
@@ -201,8 +201,9 @@ typedef struct kb_tuning {
   int32_t memint_split;   /* 1: each chunk's triangle of history tiles is streamed by two CTAs (equal
                            * halves by column blocks), then a finishing kernel adds their sums and runs
                            * the leapfrog; 2: the same for the chunks past the last whole wave of one
-                           * CTA per SM only (the others as 0); 0: one CTA per chunk. 1 and 2 need
-                           * memint_variant 1 or 2 in KB_PREC_MIXED */
+                           * CTA per SM only (the others as 0); 0 (default): one CTA per chunk, the
+                           * same arithmetic whatever the handle's size. 1 and 2 need memint_variant
+                           * 1 or 2 in KB_PREC_MIXED */
   int32_t memint_bulk;    /* 1: history tiles by plain bulk copies of whole rows instead of tensor-map
                            * boxes (the path taken when the CUDA driver has no tensor-map encoder); 0 */
   int32_t test_no_tiles;  /* test hook, 0 in use: 1 makes the memory-integral producer issue no tiles,

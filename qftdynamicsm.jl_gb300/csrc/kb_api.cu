@@ -320,7 +320,7 @@ int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out) {
   kb_handle *h = new kb_handle();
   h->device = p[0].device;
   h->fp64 = (p[0].precision == KB_PREC_FP64);
-  h->memint_variant = h->fp64 ? 0 : 1;  // FP32: two consumer groups unless kb_set_tuning/kb_autotune choose
+  h->memint_variant = h->fp64 ? 0 : 2;  // FP32: two consumer groups and leapfrog warps unless kb_set_tuning/kb_autotune choose
   if (cudaSetDevice(h->device) != cudaSuccess) { delete h; return fail(nullptr, KB_ERR_CUDA, "cudaSetDevice failed"); }
   if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess) {
     delete h;
@@ -1332,7 +1332,7 @@ int kb_autotune(kb_handle *h, int32_t trials, kb_tuning *chosen, double *ms_per_
   }
   if (sun_cands.empty()) sun_cands.push_back({h->sunset_variant, h->grid_sun});
   const int norder = h->runs.size() > 1 ? 2 : 1;
-  const int v0 = h->fp64 ? 0 : 1;  // default memint variant first
+  const int v0 = h->fp64 ? 0 : 1;  // the one-kernel FP64 or the two-group FP32 memint, whole chunks, first
   std::vector<std::pair<int, int>> mi_cands = {{v0, 1}};  // (variant, split) after (v0, 0)
   if (h->total_mi > h->num_sms && h->total_mi % h->num_sms) mi_cands.push_back({v0, 2});
   if (!h->fp64) {
