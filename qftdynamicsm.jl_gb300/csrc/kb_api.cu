@@ -283,7 +283,7 @@ static int apply_schedule(kb_handle *h, int order) {
     ssun[q] = bs;
     ssun[nr + q] = pos_sun[q];
     Rs.dev.cta_base_sun = bs;
-    bs += Rs.p.M;
+    bs += (Rs.p.M + Rs.dev.sun_rows - 1) / Rs.dev.sun_rows;
   }
   std::vector<RunDev> devs(nr);
   for (int r = 0; r < nr; ++r) devs[r] = h->runs[r].dev;
@@ -349,9 +349,15 @@ int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out) {
       h->smem_nv = std::max(h->smem_nv, kb::ninv_volterra_smem_bytes(R.Malloc));
     }
   }
-  h->total_sun = base_sun;
+  (void)base_sun;
   h->total_mi = base_mi;
   h->smem_sun = smem_sun;
+  // sunset items: FP32 runs of small lattices put several t' rows in one item
+  h->total_sun = 0;
+  for (auto &R : h->runs) {
+    R.dev.sun_rows = (h->fp64 || !kb::pexp_sunset(R.p.pexp)) ? 1 : kb::sunset_rows_per_item(R.H);
+    h->total_sun += (R.p.M + R.dev.sun_rows - 1) / R.dev.sun_rows;
+  }
   h->smem_mi = smem_mi;
   int maxsm = 0;
   cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);

@@ -51,8 +51,9 @@ struct RunDev {
   double *epart;            // [nchunks][4]
   double *rowacc;           // [2][nchunks][Malloc][KC] row sums of the memory integrals (one per half when split)
   double *colacc;           // [2][nchunks][Malloc][KC] column sums F, rho of a split step
-  int cta_base_sun, cta_base_mi;  // first CTA of this run in the batched grids
-  int pad0, pad1;
+  int cta_base_sun, cta_base_mi;  // first item of this run in the batched grids
+  int sun_rows;                   // t' rows per sunset item (taken one after the other), 1 for FP64
+  int pad1;
   // 1/N expansion at NLO (pexp 4), FP64: bubble rings (layout of hist_F) and the
   // momentum-space resummed kernels I_k, J_k of the window ([Malloc][Spad])
   double *pi_r, *pi_F, *Ik, *Jk;
@@ -103,6 +104,7 @@ cudaError_t launch_sunset(bool fp64, int variant, const RunDev *d_runs, const in
                           int total_rows, int grid, const int *d_t, void *scratch, size_t scratch_stride, size_t smem,
                           cudaStream_t st);
 size_t sunset_smem_bytes(bool fp64, int H);
+int sunset_rows_per_item(int H);  // FP32: t' rows per sunset item
 size_t sunset_scratch_elems(int H);
 int sunset_grid(bool fp64, int num_sms, int total_rows);
 int sunset_max_ctas_per_sm(bool fp64, int variant, size_t smem);

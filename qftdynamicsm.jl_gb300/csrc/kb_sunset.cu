@@ -97,6 +97,32 @@ __host__ __device__ inline bool sun_etab_fits(bool fp64, int H) {
   return sun_smem_base(fp64, H) + (size_t)g.H * g.P4 * sizeof(uint16_t) <= SUN_SMEM_CAP;
 }
 
+// byte offsets in the shared memory of sunset_kernel: the per-run tables (cosine
+// and folded matrices, pass offsets, pair list, expand table when it fits), then
+// the orbit buffer and, FP32, the two pass regions
+struct SunLayout {
+  size_t ct, off2, off3, pr, etab, regions, bytes;
+};
+__host__ __device__ inline SunLayout sun_layout(bool fp64, int H) {
+  SunGeom g(H);
+  const size_t es = fp64 ? 8 : 4;
+  SunLayout L;
+  size_t o = 0;
+  L.ct = o;
+  o += ((size_t)g.H4 * g.H4 + g.cf) * es;
+  L.off2 = o;
+  o += (size_t)(g.H + 1) * sizeof(int);
+  L.off3 = o;
+  o += (size_t)(g.P4 / 4 + 1) * sizeof(int);
+  L.pr = o;
+  o += (size_t)rup4(g.P) * sizeof(uint16_t);
+  L.etab = o;
+  if (sun_etab_fits(fp64, H)) o += (size_t)g.H * g.P4 * sizeof(uint16_t);
+  L.regions = (o + 15) & ~(size_t)15;
+  L.bytes = L.regions + ((size_t)rup4(g.S) + (fp64 ? 0 : (size_t)g.r1 + g.r2)) * es;
+  return L;
+}
+
 __device__ __forceinline__ void prefetch_l2(const void *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
 // 4-wide vector load/store for float (float4) and double (2 x double2)
@@ -364,7 +390,10 @@ __device__ void sun_transform(const SunCtx<TC> &c, In in, Out out) {
   __syncthreads();
 }
 
-// NTHR threads per CTA; MINB resident CTAs per SM the register budget allows
+// NTHR threads per CTA; MINB resident CTAs per SM the register budget allows.
+// An item of a run is R.sun_rows consecutive t' rows (several for the small
+// lattices of a batch, so that their per-item work -- finding the run, the L2
+// prefetch of the next row -- is spread over more rows), taken one after the other.
 template <typename TC, typename TS, bool SCRATCH, int NTHR, int MINB>
 __global__ void __launch_bounds__(NTHR, MINB)
 sunset_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int nruns, int total,
@@ -376,33 +405,28 @@ sunset_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   for (int w = blockIdx.x; w < total; w += gridDim.x) {
     const int r = run_at(base, nruns, w);
     const RunDev &R = runs[r];
-    const int tmin = max(1, t - R.M + 1);
-    const int tp = tmin + (w - R.cta_base_sun);
-    if (!pexp_sunset(R.pexp) || tp > t - 1 || t < 3) continue;
+    if (!pexp_sunset(R.pexp) || t < 3) continue;
     if (r != cur_run) {
-      // per-run tables: cosine matrix, pair list, pass offsets
+      // per-run tables: cosine matrix, pair list, pass offsets; then the orbit
+      // buffer and the pass regions
       __syncthreads();
       cur_run = r;
       SunGeom g(R.H);
-      TC *p = reinterpret_cast<TC *>(smem_raw);
-      TC *CT = p;
-      p += g.H4 * g.H4 + g.cf;
-      TC *bufF = p;
-      p += rup4(g.S);
+      const SunLayout L = sun_layout(sizeof(TC) == 8, g.H);
+      TC *CT = reinterpret_cast<TC *>(smem_raw + L.ct);
+      int *off2 = reinterpret_cast<int *>(smem_raw + L.off2);
+      int *off3 = reinterpret_cast<int *>(smem_raw + L.off3);
+      uint16_t *pr = reinterpret_cast<uint16_t *>(smem_raw + L.pr);
+      uint16_t *etab = sun_etab_fits(sizeof(TC) == 8, g.H) ? reinterpret_cast<uint16_t *>(smem_raw + L.etab) : nullptr;
+      TC *bufF = reinterpret_cast<TC *>(smem_raw + L.regions);
       TC *R1, *R2;
       if (SCRATCH) {
         R1 = scratch + (size_t)blockIdx.x * scratch_stride;
         R2 = R1 + g.r1;
       } else {
-        R1 = p;
-        p += g.r1;
-        R2 = p;
-        p += g.r2;
+        R1 = bufF + rup4(g.S);
+        R2 = R1 + g.r1;
       }
-      int *off2 = reinterpret_cast<int *>(p);
-      int *off3 = off2 + (g.H + 1);
-      uint16_t *pr = reinterpret_cast<uint16_t *>(off3 + (g.P4 / 4 + 1));
-      uint16_t *etab = sun_etab_fits(sizeof(TC) == 8, g.H) ? pr + rup4(g.P) : nullptr;
       for (int i = threadIdx.x; i < g.H4 * g.H4; i += blockDim.x) {
         const int x = i / g.H4, X = i - x * g.H4;
         CT[i] = (X < g.H && x < g.H) ? (TC)R.Cm[X * g.H + x] : (TC)0;
@@ -428,92 +452,116 @@ sunset_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
       __syncthreads();
       c = SunCtx<TC>{CT, pr, off2, off3, R1, R2, bufF, g, etab};
     }
+    const int tmin = max(1, t - R.M + 1);
     const int S = c.g.S;
-    const int slot = tp % R.Malloc;
     const size_t rowstride = (size_t)R.Malloc * KC;
     auto gidx = [&](int o) { return (size_t)(o / KC) * rowstride + (o % KC); };
-    // row (t-1, t') of a history ring (the storage-type copy of the state row;
-    // chunks are Malloc^2 KC apart) into shared memory, orbit layout
-    const size_t hbase = hist_off(R.Malloc, R.T, 0, t - 1, tp, 0);
     const size_t cstride = (size_t)R.Malloc * R.Malloc * KC;
-    auto stage = [&](const void *hist, TC *dst) {
-      const TS *h = reinterpret_cast<const TS *>(hist) + hbase;
-      constexpr int U = 4;
-      for (int o0 = threadIdx.x; o0 < S; o0 += U * blockDim.x) {
-        TS v[U];
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    const int nrow = SCRATCH ? 1 : R.sun_rows;
+    for (int gi = 0; gi < nrow; ++gi) {
+      const int tp = tmin + (w - R.cta_base_sun) * nrow + gi;
+      if (tp > t - 1) break;  // rows of an item are consecutive: the rest are past the window too
+      const int slot = tp % R.Malloc;
+      // row (t-1, t') of a history ring (the storage-type copy of the state row;
+      // chunks are Malloc^2 KC apart) into shared memory, orbit layout
+      const size_t hbase = hist_off(R.Malloc, R.T, 0, t - 1, tp, 0);
+      auto stage = [&](const void *hist, TC *dst) {
+        const TS *h = reinterpret_cast<const TS *>(hist) + hbase;
+        constexpr int U = 4;
+        for (int o0 = tid; o0 < S; o0 += U * nthr) {
+          TS v[U];
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-          const int o = o0 + u * blockDim.x;
-          v[u] = (o < S) ? h[(size_t)(o / KC) * cstride + (o % KC)] : (TS)0;
+          for (int u = 0; u < U; ++u) {
+            const int o = o0 + u * nthr;
+            v[u] = (o < S) ? h[(size_t)(o / KC) * cstride + (o % KC)] : (TS)0;
+          }
+#pragma unroll
+          for (int u = 0; u < U; ++u)
+            if (o0 + u * nthr < S) dst[o0 + u * nthr] = (TC)v[u];
         }
-#pragma unroll
-        for (int u = 0; u < U; ++u)
-          if (o0 + u * blockDim.x < S) dst[o0 + u * blockDim.x] = (TC)v[u];
+        __syncthreads();
+      };
+
+      // forward transforms of F(t-1,t') -> bufF and rho(t-1,t') -> R2 (orbit layout);
+      // each row is staged in the region the transform writes last, the rho row
+      // fetched into L2 meanwhile
+      for (int q = tid; q < R.nchunks; q += nthr)
+        prefetch_l2(reinterpret_cast<const TS *>(R.hist_r) + hbase + q * cstride);
+      stage(R.hist_F, c.bufF);
+      sun_transform<TC>(c, [&](int o) { return c.bufF[o]; }, [&](int o, TC v) { c.bufF[o] = v; });
+      stage(R.hist_r, c.R2);
+      sun_transform<TC>(c, [&](int o) { return c.R2[o]; }, [&](int o, TC v) { c.R2[o] = v; });
+
+      // pointwise sunset in position space (Evolution.jl:28-29, classical :114-115)
+      const bool classical = (R.pexp == 2);
+      for (int k = tid; k < S; k += nthr) {
+        const TC Fx = c.bufF[k], rx = c.R2[k];
+        const TC F2 = Fx * Fx, r2 = rx * rx;
+        c.R2[k] = classical ? rx * F2 : rx * (F2 - (TC)(1 / 12.) * r2);
+        c.bufF[k] = classical ? Fx * F2 : Fx * (F2 - (TC)0.75 * r2);
       }
       __syncthreads();
-    };
 
-    // forward transforms of F(t-1,t') -> bufF and rho(t-1,t') -> R2 (orbit layout);
-    // each row is staged in the region the transform writes last, the rho row
-    // fetched into L2 meanwhile
-    for (int q = threadIdx.x; q < R.nchunks; q += blockDim.x)
-      prefetch_l2(reinterpret_cast<const TS *>(R.hist_r) + hbase + q * cstride);
-    stage(R.hist_F, c.bufF);
-    sun_transform<TC>(c, [&](int o) { return c.bufF[o]; }, [&](int o, TC v) { c.bufF[o] = v; });
-    stage(R.hist_r, c.R2);
-    sun_transform<TC>(c, [&](int o) { return c.R2[o]; }, [&](int o, TC v) { c.R2[o] = v; });
-
-    // pointwise sunset in position space (Evolution.jl:28-29, classical :114-115)
-    const bool classical = (R.pexp == 2);
-    for (int k = threadIdx.x; k < S; k += blockDim.x) {
-      const TC Fx = c.bufF[k], rx = c.R2[k];
-      const TC F2 = Fx * Fx, r2 = rx * rx;
-      c.R2[k] = classical ? rx * F2 : rx * (F2 - (TC)(1 / 12.) * r2);
-      c.bufF[k] = classical ? Fx * F2 : Fx * (F2 - (TC)0.75 * r2);
-    }
-    __syncthreads();
-
-    // the rows of the next item of this CTA go to L2 while the inverse transforms run
-    {
-      const int w2 = w + gridDim.x;
-      if (w2 < total) {
-        const RunDev &R2n = runs[run_at(base, nruns, w2)];
-        const int tp2 = max(1, t - R2n.M + 1) + (w2 - R2n.cta_base_sun);
-        if (pexp_sunset(R2n.pexp) && tp2 <= t - 1) {
-          const size_t b2 = hist_off(R2n.Malloc, R2n.T, 0, t - 1, tp2, 0) * sizeof(TS);
-          const size_t cs2 = (size_t)R2n.Malloc * R2n.Malloc * KC * sizeof(TS);
-          for (int q = threadIdx.x; q < R2n.nchunks; q += blockDim.x) {
-            prefetch_l2(reinterpret_cast<const char *>(R2n.hist_F) + b2 + q * cs2);
-            prefetch_l2(reinterpret_cast<const char *>(R2n.hist_r) + b2 + q * cs2);
+      // the next row of this CTA goes to L2 while the inverse transforms run
+      {
+        int w2 = w, g2 = gi + 1;
+        if (g2 >= nrow) {
+          w2 = w + gridDim.x;
+          g2 = 0;
+        }
+        if (w2 < total) {
+          const RunDev &R2n = runs[run_at(base, nruns, w2)];
+          const int ng2 = SCRATCH ? 1 : R2n.sun_rows;
+          const int tp2 = max(1, t - R2n.M + 1) + (w2 - R2n.cta_base_sun) * ng2 + g2;
+          if (pexp_sunset(R2n.pexp) && tp2 <= t - 1) {
+            const size_t b2 = hist_off(R2n.Malloc, R2n.T, 0, t - 1, tp2, 0) * sizeof(TS);
+            const size_t cs2 = (size_t)R2n.Malloc * R2n.Malloc * KC * sizeof(TS);
+            for (int q = tid; q < R2n.nchunks; q += nthr) {
+              prefetch_l2(reinterpret_cast<const char *>(R2n.hist_F) + b2 + q * cs2);
+              prefetch_l2(reinterpret_cast<const char *>(R2n.hist_r) + b2 + q * cs2);
+            }
           }
         }
       }
-    }
 
-    // inverse transforms: pass 3 leaves the orbit values in R2 (free once pass 2
-    // has read B), then one coalesced sweep scales them into the Sigma rings
-    // (ivol^3 * coefficient); the next writer of R2 is behind a barrier
-    TS *sigr = reinterpret_cast<TS *>(R.sig_r) + (size_t)slot * KC;
-    TS *sigF = reinterpret_cast<TS *>(R.sig_F) + (size_t)slot * KC;
-    const TC fr = (TC)R.fac_r, fF = (TC)R.fac_F;
-    auto flush = [&](TS *sig, TC f) {
-      for (int o = threadIdx.x; o < S; o += blockDim.x) sig[gidx(o)] = (TS)(f * c.R2[o]);
-    };
-    const TC *gr = c.R2;
-    // expand reads R2 into R1 before pass 1 overwrites R2
-    sun_transform<TC>(c, [&](int o) { return gr[o]; }, [&](int o, TC v) { c.R2[o] = v; });
-    flush(sigr, fr);
-    const TC *gF = c.bufF;
-    sun_transform<TC>(c, [&](int o) { return gF[o]; }, [&](int o, TC v) { c.R2[o] = v; });
-    flush(sigF, fF);
+      // inverse transforms: pass 3 leaves the orbit values in R2 (free once pass 2
+      // has read B), then one coalesced sweep scales them into the Sigma rings
+      // (ivol^3 * coefficient); the next writer of R2 is behind a barrier
+      TS *sigr = reinterpret_cast<TS *>(R.sig_r) + (size_t)slot * KC;
+      TS *sigF = reinterpret_cast<TS *>(R.sig_F) + (size_t)slot * KC;
+      const TC fr = (TC)R.fac_r, fF = (TC)R.fac_F;
+      auto flush = [&](TS *sig, TC f) {
+        for (int o = tid; o < S; o += nthr) sig[gidx(o)] = (TS)(f * c.R2[o]);
+      };
+      const TC *gr = c.R2;
+      // expand reads R2 into R1 before pass 1 overwrites R2
+      sun_transform<TC>(c, [&](int o) { return gr[o]; }, [&](int o, TC v) { c.R2[o] = v; });
+      flush(sigr, fr);
+      const TC *gF = c.bufF;
+      sun_transform<TC>(c, [&](int o) { return gF[o]; }, [&](int o, TC v) { c.R2[o] = v; });
+      flush(sigF, fF);
+    }
   }
 }
 
 }  // namespace
 
-size_t sunset_smem_bytes(bool fp64, int H) {
+size_t sunset_smem_bytes(bool fp64, int H) { return sun_layout(fp64, H).bytes; }
+
+// t' rows per sunset item of a run (FP32): up to 8 for the small lattices whose rows
+// are short, as long as the work items of the largest pass of all the item's rows
+// together stay within 5/4 of one round of the 512-thread kernel (Ns <= 20: 8,
+// 24: 4, 32: 2, from 40 on: 1 -- longer rows would only coarsen the balance)
+int sunset_rows_per_item(int H) {
   SunGeom g(H);
-  return sun_smem_base(fp64, H) + (sun_etab_fits(fp64, H) ? (size_t)g.H * g.P4 * sizeof(uint16_t) : 0);
+  const int p1 = (g.ne4 / 4 + g.no4 / 4) * (g.P4 / 4);
+  int p2 = 0;
+  for (int X = 0; X < g.H; ++X) p2 += (g.H4 / 4 - X / 4) * (g.H4 / 4);
+  const int items = p1 > p2 ? p1 : p2;
+  for (int rows = 8; rows > 1; rows /= 2)
+    if (items * rows <= SUN_THREADS + SUN_THREADS / 4) return rows;
+  return 1;
 }
 
 size_t sunset_scratch_elems(int H) {

@@ -33,18 +33,55 @@ def evolve(cfg, precision, steps, tuning=None, autotune_at=None):
 
 @pytest.mark.parametrize("precision", [0, 1])
 def test_sunset_grids_are_bitwise_identical(precision):
+    """One CTA per sunset item (FP64: a t' row; FP32 at Ns = 12: eight rows) whatever
+    the grid, so every grid gives the same bits."""
     h = make_gpu(CFG, precision)
-    sms = h.tuning()["sunset_grid"]
+    items = h.tuning()["sunset_grid"]  # one CTA per item by default at this size
     h.close()
     a = evolve(CFG, precision, 60)
-    b = evolve(CFG, precision, 60, tuning={"sunset_grid": 2 * sms if sms < 38 else sms})
-    c = evolve(CFG, precision, 60, tuning={"sunset_grid": 7})
+    b = evolve(CFG, precision, 60, tuning={"sunset_grid": max(1, items // 2)})
+    c = evolve(CFG, precision, 60, tuning={"sunset_grid": 1})
     runs = [b, c]
     if precision == 1:  # the 512-thread FP32 sunset computes every element the same way
-        runs.append(evolve(CFG, precision, 60, tuning={"sunset_variant": 1, "sunset_grid": 9}))
+        runs.append(evolve(CFG, precision, 60, tuning={"sunset_variant": 1, "sunset_grid": max(1, items - 1)}))
     for x in runs:
         assert np.array_equal(x[0]["n"], a[0]["n"]) and x[0]["E"] == a[0]["E"]
         assert np.array_equal(x[1], a[1])
+
+
+def test_sunset_items_of_several_rows_are_bitwise_identical():
+    """FP32 runs of small lattices put several t' rows in one sunset item (Ns = 8,
+    10, 16: 8 rows, 24: 4), windows of 23..41 rows leave partial last items; with
+    every sunset variant and grid each run of the batch gives the bits of the same
+    run alone."""
+    from kb2pi import capi
+
+    cfgs = [dict(Ns=24, M=30, lam=2.0, T=1.0), dict(Ns=8, M=41, lam=4.0, T=2.0), dict(Ns=16, M=37, lam=1.0, T=0.7),
+            dict(Ns=10, M=23, lam=3.0, T=1.5)]
+
+    def params(c):
+        return capi.KbParams(Ns=c["Ns"], sdim=3, M=c["M"], N=4, pexp=1, precision=1, device=0, flags=0, dt=0.1,
+                             lam=c["lam"], mass2=1.0, mass=1.0)
+
+    out = []
+    for variant, grid in ((0, 0), (1, 0), (1, 5)):
+        h = capi.Handle([params(c) for c in cfgs])
+        for r, c in enumerate(cfgs):
+            _, k2, _ = h.orbits(r)
+            h.init(r, occupation(dict(c), k2), 1.0)
+        h.set_tuning(sunset_variant=variant, sunset_grid=grid)
+        h.steps(3, 50, 0)
+        out.append([h.measure(r, 52) for r in range(len(cfgs))])
+        h.close()
+    for r, c in enumerate(cfgs):  # each run alone
+        g = make_gpu(dict(c, dt=0.1), 1)
+        _, k2, _ = g.orbits()
+        g.init(0, occupation(dict(c), k2), 1.0)
+        g.steps(3, 50, 0)
+        m = g.measure(0, 52)
+        g.close()
+        for o in out:
+            assert o[r]["E"] == m["E"] and np.array_equal(o[r]["n"], m["n"]), r
 
 
 def test_memint_variants_agree():
