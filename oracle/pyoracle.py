@@ -1,6 +1,6 @@
 """ctypes binding of libkb_oracle.so (the CPU FP64 restatement in kb_oracle.cpp).
 
-Test infrastructure: the checker the CUDA path is compared against. Parity of
+Test infrastructure: the oracle the CUDA path is compared against. Parity of
 this oracle with the Julia reference itself is unpinned (no Julia here); see
 kb_oracle.h for what pins it.
 """

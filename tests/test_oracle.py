@@ -1,4 +1,4 @@
-"""The CPU FP64 oracle, pinned before it is trusted as the checker.
+"""The CPU FP64 oracle, pinned before the CUDA path is compared against it.
 
 The Julia reference cannot run here, so the oracle is pinned against
 independent implementations and known answers: numpy's pocketfft for the
