@@ -119,57 +119,92 @@ __global__ void adj_seed_kernel(RunDev R, int tf, AdjBuffers A, const double *wn
   }
 }
 
-// diagonal and off-diagonal leapfrog adjoints; one thread per orbit, sequential
-// over t' (the pair (t-1, t-2) receives updates from two values of t')
-__global__ void adj_step_kernel(RunDev R, int t, AdjBuffers A, double emem_weight) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= R.S) return;
-  const int c = k / KC, j = k % KC;
+// diagonal and off-diagonal leapfrog adjoints. One CTA per orbit chunk, a thread
+// per (orbit j, t') with j fastest (rows of the history and of the adjoint rings
+// are KC-contiguous per t'), t' in blocks of ADJ_TPB. Every thread first adds the
+// diagonal's terms into its element (t, t') of the adjoint of row t, then pushes
+// that element to rows t-1, t-2. The one element two t' reach, (t-1, t-2), is
+// updated by the thread of t' = t-2 alone, with the adjoint of (t, t-1) formed
+// the same way from the values read before any update. The omega adjoint of an
+// orbit is reduced over t' in a fixed order.
+constexpr int ADJ_TPB = 32;  // 256 threads = KC orbits x 32 t'
+__global__ void __launch_bounds__(KC * ADJ_TPB) adj_step_kernel(RunDev R, int t, AdjBuffers A, double emem_weight) {
+  __shared__ double red[ADJ_TPB][KC];
+  const int c = blockIdx.x;
+  const int j = (int)threadIdx.x % KC, l = (int)threadIdx.x / KC;
+  const int k = c * KC + j;
+  const bool kv = k < R.S;
   const int tmin = win_min(R, t);
   const int Ma = R.Malloc, T = R.T, Spad = R.nchunks * KC;
   const double dt3 = R.dt3;
-  const double om = (R.k2[k] + A.scal[0]) * R.dt2;
   double *aF = A.adjF, *aR = A.adjR;
   auto off = [&](int a, int b) { return hist_off(Ma, T, c, a, b, j); };
   const bool nlo = pexp_sunset(R.pexp);
   const double *sgr = reinterpret_cast<const double *>(R.sig_r) + (size_t)c * Ma * KC + j;
   const double *sgF = reinterpret_cast<const double *>(R.sig_F) + (size_t)c * Ma * KC + j;
+  double om = 0.0, Fbtt = 0.0, b1 = 0.0;
+  if (kv) {
+    om = (R.k2[k] + A.scal[0]) * R.dt2;
+    Fbtt = aF[off(t, t)];
+    b1 = aF[off(t, t - 1)];  // before any thread of this orbit adds to it
+  }
+  __syncthreads();
   // diagonal F(t,t) = (2 - om) F(t,t-1) - F(t,t-2) - dt^3 sum_z [x_rho(z) F(t,z) + x_F(z) rho(t,z)]
-  const double Fbtt = aF[off(t, t)];
   const double accd = -dt3 * Fbtt;
-  aF[off(t, t - 1)] += (2.0 - om) * Fbtt;
-  aF[off(t, t - 2)] -= Fbtt;
-  double omb = -hF(R, c, t, t - 1, j) * Fbtt;
-  if (nlo)
-    for (int z = tmin; z <= t - 1; ++z) {
-      const double w = (z == tmin) ? 0.5 : 1.0;
-      const size_t zo = (size_t)(z % Ma) * Spad + k;
-      aF[off(t, z)] += w * sgr[(size_t)(z % Ma) * KC] * accd;
-      aR[off(t, z)] += w * sgF[(size_t)(z % Ma) * KC] * accd;  // rho(t, t-1) = dt: a constant, never read
-      A.xbr[zo] = hF(R, c, t, z, j) * accd;
-      A.xbF[zo] = hR(R, c, t, z, j) * accd;
+  // the adjoint of (t, t-1) once the diagonal has added to it
+  double Fb1 = b1 + (2.0 - om) * Fbtt;
+  if (nlo) Fb1 += ((t - 1 == tmin) ? 0.5 : 1.0) * sgr[(size_t)((t - 1) % Ma) * KC] * accd;
+  double ob_sum = 0.0;
+  for (int tp0 = tmin; tp0 <= t - 1; tp0 += ADJ_TPB) {
+    const int tp = tp0 + l;
+    if (!kv || tp > t - 1) continue;
+    double Fb;
+    if (tp == t - 1) {
+      Fb = Fb1;
+    } else {
+      double v = aF[off(t, tp)];
+      if (tp == t - 2) v -= Fbtt;
+      if (nlo) v += ((tp == tmin) ? 0.5 : 1.0) * sgr[(size_t)(tp % Ma) * KC] * accd;
+      Fb = v;
     }
-  // off-diagonal t' in [tmin, t-1]
-  for (int tp = tmin; tp <= t - 1; ++tp) {
-    const double Fb = aF[off(t, tp)];
+    if (nlo) {
+      const double w = (tp == tmin) ? 0.5 : 1.0;
+      const size_t zo = (size_t)(tp % Ma) * Spad + k;
+      aR[off(t, tp)] += w * sgF[(size_t)(tp % Ma) * KC] * accd;  // rho(t, t-1) = dt: a constant, never read
+      A.xbr[zo] = hF(R, c, t, tp, j) * accd;
+      A.xbF[zo] = hR(R, c, t, tp, j) * accd;
+    }
+    aF[off(t, tp)] = Fb;
+    // off-diagonal t' = tp
     const double Rb = (tp <= t - 2) ? aR[off(t, tp)] : 0.0;  // rho(t, t-1) = dt is not evolved
     double accbF = -dt3 * Fb;
     if (tp == t - 1) accbF += emem_weight * 0.25 * R.dt * R.deg[k];  // E_mem = dt/4 sum_k deg acc_F(t-1)
     const size_t to = (size_t)(tp % Ma) * Spad + k;
     A.accF[to] = accbF;
     A.accR[to] = -dt3 * Rb;
-    aF[off(t - 1, tp)] += (2.0 - om) * Fb;
-    if (tp <= t - 2) aF[off(t - 2, tp)] -= Fb;
-    else aF[off(t - 1, t - 2)] -= Fb;  // F(t-2, t-1) is the stored F(t-1, t-2)
+    if (tp <= t - 2) {
+      double v = aF[off(t - 1, tp)] + (2.0 - om) * Fb;
+      if (tp == t - 2) v -= Fb1;  // F(t-2, t-1) is the stored F(t-1, t-2)
+      aF[off(t - 1, tp)] = v;
+      aF[off(t - 2, tp)] -= Fb;
+    } else {
+      aF[off(t - 1, tp)] += (2.0 - om) * Fb;
+    }
     double ob = hF(R, c, t - 1, tp, j) * Fb;
     if (tp <= t - 2) {
       aR[off(t - 1, tp)] += (2.0 - om) * Rb;
       if (tp <= t - 3) aR[off(t - 2, tp)] -= Rb;  // rho(t-2, t-2) = 0
       ob += hR(R, c, t - 1, tp, j) * Rb;
     }
-    omb -= ob;
+    ob_sum += ob;
   }
-  A.omb[k] = omb;
+  red[l][j] = ob_sum;
+  __syncthreads();
+  if (l == 0 && kv) {
+    double omb = -hF(R, c, t, t - 1, j) * Fbtt;
+    for (int q = 0; q < ADJ_TPB; ++q) omb -= red[q][j];
+    A.omb[k] = omb;
+  }
 }
 
 // omega^2 dt^2 = (k^2 + M^2) dt^2 with M^2 = m^2 + pref ivol sum_k deg_k F(t-1,t-1); one block
@@ -329,7 +364,7 @@ cudaError_t launch_adjoint_step(const RunDev &R, const AdjBuffers &A, int t, dou
                       sl.smem, st);
     if (e != cudaSuccess) return e;
   }
-  adj_step_kernel<<<grid_for(R.S, 64, cap), 64, 0, st>>>(R, t, A, emem_weight);
+  adj_step_kernel<<<R.nchunks, KC * ADJ_TPB, 0, st>>>(R, t, A, emem_weight);
   adj_tadpole_kernel<<<1, 256, 0, st>>>(R, t, A, dpref_ivol);
   if (nlo) {
     adj_memint_reduce_kernel<<<grid_for((long long)n * Spad, 128, cap), 128, 0, st>>>(R, t, A);
