@@ -351,7 +351,8 @@ cudaError_t launch_adjoint_seed(const RunDev &R, const AdjBuffers &A, int t_fina
 }
 
 cudaError_t launch_adjoint_step(const RunDev &R, const AdjBuffers &A, int t, double emem_weight, double lambda,
-                                double dpref_ivol, const SunsetLaunch &sl, int num_sms, cudaStream_t st) {
+                                double dpref_ivol, const SunsetLaunch &sl, int num_sms, bool sigma_ready,
+                                cudaStream_t st) {
   const int tmin = std::max(1, t - R.M + 1), n = t - tmin, Spad = R.nchunks * KC;
   const int cap = 64 * std::max(1, num_sms);
   cudaError_t e = launch_set_t(sl.d_t, t, st);
@@ -359,7 +360,7 @@ cudaError_t launch_adjoint_step(const RunDev &R, const AdjBuffers &A, int t, dou
   adj_refill_kernel<<<grid_for((long long)n * Spad, 256, cap), 256, 0, st>>>(R, t);
   adj_scalars_kernel<<<1, 256, 0, st>>>(R, t, A);
   const bool nlo = pexp_sunset(R.pexp);
-  if (nlo) {
+  if (nlo && !sigma_ready) {
     e = launch_sunset(true, 0, sl.runs, sl.base, sl.nruns, sl.total_rows, sl.grid, sl.d_t, sl.scratch, sl.stride,
                       sl.smem, st);
     if (e != cudaSuccess) return e;

@@ -1441,22 +1441,35 @@ int kb_adjoint(kb_handle *h, const double *n_init, double init_mass, int32_t t_f
   size_t snap_bytes = 0;
   for (auto &q : parts) snap_bytes += (q.n + 255) / 256 * 256;
   const size_t adj_bytes = kb::adjoint_buffer_bytes(D);
-  char *snaps = nullptr, *adj = nullptr;
+  // Sigma(t-1, .) of the steps of one block, kept when the forward step computes
+  // them (both rings, FP64), so that the reverse steps need not run the sunset again
+  const bool nlo = kb::pexp_sunset(R.p.pexp);
+  const size_t sig_bytes = R.sig_elems * R.esz;
+  char *snaps = nullptr, *adj = nullptr, *sigs = nullptr;
   double *d_vec = nullptr;  // w_n [Spad], n_init [Spad], output [2][S]
   auto release = [&]() {
     cudaStreamSynchronize(h->st);
     if (snaps) cudaFree(snaps);
     if (adj) cudaFree(adj);
+    if (sigs) cudaFree(sigs);
     if (d_vec) cudaFree(d_vec);
     cudaGetLastError();
   };
   if (cudaMalloc((void **)&snaps, snap_bytes * nsnap) != cudaSuccess ||
       cudaMalloc((void **)&adj, adj_bytes) != cudaSuccess ||
+      (nlo && cudaMalloc((void **)&sigs, 2 * sig_bytes * k) != cudaSuccess) ||
       cudaMalloc((void **)&d_vec, (size_t)(2 * R.Spad + 2 * R.S) * 8) != cudaSuccess) {
     release();
-    return fail(h, KB_ERR_OOM, "kb_adjoint: cudaMalloc of %zu + %zu bytes (state copies + adjoint) failed",
-                snap_bytes * nsnap, adj_bytes);
+    return fail(h, KB_ERR_OOM, "kb_adjoint: cudaMalloc of %zu + %zu + %zu bytes (state copies, adjoint, Sigma) failed",
+                snap_bytes * nsnap, adj_bytes, nlo ? 2 * sig_bytes * k : (size_t)0);
   }
+  auto copy_sigma = [&](int slot, bool save) -> int {  // slot: the step's place in its block
+    char *s = sigs + (size_t)slot * 2 * sig_bytes;
+    KB_CUDA(h, cudaMemcpyAsync(save ? s : R.sig_F, save ? R.sig_F : s, sig_bytes, cudaMemcpyDeviceToDevice, h->st));
+    KB_CUDA(h, cudaMemcpyAsync(save ? s + sig_bytes : R.sig_r, save ? R.sig_r : s + sig_bytes, sig_bytes,
+                               cudaMemcpyDeviceToDevice, h->st));
+    return KB_OK;
+  };
   auto copy_state = [&](int i, bool save) -> int {
     size_t off = 0;
     for (auto &q : parts) {
@@ -1477,9 +1490,11 @@ int kb_adjoint(kb_handle *h, const double *n_init, double init_mass, int32_t t_f
     int r = kb_init(h, 0, n_init, init_mass);
     if (r) return r;
     if ((r = copy_state(0, true))) return r;
+    const int s0_last = 2 + (nsnap - 1) * k;  // the last block is reversed from this forward pass
     for (int t = 3; t <= t_final; ++t) {
       if ((r = kb_step(h, t))) return r;
       if ((t - 2) % k == 0 && t < t_final && (r = copy_state((t - 2) / k, true))) return r;
+      if (nlo && t > s0_last && (r = copy_sigma(t - s0_last - 1, true))) return r;
     }
     if (loss) {  // L at t_final from the forward measurement
       kb_meas_scalars ms{};
@@ -1500,12 +1515,16 @@ int kb_adjoint(kb_handle *h, const double *n_init, double init_mass, int32_t t_f
       if (i != nsnap - 1) {  // recompute the block from its copy
         if ((r = copy_state(i, false))) return r;
         h->t_cur = s0;
-        for (int t = s0 + 1; t <= e; ++t)
+        for (int t = s0 + 1; t <= e; ++t) {
           if ((r = kb_step(h, t))) return r;
+          if (nlo && (r = copy_sigma(t - s0 - 1, true))) return r;
+        }
       }
-      for (int t = e; t > s0; --t)
+      for (int t = e; t > s0; --t) {
+        if (nlo && (r = copy_sigma(t - s0 - 1, false))) return r;
         KB_CUDA(h, kb::launch_adjoint_step(D, A, t, t == t_final ? w_E : 0.0, R.p.lambda, dpref_ivol, sl,
-                                           h->num_sms, h->st));
+                                           h->num_sms, nlo, h->st));
+      }
     }
     KB_CUDA(h, kb::launch_adjoint_init_grad(D, A, d_n0, init_mass, d_out, h->st));
     double scal[8];

@@ -156,8 +156,11 @@ size_t adjoint_buffer_bytes(const RunDev &R);
 void adjoint_carve(const RunDev &R, void *base, AdjBuffers *A);
 cudaError_t launch_adjoint_seed(const RunDev &R, const AdjBuffers &A, int t_final, const double *d_wn, double w_E,
                                 double dpref_ivol, cudaStream_t st);
+// sigma_ready: Sigma(t-1, .) is already in the rings (restored from the forward
+// step t), so the forward sunset is not run again
 cudaError_t launch_adjoint_step(const RunDev &R, const AdjBuffers &A, int t, double emem_weight, double lambda,
-                                double dpref_ivol, const SunsetLaunch &sl, int num_sms, cudaStream_t st);
+                                double dpref_ivol, const SunsetLaunch &sl, int num_sms, bool sigma_ready,
+                                cudaStream_t st);
 cudaError_t launch_adjoint_init_grad(const RunDev &R, const AdjBuffers &A, const double *d_n0, double init_mass,
                                      double *d_out, cudaStream_t st);
 // message returned by kb_last_error(NULL) (kb_api.cu)
