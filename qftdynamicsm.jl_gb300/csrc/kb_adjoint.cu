@@ -249,29 +249,28 @@ __global__ void adj_memint_reduce_kernel(RunDev R, int t, AdjBuffers A) {
   }
 }
 
-// adjoints of the history pairs (a >= b) of the window; thread per (pair, orbit)
+// adjoints of the history pairs (a >= b) of the window: one CTA per (orbit chunk,
+// row a), a thread per (column of a time tile, orbit) with the orbit fastest, so a
+// tile's row segment (T columns x KC orbits) is one contiguous access; the CTA
+// walks the tiles of the columns b <= a
 __global__ void adj_memint_update_kernel(RunDev R, int t, AdjBuffers A) {
   const int tmin = win_min(R, t);
-  const int n = t - tmin, Spad = R.nchunks * KC, Ma = R.Malloc, T = R.T;
-  const long long npairs = (long long)n * (n + 1) / 2;
+  const int Spad = R.nchunks * KC, Ma = R.Malloc, T = R.T;
+  const int c = (int)blockIdx.x % R.nchunks, a = tmin + (int)blockIdx.x / R.nchunks;
+  const int j = (int)threadIdx.x % KC, bl = (int)threadIdx.x / KC;
+  const int k = c * KC + j;
+  if (a > t - 1 || k >= R.S) return;
   const double *sg_r = reinterpret_cast<const double *>(R.sig_r);
   const double *sg_F = reinterpret_cast<const double *>(R.sig_F);
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < npairs * Spad;
-       i += (long long)gridDim.x * blockDim.x) {
-    const long long p = i / Spad;
-    const int k = (int)(i % Spad);
-    if (k >= R.S) continue;
-    int ua = (int)((sqrt(8.0 * (double)p + 1.0) - 1.0) * 0.5);  // p = ua (ua + 1) / 2 + ub
-    while ((long long)ua * (ua + 1) / 2 > p) --ua;
-    while ((long long)(ua + 1) * (ua + 2) / 2 <= p) ++ua;
-    const int ub = (int)(p - (long long)ua * (ua + 1) / 2);
-    const int a = tmin + ua, b = tmin + ub;
-    const int c = k / KC, j = k % KC;
-    const size_t cb = (size_t)c * Ma * KC + j;
-    const double xra = ((a == tmin) ? 0.5 : 1.0) * sg_r[cb + (size_t)(a % Ma) * KC];
+  const size_t cb = (size_t)c * Ma * KC + j;
+  const double xra = ((a == tmin) ? 0.5 : 1.0) * sg_r[cb + (size_t)(a % Ma) * KC];
+  const double aFa = A.accF[(size_t)(a % Ma) * Spad + k];
+  for (int b0 = (tmin / T) * T; b0 <= a; b0 += T) {
+    const int b = b0 + bl;
+    if (b < tmin || b > a) continue;
     const double xrb = ((b == tmin) ? 0.5 : 1.0) * sg_r[cb + (size_t)(b % Ma) * KC];
     const double xFb = ((b == tmin) ? 0.5 : 1.0) * sg_F[cb + (size_t)(b % Ma) * KC];
-    const double aFa = A.accF[(size_t)(a % Ma) * Spad + k], aFb = A.accF[(size_t)(b % Ma) * Spad + k];
+    const double aFb = A.accF[(size_t)(b % Ma) * Spad + k];
     const double aRb = A.accR[(size_t)(b % Ma) * Spad + k];
     const size_t o = hist_off(Ma, T, c, a, b, j);
     if (a > b) {
@@ -369,7 +368,7 @@ cudaError_t launch_adjoint_step(const RunDev &R, const AdjBuffers &A, int t, dou
   adj_tadpole_kernel<<<1, 256, 0, st>>>(R, t, A, dpref_ivol);
   if (nlo) {
     adj_memint_reduce_kernel<<<grid_for((long long)n * Spad, 128, cap), 128, 0, st>>>(R, t, A);
-    adj_memint_update_kernel<<<grid_for((long long)n * (n + 1) / 2 * Spad, 256, cap), 256, 0, st>>>(R, t, A);
+    adj_memint_update_kernel<<<n * R.nchunks, R.T * KC, 0, st>>>(R, t, A);
     e = launch_sunset_adjoint(R, t, A.xbr, A.xbF, A.adjF, A.adjR, A.lamp, sl.scratch, sl.stride,
                               std::max(1, std::min(sl.grid, n)), lambda, st);
     if (e != cudaSuccess) return e;
