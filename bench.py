@@ -286,9 +286,9 @@ def cpu_baseline(steps=1, Msample=128, budget_s=None):
     o.close()
     sec = statistics.median(ts)
     return {"value": 1.0 / sec, "unit": "steps/s", "cores": threads, "kind": "port",
-            "sample": f"oracle CPUred port (full-lattice FFT sunset), Ns=64, window {Msample} filled by "
+            "sample": f"oracle CPUred port (full-lattice FFT sunset), Ns={CFG['Ns']}, window {Msample} filled by "
                       f"expand, {len(ts)} step(s); sunset time x (M-1)/({Msample}-1), memory integrals x "
-                      f"(M/{Msample})^2 to M=1000"}
+                      f"(M/{Msample})^2 to M={CFG['M']}"}
 
 
 def run_batched(args):
