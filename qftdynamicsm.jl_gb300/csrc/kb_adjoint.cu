@@ -221,31 +221,48 @@ __global__ void adj_tadpole_kernel(RunDev R, int t, AdjBuffers A, double dpref_i
     A.adjF[hist_off(R.Malloc, R.T, k / KC, t - 1, t - 1, k % KC)] += Mb2 * R.pref_ivol * R.deg[k];
 }
 
-// adjoints of x_rho(z), x_F(z), turned into those of Sigma(t-1, z) = x / w(z);
-// thread per (z, orbit)
+// adjoints of x_rho(z), x_F(z), turned into those of Sigma(t-1, z) = x / w(z):
+// one CTA per (orbit chunk, z), a thread per (time in a tile, orbit) with the
+// orbit fastest; row z is read along its tile rows (b <= z), column z down the
+// rows a > z; each orbit's partial sums are added over the CTA in a fixed order
+constexpr int ADJ_RED_MAX_T = 32;
 __global__ void adj_memint_reduce_kernel(RunDev R, int t, AdjBuffers A) {
+  __shared__ double red[2][ADJ_RED_MAX_T][KC];
   const int tmin = win_min(R, t);
-  const int n = t - tmin, Spad = R.nchunks * KC, Ma = R.Malloc;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < (long long)n * Spad;
-       i += (long long)gridDim.x * blockDim.x) {
-    const int z = tmin + (int)(i / Spad), k = (int)(i % Spad);
-    if (k >= R.S) continue;
-    const int c = k / KC, j = k % KC;
-    double sr = 0.0, sF = 0.0;
-    for (int b = tmin; b <= z; ++b) {  // acc_F(b) <- x_rho(z) F(z, b); acc_rho(b) <- x_rho(z) rho(z, b), b < z
+  const int Spad = R.nchunks * KC, Ma = R.Malloc, T = R.T;
+  const int c = (int)blockIdx.x % R.nchunks, z = tmin + (int)blockIdx.x / R.nchunks;
+  const int j = (int)threadIdx.x % KC, bl = (int)threadIdx.x / KC;
+  const int k = c * KC + j;
+  double sr = 0.0, sF = 0.0;
+  if (k < R.S) {
+    for (int b0 = (tmin / T) * T; b0 <= z; b0 += T) {  // acc_F(b) <- x_rho(z) F(z, b); acc_rho(b) <- x_rho(z) rho(z, b), b < z
+      const int b = b0 + bl;
+      if (b < tmin || b > z) continue;
       const size_t bo = (size_t)(b % Ma) * Spad + k;
       sr += hF(R, c, z, b, j) * A.accF[bo];
       if (b < z) sr += hR(R, c, z, b, j) * A.accR[bo];
     }
-    for (int a = z + 1; a <= t - 1; ++a) {  // acc_F(a) <- x_rho(z) F(a, z) + x_F(z) rho(a, z)
+    for (int a0 = ((z + 1) / T) * T; a0 <= t - 1; a0 += T) {  // acc_F(a) <- x_rho(z) F(a, z) + x_F(z) rho(a, z)
+      const int a = a0 + bl;
+      if (a <= z || a > t - 1) continue;
       const size_t ao = (size_t)(a % Ma) * Spad + k;
       sr += hF(R, c, a, z, j) * A.accF[ao];
       sF += hR(R, c, a, z, j) * A.accF[ao];
     }
+  }
+  red[0][bl][j] = sr;
+  red[1][bl][j] = sF;
+  __syncthreads();
+  if (bl == 0 && k < R.S) {
+    double tr = 0.0, tF = 0.0;
+    for (int q = 0; q < T; ++q) {
+      tr += red[0][q][j];
+      tF += red[1][q][j];
+    }
     const size_t zo = (size_t)(z % Ma) * Spad + k;
     const double w = (z == tmin) ? 0.5 : 1.0;
-    A.xbr[zo] = w * (A.xbr[zo] + sr);
-    A.xbF[zo] = w * (A.xbF[zo] + sF);
+    A.xbr[zo] = w * (A.xbr[zo] + tr);
+    A.xbF[zo] = w * (A.xbF[zo] + tF);
   }
 }
 
@@ -367,7 +384,7 @@ cudaError_t launch_adjoint_step(const RunDev &R, const AdjBuffers &A, int t, dou
   adj_step_kernel<<<R.nchunks, KC * ADJ_TPB, 0, st>>>(R, t, A, emem_weight);
   adj_tadpole_kernel<<<1, 256, 0, st>>>(R, t, A, dpref_ivol);
   if (nlo) {
-    adj_memint_reduce_kernel<<<grid_for((long long)n * Spad, 128, cap), 128, 0, st>>>(R, t, A);
+    adj_memint_reduce_kernel<<<n * R.nchunks, R.T * KC, 0, st>>>(R, t, A);
     adj_memint_update_kernel<<<n * R.nchunks, R.T * KC, 0, st>>>(R, t, A);
     e = launch_sunset_adjoint(R, t, A.xbr, A.xbF, A.adjF, A.adjR, A.lamp, sl.scratch, sl.stride,
                               std::max(1, std::min(sl.grid, n)), lambda, st);
