@@ -21,6 +21,29 @@ def test_header_declares_the_binding_list():
     assert sorted(capi.EXPORTS) == declared_symbols()
 
 
+def test_julia_glue_calls_declared_symbols_only():
+    """julia/TwoPIScalar_GPU.jl (not executed here: no Julia) and the bindings shown in
+    INTEGRATION.md name only functions the header declares, with as many arguments in
+    each Julia ccall as the C declaration has parameters."""
+    declared = set(declared_symbols())
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    arity = {}
+    for name, params in re.findall(r"\b(kb_[a-z_0-9]+)\s*\(([^)]*)\)\s*;", src):
+        params = params.strip()
+        arity[name] = 0 if params in ("", "void") else params.count(",") + 1
+    jl = open(os.path.join(ROOT, "qftdynamicsm.jl_gb300", "julia", "TwoPIScalar_GPU.jl")).read()
+    calls = re.findall(r"ccall\(\(:(kb_[a-z_0-9]+)\s*,[^)]*\)\s*,\s*[A-Za-z_{}0-9]+\s*,\s*\(([^)]*)\)", jl)
+    assert calls
+    for name, types in calls:
+        assert name in declared, name
+        n = len([x for x in types.split(",") if x.strip()])
+        assert n == arity[name], (name, n, arity[name])
+    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    for name in set(re.findall(r"\b(kb_[a-z_0-9]+)\(", doc)):
+        assert name in declared, name
+
+
 def test_library_exports_all_symbols():
     from kb2pi import capi
 
