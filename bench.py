@@ -12,10 +12,12 @@ Reported: steps/s of the mixed-precision path (value), the plain FP64 path
 on the same workload, their relative difference in n(p,t) and E, the
 roofline of the dominant kernel (memory integral), an end-to-end number
 through the C ABI with host buffers, GPU clocks during the timed region and
-the CPU baseline (the oracle's CPUred-style port, bounded sample).
+the CPU baseline (the oracle's CPUred port: one warm-up and three timed real
+steps at the full window).
 
---impl reference times the reference's CPU algorithm (the oracle port; the
-Julia reference cannot run here) on the host cores.
+--impl reference times the reference's CPU algorithm (the oracle's CPUred
+port; the Julia reference cannot run here) on all host cores: W warm-up and
+K timed real steps at the full memory window of the same workload.
 """
 from __future__ import annotations
 
@@ -46,6 +48,18 @@ METRIC = "KB steps/s at Ns=64 (M=1000 window, mixed precision; plain FP64 GPU al
 def workload_name():
     return (f"KB step at full memory window: Ns={CFG['Ns']}, N={CFG['N']}, lambda={CFG['lam']:g}, "
             f"m={CFG['mass']:g}, dt={CFG['dt']:g}, M={CFG['M']}, tsunami initial state")
+
+
+def num_orbits(Ns):
+    """Cubic orbits of an Ns^3 lattice: C(Ns/2 + 3, 3)."""
+    return math.comb(Ns // 2 + 3, 3)
+
+
+def bench_config(ws):
+    """The workload as both arms name it (identical dicts; precision is in dtype)."""
+    return {"workload": workload_name() + ", LambdaNLO", "orbits": num_orbits(CFG["Ns"]),
+            "l2": "no flush: the two-time history (GBs) is >> 129 MB L2",
+            "parallelism": "replicas" if ws > 1 else "single"}
 
 
 def tsunami_n(k2):
@@ -256,39 +270,79 @@ def algorithmic_bytes(M, S, b_hist, b_sig):
 
 
 # ---------------------------------------------------------------------------
-def cpu_baseline(steps=1, Msample=128, budget_s=None):
-    """The oracle's CPUred-style port on all host cores, bounded sample: Ns=64 lattice
-    with a window of Msample steps filled by expandSimData! alone (as the reference
-    benchmark does, TwoPIScalar_Bechmark.jl:64-69); the timed step's self-energy time
-    is scaled by the number of t' rows (M-1)/(Msample-1), the rest of evolve! by
-    M^2/Msample^2."""
+def host_mem_available():
+    """MemAvailable of the host in bytes (None where /proc/meminfo is absent)."""
+    try:
+        with open("/proc/meminfo") as f:
+            for line in f:
+                if line.startswith("MemAvailable:"):
+                    return int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    return None
+
+
+def cpu_window():
+    """Memory window of the CPU runs: the workload's M when its FP64 orbit history
+    (2 x M(M+1)/2 x S doubles, the reference's CPUred storage) fits in 80 % of the
+    host's available memory, else the largest M that does."""
+    M, S = CFG["M"], num_orbits(CFG["Ns"])
+    avail = host_mem_available()
+    if avail is None:
+        return M
+    while M > 8 and 2 * (M * (M + 1) // 2) * S * 8 > 0.8 * avail:
+        M -= 8
+    return M
+
+
+def cpu_baseline(steps, warmup, budget_s=None, window=None):
+    """The oracle's CPUred port (ENGINE_ORBIT: orbit history, full-lattice rfft/brfft
+    sunset, memory integrals that read each history slot twice) on all host cores,
+    timed over real KB steps at a full memory window. The window is filled by
+    expandSimData! alone, as the reference benchmark does (TwoPIScalar_Bechmark.jl:62-104),
+    then `warmup` untimed and up to `steps` timed evolve! steps run; the timed loop
+    stops early (after at least min(steps, 3) steps) once budget_s seconds are spent.
+    Returns the cpu_baseline object; 'steps_timed' is the number of steps timed."""
     from oracle import ENGINE_ORBIT, Oracle
 
     threads = os.cpu_count() or 1
-    o = Oracle(CFG["Ns"], 3, M=Msample, N=CFG["N"], dt=CFG["dt"], lam=CFG["lam"], mass2=CFG["mass2"],
+    M = window or cpu_window()
+    o = Oracle(CFG["Ns"], 3, M=M, N=CFG["N"], dt=CFG["dt"], lam=CFG["lam"], mass2=CFG["mass2"],
                mass=CFG["mass"], engine=ENGINE_ORBIT, nthreads=threads)
-    _, k2, deg = o.orbits()
-    n = tsunami_n(k2)
-    o.init_occupation(n, 1.0)
-    for _ in range(3, Msample + 1):
-        o.expand()
-    t = Msample
-    ts = []
-    t_start = time.perf_counter()
-    for _ in range(steps):
-        if ts and budget_s is not None and time.perf_counter() - t_start > budget_s:
-            break
-        t += 1
-        o.step(t)
-        s_sun, s_rest = o.step_times()
-        M = CFG["M"]
-        ts.append(s_sun * (M - 1) / (Msample - 1) + s_rest * (M * M) / (Msample * Msample))
-    o.close()
-    sec = statistics.median(ts)
-    return {"value": 1.0 / sec, "unit": "steps/s", "cores": threads, "kind": "port",
-            "sample": f"oracle CPUred port (full-lattice FFT sunset), Ns={CFG['Ns']}, window {Msample} filled by "
-                      f"expand, {len(ts)} step(s); sunset time x (M-1)/({Msample}-1), memory integrals x "
-                      f"(M/{Msample})^2 to M={CFG['M']}"}
+    try:
+        _, k2, deg = o.orbits()
+        o.init_occupation(tsunami_n(k2), 1.0)
+        for _ in range(3, M + 1):
+            o.expand()
+        t = M
+        for _ in range(warmup):
+            t += 1
+            o.step(t)
+        ts, sun, rest = [], [], []
+        t_start = time.perf_counter()
+        kmin = min(steps, 3)
+        for _ in range(steps):
+            if len(ts) >= kmin and budget_s is not None and time.perf_counter() - t_start > budget_s:
+                break
+            t += 1
+            a = time.perf_counter()
+            o.step(t)
+            ts.append(time.perf_counter() - a)
+            s_sun, s_rest = o.step_times()
+            sun.append(s_sun)
+            rest.append(s_rest)
+    finally:
+        o.close()
+    total = sum(ts)
+    return {"value": len(ts) / total, "unit": "steps/s", "cores": threads, "kind": "port",
+            "steps_timed": len(ts), "s_per_step": total / len(ts),
+            "s_sunset_per_step": sum(sun) / len(ts), "s_rest_per_step": sum(rest) / len(ts),
+            "sample": f"oracle CPUred port (orbit history, full-lattice rfft/brfft sunset, memory integrals "
+                      f"reading each slot twice), Ns={CFG['Ns']}, M={M} window filled by expand, {warmup} "
+                      f"warm-up + {len(ts)} timed full-window steps, {threads} threads"
+                      + ("" if M == CFG["M"] else
+                         f"; window M={M} instead of the workload's M={CFG['M']} "
+                         + ("(command line)" if window else "(to fit host memory)"))}
 
 
 def run_batched(args):
@@ -472,17 +526,19 @@ def run_ninverse(args):
     return 0
 
 def run_reference(args):
+    """The reference's algorithm on the host cores: the oracle's CPUred port at the
+    benchmark workload, W warm-up and K timed real steps at a full window (fewer timed
+    steps, at least three, if they would run past about four minutes)."""
     ws, rank, _ = dist_setup()
     if rank != 0:
         return 0
-    # K sample steps, at most ~90 s of CPU time in total (at least one step)
-    cb = cpu_baseline(steps=max(1, args.steps), Msample=args.cpu_window, budget_s=90.0)
+    cb = cpu_baseline(steps=max(1, args.steps), warmup=args.warmup, budget_s=240.0, window=args.cpu_window)
+    k = cb["steps_timed"]
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "steps/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / cb["value"],
+            "steps": k, "warmup": args.warmup, "ms_per_step": 1000.0 / cb["value"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (tsunami initial state)",
-            "config": {"workload": workload_name(),
-                       "l2": "history >> L2"},
+            "data": "synthetic: tsunami initial state n(p)=5exp(-(|p|-1)^2/0.08), window filled by expand",
+            "config": bench_config(args.gpus),
             "cpu_baseline": cb,
             "e2e": {"value": cb["value"], "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -608,10 +664,8 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 history/sunset, f64 accumulation/leapfrog/diagnostics",
         "data": "synthetic: tsunami initial state n(p)=5exp(-(|p|-1)^2/0.08), window filled by real evolution",
-        "config": {"workload": workload_name() + ", LambdaNLO, mixed precision",
-                   "orbits": S, "history_GB": 2 * ((S + 7) // 8) * 8 * ((M + 31) // 32 * 32) ** 2 * 4 / 1e9,
-                   "l2": "no flush: the 55 GB history is >> 129 MB L2",
-                   "parallelism": "replicas" if ws > 1 else "single"},
+        "config": bench_config(ws),
+        "history_GB": 2 * ((S + 7) // 8) * 8 * ((M + 31) // 32 * 32) ** 2 * 4 / 1e9,
         "mode_steps_per_s": value * M * CFG["Ns"] ** 3,
         "graph_ms_per_step": gms / args.steps,
         "kernels_ms": {"memint": mi_ms, "sunset": sun_ms},
@@ -637,7 +691,7 @@ def run_ours(args):
     }
     if ws == 1 and not args.no_cpu:
         try:
-            line["cpu_baseline"] = cpu_baseline(steps=1, Msample=args.cpu_window)
+            line["cpu_baseline"] = cpu_baseline(steps=3, warmup=1, budget_s=30.0, window=args.cpu_window)
         except Exception as e:  # the baseline is reported, not required
             line["cpu_baseline"] = {"value": None, "error": str(e)}
     print(json.dumps(line), flush=True)
@@ -651,7 +705,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--fp64-steps", type=int, default=20)
-    ap.add_argument("--cpu-window", type=int, default=128)
+    ap.add_argument("--cpu-window", type=int, default=None,
+                    help="memory window of the CPU runs (default: the workload's M, reduced only if the "
+                         "FP64 history does not fit in host memory)")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--config", default="c5", choices=["c5", "small", "c3", "c4", "ninv"],

@@ -41,7 +41,7 @@ enum {
   KB_ERR_NODEV = -7    /* no CUDA device / library built without a device */
 };
 
-/* Perturbative expansion (src/TwoPIScalar/TwoPIScalar_Problemdefinition.jl:41-49, 115-118):
+/* Perturbative expansion (src/TwoPIScalar/TwoPIScalar_Problemdefinition.jl:34-45):
  * LambdaLO, LambdaNLO (quantum), LambdaNLOclassical, NinverseLO, NinverseNLO.
  * KB_PEXP_NINV_NLO needs KB_PREC_FP64. */
 enum { KB_PEXP_LO = 0, KB_PEXP_NLO_QUANTUM = 1, KB_PEXP_NLO_CLASSICAL = 2, KB_PEXP_NINV_LO = 3, KB_PEXP_NINV_NLO = 4 };
@@ -128,7 +128,9 @@ int kb_measure(kb_handle *h, int32_t run, int32_t t, kb_meas_scalars *s, double 
  * and returns at once; kb_measure_take(h, run, t, ...) waits for that copy only
  * and fills the outputs of kb_measure. A slot holds one step: take step t
  * before enqueuing step t+2. Device error flags travel with the copy and fail
- * the take as kb_sync would. */
+ * the take as kb_sync would; the enqueue clears them on the handle's stream right
+ * after copying them, so an error raised by step t is reported once, by the take
+ * of the first measurement enqueued after it. */
 int kb_measure_enqueue(kb_handle *h, int32_t run, int32_t t);
 int kb_measure_take(kb_handle *h, int32_t run, int32_t t, kb_meas_scalars *s, double *F, double *ddF,
                     double *n, double *omega, double *c);
@@ -260,7 +262,10 @@ int kb_adjoint(kb_handle *h, const double *n_init, double init_mass, int32_t t_f
  * address (cudaGetSymbolAddress) with that device current; make that first
  * call before any stream capture. Every call shares the array, so calls whose
  * kernels overlap on the GPU (other streams, other host threads) race; issue
- * them on one stream. Nothing in the array needs to start at zero. */
+ * them on one stream. Nothing in the array needs to start at zero. The looked-up
+ * address is kept for the life of the process: a cudaDeviceReset (or any other
+ * teardown of the device's primary context) invalidates it, so do not call this
+ * entry point on a device after resetting it. */
 int kb_sunset_rows_noalloc(int32_t Ns, int32_t N, double lambda, int32_t pexp, int32_t nrows, const double *F_rows,
                            const double *rho_rows, double *sigF_rows, double *sigr_rows, void *stream);
 

@@ -87,8 +87,250 @@ struct FFTPlan {
   }
 };
 
+// ---------------------------------------------------------------------------
+// Batched Stockham FFT (decimation in frequency, self-sorting), used for the
+// real lattice transforms rfft / brfft of the sunset. Data are split into real
+// and imaginary arrays x[i][l] (i < n the transform index, l < L independent
+// lines side by side), so every butterfly runs over L contiguous values. One
+// radix-r stage of length len = r m maps
+//   y[q + s (r p + k)] = W_len^(p k) sum_j x[q + s (p + m j)] w_r^(j k),
+// q < s (sub-transforms already split off), p < m, k < r; s grows by r per
+// stage and the last stage leaves the natural frequency order.
+// ---------------------------------------------------------------------------
+struct BatchFFT {
+  int n = 1;
+  std::vector<int> radix;         // stage radices: 4s first, then 2, then odd primes
+  std::vector<double> twr, twi;   // exp(-2 pi i j / n), j < n
+  explicit BatchFFT(int n_ = 1) : n(n_) {
+    int m = n;
+    while (m % 4 == 0) { radix.push_back(4); m /= 4; }
+    while (m % 2 == 0) { radix.push_back(2); m /= 2; }
+    for (int p = 3; m > 1; p += 2)
+      while (m % p == 0) { radix.push_back(p); m /= p; }
+    twr.resize(n);
+    twi.resize(n);
+    for (int j = 0; j < n; ++j) {
+      double a = -2.0 * M_PI * (double)j / (double)n;
+      twr[j] = std::cos(a);
+      twi[j] = std::sin(a);
+    }
+  }
+  // Transforms (xr, xi) in place (sign -1 forward, +1 backward, unnormalised);
+  // (wr, wi) are work arrays of n * L values each.
+  void run(double *xr, double *xi, double *wr, double *wi, long L, int sign) const {
+    if (n == 1) return;
+    double *ar = xr, *ai = xi, *br = wr, *bi = wi;
+    long s = 1;
+    int len = n;
+    const double sg = sign < 0 ? 1.0 : -1.0;  // conjugates the table for the backward transform
+    for (int r : radix) {
+      const int m = len / r;
+      const int tstep = n / len;
+      for (int p = 0; p < m; ++p) {
+        double wkr[64], wki[64];
+        for (int k = 0; k < r; ++k) {
+          long e = ((long)p * k * tstep) % n;
+          wkr[k] = twr[e];
+          wki[k] = sg * twi[e];
+        }
+        for (long q = 0; q < s; ++q) {
+          if (r == 2) {
+            const double *a0r = ar + (q + s * p) * L, *a0i = ai + (q + s * p) * L;
+            const double *a1r = ar + (q + s * (p + m)) * L, *a1i = ai + (q + s * (p + m)) * L;
+            double *y0r = br + (q + s * (2 * p)) * L, *y0i = bi + (q + s * (2 * p)) * L;
+            double *y1r = br + (q + s * (2 * p + 1)) * L, *y1i = bi + (q + s * (2 * p + 1)) * L;
+            const double c = wkr[1], d = wki[1];
+            for (long l = 0; l < L; ++l) {
+              double ur = a0r[l] - a1r[l], ui = a0i[l] - a1i[l];
+              y0r[l] = a0r[l] + a1r[l];
+              y0i[l] = a0i[l] + a1i[l];
+              y1r[l] = ur * c - ui * d;
+              y1i[l] = ur * d + ui * c;
+            }
+          } else if (r == 4) {
+            const double *a0r = ar + (q + s * p) * L, *a0i = ai + (q + s * p) * L;
+            const double *a1r = ar + (q + s * (p + m)) * L, *a1i = ai + (q + s * (p + m)) * L;
+            const double *a2r = ar + (q + s * (p + 2 * m)) * L, *a2i = ai + (q + s * (p + 2 * m)) * L;
+            const double *a3r = ar + (q + s * (p + 3 * m)) * L, *a3i = ai + (q + s * (p + 3 * m)) * L;
+            double *yr[4], *yi[4];
+            for (int k = 0; k < 4; ++k) {
+              yr[k] = br + (q + s * (4 * p + k)) * L;
+              yi[k] = bi + (q + s * (4 * p + k)) * L;
+            }
+            // w_4 = exp(sign i pi / 2) = sign * i
+            const double sgn = sign < 0 ? -1.0 : 1.0;
+            for (long l = 0; l < L; ++l) {
+              double s02r = a0r[l] + a2r[l], s02i = a0i[l] + a2i[l];
+              double d02r = a0r[l] - a2r[l], d02i = a0i[l] - a2i[l];
+              double s13r = a1r[l] + a3r[l], s13i = a1i[l] + a3i[l];
+              double d13r = a1r[l] - a3r[l], d13i = a1i[l] - a3i[l];
+              // w_4 * d13 = sgn * i * d13
+              double wdr = -sgn * d13i, wdi = sgn * d13r;
+              double c0r = s02r + s13r, c0i = s02i + s13i;
+              double c1r = d02r + wdr, c1i = d02i + wdi;
+              double c2r = s02r - s13r, c2i = s02i - s13i;
+              double c3r = d02r - wdr, c3i = d02i - wdi;
+              yr[0][l] = c0r;
+              yi[0][l] = c0i;
+              yr[1][l] = c1r * wkr[1] - c1i * wki[1];
+              yi[1][l] = c1r * wki[1] + c1i * wkr[1];
+              yr[2][l] = c2r * wkr[2] - c2i * wki[2];
+              yi[2][l] = c2r * wki[2] + c2i * wkr[2];
+              yr[3][l] = c3r * wkr[3] - c3i * wki[3];
+              yi[3][l] = c3r * wki[3] + c3i * wkr[3];
+            }
+          } else {
+            // generic radix: direct small DFT with w_r^(jk) = tw[(j k mod r) n / r]
+            for (long l = 0; l < L; ++l) {
+              double xr_[64], xi_[64];
+              for (int j = 0; j < r; ++j) {
+                xr_[j] = ar[(q + s * (p + (long)m * j)) * L + l];
+                xi_[j] = ai[(q + s * (p + (long)m * j)) * L + l];
+              }
+              for (int k = 0; k < r; ++k) {
+                double cr = 0.0, ci = 0.0;
+                for (int j = 0; j < r; ++j) {
+                  long e = ((long)(j * k) % r) * (n / r);
+                  double vr = twr[e], vi = sg * twi[e];
+                  cr += xr_[j] * vr - xi_[j] * vi;
+                  ci += xr_[j] * vi + xi_[j] * vr;
+                }
+                br[(q + s * ((long)r * p + k)) * L + l] = cr * wkr[k] - ci * wki[k];
+                bi[(q + s * ((long)r * p + k)) * L + l] = cr * wki[k] + ci * wkr[k];
+              }
+            }
+          }
+        }
+      }
+      std::swap(ar, br);
+      std::swap(ai, bi);
+      s *= r;
+      len = m;
+    }
+    if (ar != xr) {
+      std::memcpy(xr, ar, sizeof(double) * (size_t)n * L);
+      std::memcpy(xi, ai, sizeof(double) * (size_t)n * L);
+    }
+  }
+};
+
+// FFTW's rfft / brfft of a real column-major lattice of sdim axes of length Ns
+// (TwoPIScalar_SimDataStruct.jl:381-382): the half spectrum has H = Ns/2 + 1
+// entries along the first axis, stored [k_sdim]...[k_1] with k_0 < H fastest.
+// The first axis runs two real lines per complex transform; the other axes
+// run batched over the contiguous planes.
+struct RealFFT3 {
+  int Ns = 1, sdim = 3, H = 1;
+  long V = 1, nlines = 1, HV = 1;  // sites, lines along axis 0, half-spectrum size
+  BatchFFT f;
+  static const int B = 16;  // line pairs per batch of the first axis
+  void setup(int Ns_, int sdim_) {
+    Ns = Ns_;
+    sdim = sdim_;
+    H = Ns / 2 + 1;
+    V = 1;
+    for (int d = 0; d < sdim; ++d) V *= Ns;
+    nlines = V / Ns;
+    HV = (long)H * nlines;
+    f = BatchFFT(Ns);
+  }
+  struct Work {
+    std::vector<double> hr, hi, wr, wi, br, bi;
+  };
+  void alloc(Work &w) const {
+    w.hr.resize(HV);
+    w.hi.resize(HV);
+    size_t big = std::max<size_t>((size_t)HV, (size_t)Ns * B);
+    w.wr.resize(big);
+    w.wi.resize(big);
+    w.br.resize((size_t)Ns * B);
+    w.bi.resize((size_t)Ns * B);
+  }
+  // axes 1.. of the half spectrum (in w.hr/hi), sign as for BatchFFT::run
+  void outer_axes(Work &w, int sign) const {
+    long inner = H;
+    for (int d = 1; d < sdim; ++d) {
+      const long block = inner * Ns;
+      for (long o = 0; o < HV; o += block)
+        f.run(w.hr.data() + o, w.hi.data() + o, w.wr.data(), w.wi.data(), inner, sign);
+      inner = block;
+    }
+  }
+  // out[k] = Re rfft(x)[k] on the half spectrum (HV values)
+  void rfft_re(const double *x, double *out, Work &w) const {
+    const int n = Ns;
+    for (long l0 = 0; l0 < nlines; l0 += 2 * B) {
+      const long nb = std::min<long>(B, (nlines - l0 + 1) / 2);
+      for (int i = 0; i < n; ++i)
+        for (long b = 0; b < nb; ++b) {
+          long la = l0 + 2 * b, lb = la + 1;
+          w.br[(size_t)i * nb + b] = x[la * n + i];
+          w.bi[(size_t)i * nb + b] = lb < nlines ? x[lb * n + i] : 0.0;
+        }
+      f.run(w.br.data(), w.bi.data(), w.wr.data(), w.wi.data(), nb, -1);
+      for (long b = 0; b < nb; ++b) {
+        long la = l0 + 2 * b, lb = la + 1;
+        for (int k = 0; k < H; ++k) {
+          const int mk = (n - k) % n;
+          double zr = w.br[(size_t)k * nb + b], zi = w.bi[(size_t)k * nb + b];
+          double yr = w.br[(size_t)mk * nb + b], yi = w.bi[(size_t)mk * nb + b];
+          w.hr[la * H + k] = 0.5 * (zr + yr);
+          w.hi[la * H + k] = 0.5 * (zi - yi);
+          if (lb < nlines) {
+            w.hr[lb * H + k] = 0.5 * (zi + yi);
+            w.hi[lb * H + k] = -0.5 * (zr - yr);
+          }
+        }
+      }
+    }
+    outer_axes(w, -1);
+    for (long q = 0; q < HV; ++q) out[q] = w.hr[q];
+  }
+  // x = brfft(g) of a real half spectrum g (HV values) into V reals
+  void brfft(const double *g, double *x, Work &w) const {
+    const int n = Ns;
+    for (long q = 0; q < HV; ++q) {
+      w.hr[q] = g[q];
+      w.hi[q] = 0.0;
+    }
+    outer_axes(w, +1);
+    for (long l0 = 0; l0 < nlines; l0 += 2 * B) {
+      const long nb = std::min<long>(B, (nlines - l0 + 1) / 2);
+      for (long b = 0; b < nb; ++b) {
+        long la = l0 + 2 * b, lb = la + 1;
+        for (int k = 0; k < n; ++k) {
+          // Hermitian extension along the first axis; the imaginary parts at
+          // k = 0 and at the Nyquist index do not enter a real result
+          double pr, pi, qr = 0.0, qi = 0.0;
+          const bool lower = k < H;
+          const int kk = lower ? k : n - k;
+          const bool selfconj = (kk == 0) || (2 * kk == n);
+          pr = w.hr[la * H + kk];
+          pi = selfconj ? 0.0 : (lower ? w.hi[la * H + kk] : -w.hi[la * H + kk]);
+          if (lb < nlines) {
+            qr = w.hr[lb * H + kk];
+            qi = selfconj ? 0.0 : (lower ? w.hi[lb * H + kk] : -w.hi[lb * H + kk]);
+          }
+          w.br[(size_t)k * nb + b] = pr - qi;
+          w.bi[(size_t)k * nb + b] = pi + qr;
+        }
+      }
+      f.run(w.br.data(), w.bi.data(), w.wr.data(), w.wi.data(), nb, +1);
+      for (int i = 0; i < n; ++i)
+        for (long b = 0; b < nb; ++b) {
+          long la = l0 + 2 * b, lb = la + 1;
+          x[la * n + i] = w.br[(size_t)i * nb + b];
+          if (lb < nlines) x[lb * n + i] = w.bi[(size_t)i * nb + b];
+        }
+    }
+  }
+};
+
 struct FFTScratch {
   std::vector<cplx> a, b, tmp, lat, lat2;
+  RealFFT3::Work rw;
+  std::vector<double> h1, h2;          // half spectra of the sunset
+  std::vector<double> g1, g2, g3, g4;  // lattice copies of orbit rows (ENGINE_ORBIT)
 };
 
 // ---------------------------------------------------------------------------
@@ -221,6 +463,7 @@ struct Oracle {
   double hartreemass2 = 0.0;
   std::vector<double> Coct;          // octant cosine matrix
   std::vector<FFTPlan> plans;
+  RealFFT3 rf;  // rfft / brfft of the sunset (FULL and ORBIT engines)
   std::vector<FFTScratch> scratch;
   std::vector<std::vector<double>> rhs;  // per chunk
 
@@ -284,8 +527,10 @@ struct Oracle {
     Coct = octant_matrix(p.Ns);
     plans.clear();
     plans.emplace_back(p.Ns);
+    rf.setup(p.Ns, p.sdim);
     scratch.resize(p.nthreads);
     for (auto &s : scratch) {
+      if (p.engine != ORC_ENGINE_OCTANT) rf.alloc(s.rw);
       s.a.resize(p.Ns);
       s.b.resize(p.Ns);
       s.tmp.resize(64 * 64);
@@ -369,35 +614,32 @@ struct Oracle {
   }
 
   // One sunset on full lattices: Fin, rin (rin already times thesign).
-  // calcSelfEnergyattp! CPUfull (TwoPIScalar_Evolution.jl:25-31)
+  // calcSelfEnergyattp! CPUfull (TwoPIScalar_Evolution.jl:25-31): real parts of
+  // the two rffts, pointwise products on the half spectrum, two brffts.
   void sunset_lattice(const double *Fin, const double *rin, double *sF, double *sr, FFTScratch &sc) {
-    std::vector<cplx> &X = sc.lat, &Y = sc.lat2;
-    for (long s = 0; s < orb.V; ++s) X[s] = cplx(rin[s], 0.0);
-    fft_lattice(X.data(), -1, sc);
-    real_half_spectrum(X);  // rx
-    for (long s = 0; s < orb.V; ++s) Y[s] = cplx(Fin[s], 0.0);
-    fft_lattice(Y.data(), -1, sc);
-    real_half_spectrum(Y);  // Fx
+    const long HV = rf.HV;
+    sc.h1.resize(HV);
+    sc.h2.resize(HV);
+    rf.rfft_re(rin, sc.h1.data(), sc.rw);  // rx
+    rf.rfft_re(Fin, sc.h2.data(), sc.rw);  // Fx
     const double iv = ivol();
     const double lam2 = p.lambda * p.lambda;
     const double N = (double)p.N;
     const double fr = iv * iv * iv * (-lam2 * (N + 2.0) / (6.0 * N * N));
     const double fF = iv * iv * iv * (-lam2 * (N + 2.0) / (18.0 * N * N));
     const bool classical = (p.pexp == ORC_PEXP_NLO_CLASSICAL);
-    // pointwise products, then brfft
-    std::vector<cplx> Z(orb.V);
-    for (long s = 0; s < orb.V; ++s) {
-      double rx = X[s].real(), Fx = Y[s].real();
+    for (long s = 0; s < HV; ++s) {
+      double rx = sc.h1[s], Fx = sc.h2[s];
       double gr = classical ? rx * (Fx * Fx) : rx * (Fx * Fx - (1 / 12.) * (rx * rx));
       double gF = classical ? Fx * (Fx * Fx) : Fx * (Fx * Fx - 0.75 * (rx * rx));
-      X[s] = cplx(gr, 0.0);
-      Z[s] = cplx(gF, 0.0);
+      sc.h1[s] = gr;
+      sc.h2[s] = gF;
     }
-    fft_lattice(X.data(), +1, sc);
-    fft_lattice(Z.data(), +1, sc);
+    rf.brfft(sc.h1.data(), sr, sc.rw);
+    rf.brfft(sc.h2.data(), sF, sc.rw);
     for (long s = 0; s < orb.V; ++s) {
-      sr[s] = fr * X[s].real();
-      sF[s] = fF * Z[s].real();
+      sr[s] *= fr;
+      sF[s] *= fF;
     }
   }
 
@@ -468,7 +710,11 @@ struct Oracle {
     } else if (p.engine == ORC_ENGINE_ORBIT) {
       // copytolattice! -> FFT sunset -> copytoreducedlattice!
       // (TwoPIScalar_Evolution.jl:91-105, DefSimDataElements.jl:71-83)
-      std::vector<double> Fl(orb.V), rl(orb.V), sFl(orb.V), srl(orb.V);
+      std::vector<double> &Fl = sc.g1, &rl = sc.g2, &sFl = sc.g3, &srl = sc.g4;
+      Fl.resize(orb.V);
+      rl.resize(orb.V);
+      sFl.resize(orb.V);
+      srl.resize(orb.V);
       for (long s = 0; s < orb.V; ++s) {
         Fl[s] = F[orb.orbit_of_site[s]];
         rl[s] = r[orb.orbit_of_site[s]];

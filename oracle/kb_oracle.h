@@ -43,7 +43,7 @@ extern "C" {
 #endif
 
 enum { ORC_ENGINE_FULL = 0, ORC_ENGINE_ORBIT = 1, ORC_ENGINE_OCTANT = 2 };
-/* TwoPIScalar_Problemdefinition.jl:115-118 */
+/* TwoPIScalar_Problemdefinition.jl:34-45 (LambdaLO, LambdaNLOquantum/classical, NinverseLO/NLO) */
 enum { ORC_PEXP_LO = 0, ORC_PEXP_NLO_QUANTUM = 1, ORC_PEXP_NLO_CLASSICAL = 2, ORC_PEXP_NINV_LO = 3,
        ORC_PEXP_NINV_NLO = 4 };
 

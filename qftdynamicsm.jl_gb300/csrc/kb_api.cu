@@ -788,6 +788,9 @@ int kb_measure_enqueue(kb_handle *h, int32_t run, int32_t t) {
   KB_CUDA(h, cudaMemcpyAsync(m.host, R.meas, nm * 8, cudaMemcpyDeviceToHost, h->st));
   KB_CUDA(h, cudaMemcpyAsync(m.host + nm, R.epart, ne * 8, cudaMemcpyDeviceToHost, h->st));
   KB_CUDA(h, cudaMemcpyAsync(m.host + nm + ne, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  // the flags now travel with this measurement: clear them in stream order, so that
+  // kernels of later steps set them afresh and each error is reported once (by take)
+  KB_CUDA(h, cudaMemsetAsync(h->d_err, 0, sizeof(int), h->st));
   KB_CUDA(h, cudaEventRecord(m.ev, h->st));
   m.run = run;
   m.t = t;
@@ -807,8 +810,7 @@ int kb_measure_take(kb_handle *h, int32_t run, int32_t t, kb_meas_scalars *s, do
   const size_t nm = (size_t)5 * R.Spad, ne = (size_t)4 * R.nchunks;
   int e = 0;
   std::memcpy(&e, m.host + nm + ne, sizeof(int));
-  if (e) {
-    cudaMemset(h->d_err, 0, sizeof(int));
+  if (e) {  // the flags were cleared on the stream right after their copy (kb_measure_enqueue)
     if (e & kb::DEVERR_TIMEOUT) return fail(h, KB_ERR_TIMEOUT, "a bounded device wait expired (kernel returned early)");
     return fail(h, KB_ERR_CUDA, "device error flags 0x%x", e);
   }
@@ -1147,7 +1149,10 @@ int kb_sync(kb_handle *h) {
   int e = 0;
   KB_CUDA(h, cudaMemcpy(&e, h->d_err, sizeof(int), cudaMemcpyDeviceToHost));
   if (e) {
-    cudaMemset(h->d_err, 0, sizeof(int));
+    // cleared on the handle's stream (non-blocking, so not ordered with the legacy
+    // stream): every later kernel of this handle runs after the clear
+    KB_CUDA(h, cudaMemsetAsync(h->d_err, 0, sizeof(int), h->st));
+    KB_CUDA(h, cudaStreamSynchronize(h->st));
     if (e & kb::DEVERR_TIMEOUT) return fail(h, KB_ERR_TIMEOUT, "a bounded device wait expired (kernel returned early)");
     return fail(h, KB_ERR_CUDA, "device error flags 0x%x", e);
   }

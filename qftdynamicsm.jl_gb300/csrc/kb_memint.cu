@@ -885,9 +885,12 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   __syncthreads();  // producer done issuing; consumers done with the triangle
   if (use_tmem) tmem_fence_after();
   if (*abort_flag) {
-    // drain copies still in flight into this CTA's shared memory
+    // drain copies still in flight into this CTA's shared memory: only the last NST
+    // issued tiles can be (the producer reuses a stage after its consumers release it),
+    // and for those the stage barrier's latest phase is theirs; an older tile's phase
+    // parity repeats on its stage, so waiting on it would run to the bound
     if (tid == 0)
-      for (int q = 0; q < *issued_count; ++q)
+      for (int q = max(0, *issued_count - NST); q < *issued_count; ++q)
         (void)mbar_wait_bounded(full + (q % NST), (uint32_t)((q / NST) & 1));
   } else {
     if (split && use_tmem && rowgrp)  // this half's row sums, for memint_finish_kernel
@@ -922,10 +925,8 @@ constexpr int FIN_IT = FIN_TP * KC / FIN_THREADS;
 static_assert(FIN_IT * FIN_THREADS == FIN_TP * KC, "whole items per thread");
 
 // FP32 history: four CTAs per SM (64 registers, about 120 bytes of spills), which
-// overlaps more of the loads with the FP64 arithmetic. Memory integrals per
-// Ns = 64, M = 1000 step: 4.077 against 4.099 ms with two CTAs per SM (128
-// registers); on another GB300, 4.046 against 4.092 ms for 512-thread CTAs
-// with two items per thread, two CTAs per SM
+// overlaps more of the loads with the FP64 arithmetic than two CTAs per SM with
+// 128 registers, or 512-thread CTAs with two items per thread, did when timed
 template <typename TS>
 __global__ void __launch_bounds__(FIN_THREADS, sizeof(TS) == 4 ? 4 : 2)
 memint_finish_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int nruns, int nb_max,
@@ -1355,8 +1356,8 @@ memint_blk_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base,
   }
   __syncthreads();
   if (*abort_flag) {
-    if (tid == 0)
-      for (int q = 0; q < *issued_count; ++q)
+    if (tid == 0)  // the last NST issued tiles only, as in memint_kernel
+      for (int q = max(0, *issued_count - NST); q < *issued_count; ++q)
         (void)mbar_wait_bounded(full + (q % NST), (uint32_t)((q / NST) & 1));
     __syncthreads();
     return;

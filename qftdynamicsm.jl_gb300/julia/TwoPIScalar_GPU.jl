@@ -28,7 +28,7 @@ KbMeasScalars() = KbMeasScalars(0, 0, 0, 0, 0, 0)
 
 kbcheck(rc, h) = rc == 0 || error("libkb2pi: ", unsafe_string(ccall((:kb_last_error, libkb2pi), Cstring, (Ptr{Cvoid},), h)))
 
-# Numerics selector next to TwoPIScalarCPUfull/CPUred (TwoPIScalar_Problemdefinition.jl:171-186)
+# Numerics selector next to TwoPIScalarCPUfull/CPUred (TwoPIScalar_Problemdefinition.jl:92-106)
 struct TwoPIScalarGPU <: TwoPIScalarNumerics
     nchunks::Int       # kept for the parameter interface; the GPU ignores it
     precision::Int32   # 0 = FP64, 1 = mixed
@@ -90,12 +90,23 @@ function initialize!(thesolution::QFTdynamicsSolutionTwoPIScalar, tmpdata::Nothi
     @unpack problem, simdata = thesolution
     @unpack model, pexp, disc, init, simsetup = problem
     if isnewsimulation(simsetup)
-        n = [getparticlenr_orbit(init, disc, k2) for k2 in simdata.kL2values]
-        initmass = (model isa Phi4Tachyonic || init isa TwoPIScalarGauss || init isa TwoPIScalarQuench ||
-                    init isa TwoPIScalarTopHatT1 || init isa TwoPIScalarThermal || init isa TwoPIScalarBox) ?
-                   disc.Mass : getGapMass_orbits(model, pexp, disc, n, simdata)
-        kbcheck(ccall((:kb_init, libkb2pi), Cint, (Ptr{Cvoid}, Int32, Ptr{Float64}, Float64),
-                      simdata.h, 0, n, initmass), simdata.h)
+        if init isa TwoPIScalarGauss
+            # initSimData! for TwoPIScalarGauss (TwoPIScalar_Initialization.jl:95-112): the same three
+            # rows at every momentum, passed as rows (kb_init_rows)
+            S = simdata.S
+            F11 = fill(init.xi^2, S)
+            F21 = init.xi * init.eta * disc.dt .+ F11
+            F22 = (init.eta^2 + init.sig^2 / (4 * init.xi^2)) * disc.dt^2 .- F11 .+ 2 .* F21
+            kbcheck(ccall((:kb_init_rows, libkb2pi), Cint, (Ptr{Cvoid}, Int32, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
+                          simdata.h, 0, F11, F21, F22), simdata.h)
+        else
+            n = getparticlenr_orbits(init, disc, simdata.kL2values)
+            initmass = (model isa Phi4Tachyonic || init isa TwoPIScalarQuench || init isa TwoPIScalarTopHatT1 ||
+                        init isa TwoPIScalarThermal || init isa TwoPIScalarBox) ?
+                       disc.Mass : getGapMass_orbits(model, pexp, disc, n, simdata)
+            kbcheck(ccall((:kb_init, libkb2pi), Cint, (Ptr{Cvoid}, Int32, Ptr{Float64}, Float64),
+                          simdata.h, 0, n, initmass), simdata.h)
+        end
     end
     simsetup.lastEvolStep = 2
     measure!(thesolution, 2)
@@ -146,11 +157,24 @@ function measure_take(simdata::TwoPIScalarSimDataGPUkb, t)
     return s[], F, ddF, n, omega, c
 end
 
-# occupation per orbit with lev2 = k2 (getparticlenr, TwoPIScalar_Initialization.jl:133-203)
-getparticlenr_orbit(init::TwoPIScalarParticle, disc, k2) = init.n
-getparticlenr_orbit(init::TwoPIScalarThermal, disc, k2) = 1 / (exp(sqrt(k2 + disc.Mass^2) / (init.T * disc.Mass)) - 1)
-getparticlenr_orbit(init::TwoPIScalarTsunami, disc, k2) = 5 * exp(-(sqrt(k2) - 1)^2 / (2 * 0.2^2))
-getparticlenr_orbit(init::TwoPIScalarQuench, disc, k2) = 0.0
+# occupation per orbit, k2s = lev2 of every orbit (getparticlenr, TwoPIScalar_Initialization.jl:133-203)
+getparticlenr_orbits(init::TwoPIScalarParticle, disc, k2s) = fill(Float64(init.n), length(k2s))
+getparticlenr_orbits(init::TwoPIScalarThermal, disc, k2s) =
+    [1 / (exp(sqrt(k2 + disc.Mass^2) / (init.T * disc.Mass)) - 1) for k2 in k2s]
+getparticlenr_orbits(init::TwoPIScalarTsunami, disc, k2s) = [5 * exp(-(sqrt(k2) - 1)^2 / (2 * 0.2^2)) for k2 in k2s]
+getparticlenr_orbits(init::TwoPIScalarQuench, disc, k2s) = zeros(length(k2s))
+# TopHat states (:142-190): the reference fills eta between the lev2-sorted shells closest to
+# lo * sdim * Mass^2 and hi * sdim * Mass^2; on orbits that is every orbit whose lev2 lies between
+# those two shell values (the levels are the distinct lev2 values)
+function tophat_orbits(disc, k2s, lo, hi, eta)
+    levels = sort(unique(k2s))
+    k2min = levels[argmin(abs.(levels .- lo * disc.sdim * disc.Mass^2))]
+    k2max = levels[argmin(abs.(levels .- hi * disc.sdim * disc.Mass^2))]
+    return [(k2min <= k2 <= k2max) ? Float64(eta) : 0.0 for k2 in k2s]
+end
+getparticlenr_orbits(init::TwoPIScalarTopHatT1, disc, k2s) = tophat_orbits(disc, k2s, 0.68, 2.04, 2)
+getparticlenr_orbits(init::TwoPIScalarTopHatT2, disc, k2s) = tophat_orbits(disc, k2s, 0.0, 1.9, 1.85)
+getparticlenr_orbits(init::TwoPIScalarTopHatT3, disc, k2s) = tophat_orbits(disc, k2s, 2.04, 2.72, 1.6)
 
 # getGapMass (TwoPIScalar_Initialization.jl:250-266) summed over orbits with their degeneracy
 function getGapMass_orbits(model, pexp, disc, n, simdata)

@@ -9,5 +9,5 @@ from .capi import Handle, KbError, KbParams, load_library  # noqa: F401
 from .twopiscalar import (  # noqa: F401
     QFTdynamicsProblem, QFTdynamicsSolution, TwoPIScalarfile, createMeasurement, evolve, getGapMass,
     evolve_recorded, getparticlenr, initialize, lattice_orbits, load_measurearray, make_problem, measure,
-    run_simulation, save_measurearray,
+    orbits_to_shells, run_simulation, save_measurearray,
 )

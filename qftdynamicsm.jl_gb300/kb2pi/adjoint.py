@@ -50,8 +50,8 @@ def params_for(cfg, flags):
 def loss_and_grad(cfg, n_init, t_final, w_n=None, w_E=0.0, ckpt_every=20, init_mass=None):
     """One kb_adjoint call on a fresh FP64 handle; returns the dict of Handle.adjoint.
     The memory integrals run split in two (memint_split 1): twice the CTAs for the
-    few orbit chunks of the small lattices gradients are taken on (648 -> 609 ms per
-    gradient at Ns = 24, M = 300, 300 steps on a GB300; results differ in rounding only)."""
+    few orbit chunks of the small lattices gradients are taken on (results differ
+    from the whole-chunk kernel in rounding only)."""
     h = capi.Handle([params_for(cfg, ckpt_every)])
     try:
         h.set_tuning(memint_split=1)

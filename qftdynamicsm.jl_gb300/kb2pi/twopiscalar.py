@@ -391,3 +391,33 @@ def load_measurearray(path: str):
                 rec[k] = float(v) if v.ndim == 0 else v
         out[i] = rec
     return out, json.loads(str(z["parameters"]))
+
+
+def orbits_to_shells(k2, deg, values, rtol: float = 1e-12):
+    """Per-orbit measurement arrays on FFTWhelper-style shells (one entry per distinct
+    lev2, as the reference's MeasurementTwoPIScalar arrays index by `lev2`,
+    TwoPIScalar_Measurement.jl:24-25, 31-33).
+
+    Orbits whose lev2 agree to rtol form one shell; a shell's value is the
+    degeneracy-weighted mean of its orbits' values, which is the mean over the
+    shell's lattice sites (the CPUfull measurement averaged over the shell).
+    Returns (lev2 per shell ascending, deg per shell, values per shell); `values`
+    may be one array (S,) or a stack (..., S). FFTWhelper's own grouping rule is
+    not vendored in the reference; grouping by equal lev2 is what its `lev2`
+    field names."""
+    k2 = np.asarray(k2, np.float64)
+    deg = np.asarray(deg, np.float64)
+    vals = np.asarray(values, np.float64)
+    order = np.argsort(k2, kind="stable")
+    ks = k2[order]
+    new = np.ones(len(ks), bool)
+    new[1:] = np.abs(np.diff(ks)) > rtol * np.maximum(np.abs(ks[1:]), 1.0)
+    shell_of_sorted = np.cumsum(new) - 1
+    nshell = int(shell_of_sorted[-1]) + 1 if len(ks) else 0
+    shell = np.empty(len(k2), np.int64)
+    shell[order] = shell_of_sorted
+    dsh = np.bincount(shell, weights=deg, minlength=nshell)
+    lev2 = np.bincount(shell, weights=k2 * deg, minlength=nshell) / dsh
+    flat = vals.reshape(-1, vals.shape[-1])
+    out = np.stack([np.bincount(shell, weights=row * deg, minlength=nshell) / dsh for row in flat])
+    return lev2, dsh.astype(np.int64), out.reshape(vals.shape[:-1] + (nshell,))

@@ -83,3 +83,19 @@ def test_create_without_device_fails_loudly():
     with pytest.raises(capi.KbError) as ei:
         capi.Handle([p])
     assert ei.value.code in (-7, -3)
+
+
+def test_julia_glue_covers_the_initial_states_of_the_mirror():
+    """Every initial state the Python mirror initialises on the lattice has its
+    occupation in the Julia glue (getparticlenr_orbits), and the Gauss state goes
+    through kb_init_rows, as in the mirror (TwoPIScalar_Initialization.jl:95-203)."""
+    jl = open(os.path.join(ROOT, "qftdynamicsm.jl_gb300", "julia", "TwoPIScalar_GPU.jl")).read()
+    have = set(re.findall(r"getparticlenr_orbits\(init::TwoPIScalar(\w+),", jl))
+    assert {"Particle", "Thermal", "Tsunami", "Quench", "TopHatT1", "TopHatT2", "TopHatT3"} <= have
+    gauss = jl[jl.index("if init isa TwoPIScalarGauss"):]
+    gauss = gauss[:gauss.index("else")]
+    assert ":kb_init_rows" in gauss
+    # the TopHat ranges and heights are the mirror's (lo, hi, eta)
+    from kb2pi import twopiscalar  # noqa: F401
+    for name, lo, hi, eta in (("T1", "0.68", "2.04", "2"), ("T2", "0.0", "1.9", "1.85"), ("T3", "2.04", "2.72", "1.6")):
+        assert f"TwoPIScalarTopHat{name}, disc, k2s) = tophat_orbits(disc, k2s, {lo}, {hi}, {eta})" in jl

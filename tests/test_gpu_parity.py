@@ -294,6 +294,38 @@ def test_host_mirror_run_simulation():
     assert problem.model.Mass2 < 1.0  # RMass counterterm applied
 
 
+@pytest.mark.parametrize("num", ["GPU", "GPUmixed"])
+def test_host_mirror_tachyonic(num):
+    """Phi4Tachyonic with RMass (TwoPIScalar_ModelExpansionRenormalization.jl:11-16, 30-36):
+    the bare m^2 = -Mass^2 + counterterm is negative and initialize! uses disc.Mass
+    (TwoPIScalar_Initialization.jl:295); the GPU run follows the oracle evolved with that
+    negative m^2 (1e-10 FP64, 1e-5 mixed) in E, M^2 and n."""
+    import kb2pi
+    from oracle import Oracle
+
+    parameters = {"Mass": 1.0, "Nx": 10, "sdim": 3, "dt": 0.1, "Nsteps": 30, "NstepsinMemory": 14, "Nmeas": 0,
+                  "Mod": "phi4tachyonic", "Lambda": 3.0, "ONgroup": 4, "init": "Thermal", "T": 1.5,
+                  "Reno": "RMass", "Pexp": "LambdaNLO", "Num": num}
+    sol = kb2pi.run_simulation(dict(parameters))
+    problem = sol.problem
+    assert problem.model.tachyonic and problem.model.Mass2 < -1.0
+    o = Oracle(10, 3, M=14, N=4, dt=0.1, lam=3.0, mass2=problem.model.Mass2, mass=1.0)
+    _, k2, _ = o.orbits()
+    o.init_occupation(1.0 / (np.exp(np.sqrt(k2 + 1.0) / 1.5) - 1.0), 1.0)
+    ref = [o.measure(2)]
+    for t in range(3, 33):
+        o.step(t)
+        ref.append(o.measure(t))
+    tol = TOL64 if num == "GPU" else TOL_MIXED
+    got = sol.measurearray
+    assert len(got) == 31
+    assert rel([m["E"] for m in got], [m["E"] for m in ref]) <= tol
+    assert rel([m["M2"] for m in got], [m["M2"] for m in ref]) <= tol
+    assert max(m["M2"] for m in ref) < 0.0  # the effective mass stays negative: unstable low modes
+    for mg, mo in zip(got[1:], ref[1:]):
+        assert rel(mg["n"], mo["n"]) <= tol
+
+
 @pytest.mark.parametrize("pexp_name,pexp", [("NinverseNLO", 4), ("NinverseLO", 3)])
 def test_host_mirror_ninverse(pexp_name, pexp):
     """The driver loop with Pexp = NinverseNLO / NinverseLO and RMass renormalisation

@@ -341,3 +341,37 @@ def test_bounded_wait_runs_out_and_is_reported(precision, variant):
     assert np.isfinite(m["E"]) and np.all(np.isfinite(m["n"]))
     g.close()
 
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_pipelined_timeout_is_reported_once(precision):
+    """The measurement loop one step behind (kb_measure_enqueue / kb_measure_take):
+    step t times out (test hook: no tiles issued), step t+1 is issued before t is
+    taken. The enqueue of t clears the device flags in stream order right after
+    copying them, so the synchronising kb_set_tuning between the two steps sees a
+    clean flag, the take of t reports KB_ERR_TIMEOUT and nothing reports it again."""
+    from kb2pi import capi
+
+    cfg = dict(Ns=6, M=8, N=4, lam=2.0, dt=0.1, pexp=1, T=1.5)
+    h = make_gpu(cfg, precision)
+    _, k2, _ = h.orbits()
+    h.init(0, occupation(cfg, k2), 1.0)
+    h.steps(3, 5, 0)
+    h.sync()
+    h.set_tuning(test_no_tiles=1)
+    t0 = time.time()
+    h.step(8)
+    h.measure_enqueue(0, 8)
+    h.set_tuning(test_no_tiles=0)  # waits for step 8; its flag was cleared behind the copy
+    h.step(9)
+    h.measure_enqueue(0, 9)
+    timeouts = 0
+    for call in (lambda: h.measure_take(0, 8), lambda: h.measure_take(0, 9), h.sync):
+        try:
+            call()
+        except capi.KbError as e:
+            if "KB_ERR_TIMEOUT" in str(e):
+                timeouts += 1
+    assert timeouts == 1
+    assert time.time() - t0 < 60
+    h.close()

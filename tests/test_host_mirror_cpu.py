@@ -96,3 +96,25 @@ def test_occupation_profiles():
     assert np.all(th1[inside] == 2.0) and np.all(th1[~inside] == 0.0)
     with pytest.raises(ValueError):
         getparticlenr(Init("NoSuchInit"), disc, k2)
+
+
+def test_orbits_to_shells_groups_equal_lev2():
+    """Per-orbit arrays onto lev2 shells: the shell value is the site average, and at
+    Ns=4 the orbits (0,1,1) and (0,0,2) share lev2 = 4 and so one shell."""
+    from kb2pi.twopiscalar import lattice_orbits, orbits_to_shells
+
+    rep, k2, deg = lattice_orbits(4)
+    vals = np.arange(len(k2), dtype=float) + 1.0
+    lev2, dsh, sv = orbits_to_shells(k2, deg, vals)
+    assert np.all(np.diff(lev2) > 0) and dsh.sum() == 64
+    i011 = [i for i in range(len(k2)) if sorted(rep[i]) == [0, 1, 1]][0]
+    i002 = [i for i in range(len(k2)) if sorted(rep[i]) == [0, 0, 2]][0]
+    assert abs(k2[i011] - k2[i002]) < 1e-12
+    s = int(np.argmin(np.abs(lev2 - k2[i011])))
+    assert dsh[s] == deg[i011] + deg[i002]
+    want = (vals[i011] * deg[i011] + vals[i002] * deg[i002]) / (deg[i011] + deg[i002])
+    assert abs(sv[s] - want) <= 1e-15 * want
+    # the degeneracy-weighted total is kept, and a stack of arrays maps row by row
+    assert abs(np.dot(sv, dsh) - np.dot(vals, deg)) <= 1e-12 * np.dot(vals, deg)
+    _, _, sv2 = orbits_to_shells(k2, deg, np.stack([vals, 2 * vals]))
+    assert np.allclose(sv2[1], 2 * sv)

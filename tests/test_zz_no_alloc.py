@@ -29,25 +29,31 @@ def test_noalloc_rejects_sizes_beyond_its_scratch():
 
 
 @pytest.mark.gpu
-def test_noalloc_matches_kb_self_energies_twice():
+@pytest.mark.parametrize("Ns,nrows,pexp", [
+    (16, 10, 1),    # LambdaNLO quantum
+    (32, 300, 1),   # the largest Ns the fixed scratch takes; more rows than SMs, so a CTA reuses its slot
+    (12, 40, 2),    # LambdaNLO classical
+])
+def test_noalloc_matches_kb_self_energies_twice(Ns, nrows, pexp):
     """Two calls in a row through the C ABI, each checked against the handle path
     (kb_self_energies + kb_get_sigma) on the same rows, FP64 tolerance 1e-12."""
     import torch
 
     lib = _lib()
-    Ns, N, lam = 16, 8, 10.0
-    cfg = dict(Ns=Ns, M=14, dt=0.01, lam=lam, N=N, T=2.0)
+    N, lam = 8, 10.0
+    tmone = nrows
+    cfg = dict(Ns=Ns, M=nrows + 4, dt=0.01, lam=lam, N=N, T=2.0, pexp=pexp)
     g = make_gpu(cfg)  # KB_PREC_FP64: the same sunset as the no-alloc variant
     _, k2, _ = g.orbits(0)
     g.init(0, occupation(cfg, k2), 1.0)
     for t in range(3, 11):
         g.step(t)
-    g.expand()
-    tmone = 10
+    for _ in range(11, tmone + 2):  # the window [1, tmone + 1], rows overwritten below
+        g.expand()
     S = g.S[0]
     stream = torch.cuda.current_stream()
     for call, seed in enumerate((11, 22)):
-        rng = np.random.default_rng(seed)
+        rng = np.random.default_rng(seed + Ns + pexp)
         Frows = np.zeros((tmone, S))
         rrows = np.zeros((tmone, S))
         for i, tp in enumerate(range(1, tmone + 1)):
@@ -63,7 +69,7 @@ def test_noalloc_matches_kb_self_energies_twice():
         dr = torch.tensor(rrows, dtype=torch.float64, device="cuda")
         oF = torch.full((tmone, S), float("nan"), dtype=torch.float64, device="cuda")
         orr = torch.full((tmone, S), float("nan"), dtype=torch.float64, device="cuda")
-        rc = lib.kb_sunset_rows_noalloc(Ns, N, lam, 1, tmone, ctypes.c_void_p(dF.data_ptr()),
+        rc = lib.kb_sunset_rows_noalloc(Ns, N, lam, pexp, tmone, ctypes.c_void_p(dF.data_ptr()),
                                         ctypes.c_void_p(dr.data_ptr()), ctypes.c_void_p(oF.data_ptr()),
                                         ctypes.c_void_p(orr.data_ptr()), ctypes.c_void_p(stream.cuda_stream))
         assert rc == 0, lib.kb_last_error(None)
@@ -72,3 +78,4 @@ def test_noalloc_matches_kb_self_energies_twice():
         assert np.all(np.isfinite(gotF)) and np.all(np.isfinite(gotr)), call
         assert rel(gotF, ref_F) <= 1e-12, call
         assert rel(gotr, ref_r) <= 1e-12, call
+    g.close()
