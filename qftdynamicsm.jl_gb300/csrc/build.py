@@ -20,6 +20,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--extended-lambda", "-Xcompiler", "-fPIC,-O2",
          "-Xptxas", "-warn-spills"]
 LIB_NAME = "libkb2pi.so"
+DEBUG_LIB_NAME = "libkb2pi_debug.so"
 
 
 def nvcc() -> str:
@@ -34,17 +35,20 @@ def _newer(target: str, deps) -> bool:
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
 
 
-def build(verbose: bool = False, force: bool = False) -> str:
-    os.makedirs(BUILD_DIR, exist_ok=True)
+def build(verbose: bool = False, force: bool = False, debug: bool = False) -> str:
+    """Compile the library; debug=True builds libkb2pi_debug.so with the device-side
+    bounds checks of ring, tile and Sigma indices (-DKB_DEBUG) next to it."""
+    bdir = os.path.join(BUILD_DIR, "debug") if debug else BUILD_DIR
+    os.makedirs(bdir, exist_ok=True)
     hdrs = [os.path.join(HERE, h) for h in HEADERS]
     objs = []
     jobs = []
     for s in SOURCES:
         src = os.path.join(HERE, s)
-        obj = os.path.join(BUILD_DIR, s.replace(".cu", ".o"))
+        obj = os.path.join(bdir, s.replace(".cu", ".o"))
         objs.append(obj)
         if force or _newer(obj, [src] + hdrs + [__file__]):
-            cmd = [nvcc()] + ARCH + FLAGS + ["-c", src, "-o", obj]
+            cmd = [nvcc()] + ARCH + FLAGS + (["-DKB_DEBUG"] if debug else []) + ["-c", src, "-o", obj]
             jobs.append(cmd)
 
     def run(cmd):
@@ -59,11 +63,17 @@ def build(verbose: bool = False, force: bool = False) -> str:
         for log in ex.map(run, jobs):
             if verbose and log:
                 print(log, file=sys.stderr)
-    lib = os.path.join(OUT_DIR, LIB_NAME)
+    lib = os.path.join(OUT_DIR, DEBUG_LIB_NAME if debug else LIB_NAME)
     if force or _newer(lib, objs):
         run([nvcc()] + ARCH + ["-shared", "-o", lib] + objs + ["-lcudart"])
     return lib
 
 
+def build_all(verbose: bool = False, force: bool = False) -> list:
+    """The release and the KB_DEBUG library, compiled side by side."""
+    with cf.ThreadPoolExecutor(max_workers=2) as ex:
+        return list(ex.map(lambda d: build(verbose, force, d), (False, True)))
+
+
 if __name__ == "__main__":
-    print(build(verbose=True, force="--force" in sys.argv))
+    print(build(verbose=True, force="--force" in sys.argv, debug="--debug" in sys.argv))

@@ -15,6 +15,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>  // header-only NVTX: ranges cost a branch unless a profiler is attached
+
 #include <cuda.h>  // CUtensorMap and its enums (the encoder comes from the runtime's driver entry point)
 #include <cudaTypedefs.h>
 
@@ -286,13 +288,42 @@ static int apply_schedule(kb_handle *h, int order) {
     bs += (Rs.p.M + Rs.dev.sun_rows - 1) / Rs.dev.sun_rows;
   }
   std::vector<RunDev> devs(nr);
-  for (int r = 0; r < nr; ++r) devs[r] = h->runs[r].dev;
+  for (int r = 0; r < nr; ++r) {
+    h->runs[r].dev.err = h->d_err;
+    devs[r] = h->runs[r].dev;
+  }
   if (cudaMemcpy(h->d_runs, devs.data(), sizeof(RunDev) * nr, cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(h->d_base_mi, smi.data(), sizeof(int) * 2 * nr, cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(h->d_base_sun, ssun.data(), sizeof(int) * 2 * nr, cudaMemcpyHostToDevice) != cudaSuccess)
     return KB_ERR_CUDA;
   h->batch_order = order;
   return KB_OK;
+}
+
+// NVTX range over a scope: each step issued from the host (kb_step, every graph
+// launch of kb_steps / kb_steps_recorded) is one named range in a timeline
+struct NvtxRange {
+  explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange &) = delete;
+  NvtxRange &operator=(const NvtxRange &) = delete;
+};
+
+// message of a non-zero device error word
+static int device_error(kb_handle *h, int e) {
+  if (e & kb::DEVERR_TIMEOUT) return fail(h, KB_ERR_TIMEOUT, "a bounded device wait expired (kernel returned early)");
+  if (e & kb::DEVERR_BOUNDS) {
+    static const char *names[] = {"sunset row", "sunset Sigma index", "memory-integral tile",
+                                  "memory-integral row/column", "leapfrog write", "finishing item"};
+    char list[256] = "";
+    for (int b = 0; b < 6; ++b)
+      if (e & (kb::DCHK_SUN_ROW << b)) {
+        strncat(list, list[0] ? ", " : "", sizeof list - strlen(list) - 1);
+        strncat(list, names[b], sizeof list - strlen(list) - 1);
+      }
+    return fail(h, KB_ERR_RANGE, "device bounds check failed (KB_DEBUG build): %s", list);
+  }
+  return fail(h, KB_ERR_CUDA, "device error flags 0x%x", e);
 }
 
 // ------------------------------------------------------------------------
@@ -706,6 +737,7 @@ int kb_step(kb_handle *h, int32_t t) {
   if (h->t_cur < 2) return fail(h, KB_ERR_PARAM, "kb_step before kb_init");
   if (t != h->t_cur + 1) return fail(h, KB_ERR_PARAM, "kb_step(%d): expected t = %d (lastEvolStep + 1)", t, h->t_cur + 1);
   cudaSetDevice(h->device);
+  NvtxRange range("kb_step");
   KB_CUDA(h, kb::launch_set_t(h->d_t, t, h->st));
   int rc = launch_step(h, 1);
   if (rc) return rc;
@@ -810,10 +842,7 @@ int kb_measure_take(kb_handle *h, int32_t run, int32_t t, kb_meas_scalars *s, do
   const size_t nm = (size_t)5 * R.Spad, ne = (size_t)4 * R.nchunks;
   int e = 0;
   std::memcpy(&e, m.host + nm + ne, sizeof(int));
-  if (e) {  // the flags were cleared on the stream right after their copy (kb_measure_enqueue)
-    if (e & kb::DEVERR_TIMEOUT) return fail(h, KB_ERR_TIMEOUT, "a bounded device wait expired (kernel returned early)");
-    return fail(h, KB_ERR_CUDA, "device error flags 0x%x", e);
-  }
+  if (e) return device_error(h, e);  // flags cleared on the stream right after their copy (kb_measure_enqueue)
   double *outs[5] = {F, ddF, n, omega, c};
   for (int q = 0; q < 5; ++q)
     if (outs[q]) std::memcpy(outs[q], m.host + (size_t)q * R.Spad, (size_t)R.S * 8);
@@ -987,6 +1016,7 @@ int kb_steps(kb_handle *h, int32_t t0, int32_t count, int32_t measure_every, kb_
   int nm = 0;
   for (int i = 0; i < count; ++i) {
     const int t = t0 + i;
+    NvtxRange range("kb_steps: step");
     if (h->profiling) {
       int rc = launch_step(h, 1);
       if (rc) return rc;
@@ -1080,7 +1110,10 @@ int kb_steps_recorded(kb_handle *h, int32_t t0, int32_t count, int32_t measure_e
     if (ei != cudaSuccess) return fail(h, KB_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(ei));
   }
   KB_CUDA(h, kb::launch_set_t(h->d_t, t0, h->st));
-  for (int i = 0; i < count; ++i) KB_CUDA(h, cudaGraphLaunch(h->graph_rec, h->st));
+  for (int i = 0; i < count; ++i) {
+    NvtxRange range("kb_steps_recorded: step");
+    KB_CUDA(h, cudaGraphLaunch(h->graph_rec, h->st));
+  }
   h->t_cur = t_last;
   h->sigma_valid = h->any_nlo || h->any_ninv;
   std::vector<double> host((size_t)nmeas * block);
@@ -1153,8 +1186,7 @@ int kb_sync(kb_handle *h) {
     // stream): every later kernel of this handle runs after the clear
     KB_CUDA(h, cudaMemsetAsync(h->d_err, 0, sizeof(int), h->st));
     KB_CUDA(h, cudaStreamSynchronize(h->st));
-    if (e & kb::DEVERR_TIMEOUT) return fail(h, KB_ERR_TIMEOUT, "a bounded device wait expired (kernel returned early)");
-    return fail(h, KB_ERR_CUDA, "device error flags 0x%x", e);
+    return device_error(h, e);
   }
   return KB_OK;
 }

@@ -31,7 +31,26 @@ namespace kb {
 constexpr int KC = 8;  // orbits per chunk (innermost dimension)
 
 // device error bits (per handle)
-enum : int { DEVERR_TIMEOUT = 1, DEVERR_SMEM = 2, DEVERR_GEOM = 4 };
+enum : int { DEVERR_TIMEOUT = 1, DEVERR_SMEM = 2, DEVERR_GEOM = 4, DEVERR_BOUNDS = 8 };
+// sites of the bounds checks of KB_DEBUG builds, bits 8.. of the error word
+enum : int {
+  DCHK_SUN_ROW = 1 << 8,     // sunset: t' outside [tmin, t-1] or its slot outside the ring
+  DCHK_SUN_SIGMA = 1 << 9,   // sunset: Sigma ring index outside [0, nchunks Malloc KC)
+  DCHK_MI_TILE = 1 << 10,    // memory integrals: time tile or Sigma slot outside the ring
+  DCHK_MI_ROW = 1 << 11,     // memory integrals: row / column outside the window
+  DCHK_LF_WRITE = 1 << 12,   // leapfrog: history or state-row write outside the ring
+  DCHK_FIN = 1 << 13         // finishing kernel of a split step: item outside the window
+};
+
+// KB_DEBUG builds check ring, tile and Sigma indices on the device: a failed
+// check ORs DEVERR_BOUNDS and its site into the handle's error word (RunDev.err)
+// and the caller skips the access. Nothing traps; release builds compile the
+// checks away (KB_DCHECK is true).
+#ifdef KB_DEBUG
+#define KB_DCHECK(cond, errp, site) (::kb::dcheck((cond), (errp), (site)))
+#else
+#define KB_DCHECK(cond, errp, site) (true)
+#endif
 
 struct RunDev {
   int Ns, H, S, nchunks;
@@ -69,7 +88,15 @@ struct RunDev {
   // tensor maps (CUtensorMap, 64-byte aligned, device memory) of hist_F and hist_r
   // as [tiles][T rows][T KC]: a tile is one box; null when the CUDA driver has no encoder
   const void *tmap;
+  int *err;  // the handle's device error word (timeouts; bounds checks of KB_DEBUG builds)
 };
+
+#ifdef KB_DEBUG
+__device__ inline bool dcheck(bool ok, int *err, int site) {
+  if (!ok && err) atomicOr(err, DEVERR_BOUNDS | site);
+  return ok;
+}
+#endif
 
 // perturbative expansions (kb2pi.h): 0 LambdaLO, 1 LambdaNLO, 2 LambdaNLOclassical,
 // 3 NinverseLO, 4 NinverseNLO

@@ -215,6 +215,56 @@ struct Vec<double, 1> {
   __device__ __forceinline__ void add(const Vec &o) { v += o.v; }
 };
 
+// Tile partial sums of the consumers. FP32 history: compensated (Kahan) sums of
+// packed pairs -- s is the running FP32 sum, m minus its compensation, so that each
+// addition's rounding error is carried in m and s + m (formed in FP64) is the
+// partial sum; four packed operations per term (fma, add, sub, sub) against one.
+// FP64 history: plain FP64 sums.
+template <typename TS, int OPT>
+struct Acc;
+template <>
+struct Acc<float, 2> {
+  unsigned long long s, m;
+  __device__ __forceinline__ static Acc zero() { return Acc{0ull, 0ull}; }
+  __device__ __forceinline__ static unsigned long long bits(const Vec<float, 2> &a) {
+    return *reinterpret_cast<const unsigned long long *>(&a.v);
+  }
+  // one compensated step with the term y already formed
+  __device__ __forceinline__ void step(unsigned long long y) {
+    unsigned long long t, u;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(t) : "l"(s), "l"(y));
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(u) : "l"(t), "l"(s));
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(m) : "l"(y), "l"(u));
+    s = t;
+  }
+  // s + m += a * b: the product and the previous compensation in one fma
+  __device__ __forceinline__ void fma(const Vec<float, 2> &a, const Vec<float, 2> &b) {
+    unsigned long long y;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(y) : "l"(bits(a)), "l"(bits(b)), "l"(m));
+    step(y);
+  }
+  // s + m += o.s + o.m: both parts of o, one compensated step each
+  __device__ __forceinline__ void add(const Acc &o) {
+    unsigned long long y;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(y) : "l"(o.s), "l"(m));
+    step(y);
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(y) : "l"(o.m), "l"(m));
+    step(y);
+  }
+  __device__ __forceinline__ double get(int i) const {
+    const float2 a = *reinterpret_cast<const float2 *>(&s), b = *reinterpret_cast<const float2 *>(&m);
+    return i == 0 ? (double)a.x + (double)b.x : (double)a.y + (double)b.y;
+  }
+};
+template <>
+struct Acc<double, 1> {
+  Vec<double, 1> a;
+  __device__ __forceinline__ static Acc zero() { return Acc{Vec<double, 1>::zero()}; }
+  __device__ __forceinline__ void fma(const Vec<double, 1> &x, const Vec<double, 1> &y) { a.fma(x, y); }
+  __device__ __forceinline__ void add(const Acc &o) { a.add(o.a); }
+  __device__ __forceinline__ double get(int i) const { return a.get(i); }
+};
+
 template <typename TS, int T_, int NST_, int OPT_>
 struct Cfg {
   static constexpr int T = T_;
@@ -290,6 +340,10 @@ __device__ __forceinline__ void issue_tile(int stage, int I, int J, const RunDev
   const TS *hR = reinterpret_cast<const TS *>(R.hist_r);
   if (lane == 0) {
     constexpr int T = C::T;
+    (void)KB_DCHECK(I >= J && J * T <= tlast && I * T <= tlast && (I + 1) * T - 1 >= tmin && c >= 0 &&
+                        c < R.nchunks && (I - J) * T < R.M + T && R.Malloc % T == 0 && sa0 + T <= R.Malloc &&
+                        sb0 + T <= R.Malloc,
+                    R.err, DCHK_MI_TILE);
     if (use_tmap) {
       int r0, x0;
       tile_box<C>(I, J, tmin, tlast, r0, x0);
@@ -414,6 +468,9 @@ __device__ __forceinline__ void leapfrog_column(const RunDev &R, int c, int t, i
   double *RNrow = R.st_r + (size_t)(t % 3) * st_row + cs;
   TS *hF = reinterpret_cast<TS *>(R.hist_F);
   TS *hR = reinterpret_cast<TS *>(R.hist_r);
+  if (!KB_DCHECK(b >= tmin && b <= t - 1 && t - b < R.M && c >= 0 && c < R.nchunks && j0 >= 0 && j0 + OPT <= KC,
+                 R.err, DCHK_LF_WRITE))
+    return;
   for (int o = 0; o < OPT; ++o) {
     const int j = j0 + o;
     const int k = c * KC + j;
@@ -504,6 +561,7 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
               const int *__restrict__ d_t, int *__restrict__ d_err, int measure, int nwhole, int use_maps) {
   using C = Cfg<TS, T, NST, OPT>;
   using V = Vec<TS, OPT>;
+  using A = Acc<TS, OPT>;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   TS *stages = reinterpret_cast<TS *>(smem_raw);
   uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw + (size_t)NST * C::STAGE_BYTES);
@@ -725,7 +783,7 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
           int lo = max(b, tmin) - I * T, hi = min(T - 1, t - 1 - I * T);
           if (!bvalid) hi = -1;
           lo = max(lo, 0);
-          V cF0 = V::zero(), cF1 = V::zero(), cR0 = V::zero(), cR1 = V::zero();
+          A cF0 = A::zero(), cF1 = A::zero(), cR0 = A::zero(), cR1 = A::zero();
           // column loc of row rr sits at swizzled position loc ^ (rr & 3)
           auto el = [&](int rr) { return rr * C::RS + (loc ^ (rr & 3)) * KC + j0; };
           const TS *xb = xr_row + j0;
@@ -763,6 +821,7 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
           // row sums over the valid columns b of the tile: b in [tmin, a-1]; row a = I*T + loc
           const int a = I * T + loc;
           const bool av = (a >= tmin) && (a <= t - 1);
+          (void)KB_DCHECK(!use_tmem || ((I * T) % Ma) / T * OPT * 2 + OPT * 2 <= (int)TMEM_COLS, R.err, DCHK_MI_ROW);
           double *racc = rowacc + (size_t)(a % Ma) * KC + j0;
           double prev[OPT];
           int an = -1;
@@ -778,7 +837,7 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
           }
           int lo = max(0, tmin - J * T), hi = min(T - 1, a - 1 - J * T);
           if (!av) hi = -1;
-          V s0 = V::zero(), s1 = V::zero();
+          A s0 = A::zero(), s1 = A::zero();
           // column bb of row loc sits at swizzled position bb ^ (loc & 3)
           const int sw = loc & 3;
           const TS *fr = tF + loc * C::RS + j0;
@@ -984,6 +1043,7 @@ memint_finish_kernel(const RunDev *__restrict__ runs, const int *__restrict__ ba
     const int q = blk * FIN_TP * KC + u * FIN_THREADS + tid;
     if (q >= nq) break;
     const int b = tmin + q / KC;
+    if (!KB_DCHECK(b >= tmin && b <= t - 1 && t - b < R.M && c >= 0 && c < R.nchunks, R.err, DCHK_FIN)) break;
     const size_t e = cs + (size_t)(b % Ma) * KC + j;
     const double Fn = fma(c2, f1[u], -fma(aF[u], dt3, f2[u]));
     const double rn = (b == t - 1) ? R.dt : fma(c2, r1[u], -fma(aR[u], dt3, r2[u]));

@@ -463,6 +463,9 @@ sunset_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
       const int tp = tmin + (w - R.cta_base_sun) * nrow + gi;
       if (tp > t - 1) break;  // rows of an item are consecutive: the rest are past the window too
       const int slot = tp % R.Malloc;
+      // (uniform over the CTA: the skip passes no barrier another thread waits at)
+      if (!KB_DCHECK(tp >= tmin && t - 1 - tp < R.M && slot >= 0 && S <= R.nchunks * KC, R.err, DCHK_SUN_ROW))
+        continue;
       // row (t-1, t') of a history ring (the storage-type copy of the state row;
       // chunks are Malloc^2 KC apart) into shared memory, orbit layout
       const size_t hbase = hist_off(R.Malloc, R.T, 0, t - 1, tp, 0);
@@ -532,7 +535,9 @@ sunset_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
       TS *sigF = reinterpret_cast<TS *>(R.sig_F) + (size_t)slot * KC;
       const TC fr = (TC)R.fac_r, fF = (TC)R.fac_F;
       auto flush = [&](TS *sig, TC f) {
-        for (int o = tid; o < S; o += nthr) sig[gidx(o)] = (TS)(f * c.R2[o]);
+        for (int o = tid; o < S; o += nthr)
+          if (KB_DCHECK((size_t)slot * KC + gidx(o) < (size_t)R.nchunks * rowstride, R.err, DCHK_SUN_SIGMA))
+            sig[gidx(o)] = (TS)(f * c.R2[o]);
       };
       const TC *gr = c.R2;
       // expand reads R2 into R1 before pass 1 overwrites R2

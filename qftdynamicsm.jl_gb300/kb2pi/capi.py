@@ -12,7 +12,9 @@ import threading
 
 import numpy as np
 
-LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libkb2pi.so")
+# KB2PI_LIB selects another build of the library (e.g. libkb2pi_debug.so, the
+# build with device-side bounds checks) for the whole process
+LIB_PATH = os.environ.get("KB2PI_LIB") or os.path.join(os.path.dirname(os.path.abspath(__file__)), "libkb2pi.so")
 
 KB_OK = 0
 KB_ERR = {

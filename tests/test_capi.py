@@ -53,6 +53,16 @@ def test_library_exports_all_symbols():
         assert ctypes.cast(getattr(lib, name), ctypes.c_void_p).value
 
 
+def test_debug_library_exports_all_symbols():
+    """libkb2pi_debug.so (the KB_DEBUG build with device-side bounds checks) is built
+    by __graft_entry__.build() next to the release library and has the same ABI."""
+    path = os.path.join(ROOT, "qftdynamicsm.jl_gb300", "kb2pi", "libkb2pi_debug.so")
+    assert os.path.exists(path)
+    lib = ctypes.CDLL(path)
+    for name in declared_symbols():
+        assert ctypes.cast(getattr(lib, name), ctypes.c_void_p).value, name
+
+
 def test_create_rejects_bad_parameters_without_touching_a_gpu():
     from kb2pi import capi
 

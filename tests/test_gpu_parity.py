@@ -548,3 +548,38 @@ def test_ninverse_mixed_precision_is_rejected():
 
     with pytest.raises(capi.KbError, match="1/N"):
         make_gpu(dict(Ns=6, M=8, dt=0.1, lam=2.0, pexp=4), precision=1)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_nan_in_one_run_stays_in_that_run(precision):
+    """Host-side fault injection: a NaN in one run's initial occupation surfaces as
+    KB_ERR_NAN from that run's measurement alone; the other runs of the batch are
+    bitwise those of the same batch without the NaN."""
+    from kb2pi import capi
+
+    runs = [dict(Ns=8, M=9, lam=2.0, T=1.5), dict(Ns=6, M=7, lam=3.0, T=2.0), dict(Ns=8, M=12, lam=1.5, T=1.0)]
+
+    def batch(poison):
+        ps = [capi.KbParams(Ns=c["Ns"], sdim=3, M=c["M"], N=4, pexp=1, precision=precision, device=0, flags=0,
+                            dt=0.1, lam=c["lam"], mass2=1.0, mass=1.0) for c in runs]
+        h = capi.Handle(ps)
+        for r, c in enumerate(runs):
+            _, k2, _ = h.orbits(r)
+            n = occupation(c, k2)
+            if poison and r == 1:
+                n[3] = np.nan
+            h.init(r, n, 1.0)
+        h.steps(3, 16, 0)
+        return h
+
+    clean, bad = batch(False), batch(True)
+    t = 18
+    with pytest.raises(capi.KbError) as ei:
+        bad.measure(1, t)
+    assert ei.value.code == -4  # KB_ERR_NAN
+    for r in (0, 2):
+        a, b = clean.measure(r, t), bad.measure(r, t)
+        assert a["E"] == b["E"] and np.array_equal(a["n"], b["n"])
+        assert np.array_equal(clean.get(r, 0, t, t - 3), bad.get(r, 0, t, t - 3))
+    clean.close()
+    bad.close()
