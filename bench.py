@@ -184,6 +184,23 @@ def init_and_fill(h):
     return CFG["M"]
 
 
+def sample_rows(h, t):
+    """F(t, t') and rho(t, t') of run 0 at a few t' across the window (host copies)."""
+    tmin, _ = h.window(0)
+    tps = [tp for tp in (t, t - 1, t - 10, t - 100, t - 500, tmin) if tp >= tmin]
+    return [np.array([h.get(0, w, t, tp) for tp in tps]) for w in (0, 1)]
+
+
+def rows_rel_err(a, b):
+    """max over rows of max|a - b| / max|b| (rows whose reference is zero, rho(t,t), skipped)."""
+    worst = 0.0
+    for x, y in zip(a, b):
+        m = float(np.max(np.abs(y)))
+        if m > 0.0:
+            worst = max(worst, float(np.max(np.abs(x - y))) / m)
+    return worst
+
+
 def timed_steps(h, t0, K, stream_ptr):
     import torch
 
@@ -561,6 +578,7 @@ def run_ours(args):
     S = h.S[0]
     t = init_and_fill(h)
     meas_mixed = h.measure(0, t)
+    rows_mixed = sample_rows(h, t)
     tuning = apply_tuning(h, args)
     for i in range(args.warmup):
         h.step(t + 1 + i)
@@ -611,6 +629,7 @@ def run_ours(args):
         h64 = make_handle(capi.KB_PREC_FP64, dev)
         t64 = init_and_fill(h64)
         meas64 = h64.measure(0, t64)
+        rows64 = sample_rows(h64, t64)
         tuning64 = apply_tuning(h64, args, fp64=True)
         for i in range(min(args.warmup, 3)):
             h64.step(t64 + 1 + i)
@@ -629,7 +648,10 @@ def run_ours(args):
                 "mixed_vs_fp64_rel_err": {
                     "n": float(np.max(np.abs(meas_mixed["n"] - nn)) / np.max(np.abs(nn))),
                     "E": abs(meas_mixed["E"] - meas64["E"]) / abs(meas64["E"]),
-                    "at_t": t64 - min(args.warmup, 3)}}
+                    "F": rows_rel_err(rows_mixed[0], rows64[0]), "rho": rows_rel_err(rows_mixed[1], rows64[1]),
+                    "at_t": t64 - min(args.warmup, 3),
+                    "rows": "F(t,t'), rho(t,t') at t' = t, t-1, t-10, t-100, t-500, tmin; each row's error "
+                            "normalised by its max"}}
 
     if rank != 0:
         return 0
