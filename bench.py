@@ -620,6 +620,19 @@ def run_ours(args):
     e2e_s = max_over_ranks(ws, e2e_s)
     e2e_val = ws * args.steps / e2e_s
     d2h = 5 * S * 8 + (4 * ((S + 7) // 8)) * 8  # per-orbit arrays + energy partials
+
+    # the same steps with Kahan-compensated FP32 tile sums in the memory integrals
+    comp = None
+    if tuning.get("memint_variant") == 2:
+        h.set_tuning(memint_compensated=1)
+        for i in range(2):
+            h.step(t + 1 + i)
+        t += 2
+        cms = timed_steps(h, t + 1, args.steps, stream)
+        t += args.steps
+        h.set_tuning(memint_compensated=0)
+        comp = {"steps_per_s": args.steps / (cms / 1000.0), "ms_per_step": cms / args.steps,
+                "what": "memint_compensated = 1 (Kahan sums of the FP32 tile partials), same tuning otherwise"}
     h.close()
     del h
 
@@ -709,6 +722,7 @@ def run_ours(args):
         # per timed step: set_t_kernel, sunset_kernel, memint_kernel (+ memint_finish_kernel when split)
         "gpu_launches": (4 if split else 3) * args.steps,
         "fp64_plain": fp64,
+        "compensated_sums": comp,
         "speedup_mixed_vs_fp64": (value / fp64["steps_per_s"]) if fp64 else None,
     }
     if ws == 1 and not args.no_cpu:

@@ -211,7 +211,11 @@ typedef struct kb_tuning {
   int32_t test_no_tiles;  /* test hook, 0 in use: 1 makes the memory-integral producer issue no tiles,
                            * so every consumer's bounded wait runs out (about 2 s) and the step ends
                            * with KB_ERR_TIMEOUT at the next kb_sync, the device still usable */
-  int32_t reserved[1];
+  int32_t memint_compensated; /* KB_PREC_MIXED with memint_variant 2: 1 = the FP32 partial sums of each
+                               * history tile are compensated (Kahan: four FP32 operations per term
+                               * instead of one fma) before they join the FP64 accumulators; 0
+                               * (default) plain FP32 tile partials of at most 32 terms. Kept by
+                               * kb_autotune, which then times memint_variant 2 only */
 } kb_tuning;
 int kb_get_tuning(const kb_handle *h, kb_tuning *out);
 int kb_set_tuning(kb_handle *h, const kb_tuning *in);

@@ -74,6 +74,7 @@ struct kb_handle {
   size_t smem_sun = 0, smem_mi = 0;
   int num_sms = 0, grid_sun = 0, grid_sun_max = 0;
   int memint_variant = 0;         // FP32 consumer layout of the memory-integral kernel
+  int memint_compensated = 0;     // FP32 with variant 2: Kahan-compensated tile partial sums
   int memint_bulk = 0;            // 1: history tiles by bulk copies instead of tensor-map boxes
   int test_no_tiles = 0;          // test hook: the memint producer issues no tiles (waits run out)
   int memint_split = 0;           // 1: two half-triangle CTAs per chunk and a finishing kernel;
@@ -308,6 +309,12 @@ struct NvtxRange {
   NvtxRange(const NvtxRange &) = delete;
   NvtxRange &operator=(const NvtxRange &) = delete;
 };
+
+// the memory-integral kernel of the handle's tuning (launch_memint: variant 3 is
+// variant 2 with compensated tile sums)
+static int memint_launch_variant(const kb_handle *h) {
+  return (!h->fp64 && h->memint_variant == 2 && h->memint_compensated) ? 3 : h->memint_variant;
+}
 
 // message of a non-zero device error word
 static int device_error(kb_handle *h, int e) {
@@ -722,7 +729,7 @@ static int launch_step(kb_handle *h, int measure) {
     KB_CUDA(h, cudaEventRecord(e1, h->st));
     if (h->any_nlo || h->any_ninv) h->ev_pending.push_back({0, {e0, e1}});
   }
-  KB_CUDA(h, kb::launch_memint(h->fp64, h->memint_variant, h->memint_split, memint_nwhole(h), h->d_runs, h->d_base_mi,
+  KB_CUDA(h, kb::launch_memint(h->fp64, memint_launch_variant(h), h->memint_split, memint_nwhole(h), h->d_runs, h->d_base_mi,
                                    (int)h->runs.size(),
                                h->total_mi, h->fin_nb_max, !h->memint_bulk + 2 * h->test_no_tiles, h->d_t, h->d_err, measure, h->smem_mi, h->st));
   if (h->profiling) {
@@ -1272,6 +1279,7 @@ int kb_get_tuning(const kb_handle *h, kb_tuning *out) {
   if (!h || !out) return KB_ERR_PARAM;
   *out = kb_tuning{};
   out->memint_variant = h->memint_variant;
+  out->memint_compensated = h->memint_compensated;
   out->sunset_grid = h->grid_sun;
   out->batch_order = h->batch_order;
   out->sunset_variant = h->sunset_variant;
@@ -1303,12 +1311,17 @@ int kb_set_tuning(kb_handle *h, const kb_tuning *in) {
     return fail(h, KB_ERR_PARAM, "memint_bulk=%d: 0 (tensor-map boxes) or 1 (bulk copies)", in->memint_bulk);
   if (in->test_no_tiles < 0 || in->test_no_tiles > 1)
     return fail(h, KB_ERR_PARAM, "test_no_tiles=%d: 0 or 1", in->test_no_tiles);
+  if (in->memint_compensated < 0 || in->memint_compensated > 1 ||
+      (in->memint_compensated && (h->fp64 || in->memint_variant != 2)))
+    return fail(h, KB_ERR_PARAM, "memint_compensated=%d: 0 or 1, and 1 only with memint_variant 2 in KB_PREC_MIXED",
+                in->memint_compensated);
   cudaSetDevice(h->device);
   int rc = kb_sync(h);
   if (rc) return rc;
   if (in->batch_order != h->batch_order && apply_schedule(h, in->batch_order) != KB_OK)
     return fail(h, KB_ERR_CUDA, "upload of the run schedule failed");
   h->memint_variant = in->memint_variant;
+  h->memint_compensated = in->memint_compensated;
   h->memint_split = in->memint_split;
   h->memint_bulk = in->memint_bulk;
   h->test_no_tiles = in->test_no_tiles;
@@ -1345,7 +1358,7 @@ int kb_autotune(kb_handle *h, int32_t trials, kb_tuning *chosen, double *ms_per_
       KB_CUDA(h, cudaEventRecord(e[0], h->st));
       if ((rc = launch_self_energies(h))) return rc;
       KB_CUDA(h, cudaEventRecord(e[1], h->st));
-      KB_CUDA(h, kb::launch_memint(h->fp64, h->memint_variant, h->memint_split, memint_nwhole(h), h->d_runs, h->d_base_mi,
+      KB_CUDA(h, kb::launch_memint(h->fp64, memint_launch_variant(h), h->memint_split, memint_nwhole(h), h->d_runs, h->d_base_mi,
                                    (int)h->runs.size(),
                                    h->total_mi, h->fin_nb_max, !h->memint_bulk + 2 * h->test_no_tiles, h->d_t, h->d_err, 1, h->smem_mi, h->st));
       KB_CUDA(h, cudaEventRecord(e[2], h->st));
@@ -1375,10 +1388,12 @@ int kb_autotune(kb_handle *h, int32_t trials, kb_tuning *chosen, double *ms_per_
   }
   if (sun_cands.empty()) sun_cands.push_back({h->sunset_variant, h->grid_sun});
   const int norder = h->runs.size() > 1 ? 2 : 1;
-  const int v0 = h->fp64 ? 0 : 1;  // the one-kernel FP64 or the two-group FP32 memint, whole chunks, first
+  // the one-kernel FP64 or the two-group FP32 memint, whole chunks, first; compensated
+  // tile sums exist for the leapfrog-warp kernel only, so with them it is the one timed
+  const int v0 = h->fp64 ? 0 : (h->memint_compensated ? 2 : 1);
   std::vector<std::pair<int, int>> mi_cands = {{v0, 1}};  // (variant, split) after (v0, 0)
   if (h->total_mi > h->num_sms && h->total_mi % h->num_sms) mi_cands.push_back({v0, 2});
-  if (!h->fp64) {
+  if (!h->fp64 && !h->memint_compensated) {
     mi_cands.push_back({0, 0});
     // whole chunks with their leapfrog on the leapfrog warps: alone, or for the whole waves
     mi_cands.push_back({2, 0});

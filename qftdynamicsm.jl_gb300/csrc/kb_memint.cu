@@ -27,6 +27,7 @@
 // whole step needs no grid barrier. In split mode two CTAs share a chunk's
 // triangle and memint_finish_kernel runs the leapfrog (memint_kernel below).
 #include <cstdio>
+#include <type_traits>
 
 #include "kb_internal.cuh"
 
@@ -215,11 +216,11 @@ struct Vec<double, 1> {
   __device__ __forceinline__ void add(const Vec &o) { v += o.v; }
 };
 
-// Tile partial sums of the consumers. FP32 history: compensated (Kahan) sums of
-// packed pairs -- s is the running FP32 sum, m minus its compensation, so that each
-// addition's rounding error is carried in m and s + m (formed in FP64) is the
-// partial sum; four packed operations per term (fma, add, sub, sub) against one.
-// FP64 history: plain FP64 sums.
+// Compensated tile partial sums of the consumers (memint_kernel<..., COMP = true>).
+// FP32 history: Kahan sums of packed pairs -- s is the running FP32 sum, m minus its
+// compensation, so that each addition's rounding error is carried in m and s + m
+// (formed in FP64) is the partial sum; four packed operations per term (fma, add,
+// sub, sub) against one. FP64 history: plain FP64 sums.
 template <typename TS, int OPT>
 struct Acc;
 template <>
@@ -255,6 +256,15 @@ struct Acc<float, 2> {
     const float2 a = *reinterpret_cast<const float2 *>(&s), b = *reinterpret_cast<const float2 *>(&m);
     return i == 0 ? (double)a.x + (double)b.x : (double)a.y + (double)b.y;
   }
+};
+// plain FP32 (or FP64) tile partial sums: one fma per term
+template <typename TS, int OPT>
+struct PlainAcc {
+  Vec<TS, OPT> a;
+  __device__ __forceinline__ static PlainAcc zero() { return PlainAcc{Vec<TS, OPT>::zero()}; }
+  __device__ __forceinline__ void fma(const Vec<TS, OPT> &x, const Vec<TS, OPT> &y) { a.fma(x, y); }
+  __device__ __forceinline__ void add(const PlainAcc &o) { a.add(o.a); }
+  __device__ __forceinline__ double get(int i) const { return a.get(i); }
 };
 template <>
 struct Acc<double, 1> {
@@ -555,13 +565,13 @@ __host__ __device__ inline int split_block(int J0, int Jn) {
 // streaming; leapfrog warp q reads the row sums from TMEM quadrant q, the lanes
 // the column group's warp q reads, and takes over that warp's columns and
 // orbits, so the arithmetic and its order are the column group's.
-template <typename TS, int T, int NST, int OPT, bool SPLIT, bool LFW = false>
+template <typename TS, int T, int NST, int OPT, bool SPLIT, bool LFW = false, bool COMP = false>
 __global__ void __launch_bounds__(2 * T * (KC / OPT) + 32 + (LFW ? T * (KC / OPT) : 0))
 memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int nruns,
               const int *__restrict__ d_t, int *__restrict__ d_err, int measure, int nwhole, int use_maps) {
   using C = Cfg<TS, T, NST, OPT>;
   using V = Vec<TS, OPT>;
-  using A = Acc<TS, OPT>;
+  using A = typename std::conditional<COMP, Acc<TS, OPT>, PlainAcc<TS, OPT>>::type;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   TS *stages = reinterpret_cast<TS *>(smem_raw);
   uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw + (size_t)NST * C::STAGE_BYTES);
@@ -1564,9 +1574,9 @@ int memint_tile(bool fp64) { return fp64 ? CfgF64::T : CfgF32::T; }
 size_t memint_smem_bytes(bool fp64, int Malloc, int variant) {
   (void)Malloc;
   if (fp64) return smem_fixed_bytes<CfgF64>();
-  return variant == 1   ? smem_fixed_bytes<CfgF32>()
-         : variant == 2 ? smem_fixed_bytes<CfgF32>() + LF_STAGE_BYTES
-                        : smem_fixed_bytes<CfgF32>() + BLK_COLBUF_BYTES;
+  return variant == 1                    ? smem_fixed_bytes<CfgF32>()
+         : (variant == 2 || variant == 3) ? smem_fixed_bytes<CfgF32>() + LF_STAGE_BYTES
+                                          : smem_fixed_bytes<CfgF32>() + BLK_COLBUF_BYTES;
 }
 
 cudaError_t configure_memint(bool fp64, size_t smem) {
@@ -1589,6 +1599,12 @@ cudaError_t configure_memint(bool fp64, size_t smem) {
   e = cudaFuncSetAttribute(memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT, true, true>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT, false, true, true>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT, true, true, true>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
   return cudaFuncSetAttribute(memint_blk_kernel<CfgF32::NST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)smem);
 }
@@ -1602,12 +1618,19 @@ cudaError_t launch_memint(bool fp64, int variant, int split, int nwhole, const R
   // and completed by the finishing kernel
   const int nsplit = total_ctas - nwhole;
   constexpr int NTHR_LF = CfgF32::NT + 32 + CfgF32::NG;  // consumers, producer, leapfrog warps
-  if (!fp64 && variant == 2) {  // leapfrog warps for the whole chunks
+  if (!fp64 && (variant == 2 || variant == 3)) {  // leapfrog warps for the whole chunks; 3: compensated sums
     if (split && nsplit > 0) {
-      memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT, true, true>
-          <<<nwhole + 2 * nsplit, NTHR_LF, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, nwhole, use_maps);
+      if (variant == 3)
+        memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT, true, true, true>
+            <<<nwhole + 2 * nsplit, NTHR_LF, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, nwhole, use_maps);
+      else
+        memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT, true, true>
+            <<<nwhole + 2 * nsplit, NTHR_LF, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, nwhole, use_maps);
       memint_finish_kernel<float><<<nsplit * fin_nb_max, FIN_THREADS, 0, st>>>(d_runs, d_base, nruns, fin_nb_max,
                                                                                nwhole, d_t, measure);
+    } else if (variant == 3) {
+      memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT, false, true, true>
+          <<<total_ctas, NTHR_LF, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, total_ctas, use_maps);
     } else {
       memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT, false, true>
           <<<total_ctas, NTHR_LF, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, total_ctas, use_maps);

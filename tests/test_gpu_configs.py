@@ -77,18 +77,22 @@ def compare(h, run, g, scal, nsnap, t, tol):
     return worst
 
 
-@pytest.mark.parametrize("precision", [0, 1])
-def test_config2_full_size(precision):
+@pytest.mark.parametrize("precision,compensated", [(0, 0), (1, 0), (1, 1)])
+def test_config2_full_size(precision, compensated):
+    """compensated = 1: the mixed path with Kahan-compensated FP32 tile sums."""
     g = load("c2_ns32_m400")
     Ns, M, N, lam, dt, _, steps = g["cfg"]
     cfg = dict(Ns=int(Ns), M=int(M), N=int(N), lam=float(lam), dt=float(dt))
     h = make_gpu(cfg, precision)
+    if compensated:
+        h.set_tuning(memint_variant=2, memint_compensated=1)
+        assert h.tuning()["memint_compensated"] == 1
     h.init(0, g["n0"], float(g["init_mass"]))
     scal, nsnap, t = evolve_recording(h, [0], int(steps), 50)
     assert t == 1002 and np.array_equal(g["n_t"], np.arange(52, 1003, 50))
     worst = compare(h, 0, g, scal[0], nsnap[0], t, TOL64)
     h.close()
-    print(f"\nconfig 2 {'FP64' if precision == 0 else 'mixed'} vs oracle: " +
+    print(f"\nconfig 2 {'FP64' if precision == 0 else 'mixed'}{' compensated' if compensated else ''} vs oracle: " +
           ", ".join(f"{k} {v:.2e}" for k, v in worst.items()))
     if precision == 0:
         for k, v in worst.items():
