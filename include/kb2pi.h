@@ -199,7 +199,8 @@ typedef struct kb_tuning {
   int32_t sunset_grid;    /* CTAs of the persistent sunset kernel; 0 = one per SM */
   int32_t batch_order;    /* batched handles: 0 runs in order, 1 costliest runs first in both grids */
   int32_t sunset_variant; /* KB_PREC_MIXED: 0 1024 threads per CTA, 1 512 threads (two CTAs per SM where
-                           * their shared memory fits); KB_PREC_FP64: 0 */
+                           * their shared memory fits), 2 tensor cores (tcgen05.mma kind::tf32 with
+                           * TF32 head/tail operands, Ns <= 78); KB_PREC_FP64: 0 */
   int32_t memint_split;   /* 1: each chunk's triangle of history tiles is streamed by two CTAs (equal
                            * halves by column blocks), then a finishing kernel adds their sums and runs
                            * the leapfrog; 2: the same for the chunks past the last whole wave of one

@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.dirname(HERE)
 OUT_DIR = os.path.join(PKG, "kb2pi")
 BUILD_DIR = os.path.join(PKG, "_build")
-SOURCES = ["kb_api.cu", "kb_sunset.cu", "kb_memint.cu", "kb_adjoint.cu"]
+SOURCES = ["kb_api.cu", "kb_sunset.cu", "kb_sunset_tc.cu", "kb_memint.cu", "kb_adjoint.cu"]
 HEADERS = ["kb_internal.cuh", os.path.join("..", "..", "include", "kb2pi.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--extended-lambda", "-Xcompiler", "-fPIC,-O2",

@@ -72,6 +72,7 @@ struct kb_handle {
   } mslot[2];
   int *d_t = nullptr, *d_err = nullptr;
   size_t smem_sun = 0, smem_mi = 0;
+  size_t smem_sun_tc = 0;  // tensor-core sunset (sunset_variant 2); 0 where it does not apply
   int num_sms = 0, grid_sun = 0, grid_sun_max = 0;
   int memint_variant = 0;         // FP32 consumer layout of the memory-integral kernel
   int memint_compensated = 0;     // FP32 with variant 2: Kahan-compensated tile partial sums
@@ -80,7 +81,8 @@ struct kb_handle {
   int memint_split = 0;           // 1: two half-triangle CTAs per chunk and a finishing kernel;
                                   // 2: the same for the chunks past the last whole wave only
   int batch_order = 0;            // order of the runs' CTA ranges in the batched grids
-  int sunset_variant = 0;         // FP32 sunset: 0 1024 threads per CTA, 1 512 threads (2 CTAs per SM)
+  int sunset_variant = 0;         // FP32 sunset: 0 1024 threads per CTA, 1 512 threads (2 CTAs per SM),
+                                  // 2 tensor cores (kb_sunset_tc.cu; one CTA per SM)
   void *sun_scratch = nullptr;    // FP64 cosine-transform intermediates, one slot per CTA
   size_t sun_scratch_stride = 0;  // elements per slot
   int t_cur = 0;      // last evolved (or initialised) step; window is [tmin(t_cur), t_cur]
@@ -367,6 +369,8 @@ int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out) {
   const int T = kb::memint_tile(h->fp64);
   h->runs.resize(nruns);
   size_t smem_sun = 0, smem_mi = 0;
+  size_t smem_tc = 0;      // tensor-core sunset (FP32 handles whose lattices it takes), 0 = not available
+  bool tc_ok = !h->fp64;
   int base_sun = 0, base_mi = 0;
   for (int r = 0; r < nruns; ++r) {
     Run &R = h->runs[r];
@@ -376,6 +380,11 @@ int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out) {
     R.Malloc = ((R.p.M + (R.p.flags & 0xffff) + T - 1) / T) * T;  // extra slots for kb_adjoint
     R.esz = h->fp64 ? 8 : 4;
     smem_sun = std::max(smem_sun, kb::sunset_smem_bytes(h->fp64, R.H));
+    if (kb::pexp_sunset(R.p.pexp)) {
+      const size_t b = kb::sunset_tc_smem_bytes(R.H);
+      if (b == 0) tc_ok = false;
+      smem_tc = std::max(smem_tc, b);
+    }
     smem_mi = std::max({smem_mi, kb::memint_smem_bytes(h->fp64, R.Malloc, 0), kb::memint_smem_bytes(h->fp64, R.Malloc, 1),
                         kb::memint_smem_bytes(h->fp64, R.Malloc, 2)});
     base_sun += R.p.M;
@@ -399,6 +408,8 @@ int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out) {
   h->smem_mi = smem_mi;
   int maxsm = 0;
   cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
+  // the tensor-core kernel also has static shared memory (mbarriers, TMEM slot)
+  h->smem_sun_tc = (tc_ok && smem_tc > 0 && smem_tc + kb::sunset_tc_static_bytes() <= (size_t)maxsm) ? smem_tc : 0;
   if ((int)smem_mi > maxsm || (int)smem_sun > maxsm || (int)h->smem_ninv > maxsm || (int)h->smem_nv > maxsm) {
     fail(nullptr, KB_ERR_PARAM, "shared memory need (%zu / %zu B) exceeds the device limit %d B", smem_sun, smem_mi, maxsm);
     kb_destroy(h);
@@ -518,6 +529,7 @@ int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out) {
   // the attribute is per kernel, shared by all handles: allow the device maximum
   cudaError_t e1 = kb::configure_sunset(h->fp64, (size_t)maxsm);
   cudaError_t e2 = kb::configure_memint(h->fp64, (size_t)maxsm);
+  if (e1 == cudaSuccess && !h->fp64) e1 = kb::configure_sunset_tc((size_t)maxsm);
   if (e1 != cudaSuccess || e2 != cudaSuccess) {
     fail(nullptr, KB_ERR_CUDA, "kernel configuration failed: %s", cudaGetErrorString(e1 != cudaSuccess ? e1 : e2));
     kb_destroy(h);
@@ -701,7 +713,10 @@ static int memint_nwhole(const kb_handle *h) {
 }
 
 static int launch_self_energies(kb_handle *h) {
-  if (h->any_nlo)
+  if (h->any_nlo && h->sunset_variant == 2)
+    KB_CUDA(h, kb::launch_sunset_tc(h->d_runs, h->d_base_sun, (int)h->runs.size(), h->total_sun,
+                                    std::min(h->grid_sun, h->num_sms), h->d_t, h->smem_sun_tc, h->st));
+  else if (h->any_nlo)
     KB_CUDA(h, kb::launch_sunset(h->fp64, h->sunset_variant, h->d_runs, h->d_base_sun, (int)h->runs.size(),
                                  h->total_sun, h->grid_sun, h->d_t, h->sun_scratch, h->sun_scratch_stride, h->smem_sun,
                                  h->st));
@@ -1297,8 +1312,10 @@ int kb_set_tuning(kb_handle *h, const kb_tuning *in) {
   if (g < 1 || g > h->grid_sun_max)
     return fail(h, KB_ERR_PARAM, "sunset_grid=%d: at most %d CTAs fit on this device", in->sunset_grid,
                 h->grid_sun_max);
-  if (in->sunset_variant < 0 || in->sunset_variant > 1 || (h->fp64 && in->sunset_variant != 0))
-    return fail(h, KB_ERR_PARAM, "sunset_variant=%d: 0 or 1, and 0 for KB_PREC_FP64", in->sunset_variant);
+  if (in->sunset_variant < 0 || in->sunset_variant > 2 || (h->fp64 && in->sunset_variant != 0))
+    return fail(h, KB_ERR_PARAM, "sunset_variant=%d: 0, 1 or 2, and 0 for KB_PREC_FP64", in->sunset_variant);
+  if (in->sunset_variant == 2 && h->smem_sun_tc == 0)
+    return fail(h, KB_ERR_PARAM, "sunset_variant=2: the tensor-core sunset takes Ns <= 78 and needs its shared memory");
   if (in->sunset_grid != 0 &&
       in->sunset_grid > h->num_sms * kb::sunset_max_ctas_per_sm(h->fp64, in->sunset_variant, h->smem_sun) * 4)
     return fail(h, KB_ERR_PARAM, "sunset_grid=%d: too large for this variant", in->sunset_grid);
@@ -1386,6 +1403,7 @@ int kb_autotune(kb_handle *h, int32_t trials, kb_tuning *chosen, double *ms_per_
       last = g;
     }
   }
+  if (!h->fp64 && h->smem_sun_tc) sun_cands.push_back({2, std::min(h->total_sun, h->num_sms)});  // tensor cores
   if (sun_cands.empty()) sun_cands.push_back({h->sunset_variant, h->grid_sun});
   const int norder = h->runs.size() > 1 ? 2 : 1;
   // the one-kernel FP64 or the two-group FP32 memint, whole chunks, first; compensated

@@ -131,6 +131,12 @@ cudaError_t launch_sunset(bool fp64, int variant, const RunDev *d_runs, const in
                           int total_rows, int grid, const int *d_t, void *scratch, size_t scratch_stride, size_t smem,
                           cudaStream_t st);
 size_t sunset_smem_bytes(bool fp64, int H);
+// tensor-core sunset of KB_PREC_MIXED (kb_sunset_tc.cu): sunset variant 2
+size_t sunset_tc_smem_bytes(int H);  // dynamic shared memory; 0 when H is beyond the kernel
+size_t sunset_tc_static_bytes();
+cudaError_t configure_sunset_tc(size_t max_block_smem);  // the device's per-block maximum
+cudaError_t launch_sunset_tc(const RunDev *d_runs, const int *d_base, int nruns, int total_rows, int grid,
+                             const int *d_t, size_t smem, cudaStream_t st);
 int sunset_rows_per_item(int H);  // FP32: t' rows per sunset item
 size_t sunset_scratch_elems(int H);
 int sunset_grid(bool fp64, int num_sms, int total_rows);

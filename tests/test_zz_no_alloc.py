@@ -12,7 +12,7 @@ import ctypes
 import numpy as np
 import pytest
 
-from kbtest_util import make_gpu, occupation, random_symmetric_row, rel
+from kbtest_util import make_gpu, make_oracle, occupation, random_symmetric_row, rel
 
 
 def _lib():
@@ -44,6 +44,7 @@ def test_noalloc_matches_kb_self_energies_twice(Ns, nrows, pexp):
     tmone = nrows
     cfg = dict(Ns=Ns, M=nrows + 4, dt=0.01, lam=lam, N=N, T=2.0, pexp=pexp)
     g = make_gpu(cfg)  # KB_PREC_FP64: the same sunset as the no-alloc variant
+    oracle = make_oracle(cfg)
     _, k2, _ = g.orbits(0)
     g.init(0, occupation(cfg, k2), 1.0)
     for t in range(3, 11):
@@ -78,4 +79,10 @@ def test_noalloc_matches_kb_self_energies_twice(Ns, nrows, pexp):
         assert np.all(np.isfinite(gotF)) and np.all(np.isfinite(gotr)), call
         assert rel(gotF, ref_F) <= 1e-12, call
         assert rel(gotr, ref_r) <= 1e-12, call
+        # and directly against the CPU FP64 oracle's sunset on a few of the same rows
+        for i in (0, tmone // 2, tmone - 1):
+            oF, orr = oracle.sunset_rows(Frows[i], rrows[i])
+            assert rel(gotF[i], oF) <= 1e-12, (call, i)
+            assert rel(gotr[i], orr) <= 1e-12 or np.max(np.abs(orr)) == 0.0, (call, i)
     g.close()
+    oracle.close()
