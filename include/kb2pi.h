@@ -167,7 +167,10 @@ int kb_steps_recorded(kb_handle *h, int32_t t0, int32_t count, int32_t measure_e
 
 /* Snapshot of the full state (history, self-energies, window) into a host
  * buffer and back; replaces the serialisation the reference could not do
- * ("Serialization broke because of pointers in simdata", G_SimulationArgs.jl:117). */
+ * ("Serialization broke because of pointers in simdata", G_SimulationArgs.jl:117).
+ * Restore refuses (KB_ERR_PARAM, nothing copied) a buffer shorter than
+ * kb_checkpoint_size, a damaged header, or a snapshot of a handle whose runs
+ * differ in Ns, M, N, pexp, precision or ring slots. */
 int kb_checkpoint_size(const kb_handle *h, size_t *bytes);
 int kb_checkpoint_save(kb_handle *h, void *host_buf, size_t bytes);
 int kb_checkpoint_restore(kb_handle *h, const void *host_buf, size_t bytes);

@@ -1217,7 +1217,28 @@ int kb_sync(kb_handle *h) {
 struct CkptHeader {
   uint64_t magic, bytes;
   int32_t nruns, t_cur, fp64, sigma_valid;
+  uint64_t shape;  // hash of every run's Ns, M, N, pexp and ring slots (ckpt_shape)
 };
+// runs of equal storage size can differ in M (the ring is rounded up to the tile) or
+// in N, pexp: the shape hash tells a checkpoint of another handle from this one's
+static uint64_t ckpt_shape(const kb_handle *h) {
+  uint64_t x = 1469598103934665603ull;  // FNV-1a over the fields
+  auto mix = [&](int64_t v) {
+    for (int b = 0; b < 8; ++b) {
+      x ^= (uint64_t)((v >> (8 * b)) & 0xff);
+      x *= 1099511628211ull;
+    }
+  };
+  for (const Run &R : h->runs) {
+    mix(R.p.Ns);
+    mix(R.p.M);
+    mix(R.p.N);
+    mix(R.p.pexp);
+    mix(R.p.flags & 0xffff);
+    mix(R.Malloc);
+  }
+  return x;
+}
 static const uint64_t kCkptMagic = 0x6b623270692d636bull;
 
 int kb_checkpoint_size(const kb_handle *h, size_t *bytes) {
@@ -1238,13 +1259,15 @@ static int ckpt_copy(kb_handle *h, char *host, size_t bytes, bool save) {
   cudaSetDevice(h->device);
   int rc = kb_sync(h);
   if (rc) return rc;
-  CkptHeader hd{kCkptMagic, need, (int32_t)h->runs.size(), h->t_cur, h->fp64 ? 1 : 0, h->sigma_valid ? 1 : 0};
+  CkptHeader hd{kCkptMagic, need, (int32_t)h->runs.size(), h->t_cur, h->fp64 ? 1 : 0, h->sigma_valid ? 1 : 0,
+                ckpt_shape(h)};
   if (save) {
     std::memcpy(host, &hd, sizeof hd);
   } else {
     CkptHeader in;
     std::memcpy(&in, host, sizeof in);
-    if (in.magic != kCkptMagic || in.bytes != need || in.nruns != hd.nruns || in.fp64 != hd.fp64)
+    if (in.magic != kCkptMagic || in.bytes != need || in.nruns != hd.nruns || in.fp64 != hd.fp64 ||
+        in.shape != hd.shape)
       return fail(h, KB_ERR_PARAM, "checkpoint does not match this handle");
     hd = in;
   }

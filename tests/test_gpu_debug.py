@@ -18,8 +18,9 @@ ROOT = os.path.dirname(HERE)
 DEBUG_LIB = os.path.join(ROOT, "qftdynamicsm.jl_gb300", "kb2pi", "libkb2pi_debug.so")
 
 CASES = [
-    # (runs, precision, memint_split): each run (Ns, M, lambda, T)
+    # (runs, precision, memint_split[, sunset_variant]): each run (Ns, M, lambda, T)
     ([(4, 3, 2.0, 1.5)], 0, 0),
+    ([(8, 9, 2.0, 1.5), (6, 5, 3.0, 2.0)], 1, 0, 2),  # the tensor-core sunset
     ([(6, 5, 3.0, 2.0)], 0, 1),
     ([(8, 10, 2.0, 1.0)], 1, 0),
     ([(8, 7, 4.0, 2.0)], 1, 1),
@@ -38,13 +39,15 @@ def run_cases():
     from kb2pi import capi
 
     out = []
-    for runs, prec, split in CASES:
+    for runs, prec, split, *sv in CASES:
         ps = [capi.KbParams(Ns=Ns, sdim=3, M=M, N=4, pexp=1, precision=prec, device=0, flags=0, dt=0.1, lam=lam,
                             mass2=1.0, mass=1.0) for Ns, M, lam, _ in runs]
         h = capi.Handle(ps)
         for r, (_, _, _, T) in enumerate(runs):
             _, k2, _ = h.orbits(r)
             h.init(r, 1.0 / (np.exp(np.sqrt(k2 + 1.0) / T) - 1.0), 1.0)
+        if sv:
+            h.set_tuning(sunset_variant=sv[0])
         h.steps(3, 4, 0)
         if split and prec == 1:
             h.set_tuning(memint_variant=2 if split == 2 else 1, memint_split=split)

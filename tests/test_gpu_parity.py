@@ -198,6 +198,43 @@ def test_checkpoint_roundtrip():
     assert np.array_equal(g.get(0, 0, 16, 10), row1)
 
 
+def test_bad_checkpoints_are_refused():
+    """Host-side faults on the checkpoint path: a buffer that is too small, one whose
+    header was damaged, and one taken from a handle of another shape are refused
+    with KB_ERR_PARAM before anything is copied; the handle then evolves on as if
+    nothing had happened."""
+    from kb2pi import capi
+
+    cfg = dict(Ns=8, M=9, dt=0.1, lam=2.0, T=2.0)
+    g = make_gpu(cfg)
+    _, k2, _ = g.orbits(0)
+    g.init(0, occupation(cfg, k2), 1.0)
+    for t in range(3, 12):
+        g.step(t)
+    good = g.checkpoint()
+    other = make_gpu(dict(cfg, M=10))
+    other.init(0, occupation(cfg, k2), 1.0)
+    for t in range(3, 6):
+        other.step(t)
+    wrong_shape = other.checkpoint()
+    other.close()
+    damaged = good.copy()
+    damaged[:8] ^= 0xFF
+    for buf in (good[:-64].copy(), damaged, wrong_shape):
+        with pytest.raises(capi.KbError) as ei:
+            g.restore(buf)
+        assert ei.value.code == -1
+    ref = make_gpu(cfg)
+    ref.init(0, occupation(cfg, k2), 1.0)
+    for t in range(3, 16):
+        ref.step(t)
+    for t in range(12, 16):
+        g.step(t)
+    assert g.measure(0, 15)["E"] == ref.measure(0, 15)["E"]
+    g.close()
+    ref.close()
+
+
 def test_errors_are_reported():
     from kb2pi import capi
 
