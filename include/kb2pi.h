@@ -220,6 +220,11 @@ typedef struct kb_tuning {
                                * instead of one fma) before they join the FP64 accumulators; 0
                                * (default) plain FP32 tile partials of at most 32 terms. Kept by
                                * kb_autotune, which then times memint_variant 2 only */
+  int32_t batch_overlap;      /* batches of two or more runs (no 1/N expansion): 0 (default) one
+                               * launch per kernel for all runs; n > 0 splits the runs into two
+                               * groups of about equal memory-integral work and runs the second
+                               * group's sunset on n CTAs, on a second stream, while the first
+                               * group's memory integrals stream (the same arithmetic per run) */
 } kb_tuning;
 int kb_get_tuning(const kb_handle *h, kb_tuning *out);
 int kb_set_tuning(kb_handle *h, const kb_tuning *in);

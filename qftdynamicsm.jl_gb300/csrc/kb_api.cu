@@ -81,6 +81,15 @@ struct kb_handle {
   int memint_split = 0;           // 1: two half-triangle CTAs per chunk and a finishing kernel;
                                   // 2: the same for the chunks past the last whole wave only
   int batch_order = 0;            // order of the runs' CTA ranges in the batched grids
+  // concurrent halves of a batch (kb_tuning.batch_overlap > 0): the runs split into two
+  // groups of about equal memory-integral work, each with its own schedule tables;
+  // group 1's sunset (batch_overlap CTAs) runs on a second, higher-priority stream
+  // beside group 0's memory integrals, then group 1's memory integrals follow there
+  int batch_overlap = 0;
+  int *d_grp_sun[2] = {nullptr, nullptr}, *d_grp_mi[2] = {nullptr, nullptr};
+  int grp_n[2] = {0, 0}, grp_sun[2] = {0, 0}, grp_mi[2] = {0, 0};
+  cudaStream_t st2 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int sunset_variant = 0;         // FP32 sunset: 0 1024 threads per CTA, 1 512 threads (2 CTAs per SM),
                                   // 2 tensor cores (kb_sunset_tc.cu; one CTA per SM)
   void *sun_scratch = nullptr;    // FP64 cosine-transform intermediates, one slot per CTA
@@ -276,28 +285,74 @@ static int apply_schedule(kb_handle *h, int order) {
     std::stable_sort(pos_mi.begin(), pos_mi.end(), [&](int a, int b) { return cost_mi(a) > cost_mi(b); });
     std::stable_sort(pos_sun.begin(), pos_sun.end(), [&](int a, int b) { return cost_sun(a) > cost_sun(b); });
   }
+  // group of every run: all in group 0, or (batch_overlap) each run, costliest memory
+  // integrals first, to the group with less such work so far
+  std::vector<int> grp(nr, 0);
+  if (h->batch_overlap > 0) {
+    auto cost_mi = [&](int r) {
+      const double nb = std::ceil((double)h->runs[r].p.M / h->runs[r].T) + 1;
+      return nb * (nb + 1) / 2 * h->runs[r].nchunks;
+    };
+    std::vector<int> by(nr);
+    for (int r = 0; r < nr; ++r) by[r] = r;
+    std::stable_sort(by.begin(), by.end(), [&](int a, int b) { return cost_mi(a) > cost_mi(b); });
+    double load[2] = {0.0, 0.0};
+    for (int r : by) {
+      const int g = load[0] <= load[1] ? 0 : 1;
+      grp[r] = g;
+      load[g] += cost_mi(r);
+    }
+  }
+  // one table pair per group; a run's CTA bases count from its group's first item
   std::vector<int> smi(2 * nr), ssun(2 * nr);
-  int bm = 0, bs = 0;
-  for (int q = 0; q < nr; ++q) {
-    Run &Rm = h->runs[pos_mi[q]];
-    smi[q] = bm;
-    smi[nr + q] = pos_mi[q];
-    Rm.dev.cta_base_mi = bm;
-    bm += Rm.nchunks;
-    Run &Rs = h->runs[pos_sun[q]];
-    ssun[q] = bs;
-    ssun[nr + q] = pos_sun[q];
-    Rs.dev.cta_base_sun = bs;
-    bs += (Rs.p.M + Rs.dev.sun_rows - 1) / Rs.dev.sun_rows;
+  std::vector<int> gsmi[2], gssun[2];
+  for (int g = 0; g < (h->batch_overlap > 0 ? 2 : 1); ++g) {
+    std::vector<int> qm, qs;
+    for (int q = 0; q < nr; ++q) {
+      if (grp[pos_mi[q]] == g) qm.push_back(pos_mi[q]);
+      if (grp[pos_sun[q]] == g) qs.push_back(pos_sun[q]);
+    }
+    const int n = (int)qm.size();
+    gsmi[g].assign(2 * n, 0);
+    gssun[g].assign(2 * n, 0);
+    int bm = 0, bs = 0;
+    for (int q = 0; q < n; ++q) {
+      Run &Rm = h->runs[qm[q]];
+      gsmi[g][q] = bm;
+      gsmi[g][n + q] = qm[q];
+      Rm.dev.cta_base_mi = bm;
+      bm += Rm.nchunks;
+      Run &Rs = h->runs[qs[q]];
+      gssun[g][q] = bs;
+      gssun[g][n + q] = qs[q];
+      Rs.dev.cta_base_sun = bs;
+      bs += (Rs.p.M + Rs.dev.sun_rows - 1) / Rs.dev.sun_rows;
+    }
+    h->grp_n[g] = n;
+    h->grp_mi[g] = bm;
+    h->grp_sun[g] = bs;
+  }
+  if (h->batch_overlap > 0) {
+    for (int g = 0; g < 2; ++g)
+      if (cudaMemcpy(h->d_grp_mi[g], gsmi[g].data(), sizeof(int) * gsmi[g].size(), cudaMemcpyHostToDevice) !=
+              cudaSuccess ||
+          cudaMemcpy(h->d_grp_sun[g], gssun[g].data(), sizeof(int) * gssun[g].size(), cudaMemcpyHostToDevice) !=
+              cudaSuccess)
+        return KB_ERR_CUDA;
+  } else {
+    smi = gsmi[0];
+    ssun = gssun[0];
   }
   std::vector<RunDev> devs(nr);
   for (int r = 0; r < nr; ++r) {
     h->runs[r].dev.err = h->d_err;
     devs[r] = h->runs[r].dev;
   }
-  if (cudaMemcpy(h->d_runs, devs.data(), sizeof(RunDev) * nr, cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemcpy(h->d_base_mi, smi.data(), sizeof(int) * 2 * nr, cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemcpy(h->d_base_sun, ssun.data(), sizeof(int) * 2 * nr, cudaMemcpyHostToDevice) != cudaSuccess)
+  if (cudaMemcpy(h->d_runs, devs.data(), sizeof(RunDev) * nr, cudaMemcpyHostToDevice) != cudaSuccess)
+    return KB_ERR_CUDA;
+  if (h->batch_overlap == 0 &&
+      (cudaMemcpy(h->d_base_mi, smi.data(), sizeof(int) * 2 * nr, cudaMemcpyHostToDevice) != cudaSuccess ||
+       cudaMemcpy(h->d_base_sun, ssun.data(), sizeof(int) * 2 * nr, cudaMemcpyHostToDevice) != cudaSuccess))
     return KB_ERR_CUDA;
   h->batch_order = order;
   return KB_OK;
@@ -311,6 +366,26 @@ struct NvtxRange {
   NvtxRange(const NvtxRange &) = delete;
   NvtxRange &operator=(const NvtxRange &) = delete;
 };
+
+// switch the concurrent-group step on (value = CTAs of group 1's sunset) or off and
+// upload the schedules for the given run order; the second stream (higher priority,
+// so its sunset CTAs take the SMs group 0's memory-integral CTAs free) and its two
+// events are created on first use
+static int set_overlap(kb_handle *h, int value, int order) {
+  if (value > 0 && !h->st2) {
+    int lo = 0, hi = 0;
+    cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    if (cudaStreamCreateWithPriority(&h->st2, cudaStreamNonBlocking, hi) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess)
+      return fail(h, KB_ERR_CUDA, "second stream for batch_overlap: %s", cudaGetErrorString(cudaGetLastError()));
+  }
+  if (value != h->batch_overlap || order != h->batch_order) {
+    h->batch_overlap = value;
+    if (apply_schedule(h, order) != KB_OK) return fail(h, KB_ERR_CUDA, "upload of the run schedule failed");
+  }
+  return KB_OK;
+}
 
 // the memory-integral kernel of the handle's tuning (launch_memint: variant 3 is
 // variant 2 with compensated tile sums)
@@ -510,7 +585,13 @@ int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out) {
   bool ok = cudaMalloc(&h->d_runs, sizeof(RunDev) * nruns) == cudaSuccess &&
             cudaMalloc(&h->d_base_sun, sizeof(int) * 2 * nruns) == cudaSuccess &&
             cudaMalloc(&h->d_base_mi, sizeof(int) * 2 * nruns) == cudaSuccess &&
+            cudaMalloc(&h->d_grp_sun[0], sizeof(int) * 8 * nruns) == cudaSuccess &&
+            cudaMalloc(&h->d_grp_mi[0], sizeof(int) * 8 * nruns) == cudaSuccess &&
             cudaMalloc(&h->d_t, sizeof(int)) == cudaSuccess && cudaMalloc(&h->d_err, sizeof(int)) == cudaSuccess;
+  if (ok) {  // the second group's tables follow the first's
+    h->d_grp_sun[1] = h->d_grp_sun[0] + 4 * nruns;
+    h->d_grp_mi[1] = h->d_grp_mi[0] + 4 * nruns;
+  }
   if (!ok) {
     cudaGetLastError();
     fail(nullptr, KB_ERR_OOM, "cudaMalloc of the run table failed");
@@ -585,9 +666,13 @@ void kb_destroy(kb_handle *h) {
     if (m.host) cudaFreeHost(m.host);
   }
   for (auto &R : h->runs) free_run(R);
-  void *ptrs[] = {h->d_runs, h->d_base_sun, h->d_base_mi, h->d_t, h->d_err, h->sun_scratch};
+  void *ptrs[] = {h->d_runs, h->d_base_sun, h->d_base_mi, h->d_grp_sun[0], h->d_grp_mi[0], h->d_t, h->d_err,
+                  h->sun_scratch};
   for (void *q : ptrs)
     if (q) cudaFree(q);
+  if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+  if (h->ev_join) cudaEventDestroy(h->ev_join);
+  if (h->st2) cudaStreamDestroy(h->st2);
   if (h->st) cudaStreamDestroy(h->st);
   delete h;
 }
@@ -712,18 +797,66 @@ static int memint_nwhole(const kb_handle *h) {
   return (h->total_mi / h->num_sms) * h->num_sms;
 }
 
+// the sunset of the runs of one schedule table (all runs, or one group)
+static int launch_sun(kb_handle *h, const int *base, int n, int total, int grid, cudaStream_t st) {
+  if (!h->any_nlo || total <= 0) return KB_OK;
+  grid = std::max(1, std::min(grid, total));
+  if (h->sunset_variant == 2)
+    KB_CUDA(h, kb::launch_sunset_tc(h->d_runs, base, n, total, std::min(grid, h->num_sms), h->d_t, h->smem_sun_tc,
+                                    st));
+  else
+    KB_CUDA(h, kb::launch_sunset(h->fp64, h->sunset_variant, h->d_runs, base, n, total, grid, h->d_t,
+                                 h->sun_scratch, h->sun_scratch_stride, h->smem_sun, st));
+  return KB_OK;
+}
+// the memory integrals of the runs of one schedule table
+static int launch_mi(kb_handle *h, const int *base, int n, int total, int measure, cudaStream_t st) {
+  const int nwhole = h->memint_split == 2 ? (total / h->num_sms) * h->num_sms : 0;
+  KB_CUDA(h, kb::launch_memint(h->fp64, memint_launch_variant(h), h->memint_split, nwhole, h->d_runs, base, n, total,
+                               h->fin_nb_max, !h->memint_bulk + 2 * h->test_no_tiles, h->d_t, h->d_err, measure,
+                               h->smem_mi, st));
+  return KB_OK;
+}
+
 static int launch_self_energies(kb_handle *h) {
-  if (h->any_nlo && h->sunset_variant == 2)
-    KB_CUDA(h, kb::launch_sunset_tc(h->d_runs, h->d_base_sun, (int)h->runs.size(), h->total_sun,
-                                    std::min(h->grid_sun, h->num_sms), h->d_t, h->smem_sun_tc, h->st));
-  else if (h->any_nlo)
-    KB_CUDA(h, kb::launch_sunset(h->fp64, h->sunset_variant, h->d_runs, h->d_base_sun, (int)h->runs.size(),
-                                 h->total_sun, h->grid_sun, h->d_t, h->sun_scratch, h->sun_scratch_stride, h->smem_sun,
-                                 h->st));
+  if (h->batch_overlap > 0) {  // both groups in turn (kb_self_energies, autotuning)
+    for (int g = 0; g < 2; ++g) {
+      const int rc = launch_sun(h, h->d_grp_sun[g], h->grp_n[g], h->grp_sun[g], h->grid_sun, h->st);
+      if (rc) return rc;
+    }
+    return KB_OK;
+  }
+  if (h->any_nlo) {
+    const int rc = launch_sun(h, h->d_base_sun, (int)h->runs.size(), h->total_sun, h->grid_sun, h->st);
+    if (rc) return rc;
+  }
   if (h->any_ninv)
     KB_CUDA(h, kb::launch_ninv(h->d_runs, h->d_base_sun, h->d_base_mi, (int)h->runs.size(), h->total_sun, h->total_mi,
                                std::min(h->grid_sun, h->grid_sun_max), h->d_t, h->sun_scratch, h->sun_scratch_stride,
                                h->smem_ninv, h->smem_nv, h->st));
+  return KB_OK;
+}
+
+// a step of a batch in two concurrent groups: group 0's sunset on the handle's
+// stream; then group 0's memory integrals there while group 1's sunset (on
+// batch_overlap CTAs) and memory integrals run on the second stream; joined at the end
+static int launch_step_overlap(kb_handle *h, int measure, cudaEvent_t e0, cudaEvent_t e1, cudaEvent_t e2) {
+  if (e0) KB_CUDA(h, cudaEventRecord(e0, h->st));
+  int rc = launch_sun(h, h->d_grp_sun[0], h->grp_n[0], h->grp_sun[0], h->grid_sun, h->st);
+  if (rc) return rc;
+  if (e1) KB_CUDA(h, cudaEventRecord(e1, h->st));
+  KB_CUDA(h, cudaEventRecord(h->ev_fork, h->st));
+  KB_CUDA(h, cudaStreamWaitEvent(h->st2, h->ev_fork, 0));
+  if ((rc = launch_sun(h, h->d_grp_sun[1], h->grp_n[1], h->grp_sun[1], h->batch_overlap, h->st2))) return rc;
+  if ((rc = launch_mi(h, h->d_grp_mi[0], h->grp_n[0], h->grp_mi[0], measure, h->st))) return rc;
+  if ((rc = launch_mi(h, h->d_grp_mi[1], h->grp_n[1], h->grp_mi[1], measure, h->st2))) return rc;
+  KB_CUDA(h, cudaEventRecord(h->ev_join, h->st2));
+  KB_CUDA(h, cudaStreamWaitEvent(h->st, h->ev_join, 0));
+  if (e2) {
+    KB_CUDA(h, cudaEventRecord(e2, h->st));
+    h->ev_pending.push_back({0, {e0, e1}});  // group 0's sunset alone
+    h->ev_pending.push_back({1, {e1, e2}});  // the rest of the step
+  }
   return KB_OK;
 }
 
@@ -734,8 +867,9 @@ static int launch_step(kb_handle *h, int measure) {
     e1 = next_event(h);
     e2 = next_event(h);
     if (!e0 || !e1 || !e2) return fail(h, KB_ERR_CUDA, "cudaEventCreate failed");
-    KB_CUDA(h, cudaEventRecord(e0, h->st));
   }
+  if (h->batch_overlap > 0) return launch_step_overlap(h, measure, e0, e1, e2);
+  if (e0) KB_CUDA(h, cudaEventRecord(e0, h->st));
   {
     const int rc = launch_self_energies(h);
     if (rc) return rc;
@@ -1318,6 +1452,7 @@ int kb_get_tuning(const kb_handle *h, kb_tuning *out) {
   *out = kb_tuning{};
   out->memint_variant = h->memint_variant;
   out->memint_compensated = h->memint_compensated;
+  out->batch_overlap = h->batch_overlap;
   out->sunset_grid = h->grid_sun;
   out->batch_order = h->batch_order;
   out->sunset_variant = h->sunset_variant;
@@ -1355,11 +1490,16 @@ int kb_set_tuning(kb_handle *h, const kb_tuning *in) {
       (in->memint_compensated && (h->fp64 || in->memint_variant != 2)))
     return fail(h, KB_ERR_PARAM, "memint_compensated=%d: 0 or 1, and 1 only with memint_variant 2 in KB_PREC_MIXED",
                 in->memint_compensated);
+  if (in->batch_overlap < 0 || in->batch_overlap >= h->num_sms ||
+      (in->batch_overlap > 0 && (h->runs.size() < 2 || h->any_ninv)))
+    return fail(h, KB_ERR_PARAM,
+                "batch_overlap=%d: 0, or the CTAs (below the SM count %d) of the second group's sunset in a "
+                "batch of two or more runs without the 1/N expansion",
+                in->batch_overlap, h->num_sms);
   cudaSetDevice(h->device);
   int rc = kb_sync(h);
   if (rc) return rc;
-  if (in->batch_order != h->batch_order && apply_schedule(h, in->batch_order) != KB_OK)
-    return fail(h, KB_ERR_CUDA, "upload of the run schedule failed");
+  if ((rc = set_overlap(h, in->batch_overlap, in->batch_order))) return rc;
   h->memint_variant = in->memint_variant;
   h->memint_compensated = in->memint_compensated;
   h->memint_split = in->memint_split;
@@ -1385,6 +1525,9 @@ int kb_autotune(kb_handle *h, int32_t trials, kb_tuning *chosen, double *ms_per_
   int rc = kb_sync(h);
   if (rc) return rc;
   const int t = h->t_cur;
+  // the kernel candidates are timed on the one-launch schedule; the concurrent-group
+  // step of a batch is timed afterwards, on whole steps, with the chosen kernels
+  if ((rc = set_overlap(h, 0, h->batch_order))) return rc;
   cudaEvent_t e[3];
   for (auto &x : e) KB_CUDA(h, cudaEventCreate(&x));
   auto time_cfg = [&](int variant, int split, int svar, int grid, float *ms_sun, float *ms_mi) -> int {
@@ -1473,14 +1616,50 @@ int kb_autotune(kb_handle *h, int32_t trials, kb_tuning *chosen, double *ms_per_
       best_m_all = bm;
     }
   }
-  for (auto &x : e) cudaEventDestroy(x);
-  if (rc) return rc;
+  if (rc) {
+    for (auto &x : e) cudaEventDestroy(x);
+    return rc;
+  }
   if (best_o != h->batch_order && apply_schedule(h, best_o) != KB_OK)
     return fail(h, KB_ERR_CUDA, "upload of the run schedule failed");
   h->memint_variant = best_v;
   h->memint_split = best_split;
   h->sunset_variant = best_sc.first;
   h->grid_sun = best_sc.second;
+  // batches: whole steps without and with the concurrent groups (second group's sunset
+  // on a quarter, a third or half of the SMs)
+  if (h->runs.size() >= 2 && !h->any_ninv) {
+    int best_ov = 0;
+    float best_step = 1e30f;
+    const int cands[4] = {0, h->num_sms / 4, h->num_sms / 3, h->num_sms / 2};
+    for (int ov : cands) {
+      if (ov < 0 || (ov == 0 && best_step < 1e30f)) continue;
+      if ((rc = set_overlap(h, ov, best_o))) break;
+      float best = 1e30f;
+      for (int q = 0; q < trials && !rc; ++q) {
+        KB_CUDA(h, kb::launch_set_t(h->d_t, t, h->st));
+        KB_CUDA(h, cudaEventRecord(e[0], h->st));
+        if ((rc = launch_step(h, 1))) break;
+        KB_CUDA(h, cudaEventRecord(e[2], h->st));
+        KB_CUDA(h, cudaEventSynchronize(e[2]));
+        float a = 0;
+        KB_CUDA(h, cudaEventElapsedTime(&a, e[0], e[2]));
+        best = std::min(best, a);
+      }
+      if (rc) break;
+      if (best < best_step) {
+        best_step = best;
+        best_ov = ov;
+      }
+    }
+    if (!rc) rc = set_overlap(h, best_ov, best_o);
+    if (!rc && best_step < 1e30f) {
+      best_s_all = 0.0f;
+      best_m_all = best_step;
+    }
+  }
+  for (auto &x : e) cudaEventDestroy(x);
+  if (rc) return rc;
   if (h->graph) {
     cudaGraphExecDestroy(h->graph);
     h->graph = nullptr;

@@ -54,13 +54,14 @@ class KbMeasScalars(C.Structure):
 class KbTuning(C.Structure):
     _fields_ = [("memint_variant", C.c_int32), ("sunset_grid", C.c_int32), ("batch_order", C.c_int32),
                 ("sunset_variant", C.c_int32), ("memint_split", C.c_int32), ("memint_bulk", C.c_int32),
-                ("test_no_tiles", C.c_int32), ("memint_compensated", C.c_int32)]
+                ("test_no_tiles", C.c_int32), ("memint_compensated", C.c_int32), ("batch_overlap", C.c_int32)]
 
     def as_dict(self):
         return {"memint_variant": self.memint_variant, "sunset_grid": self.sunset_grid,
                 "batch_order": self.batch_order, "sunset_variant": self.sunset_variant,
                 "memint_split": self.memint_split, "memint_bulk": self.memint_bulk,
-                "test_no_tiles": self.test_no_tiles, "memint_compensated": self.memint_compensated}
+                "test_no_tiles": self.test_no_tiles, "memint_compensated": self.memint_compensated,
+                "batch_overlap": self.batch_overlap}
 
 
 class KbError(RuntimeError):
@@ -320,7 +321,8 @@ class Handle:
         return out.as_dict()
 
     def set_tuning(self, memint_variant=None, sunset_grid=None, batch_order=None, sunset_variant=None,
-                   memint_split=None, memint_bulk=None, test_no_tiles=None, memint_compensated=None):
+                   memint_split=None, memint_bulk=None, test_no_tiles=None, memint_compensated=None,
+                   batch_overlap=None):
         cur = KbTuning()
         self._check(self.lib.kb_get_tuning(self.h, C.byref(cur)))
         if memint_variant is not None:
@@ -339,6 +341,8 @@ class Handle:
             cur.test_no_tiles = int(test_no_tiles)
         if memint_compensated is not None:
             cur.memint_compensated = int(memint_compensated)
+        if batch_overlap is not None:
+            cur.batch_overlap = int(batch_overlap)
         self._check(self.lib.kb_set_tuning(self.h, C.byref(cur)))
 
     def autotune(self, trials=3):

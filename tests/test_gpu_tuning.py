@@ -375,3 +375,57 @@ def test_pipelined_timeout_is_reported_once(precision):
     assert timeouts == 1
     assert time.time() - t0 < 60
     h.close()
+
+
+@pytest.mark.parametrize("precision,split", [(0, 0), (1, 0), (1, 2)])
+def test_batch_overlap_is_bitwise_the_one_launch_step(precision, split):
+    """Concurrent groups (batch_overlap: the second group's sunset on its own stream
+    beside the first group's memory integrals) change which launch computes a run,
+    not how: every run is bitwise the same as with one launch per kernel, through
+    kb_step and the captured graph of kb_steps alike."""
+    from kb2pi import capi
+
+    cfgs = [dict(Ns=8, M=20, lam=2.0, T=1.0), dict(Ns=16, M=45, lam=4.0, T=2.0), dict(Ns=12, M=33, lam=1.0, T=0.7),
+            dict(Ns=6, M=9, lam=3.0, T=1.5), dict(Ns=10, M=27, lam=2.5, T=1.2)]
+    out = []
+    for ov in (0, 20, 76):
+        ps = [capi.KbParams(Ns=c["Ns"], sdim=3, M=c["M"], N=4, pexp=1, precision=precision, device=0, flags=0,
+                            dt=0.1, lam=c["lam"], mass2=1.0, mass=1.0) for c in cfgs]
+        h = capi.Handle(ps)
+        for r, c in enumerate(cfgs):
+            _, k2, _ = h.orbits(r)
+            h.init(r, occupation(dict(c), k2), 1.0)
+        h.set_tuning(batch_overlap=ov, memint_split=split)
+        assert h.tuning()["batch_overlap"] == ov
+        h.steps(3, 30, 0)
+        for t in range(33, 41):
+            h.step(t)
+        out.append([(h.measure(r, 40), h.get(r, 0, 40, 37)) for r in range(len(cfgs))])
+        h.close()
+    for o in out[1:]:
+        for (ma, ra), (mb, rb) in zip(out[0], o):
+            assert ma["E"] == mb["E"] and np.array_equal(ma["n"], mb["n"]) and np.array_equal(ra, rb)
+
+
+def test_batch_overlap_errors_and_autotune():
+    from kb2pi import capi
+
+    h = make_gpu(CFG, 1)
+    with pytest.raises(capi.KbError, match="batch_overlap"):
+        h.set_tuning(batch_overlap=10)  # one run: nothing to overlap
+    h.close()
+    cfgs = [dict(Ns=8, M=20, lam=2.0, T=1.0), dict(Ns=12, M=30, lam=3.0, T=1.5)]
+    ps = [capi.KbParams(Ns=c["Ns"], sdim=3, M=c["M"], N=4, pexp=1, precision=1, device=0, flags=0, dt=0.1,
+                        lam=c["lam"], mass2=1.0, mass=1.0) for c in cfgs]
+    h = capi.Handle(ps)
+    for r, c in enumerate(cfgs):
+        _, k2, _ = h.orbits(r)
+        h.init(r, occupation(dict(c), k2), 1.0)
+    h.steps(3, 25, 0)
+    d = h.autotune(trials=1)
+    assert d["batch_overlap"] >= 0
+    m = [h.measure(r, 27)["E"] for r in range(2)]
+    assert all(np.isfinite(m))
+    with pytest.raises(capi.KbError, match="batch_overlap"):
+        h.set_tuning(batch_overlap=10 ** 6)
+    h.close()
