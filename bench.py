@@ -169,10 +169,10 @@ def make_handle(precision, device):
 def apply_tuning(h, args, fp64=False):
     """Autotune the launch configuration on the filled window (untimed), unless fixed on the command line."""
     if any(v is not None for v in (args.memint_variant, args.sunset_grid, args.batch_order, args.sunset_variant,
-                                   args.memint_split)):
+                                   args.memint_split, args.batch_overlap)):
         h.set_tuning(memint_variant=None if fp64 else args.memint_variant, sunset_grid=args.sunset_grid,
                      batch_order=args.batch_order, sunset_variant=None if fp64 else args.sunset_variant,
-                     memint_split=args.memint_split)
+                     memint_split=args.memint_split, batch_overlap=args.batch_overlap)
         d = h.tuning()
         d["source"] = "command line"
         return d
@@ -421,7 +421,11 @@ def run_batched(args):
             "config": {"workload": "64 runs, Ns in {16,24,32,48}, lambda U[0.5,8], T U[0.5,3], M U{100..500}, "
                                    "dt=0.05, steps 478..500 of 500", "runs": runs},
             # per graph step: advance_t_kernel, sunset_kernel, memint_kernel (+ memint_finish_kernel when split)
-            "clocks": clk.summary(), "gpu_launches": (3 + bool(tuning.get("memint_split"))) * args.steps,
+            # per graph step: advance_t_kernel, then per group (one, or two with batch_overlap) the
+            # sunset and memint kernels (+ memint_finish_kernel when split)
+            "clocks": clk.summary(),
+            "gpu_launches": (1 + (2 if tuning.get("batch_overlap") else 1) * (2 + bool(tuning.get("memint_split"))))
+            * args.steps,
             "tuning": tuning,
             "kernels_ms": {"memint": prof["memint"][0] / max(1, prof["memint"][1]),
                            "sunset": prof["sunset"][0] / max(1, prof["sunset"][1])}}
@@ -764,7 +768,10 @@ def main():
     ap.add_argument("--sunset-grid", type=int, default=None, help="fix the sunset grid instead of autotuning")
     ap.add_argument("--batch-order", type=int, default=None, help="fix the run order of the batched grids (c3)")
     ap.add_argument("--memint-split", type=int, default=None, help="fix the split mode of the memory integrals")
-    ap.add_argument("--sunset-variant", type=int, default=None, help="fix the FP32 sunset variant (0: 1024, 1: 512 threads)")
+    ap.add_argument("--sunset-variant", type=int, default=None,
+                    help="fix the FP32 sunset variant (0: 1024, 1: 512 threads, 2: tensor cores)")
+    ap.add_argument("--batch-overlap", type=int, default=None,
+                    help="c3: fix the concurrent-group step (CTAs of the second group's sunset; 0 = off)")
     args = ap.parse_args()
     if args.config == "c3" and args.impl == "ours":
         return run_batched(args)
