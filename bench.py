@@ -420,7 +420,6 @@ def run_batched(args):
             "data": f"synthetic: thermal states, per-run draws seeded with {args.seed}",
             "config": {"workload": "64 runs, Ns in {16,24,32,48}, lambda U[0.5,8], T U[0.5,3], M U{100..500}, "
                                    "dt=0.05, steps 478..500 of 500", "runs": runs},
-            # per graph step: advance_t_kernel, sunset_kernel, memint_kernel (+ memint_finish_kernel when split)
             # per graph step: advance_t_kernel, then per group (one, or two with batch_overlap) the
             # sunset and memint kernels (+ memint_finish_kernel when split)
             "clocks": clk.summary(),
