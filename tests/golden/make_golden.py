@@ -16,6 +16,8 @@ Fixtures at the stated sizes of the benchmark configurations:
                 config 3: the first Ns=48 and the first Ns=24 run of the 64-run batch
                 drawn with seed 12345 (the benchmark's draw), 500 steps each, so the
                 window wraps
+  c5_ns64_m128  the headline lattice of config 5 (Ns=64, lambda=2, dt=0.05, tsunami state with
+                the gap mass) on a 128-step window, 200 steps (the window wraps)
   c4_adjoint_ns24_m300
                 config 4: loss = 8 radial-shell means of n(p, 302) + E(302) at Ns=24,
                 M=300, 300 steps; forward-mode dual-number derivatives along lambda,
@@ -68,6 +70,10 @@ C2 = dict(name="c2_ns32_m400", Ns=32, M=400, N=4, lam=4.0, dt=0.05, T=0.0, steps
           init="tsunami", every=50)
 C3A = _c3(10)   # Ns=48, M=442
 C3B = _c3(7)    # Ns=24, M=164
+# the headline lattice (Ns=64, lambda=2, tsunami with the gap mass) on a 128-step window
+# that wraps: the full M=1000 history (52 GB FP64) is beyond a fixture run
+C5S = dict(name="c5_ns64_m128", Ns=64, M=128, N=4, lam=2.0, dt=0.05, T=0.0, steps=200, engine=ENGINE_OCTANT,
+           init="tsunami", every=50, rows=10)
 C4 = dict(name="c4_adjoint_ns24_m300", Ns=24, M=300, N=4, lam=2.0, dt=0.05, mass2=1.0, t_final=302, nbumps=8,
           seed=12345)
 
@@ -101,7 +107,7 @@ def generate(cfg):
             tsnap.append(t)
     t = 2 + cfg["steps"]
     tmin, tmax = o.window()
-    tps = np.arange(tmin, t + 1, max(1, (t - tmin) // 40))
+    tps = np.arange(tmin, t + 1, max(1, (t - tmin) // cfg.get("rows", 40)))
     if tps[-1] != t:
         tps = np.append(tps, t)
     Frow = np.array([o.F(t, tp) for tp in tps])
@@ -148,7 +154,7 @@ def generate_adjoint(cfg):
 
 
 ALL = {"small": (generate, SMALL), "c1": (generate, C1), "c2": (generate, C2), "c3_ns48": (generate, C3A),
-       "c3_ns24": (generate, C3B), "c4": (generate_adjoint, C4)}
+       "c3_ns24": (generate, C3B), "c4": (generate_adjoint, C4), "c5_short": (generate, C5S)}
 
 if __name__ == "__main__":
     names = sys.argv[1:] or list(ALL)

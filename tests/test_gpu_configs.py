@@ -6,6 +6,8 @@ oracle trajectories (tests/golden/make_golden.py):
   config 3  the 64-run batch (Ns from {16,24,32,48}, lambda U[0.5,8], T U[0.5,3],
             M U{100..500}, dt=0.05, 500 steps, seed 12345) in one handle; its
             first Ns=48 run (M=442) and first Ns=24 run (M=164) are compared
+  Ns=64     the headline lattice (config 5's Ns, N, lambda, dt and initial state) on a
+            128-step window, 200 steps
   config 4  kb_adjoint at Ns=24, M=300, 300 steps, checkpoint every 20, against
             forward-mode dual numbers through the oracle (orc_dual_loss)
 
@@ -139,6 +141,30 @@ def test_config3_full_batch(precision):
             for k in ("n", "E", "F", "rho"):
                 assert worst[k] <= TOL_MIXED, (r, k, worst[k])
     h.close()
+
+
+@pytest.mark.parametrize("precision,sunset_variant", [(0, 0), (1, 0), (1, 2)])
+def test_headline_lattice_ns64(precision, sunset_variant):
+    """The headline lattice (Ns=64, N=4, lambda=2, dt=0.05, tsunami state with the gap
+    mass) on a 128-step window for 200 steps, so the window wraps; sunset_variant 2 is
+    the tensor-core sunset."""
+    g = load("c5_ns64_m128")
+    Ns, M, N, lam, dt, _, steps = g["cfg"]
+    h = make_gpu(dict(Ns=int(Ns), M=int(M), N=int(N), lam=float(lam), dt=float(dt)), precision)
+    h.set_tuning(sunset_variant=sunset_variant)
+    h.init(0, g["n0"], float(g["init_mass"]))
+    scal, nsnap, t = evolve_recording(h, [0], int(steps), 50)
+    assert t == 202 and h.window(0) == (202 - int(M) + 1, 202)
+    worst = compare(h, 0, g, scal[0], nsnap[0], t, TOL64)
+    h.close()
+    print(f"\nNs=64 {'FP64' if precision == 0 else 'mixed'} sunset variant {sunset_variant} vs oracle: " +
+          ", ".join(f"{k} {v:.2e}" for k, v in worst.items()))
+    if precision == 0:
+        for k, v in worst.items():
+            assert v <= TOL64, (k, v)
+    else:
+        for k in ("n", "E", "F", "rho"):
+            assert worst[k] <= TOL_MIXED, (k, worst[k])
 
 
 def test_config4_adjoint_matches_dual_numbers():
