@@ -43,8 +43,16 @@ namespace {
 constexpr int SUN_THREADS = 512;
 constexpr int SUN_THREADS_F32 = 1024;
 
-__host__ __device__ inline int rup4(int v) { return (v + 3) & ~3; }
-constexpr int rup4_c(int v) { return (v + 3) & ~3; }
+__host__ __device__ constexpr int rup4(int v) { return (v + 3) & ~3; }
+__host__ __device__ constexpr int cmax(int a, int b) { return a > b ? a : b; }
+__host__ __device__ constexpr int sun_tri(int b) { return b * (b + 1) / 2; }
+__host__ __device__ constexpr int sun_tet(int c) { return c * (c + 1) * (c + 2) / 6; }
+
+// the two intermediate regions: R1 holds E then D (both [H][P4]), R2 holds B
+// ([H][P4], pass 2 reads up to 3 entries past its last row); both also take rows
+// of orbit values (S)
+__host__ __device__ constexpr int sun_r1(int H) { return rup4(cmax(H * rup4(sun_tri(H)), sun_tet(H))); }
+__host__ __device__ constexpr int sun_r2(int H) { return rup4(cmax(H * rup4(sun_tri(H)) + 4, sun_tet(H))); }
 
 struct SunGeom {
   int H, H4, P, P4, S;
@@ -52,12 +60,13 @@ struct SunGeom {
   // pass 1 folded by C[X][h-x] = (-1)^X C[X][x] (h = Ns/2 = H-1): npair pairs
   // x < h-x, a middle x = h/2 when h is even; ne even and no odd outputs X
   int npair, mid, ne, no, ne4, no4, cf;  // cf: elements of the two folded matrices
+  int n2, n3;                            // work items of passes 2 and 3
   __host__ __device__ SunGeom(int H_) {
     H = H_;
     H4 = rup4(H);
-    P = H * (H + 1) / 2;
+    P = sun_tri(H);
     P4 = rup4(P);
-    S = H * (H + 1) * (H + 2) / 6;
+    S = sun_tet(H);
     npair = H / 2;  // (h + 1) / 2
     mid = (H - 1) % 2 == 0;
     ne = npair + mid;
@@ -65,61 +74,46 @@ struct SunGeom {
     ne4 = rup4(ne);
     no4 = rup4(no);
     cf = rup4(ne * ne4 + no * no4);
-    r1 = H * P4;  // E, then D (both [H][P4])
-    if (S > r1) r1 = S;
-    r2 = H * P4 + 4;  // B: pass 2 reads up to 3 entries past the last row
-    if (S > r2) r2 = S;
-    r1 = rup4(r1);
-    r2 = rup4(r2);
+    r1 = sun_r1(H);
+    r2 = sun_r2(H);
+    // pass 2: (H4/4 - X/4) Y blocks by H4/4 z blocks for every X
+    const int nzb = H4 / 4, a = H >> 2, b = H & 3;
+    n2 = nzb * (nzb * H - (2 * a * (a - 1) + a * b));
+    // pass 3: items3(Y) for each block of four pairs whose first pair has row Y
+    n3 = 0;
+    for (int Y = 0; Y < H; ++Y) n3 += (((sun_tri(Y + 1) + 3) >> 2) - ((sun_tri(Y) + 3) >> 2)) * items3(Y);
   }
+  // pass 3 items of a block of four pairs whose smallest Y is Ymin: blocks of four
+  // even outputs Z = 2j >= Ymin, then blocks of four odd outputs Z = 2j+1 >= Ymin
+  __host__ __device__ int items3(int Ymin) const { return (ne4 / 4 - ((Ymin + 1) / 2) / 4) + (no4 / 4 - (Ymin / 2) / 4); }
 };
 
-// pass 3 items of a block of four pairs whose smallest Y is Ymin: blocks of four
-// even outputs Z = 2j >= Ymin, then blocks of four odd outputs Z = 2j+1 >= Ymin
-__host__ __device__ inline int sun_items3(const SunGeom &g, int Ymin) {
-  return (g.ne4 / 4 - ((Ymin + 1) / 2) / 4) + (g.no4 / 4 - (Ymin / 2) / 4);
-}
-
-// shared memory of sunset_kernel without the expand table: cosine matrix,
-// one orbit buffer, the two pass regions (FP32 only), pass tables, pair list
-__host__ __device__ inline size_t sun_smem_base(bool fp64, int H) {
-  SunGeom g(H);
+// shared memory of the tables of sun_transform without the expand table: cosine and
+// folded matrices (compute type), the pair list, the work items of passes 2 and 3
+__host__ __device__ inline size_t sun_tables_bytes(bool fp64, const SunGeom &g) {
   const size_t es = fp64 ? 8 : 4;
-  size_t elems = (size_t)g.H4 * g.H4 + g.cf + rup4(g.S);
-  if (!fp64) elems += (size_t)g.r1 + g.r2;
-  return elems * es + (size_t)(g.H + 1 + g.P4 / 4 + 1) * sizeof(int) + (size_t)rup4(g.P) * sizeof(uint16_t) + 64;
-}
-// the expand table ([H][P4] orbit indices) is kept when it fits next to the
-// rest in the 227 KB a CTA may use
-constexpr size_t SUN_SMEM_CAP = 232448;
-__host__ __device__ inline bool sun_etab_fits(bool fp64, int H) {
-  SunGeom g(H);
-  return sun_smem_base(fp64, H) + (size_t)g.H * g.P4 * sizeof(uint16_t) <= SUN_SMEM_CAP;
+  const size_t b = ((size_t)g.H4 * g.H4 + g.cf) * es + (size_t)(g.P4 + g.n2 + g.n3) * sizeof(uint16_t);
+  return (b + 15) & ~(size_t)15;
 }
 
-// byte offsets in the shared memory of sunset_kernel: the per-run tables (cosine
-// and folded matrices, pass offsets, pair list, expand table when it fits), then
-// the orbit buffer and, FP32, the two pass regions
+// shared memory of sunset_kernel: the tables, the expand table ([H][P4] orbit
+// indices) when everything fits in the 227 KB a CTA may use, one orbit buffer and,
+// FP32, the two pass regions (FP64 keeps them in a per-CTA global scratch slot)
+constexpr size_t SUN_SMEM_CAP = 232448;
 struct SunLayout {
-  size_t ct, off2, off3, pr, etab, regions, bytes;
+  size_t etab, regions, bytes;
+  bool has_etab;
 };
-__host__ __device__ inline SunLayout sun_layout(bool fp64, int H) {
-  SunGeom g(H);
+__host__ __device__ inline SunLayout sun_layout(bool fp64, const SunGeom &g) {
   const size_t es = fp64 ? 8 : 4;
   SunLayout L;
-  size_t o = 0;
-  L.ct = o;
-  o += ((size_t)g.H4 * g.H4 + g.cf) * es;
-  L.off2 = o;
-  o += (size_t)(g.H + 1) * sizeof(int);
-  L.off3 = o;
-  o += (size_t)(g.P4 / 4 + 1) * sizeof(int);
-  L.pr = o;
-  o += (size_t)rup4(g.P) * sizeof(uint16_t);
-  L.etab = o;
-  if (sun_etab_fits(fp64, H)) o += (size_t)g.H * g.P4 * sizeof(uint16_t);
-  L.regions = (o + 15) & ~(size_t)15;
-  L.bytes = L.regions + ((size_t)rup4(g.S) + (fp64 ? 0 : (size_t)g.r1 + g.r2)) * es;
+  const size_t t0 = sun_tables_bytes(fp64, g);
+  const size_t et = ((size_t)g.H * g.P4 * sizeof(uint16_t) + 15) & ~(size_t)15;
+  const size_t rest = ((size_t)rup4(g.S) + (fp64 ? 0 : (size_t)g.r1 + g.r2)) * es;
+  L.has_etab = t0 + et + rest <= SUN_SMEM_CAP;
+  L.etab = t0;
+  L.regions = t0 + (L.has_etab ? et : 0);
+  L.bytes = L.regions + rest;
   return L;
 }
 
@@ -143,9 +137,8 @@ __device__ __forceinline__ void st4(double *p, const double v[4]) {
   *reinterpret_cast<double2 *>(p + 2) = make_double2(v[2], v[3]);
 }
 
-// orbit index of the sorted triple a <= b <= c in 32-bit arithmetic (c < 256
-// here: the pair list packs coordinates into bytes)
-__device__ __forceinline__ int orb3s(int a, int b, int c) { return c * (c + 1) * (c + 2) / 6 + tri2(b) + a; }
+// orbit index of the sorted triple a <= b <= c
+__device__ __forceinline__ int orb3s(int a, int b, int c) { return sun_tet(c) + sun_tri(b) + a; }
 
 // orbit index of (x, y, z) given y <= z
 __device__ __forceinline__ int orb_of(int x, int y, int z) {
@@ -159,12 +152,12 @@ template <typename TC>
 struct SunCtx {
   const TC *CT;         // [H4][H4]: CT[x][X] = C[X][x], zero where x or X >= H; followed by CF:
                         // [ne][ne4] C[2j][k] (even X = 2j), then [no][no4] C[2j+1][k] (odd X)
-  const uint16_t *pr;   // [P]: pair p -> (lo | hi << 8)
-  const int *off2;      // [H+1] item offsets of pass 2
-  const int *off3;      // [P4/4 + 1] item offsets of pass 3
+  const uint16_t *pr;   // [P4]: pair p = tri(z) + y -> (y | z << 8)
+  const uint16_t *it2;  // [n2]: pass 2 items (X | z block << 6 | Y block << 10)
+  const uint16_t *it3;  // [n3]: pass 3 items (pair block | output block << 8)
+  const uint16_t *etab; // [H][P4]: orbit of E[x][p] (0 in the padding), or null
   TC *R1, *R2, *bufF;
   SunGeom g;
-  const uint16_t *etab = nullptr;  // [H][P4]: orbit of E[x][p] (0 in the padding), when it fits
 };
 
 // expand: E[x][p] = in(orbit of (x, y_p, z_p)) for x < H, p < P
@@ -183,14 +176,6 @@ __device__ void sun_expand(const SunCtx<TC> &c, TC *E, In in) {
   }
 }
 
-// orbit table of sun_expand in the layout of E
-__device__ void sun_build_etab(const SunGeom &g, const uint16_t *pr, uint16_t *etab) {
-  for (int i = threadIdx.x; i < g.H * g.P4; i += blockDim.x) {
-    const int x = i / g.P4, p = i - x * g.P4;
-    etab[i] = (p < g.P) ? (uint16_t)orb_of(x, pr[p] & 255, pr[p] >> 8) : (uint16_t)0;
-  }
-}
-
 // folded cosine matrices of pass 1 at CF = CT + H4^2, from cm(X, x) = C[X][x]
 template <typename TC, typename Cm>
 __device__ void sun_build_cf(const SunGeom &g, TC *CF, Cm cm) {
@@ -203,6 +188,63 @@ __device__ void sun_build_cf(const SunGeom &g, TC *CF, Cm cm) {
     const int k = i / g.no4, j = i - k * g.no4;
     CFo[i] = (j < g.no) ? (TC)cm(2 * j + 1, k) : (TC)0;
   }
+}
+
+// the tables of sun_transform for octant size g.H in shared memory at `base`
+// (sun_tables_bytes), the expand table at `etab` unless null, the cosine matrix
+// from cm(X, x) = C[X][x]; ends with a barrier. The regions and the orbit buffer of
+// the returned context are left to the caller.
+template <typename TC, typename Cm>
+__device__ SunCtx<TC> sun_build_tables(const SunGeom &g, unsigned char *base, uint16_t *etab, Cm cm) {
+  TC *CT = reinterpret_cast<TC *>(base);
+  uint16_t *pr = reinterpret_cast<uint16_t *>(CT + g.H4 * g.H4 + g.cf);
+  uint16_t *it2 = pr + g.P4;
+  uint16_t *it3 = it2 + g.n2;
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  for (int i = tid; i < g.H4 * g.H4; i += nthr) {
+    const int x = i / g.H4, X = i - x * g.H4;
+    CT[i] = (X < g.H && x < g.H) ? (TC)cm(X, x) : (TC)0;
+  }
+  sun_build_cf(g, CT + g.H4 * g.H4, cm);
+  for (int z = tid; z < g.H; z += nthr)
+    for (int y = 0; y <= z; ++y) pr[sun_tri(z) + y] = (uint16_t)(y | (z << 8));
+  // pass 2: the items of X are its (z block, Y block) pairs, Y blocks from X/4 on,
+  // neighbouring items in the same z block; they start after sum_{X'<X} (nzb - X'/4) nzb
+  const int nzb = g.H4 / 4;
+  for (int X = tid; X < g.H; X += nthr) {
+    const int a = X >> 2, b = X & 3, nyb = nzb - a;
+    const int off = nzb * (nzb * X - (2 * a * (a - 1) + a * b));
+    for (int zb = 0; zb < nzb; ++zb)
+      for (int yb = 0; yb < nyb; ++yb) it2[off + zb * nyb + yb] = (uint16_t)(X | (zb << 6) | (yb << 10));
+  }
+  // pass 3: the items3(Y) items of every block of four pairs whose first pair has
+  // row Y; offsets by a scan over Y in warp 0 (lane = Y, 32 rows per round)
+  if (tid < 32) {
+    int off = 0;
+    for (int Y0 = 0; Y0 < g.H; Y0 += 32) {
+      const int Y = Y0 + tid;
+      const int qa = (sun_tri(Y) + 3) >> 2, qe = (sun_tri(Y + 1) + 3) >> 2;
+      const int n = Y < g.H ? g.items3(Y) : 0, cnt = Y < g.H ? (qe - qa) * n : 0;
+      int inc = cnt;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, inc, o);
+        if (tid >= o) inc += v;
+      }
+      int w = off + inc - cnt;
+      for (int qb = qa; qb < qe && Y < g.H; ++qb)
+        for (int r = 0; r < n; ++r) it3[w++] = (uint16_t)(qb | (r << 8));
+      off += __shfl_sync(0xffffffffu, inc, 31);
+    }
+  }
+  if (etab) {
+    __syncthreads();  // pr
+    for (int i = tid; i < g.H * g.P4; i += nthr) {
+      const int x = i / g.P4, p = i - x * g.P4;
+      etab[i] = (p < g.P) ? (uint16_t)orb_of(x, pr[p] & 255, pr[p] >> 8) : (uint16_t)0;
+    }
+  }
+  __syncthreads();
+  return SunCtx<TC>{CT, pr, it2, it3, etab, nullptr, nullptr, nullptr, g};
 }
 
 // unroll of the pass loops (FP64 at 2: the 4 x 4 double tile fills the registers)
@@ -258,8 +300,8 @@ __device__ void sun_pass1(const SunCtx<TC> &c, const TC *E, TC *B) {
   }
 }
 
-// pass 2: D[z][tri2(Y)+X] = sum_y CT[y][Y] B[X][(min(y,z), max(y,z))], Y >= X.
-// B[X] holds the pairs (y <= z) at tri2(z) + y. Every thread walks y in blocks
+// pass 2: D[z][tri(Y)+X] = sum_y CT[y][Y] B[X][(min(y,z), max(y,z))], Y >= X.
+// B[X] holds the pairs (y <= z) at tri(z) + y. Every thread walks y in blocks
 // of four and reads the 4 x 4 block of the symmetric B[X] at (y0.., z0..) as
 // four rows of four packed entries: rows y0 + k at columns z0.. when y0 >= z0,
 // rows z0 + k at columns y0.. (the transposed block) when y0 < z0; the block
@@ -270,18 +312,9 @@ __device__ void sun_pass1(const SunCtx<TC> &c, const TC *E, TC *B) {
 template <typename TC>
 __device__ void sun_pass2(const SunCtx<TC> &c, const TC *B, TC *D) {
   const int H = c.g.H, H4 = c.g.H4, P4 = c.g.P4;
-  const int nzb = H4 / 4;
-  const int total = c.off2[H];
-  for (int it = threadIdx.x; it < total; it += blockDim.x) {
-    int lo = 0, hi = H - 1;  // X with off2[X] <= it < off2[X+1]
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (c.off2[mid] <= it) lo = mid; else hi = mid - 1;
-    }
-    const int X = lo;
-    const int nyb = nzb - X / 4;  // Y blocks of this X (Y >= 4 (X / 4))
-    const int r = it - c.off2[X];
-    const int zb = r / nyb, yb = r - zb * nyb;  // neighbouring threads share z0
+  for (int it = threadIdx.x; it < c.g.n2; it += blockDim.x) {
+    const int code = c.it2[it];  // neighbouring items share the z block
+    const int X = code & 63, zb = (code >> 6) & 15, yb = code >> 10;
     const int Y0 = 4 * (X / 4) + 4 * yb, z0 = 4 * zb;
     const TC *Bx = B + X * P4;
     TC acc[4][4] = {};
@@ -294,7 +327,7 @@ __device__ void sun_pass2(const SunCtx<TC> &c, const TC *B, TC *D) {
       TC L[4][4];
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
-        const TC *row = Bx + tri2(min(rb + k, H - 1)) + cb;
+        const TC *row = Bx + sun_tri(min(rb + k, H - 1)) + cb;
 #pragma unroll
         for (int m = 0; m < 4; ++m) L[k][m] = row[m];
       }
@@ -314,7 +347,7 @@ __device__ void sun_pass2(const SunCtx<TC> &c, const TC *B, TC *D) {
     for (int a = 0; a < 4; ++a) {
       const int Y = Y0 + a;
       if (Y < X || Y >= H) continue;
-      const int q = tri2(Y) + X;
+      const int q = sun_tri(Y) + X;
 #pragma unroll
       for (int j = 0; j < 4; ++j)
         if (z0 + j < H) D[(z0 + j) * P4 + q] = acc[a][j];
@@ -328,19 +361,12 @@ __device__ void sun_pass2(const SunCtx<TC> &c, const TC *B, TC *D) {
 template <typename TC, typename Out>
 __device__ void sun_pass3(const SunCtx<TC> &c, const TC *D, Out out) {
   const int H = c.g.H, P = c.g.P, P4 = c.g.P4, h = H - 1, npair = c.g.npair;
-  const int nqb = c.g.P4 / 4;
-  const int total = c.off3[nqb];
   const TC *CF = c.CT + c.g.H4 * c.g.H4;
-  for (int it = threadIdx.x; it < total; it += blockDim.x) {
-    int lo = 0, hi = nqb - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (c.off3[mid] <= it) lo = mid; else hi = mid - 1;
-    }
-    const int qb = lo;
+  for (int it = threadIdx.x; it < c.g.n3; it += blockDim.x) {
+    const int code = c.it3[it];
+    const int qb = code & 255, r = code >> 8;
     const int q0 = 4 * qb;
     const int Ymin = c.pr[min(q0, P - 1)] >> 8;
-    const int r = it - c.off3[qb];
     const int jbe = ((Ymin + 1) / 2) / 4, ne_items = c.g.ne4 / 4 - jbe;
     const int odd = r >= ne_items ? 1 : 0;
     const int j0 = odd ? 4 * ((Ymin / 2) / 4 + (r - ne_items)) : 4 * (jbe + r);
@@ -393,6 +419,10 @@ __device__ void sun_transform(const SunCtx<TC> &c, In in, Out out) {
 // NTHR threads per CTA; MINB resident CTAs per SM the register budget allows.
 // An item of a run is R.sun_rows consecutive t' rows (several for the small
 // lattices of a batch, so that their per-item work -- finding the run, the L2
+
+// NTHR threads per CTA; MINB resident CTAs per SM the register budget allows.
+// An item of a run is R.sun_rows consecutive t' rows (several for the small
+// lattices of a batch, so that their per-item work -- finding the run, the L2
 // prefetch of the next row -- is spread over more rows), taken one after the other.
 template <typename TC, typename TS, bool SCRATCH, int NTHR, int MINB>
 __global__ void __launch_bounds__(NTHR, MINB)
@@ -400,57 +430,29 @@ sunset_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
               const int *__restrict__ d_t, TC *__restrict__ scratch, size_t scratch_stride) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int t = *d_t;  // Sigma(t-1, t') for t' in [tmin, t-1]
-  int cur_run = -1;
-  SunCtx<TC> c{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, SunGeom(1)};
+  int cur_ns = -1;
+  SunCtx<TC> c{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, SunGeom(1)};
   for (int w = blockIdx.x; w < total; w += gridDim.x) {
     const int r = run_at(base, nruns, w);
     const RunDev &R = runs[r];
     if (!pexp_sunset(R.pexp) || t < 3) continue;
-    if (r != cur_run) {
-      // per-run tables: cosine matrix, pair list, pass offsets; then the orbit
-      // buffer and the pass regions
+    if (R.Ns != cur_ns) {
+      // tables of the lattice size (runs of the same Ns share them), then the
+      // orbit buffer and the pass regions
       __syncthreads();
-      cur_run = r;
-      SunGeom g(R.H);
-      const SunLayout L = sun_layout(sizeof(TC) == 8, g.H);
-      TC *CT = reinterpret_cast<TC *>(smem_raw + L.ct);
-      int *off2 = reinterpret_cast<int *>(smem_raw + L.off2);
-      int *off3 = reinterpret_cast<int *>(smem_raw + L.off3);
-      uint16_t *pr = reinterpret_cast<uint16_t *>(smem_raw + L.pr);
-      uint16_t *etab = sun_etab_fits(sizeof(TC) == 8, g.H) ? reinterpret_cast<uint16_t *>(smem_raw + L.etab) : nullptr;
-      TC *bufF = reinterpret_cast<TC *>(smem_raw + L.regions);
-      TC *R1, *R2;
+      cur_ns = R.Ns;
+      const SunGeom g(R.H);
+      const SunLayout L = sun_layout(sizeof(TC) == 8, g);
+      c = sun_build_tables<TC>(g, smem_raw, L.has_etab ? reinterpret_cast<uint16_t *>(smem_raw + L.etab) : nullptr,
+                               [&](int X, int x) { return R.Cm[X * g.H + x]; });
+      c.bufF = reinterpret_cast<TC *>(smem_raw + L.regions);
       if (SCRATCH) {
-        R1 = scratch + (size_t)blockIdx.x * scratch_stride;
-        R2 = R1 + g.r1;
+        c.R1 = scratch + (size_t)blockIdx.x * scratch_stride;
+        c.R2 = c.R1 + g.r1;
       } else {
-        R1 = bufF + rup4(g.S);
-        R2 = R1 + g.r1;
+        c.R1 = c.bufF + rup4(g.S);
+        c.R2 = c.R1 + g.r1;
       }
-      for (int i = threadIdx.x; i < g.H4 * g.H4; i += blockDim.x) {
-        const int x = i / g.H4, X = i - x * g.H4;
-        CT[i] = (X < g.H && x < g.H) ? (TC)R.Cm[X * g.H + x] : (TC)0;
-      }
-      for (int z = threadIdx.x; z < g.H; z += blockDim.x)
-        for (int y = 0; y <= z; ++y) pr[tri2(z) + y] = (uint16_t)(y | (z << 8));
-      if (threadIdx.x == 0) {
-        const int nzb = g.H4 / 4;
-        off2[0] = 0;
-        for (int X = 0; X < g.H; ++X) off2[X + 1] = off2[X] + (g.H4 / 4 - X / 4) * nzb;
-      }
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        const int nqb = g.P4 / 4;
-        off3[0] = 0;
-        for (int qb = 0; qb < nqb; ++qb) {
-          const int Ymin = pr[min(4 * qb, g.P - 1)] >> 8;
-          off3[qb + 1] = off3[qb] + sun_items3(g, Ymin);
-        }
-      }
-      if (etab) sun_build_etab(g, pr, etab);
-      sun_build_cf(g, CT + g.H4 * g.H4, [&](int X, int x) { return R.Cm[X * g.H + x]; });
-      __syncthreads();
-      c = SunCtx<TC>{CT, pr, off2, off3, R1, R2, bufF, g, etab};
     }
     const int tmin = max(1, t - R.M + 1);
     const int S = c.g.S;
@@ -552,7 +554,7 @@ sunset_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
 
 }  // namespace
 
-size_t sunset_smem_bytes(bool fp64, int H) { return sun_layout(fp64, H).bytes; }
+size_t sunset_smem_bytes(bool fp64, int H) { return sun_layout(fp64, SunGeom(H)).bytes; }
 
 // t' rows per sunset item of a run (FP32): up to 8 for the small lattices whose rows
 // are short, as long as the work items of the largest pass of all the item's rows
@@ -561,9 +563,7 @@ size_t sunset_smem_bytes(bool fp64, int H) { return sun_layout(fp64, H).bytes; }
 int sunset_rows_per_item(int H) {
   SunGeom g(H);
   const int p1 = (g.ne4 / 4 + g.no4 / 4) * (g.P4 / 4);
-  int p2 = 0;
-  for (int X = 0; X < g.H; ++X) p2 += (g.H4 / 4 - X / 4) * (g.H4 / 4);
-  const int items = p1 > p2 ? p1 : p2;
+  const int items = p1 > g.n2 ? p1 : g.n2;
   for (int rows = 8; rows > 1; rows /= 2)
     if (items * rows <= SUN_THREADS + SUN_THREADS / 4) return rows;
   return 1;
@@ -630,7 +630,7 @@ cudaError_t launch_sunset(bool fp64, int variant, const RunDev *d_runs, const in
 // the caller passes in device memory, with the per-CTA transform scratch in a
 // file-scope device array instead of a cudaMalloc'd buffer. The array holds
 // NOALLOC_MAX_CTAS slots sized for the largest lattice accepted
-// (Ns <= NOALLOC_MAX_NS): 160 x 5712 doubles = 7.3 MB, resident on every GPU
+// (Ns <= NOALLOC_MAX_NS): 160 x 6120 doubles = 7.8 MB, resident on every GPU
 // that loads the library until the process exits.
 // ---------------------------------------------------------------------------
 namespace kb {
@@ -641,8 +641,7 @@ constexpr int NOALLOC_MAX_CTAS = 160;
 
 constexpr size_t na_slot_elems(int H) {
   // the R1 + R2 regions of SunGeom for octant size H (pass intermediates)
-  return (size_t)rup4_c(std::max(H * rup4_c(H * (H + 1) / 2), H * (H + 1) * (H + 2) / 6)) +
-         (size_t)rup4_c(std::max(H * rup4_c(H * (H + 1) / 2) + 4, H * (H + 1) * (H + 2) / 6));
+  return (size_t)sun_r1(H) + (size_t)sun_r2(H);
 }
 constexpr size_t NOALLOC_SLOT_ELEMS = na_slot_elems(NOALLOC_MAX_NS / 2 + 1);
 
@@ -657,42 +656,15 @@ sunset_rows_noalloc_kernel(int Ns, double fac_r, double fac_F, int classical, in
                            size_t stride) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int H = Ns / 2 + 1;
-  SunGeom g(H);
-  double *CT = reinterpret_cast<double *>(smem_raw);
-  double *bufF = CT + g.H4 * g.H4 + g.cf;
-  int *off2 = reinterpret_cast<int *>(bufF + rup4(g.S));
-  int *off3 = off2 + (g.H + 1);
-  uint16_t *pr = reinterpret_cast<uint16_t *>(off3 + (g.P4 / 4 + 1));
-  double *R1 = scratch + (size_t)blockIdx.x * stride;
-  double *R2 = R1 + g.r1;
-  // cosine matrix of the even octant, C[X][x] = m(x) cos(2 pi x X / Ns), stored transposed
-  for (int i = threadIdx.x; i < g.H4 * g.H4; i += blockDim.x) {
-    const int x = i / g.H4, X = i - x * g.H4;
-    const double m = (x == 0 || 2 * x == Ns) ? 1.0 : 2.0;
-    CT[i] = (X < g.H && x < g.H) ? m * cospi(2.0 * (double)((x * X) % Ns) / (double)Ns) : 0.0;
-  }
-  sun_build_cf(g, CT + g.H4 * g.H4, [&](int X, int x) {
+  const SunGeom g(H);
+  // cosine matrix of the even octant, C[X][x] = m(x) cos(2 pi x X / Ns)
+  SunCtx<double> c = sun_build_tables<double>(g, smem_raw, nullptr, [&](int X, int x) {
     const double m = (x == 0 || 2 * x == Ns) ? 1.0 : 2.0;
     return m * cospi(2.0 * (double)((x * X) % Ns) / (double)Ns);
   });
-  for (int z = threadIdx.x; z < g.H; z += blockDim.x)
-    for (int y = 0; y <= z; ++y) pr[tri2(z) + y] = (uint16_t)(y | (z << 8));
-  if (threadIdx.x == 0) {
-    const int nzb = g.H4 / 4;
-    off2[0] = 0;
-    for (int X = 0; X < g.H; ++X) off2[X + 1] = off2[X] + (g.H4 / 4 - X / 4) * nzb;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    const int nqb = g.P4 / 4;
-    off3[0] = 0;
-    for (int qb = 0; qb < nqb; ++qb) {
-      const int Ymin = pr[min(4 * qb, g.P - 1)] >> 8;
-      off3[qb + 1] = off3[qb] + sun_items3(g, Ymin);
-    }
-  }
-  __syncthreads();
-  const SunCtx<double> c{CT, pr, off2, off3, R1, R2, bufF, g};
+  c.bufF = reinterpret_cast<double *>(smem_raw + sun_tables_bytes(true, g));
+  c.R1 = scratch + (size_t)blockIdx.x * stride;
+  c.R2 = c.R1 + g.r1;
   const int S = g.S;
   for (int row = blockIdx.x; row < nrows; row += gridDim.x) {
     const double *Fin = F_rows + (size_t)row * S;
@@ -775,9 +747,7 @@ extern "C" int kb_sunset_rows_noalloc(int32_t Ns, int32_t N, double lambda, int3
   const double V = (double)Ns * Ns * Ns, iv = 1.0 / V, Nd = (double)N;
   const double fac_r = iv * iv * iv * (-(lambda * lambda) * (Nd + 2.0) / (6.0 * Nd * Nd));
   const double fac_F = iv * iv * iv * (-(lambda * lambda) * (Nd + 2.0) / (18.0 * Nd * Nd));
-  SunGeom g(H);
-  const size_t smem = ((size_t)g.H4 * g.H4 + g.cf + rup4(g.S)) * sizeof(double) +
-                      (size_t)(g.H + 1 + g.P4 / 4 + 1) * sizeof(int) + (size_t)g.P * sizeof(uint16_t) + 64;
+  const size_t smem = sun_tables_bytes(true, SunGeom(H)) + (size_t)rup4(sun_tet(H)) * sizeof(double);
   sunset_rows_noalloc_kernel<<<grid, SUN_THREADS, smem, (cudaStream_t)stream>>>(
       Ns, fac_r, fac_F, pexp == KB_PEXP_NLO_CLASSICAL ? 1 : 0, nrows, F_rows, rho_rows, sigF_rows, sigr_rows,
       scratch, stride);
@@ -812,41 +782,16 @@ sunset_adjoint_kernel(RunDev R, int t, const double *__restrict__ sbar_r, const 
                       double *scratch, size_t stride, double lambda) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int tmin = max(1, t - R.M + 1);
-  SunGeom g(R.H);
-  double *CT = reinterpret_cast<double *>(smem_raw);
-  double *bFx = CT + g.H4 * g.H4 + g.cf;  // Fx, then adjoint of Fx / deg
+  const SunGeom g(R.H);
+  double *bFx = reinterpret_cast<double *>(smem_raw + sun_tables_bytes(true, g));  // Fx, then adjoint of Fx / deg
   double *brx = bFx + rup4(g.S);      // rx, then adjoint of rx / deg
   double *bgr = brx + rup4(g.S);      // adjoint of g_r
   double *bgF = bgr + rup4(g.S);      // adjoint of g_F
-  int *off2 = reinterpret_cast<int *>(bgF + rup4(g.S));
-  int *off3 = off2 + (g.H + 1);
-  uint16_t *pr = reinterpret_cast<uint16_t *>(off3 + (g.P4 / 4 + 1));
-  double *R1 = scratch + (size_t)blockIdx.x * stride;
-  double *R2 = R1 + g.r1;
   __shared__ double red[SUN_THREADS / 32];
-  for (int i = threadIdx.x; i < g.H4 * g.H4; i += blockDim.x) {
-    const int x = i / g.H4, X = i - x * g.H4;
-    CT[i] = (X < g.H && x < g.H) ? R.Cm[X * g.H + x] : 0.0;
-  }
-  sun_build_cf(g, CT + g.H4 * g.H4, [&](int X, int x) { return R.Cm[X * g.H + x]; });
-  for (int z = threadIdx.x; z < g.H; z += blockDim.x)
-    for (int y = 0; y <= z; ++y) pr[tri2(z) + y] = (uint16_t)(y | (z << 8));
-  if (threadIdx.x == 0) {
-    const int nzb = g.H4 / 4;
-    off2[0] = 0;
-    for (int X = 0; X < g.H; ++X) off2[X + 1] = off2[X] + (g.H4 / 4 - X / 4) * nzb;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    const int nqb = g.P4 / 4;
-    off3[0] = 0;
-    for (int qb = 0; qb < nqb; ++qb) {
-      const int Ymin = pr[min(4 * qb, g.P - 1)] >> 8;
-      off3[qb + 1] = off3[qb] + sun_items3(g, Ymin);
-    }
-  }
-  __syncthreads();
-  const SunCtx<double> c{CT, pr, off2, off3, R1, R2, bFx, g};
+  SunCtx<double> c = sun_build_tables<double>(g, smem_raw, nullptr, [&](int X, int x) { return R.Cm[X * g.H + x]; });
+  c.R1 = scratch + (size_t)blockIdx.x * stride;
+  c.R2 = c.R1 + g.r1;
+  c.bufF = bFx;
   const int S = g.S, Spad = R.nchunks * KC;
   const bool classical = (R.pexp == 2);
   const size_t rowstride = (size_t)R.Malloc * KC;
@@ -909,9 +854,7 @@ sunset_adjoint_kernel(RunDev R, int t, const double *__restrict__ sbar_r, const 
 }  // namespace
 
 size_t sunset_adjoint_smem_bytes(int H) {
-  SunGeom g(H);
-  return ((size_t)g.H4 * g.H4 + g.cf + 4 * (size_t)rup4(g.S)) * sizeof(double) +
-         (size_t)(g.H + 1 + g.P4 / 4 + 1) * sizeof(int) + (size_t)g.P * sizeof(uint16_t) + 64;
+  return sun_tables_bytes(true, SunGeom(H)) + 4 * (size_t)rup4(sun_tet(H)) * sizeof(double);
 }
 
 cudaError_t launch_sunset_adjoint(const RunDev &R, int t, const double *sbar_r, const double *sbar_F, double *adjF,
@@ -952,37 +895,9 @@ cudaError_t launch_sunset_adjoint(const RunDev &R, int t, const double *sbar_r, 
 namespace kb {
 namespace {
 
-// cosine matrix and pass tables of one lattice size (as sunset_kernel builds them)
-__device__ void ninv_tables(const RunDev &R, const SunGeom &g, double *CT, uint16_t *pr, int *off2, int *off3) {
-  for (int i = threadIdx.x; i < g.H4 * g.H4; i += blockDim.x) {
-    const int x = i / g.H4, X = i - x * g.H4;
-    CT[i] = (X < g.H && x < g.H) ? R.Cm[X * g.H + x] : 0.0;
-  }
-  sun_build_cf(g, CT + g.H4 * g.H4, [&](int X, int x) { return R.Cm[X * g.H + x]; });
-  for (int z = threadIdx.x; z < g.H; z += blockDim.x)
-    for (int y = 0; y <= z; ++y) pr[tri2(z) + y] = (uint16_t)(y | (z << 8));
-  if (threadIdx.x == 0) {
-    const int nzb = g.H4 / 4;
-    off2[0] = 0;
-    for (int X = 0; X < g.H; ++X) off2[X + 1] = off2[X] + (g.H4 / 4 - X / 4) * nzb;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    const int nqb = g.P4 / 4;
-    off3[0] = 0;
-    for (int qb = 0; qb < nqb; ++qb) {
-      const int Ymin = pr[min(4 * qb, g.P - 1)] >> 8;
-      off3[qb + 1] = off3[qb] + sun_items3(g, Ymin);
-    }
-  }
-  __syncthreads();
-}
-
-// shared memory: CT, NB orbit buffers, pass tables
+// shared memory: the tables of sun_transform, then NB orbit buffers
 __host__ __device__ inline size_t ninv_rows_smem(int H, int NB) {
-  SunGeom g(H);
-  return ((size_t)g.H4 * g.H4 + g.cf + (size_t)NB * rup4(g.S)) * sizeof(double) +
-         (size_t)(g.H + 1 + g.P4 / 4 + 1) * sizeof(int) + (size_t)g.P * sizeof(uint16_t) + 64;
+  return sun_tables_bytes(true, SunGeom(H)) + (size_t)NB * rup4(sun_tet(H)) * sizeof(double);
 }
 
 // MODE 0: bubbles of row t-1 (and of the pair (1,1) at t = 3); MODE 1: self-energies
@@ -992,8 +907,8 @@ ninv_rows_kernel(const RunDev *__restrict__ runs, const int *__restrict__ sched,
                  const int *__restrict__ d_t, double *__restrict__ scratch, size_t stride) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int t = *d_t;
-  int cur_run = -1;
-  SunCtx<double> c{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, SunGeom(1)};
+  int cur_ns = -1;
+  SunCtx<double> c{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, SunGeom(1)};
   double *buf[4] = {nullptr, nullptr, nullptr, nullptr};
   for (int w = blockIdx.x; w < total; w += gridDim.x) {
     const int r = run_at(sched, nruns, w);
@@ -1010,23 +925,19 @@ ninv_rows_kernel(const RunDev *__restrict__ runs, const int *__restrict__ sched,
         continue;
       }
     }
-    if (r != cur_run) {
+    if (R.Ns != cur_ns) {
       __syncthreads();
-      cur_run = r;
-      SunGeom g(R.H);
-      double *p = reinterpret_cast<double *>(smem_raw);
-      double *CT = p;
-      p += g.H4 * g.H4 + g.cf;
+      cur_ns = R.Ns;
+      const SunGeom g(R.H);
+      double *p = reinterpret_cast<double *>(smem_raw + sun_tables_bytes(true, g));
       for (int q = 0; q < (MODE == 0 ? 2 : 4); ++q) {
         buf[q] = p;
         p += rup4(g.S);
       }
-      int *off2 = reinterpret_cast<int *>(p);
-      int *off3 = off2 + (g.H + 1);
-      uint16_t *pr = reinterpret_cast<uint16_t *>(off3 + (g.P4 / 4 + 1));
-      ninv_tables(R, g, CT, pr, off2, off3);
-      double *R1 = scratch + (size_t)blockIdx.x * stride;
-      c = SunCtx<double>{CT, pr, off2, off3, R1, R1 + g.r1, buf[0], g};
+      c = sun_build_tables<double>(g, smem_raw, nullptr, [&](int X, int x) { return R.Cm[X * g.H + x]; });
+      c.R1 = scratch + (size_t)blockIdx.x * stride;
+      c.R2 = c.R1 + g.r1;
+      c.bufF = buf[0];
     }
     const int S = c.g.S, Spad = R.nchunks * KC;
     const size_t rowstride = (size_t)R.Malloc * KC;

@@ -356,16 +356,16 @@ sunset_tc_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, 
   c.ph = 0;
   c.ok = true;
   c.err = nullptr;
-  int cur_run = -1;
+  int cur_ns = -1;
   float *rowF = nullptr, *rowR = nullptr;
   for (int w = blockIdx.x; w < total && c.ok; w += gridDim.x) {
     const int r = run_at(base, nruns, w);
     const RunDev &R = runs[r];
     if (!pexp_sunset(R.pexp) || t < 3) continue;
     c.err = R.err;
-    if (r != cur_run) {
+    if (R.Ns != cur_ns) {  // tables of the lattice size, shared by the runs of the same Ns
       __syncthreads();
-      cur_run = r;
+      cur_ns = R.Ns;
       const TcGeom g(R.H);
       const TcLayout L = tc_layout(g.H);
       float *bh = reinterpret_cast<float *>(smem_raw + L.bh), *bl = reinterpret_cast<float *>(smem_raw + L.bl);
