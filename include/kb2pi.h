@@ -268,7 +268,7 @@ int kb_adjoint(kb_handle *h, const double *n_init, double init_mass, int32_t t_f
  * the device in orbit order (row i = F(t-1, t'_i) / rho(t-1, t'_i), S values
  * each, rho sign-corrected), on `stream` (a cudaStream_t, NULL for the legacy
  * default stream). The transform scratch is one fixed device array of
- * 160 x 6120 doubles (7.8 MB) compiled into the library, held on every GPU
+ * 160 x 5308 doubles (6.8 MB) compiled into the library, held on every GPU
  * that loads it until the process exits, so Ns is limited to 1 or an even
  * value in [2, 32]; larger Ns fails with KB_ERR_PARAM and a message in
  * kb_last_error(NULL). The first call on a device looks up the array's device

@@ -630,7 +630,7 @@ cudaError_t launch_sunset(bool fp64, int variant, const RunDev *d_runs, const in
 // the caller passes in device memory, with the per-CTA transform scratch in a
 // file-scope device array instead of a cudaMalloc'd buffer. The array holds
 // NOALLOC_MAX_CTAS slots sized for the largest lattice accepted
-// (Ns <= NOALLOC_MAX_NS): 160 x 6120 doubles = 7.8 MB, resident on every GPU
+// (Ns <= NOALLOC_MAX_NS): 160 x 5308 doubles = 6.8 MB, resident on every GPU
 // that loads the library until the process exits.
 // ---------------------------------------------------------------------------
 namespace kb {
