@@ -169,10 +169,11 @@ def make_handle(precision, device):
 def apply_tuning(h, args, fp64=False):
     """Autotune the launch configuration on the filled window (untimed), unless fixed on the command line."""
     if any(v is not None for v in (args.memint_variant, args.sunset_grid, args.batch_order, args.sunset_variant,
-                                   args.memint_split, args.batch_overlap)):
+                                   args.memint_split, args.batch_overlap, args.memint_persistent)):
         h.set_tuning(memint_variant=None if fp64 else args.memint_variant, sunset_grid=args.sunset_grid,
                      batch_order=args.batch_order, sunset_variant=None if fp64 else args.sunset_variant,
-                     memint_split=args.memint_split, batch_overlap=args.batch_overlap)
+                     memint_split=args.memint_split, batch_overlap=args.batch_overlap,
+                     memint_persistent=args.memint_persistent)
         d = h.tuning()
         d["source"] = "command line"
         return d
@@ -767,6 +768,8 @@ def main():
     ap.add_argument("--sunset-grid", type=int, default=None, help="fix the sunset grid instead of autotuning")
     ap.add_argument("--batch-order", type=int, default=None, help="fix the run order of the batched grids (c3)")
     ap.add_argument("--memint-split", type=int, default=None, help="fix the split mode of the memory integrals")
+    ap.add_argument("--memint-persistent", type=int, default=None,
+                    help="1: persistent memory-integral grid (one CTA per SM taking items from a queue)")
     ap.add_argument("--sunset-variant", type=int, default=None,
                     help="fix the FP32 sunset variant (0: 1024, 1: 512 threads, 2: tensor cores)")
     ap.add_argument("--batch-overlap", type=int, default=None,

@@ -225,13 +225,18 @@ typedef struct kb_tuning {
                                * groups of about equal memory-integral work and runs the second
                                * group's sunset on n CTAs, on a second stream, while the first
                                * group's memory integrals stream (the same arithmetic per run) */
+  int32_t memint_persistent;  /* 1: the memory-integral grid is persistent -- one CTA per SM takes
+                               * chunk items (whole or split) from a device counter until none are
+                               * left, keeping its TMEM, stage barriers and the run's tadpole sum
+                               * across items (the same arithmetic per item); 0 (default): one CTA
+                               * per item. 1 needs memint_variant 1 or 2 in KB_PREC_MIXED */
 } kb_tuning;
 int kb_get_tuning(const kb_handle *h, kb_tuning *out);
 int kb_set_tuning(kb_handle *h, const kb_tuning *in);
 /* Autotuner: times every candidate configuration (memory-integral variants,
  * whole or split;
- * sunset variants with grids of 1..4 CTAs per SM that fit; both run orders of a batched
- * handle) by re-running the last evolved
+ * sunset variants with grids of 1..4 CTAs per SM that fit; the chosen memory-integral
+ * kernel as a persistent grid; both run orders of a batched handle) by re-running the last evolved
  * step t -- which reads rows < t and rewrites row t, so the state is unchanged
  * -- `trials` times each, keeps the fastest kernel configurations, re-runs step
  * t once with them and returns the choice and its time per step (ms) if the

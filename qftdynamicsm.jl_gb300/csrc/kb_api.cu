@@ -80,6 +80,8 @@ struct kb_handle {
   int test_no_tiles = 0;          // test hook: the memint producer issues no tiles (waits run out)
   int memint_split = 0;           // 1: two half-triangle CTAs per chunk and a finishing kernel;
                                   // 2: the same for the chunks past the last whole wave only
+  int memint_persistent = 0;      // 1: one memory-integral CTA per SM taking items from a queue
+  int *d_mi_queue = nullptr;      // [2] item counters of the persistent memory-integral grids (per group)
   int batch_order = 0;            // order of the runs' CTA ranges in the batched grids
   // concurrent halves of a batch (kb_tuning.batch_overlap > 0): the runs split into two
   // groups of about equal memory-integral work, each with its own schedule tables;
@@ -587,7 +589,8 @@ int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out) {
             cudaMalloc(&h->d_base_mi, sizeof(int) * 2 * nruns) == cudaSuccess &&
             cudaMalloc(&h->d_grp_sun[0], sizeof(int) * 8 * nruns) == cudaSuccess &&
             cudaMalloc(&h->d_grp_mi[0], sizeof(int) * 8 * nruns) == cudaSuccess &&
-            cudaMalloc(&h->d_t, sizeof(int)) == cudaSuccess && cudaMalloc(&h->d_err, sizeof(int)) == cudaSuccess;
+            cudaMalloc(&h->d_t, sizeof(int)) == cudaSuccess && cudaMalloc(&h->d_err, sizeof(int)) == cudaSuccess &&
+            cudaMalloc(&h->d_mi_queue, 2 * sizeof(int)) == cudaSuccess;
   if (ok) {  // the second group's tables follow the first's
     h->d_grp_sun[1] = h->d_grp_sun[0] + 4 * nruns;
     h->d_grp_mi[1] = h->d_grp_mi[0] + 4 * nruns;
@@ -666,7 +669,7 @@ void kb_destroy(kb_handle *h) {
     if (m.host) cudaFreeHost(m.host);
   }
   for (auto &R : h->runs) free_run(R);
-  void *ptrs[] = {h->d_runs, h->d_base_sun, h->d_base_mi, h->d_grp_sun[0], h->d_grp_mi[0], h->d_t, h->d_err,
+  void *ptrs[] = {h->d_runs, h->d_base_sun, h->d_base_mi, h->d_grp_sun[0], h->d_grp_mi[0], h->d_t, h->d_err, h->d_mi_queue,
                   h->sun_scratch};
   for (void *q : ptrs)
     if (q) cudaFree(q);
@@ -790,12 +793,6 @@ static cudaEvent_t next_event(kb_handle *h) {
 
 // Sigma(t-1, .) of every run: the sunset (lambda expansion) and/or the 1/N
 // kernels; each kernel skips the runs of the other expansion.
-// chunks streamed whole by one CTA before the split ones (memint_split 2: the
-// whole waves of one CTA per SM; 1: none)
-static int memint_nwhole(const kb_handle *h) {
-  if (h->memint_split != 2) return 0;
-  return (h->total_mi / h->num_sms) * h->num_sms;
-}
 
 // the sunset of the runs of one schedule table (all runs, or one group)
 static int launch_sun(kb_handle *h, const int *base, int n, int total, int grid, cudaStream_t st) {
@@ -809,12 +806,12 @@ static int launch_sun(kb_handle *h, const int *base, int n, int total, int grid,
                                  h->sun_scratch, h->sun_scratch_stride, h->smem_sun, st));
   return KB_OK;
 }
-// the memory integrals of the runs of one schedule table
-static int launch_mi(kb_handle *h, const int *base, int n, int total, int measure, cudaStream_t st) {
+// the memory integrals of the runs of one schedule table (group g's queue when persistent)
+static int launch_mi(kb_handle *h, const int *base, int n, int total, int measure, cudaStream_t st, int g) {
   const int nwhole = h->memint_split == 2 ? (total / h->num_sms) * h->num_sms : 0;
   KB_CUDA(h, kb::launch_memint(h->fp64, memint_launch_variant(h), h->memint_split, nwhole, h->d_runs, base, n, total,
                                h->fin_nb_max, !h->memint_bulk + 2 * h->test_no_tiles, h->d_t, h->d_err, measure,
-                               h->smem_mi, st));
+                               h->smem_mi, h->memint_persistent ? h->d_mi_queue + g : nullptr, h->num_sms, st));
   return KB_OK;
 }
 
@@ -848,8 +845,8 @@ static int launch_step_overlap(kb_handle *h, int measure, cudaEvent_t e0, cudaEv
   KB_CUDA(h, cudaEventRecord(h->ev_fork, h->st));
   KB_CUDA(h, cudaStreamWaitEvent(h->st2, h->ev_fork, 0));
   if ((rc = launch_sun(h, h->d_grp_sun[1], h->grp_n[1], h->grp_sun[1], h->batch_overlap, h->st2))) return rc;
-  if ((rc = launch_mi(h, h->d_grp_mi[0], h->grp_n[0], h->grp_mi[0], measure, h->st))) return rc;
-  if ((rc = launch_mi(h, h->d_grp_mi[1], h->grp_n[1], h->grp_mi[1], measure, h->st2))) return rc;
+  if ((rc = launch_mi(h, h->d_grp_mi[0], h->grp_n[0], h->grp_mi[0], measure, h->st, 0))) return rc;
+  if ((rc = launch_mi(h, h->d_grp_mi[1], h->grp_n[1], h->grp_mi[1], measure, h->st2, 1))) return rc;
   KB_CUDA(h, cudaEventRecord(h->ev_join, h->st2));
   KB_CUDA(h, cudaStreamWaitEvent(h->st, h->ev_join, 0));
   if (e2) {
@@ -878,9 +875,10 @@ static int launch_step(kb_handle *h, int measure) {
     KB_CUDA(h, cudaEventRecord(e1, h->st));
     if (h->any_nlo || h->any_ninv) h->ev_pending.push_back({0, {e0, e1}});
   }
-  KB_CUDA(h, kb::launch_memint(h->fp64, memint_launch_variant(h), h->memint_split, memint_nwhole(h), h->d_runs, h->d_base_mi,
-                                   (int)h->runs.size(),
-                               h->total_mi, h->fin_nb_max, !h->memint_bulk + 2 * h->test_no_tiles, h->d_t, h->d_err, measure, h->smem_mi, h->st));
+  {
+    const int rc = launch_mi(h, h->d_base_mi, (int)h->runs.size(), h->total_mi, measure, h->st, 0);
+    if (rc) return rc;
+  }
   if (h->profiling) {
     KB_CUDA(h, cudaEventRecord(e2, h->st));
     h->ev_pending.push_back({1, {e1, e2}});
@@ -1457,6 +1455,7 @@ int kb_get_tuning(const kb_handle *h, kb_tuning *out) {
   out->batch_order = h->batch_order;
   out->sunset_variant = h->sunset_variant;
   out->memint_split = h->memint_split;
+  out->memint_persistent = h->memint_persistent;
   out->memint_bulk = h->memint_bulk;
   out->test_no_tiles = h->test_no_tiles;
   return KB_OK;
@@ -1480,6 +1479,11 @@ int kb_set_tuning(kb_handle *h, const kb_tuning *in) {
   if (in->memint_split < 0 || in->memint_split > 2 || (in->memint_split && !h->fp64 && in->memint_variant == 0))
     return fail(h, KB_ERR_PARAM, "memint_split=%d: 0, 1 or 2, and 1, 2 only with memint_variant 1 or 2 in KB_PREC_MIXED",
                 in->memint_split);
+  if (in->memint_persistent < 0 || in->memint_persistent > 1 ||
+      (in->memint_persistent && !h->fp64 && in->memint_variant == 0))
+    return fail(h, KB_ERR_PARAM,
+                "memint_persistent=%d: 0 or 1, and 1 only with memint_variant 1 or 2 in KB_PREC_MIXED",
+                in->memint_persistent);
   if (in->batch_order < 0 || in->batch_order > 1)
     return fail(h, KB_ERR_PARAM, "batch_order=%d: 0 (runs in order) or 1 (costliest first)", in->batch_order);
   if (in->memint_bulk < 0 || in->memint_bulk > 1)
@@ -1503,6 +1507,7 @@ int kb_set_tuning(kb_handle *h, const kb_tuning *in) {
   h->memint_variant = in->memint_variant;
   h->memint_compensated = in->memint_compensated;
   h->memint_split = in->memint_split;
+  h->memint_persistent = in->memint_persistent;
   h->memint_bulk = in->memint_bulk;
   h->test_no_tiles = in->test_no_tiles;
   h->sunset_variant = in->sunset_variant;
@@ -1530,9 +1535,10 @@ int kb_autotune(kb_handle *h, int32_t trials, kb_tuning *chosen, double *ms_per_
   if ((rc = set_overlap(h, 0, h->batch_order))) return rc;
   cudaEvent_t e[3];
   for (auto &x : e) KB_CUDA(h, cudaEventCreate(&x));
-  auto time_cfg = [&](int variant, int split, int svar, int grid, float *ms_sun, float *ms_mi) -> int {
+  auto time_cfg = [&](int variant, int split, int pers, int svar, int grid, float *ms_sun, float *ms_mi) -> int {
     h->memint_variant = variant;
     h->memint_split = split;
+    h->memint_persistent = pers;
     h->sunset_variant = svar;
     h->grid_sun = grid;
     float best_s = 1e30f, best_m = 1e30f;
@@ -1541,9 +1547,7 @@ int kb_autotune(kb_handle *h, int32_t trials, kb_tuning *chosen, double *ms_per_
       KB_CUDA(h, cudaEventRecord(e[0], h->st));
       if ((rc = launch_self_energies(h))) return rc;
       KB_CUDA(h, cudaEventRecord(e[1], h->st));
-      KB_CUDA(h, kb::launch_memint(h->fp64, memint_launch_variant(h), h->memint_split, memint_nwhole(h), h->d_runs, h->d_base_mi,
-                                   (int)h->runs.size(),
-                                   h->total_mi, h->fin_nb_max, !h->memint_bulk + 2 * h->test_no_tiles, h->d_t, h->d_err, 1, h->smem_mi, h->st));
+      if ((rc = launch_mi(h, h->d_base_mi, (int)h->runs.size(), h->total_mi, 1, h->st, 0))) return rc;
       KB_CUDA(h, cudaEventRecord(e[2], h->st));
       KB_CUDA(h, cudaEventSynchronize(e[2]));
       float a = 0, b = 0;
@@ -1583,7 +1587,7 @@ int kb_autotune(kb_handle *h, int32_t trials, kb_tuning *chosen, double *ms_per_
     mi_cands.push_back({2, 0});
     if (h->total_mi > h->num_sms && h->total_mi % h->num_sms) mi_cands.push_back({2, 2});
   }
-  int best_o = h->batch_order, best_v = v0, best_split = 0;
+  int best_o = h->batch_order, best_v = v0, best_split = 0, best_pers = 0;
   std::pair<int, int> best_sc = sun_cands[0];
   float best_total = 1e30f, best_s_all = 0, best_m_all = 0;
   for (int o = 0; o < norder && !rc; ++o) {
@@ -1593,18 +1597,27 @@ int kb_autotune(kb_handle *h, int32_t trials, kb_tuning *chosen, double *ms_per_
       break;
     }
     std::pair<int, int> sc_o = sun_cands[0];
-    int v_o = v0, sp_o = 0;
+    int v_o = v0, sp_o = 0, pe_o = 0;
     float bs = 1e30f, bm = 1e30f;
     for (size_t q = 0; q < sun_cands.size(); ++q) {
       float ms_s, ms_m;
-      if ((rc = time_cfg(v0, 0, sun_cands[q].first, sun_cands[q].second, &ms_s, &ms_m))) break;
+      if ((rc = time_cfg(v0, 0, 0, sun_cands[q].first, sun_cands[q].second, &ms_s, &ms_m))) break;
       if (ms_s < bs) { bs = ms_s; sc_o = sun_cands[q]; }
       if (q == 0) bm = ms_m;
     }
     for (size_t q = 0; q < mi_cands.size() && !rc; ++q) {
       float ms_s, ms_m;
-      if ((rc = time_cfg(mi_cands[q].first, mi_cands[q].second, sc_o.first, sc_o.second, &ms_s, &ms_m))) break;
+      if ((rc = time_cfg(mi_cands[q].first, mi_cands[q].second, 0, sc_o.first, sc_o.second, &ms_s, &ms_m))) break;
       if (ms_m < bm) { bm = ms_m; v_o = mi_cands[q].first; sp_o = mi_cands[q].second; }
+    }
+    // the chosen memory-integral kernel once more as a persistent grid (one CTA per SM
+    // taking items from a queue)
+    if (!rc && (h->fp64 || v_o != 0)) {
+      float ms_s, ms_m;
+      if (!(rc = time_cfg(v_o, sp_o, 1, sc_o.first, sc_o.second, &ms_s, &ms_m)) && ms_m < bm) {
+        bm = ms_m;
+        pe_o = 1;
+      }
     }
     if (!rc && bs + bm < best_total) {
       best_total = bs + bm;
@@ -1612,6 +1625,7 @@ int kb_autotune(kb_handle *h, int32_t trials, kb_tuning *chosen, double *ms_per_
       best_sc = sc_o;
       best_v = v_o;
       best_split = sp_o;
+      best_pers = pe_o;
       best_s_all = bs;
       best_m_all = bm;
     }
@@ -1624,6 +1638,7 @@ int kb_autotune(kb_handle *h, int32_t trials, kb_tuning *chosen, double *ms_per_
     return fail(h, KB_ERR_CUDA, "upload of the run schedule failed");
   h->memint_variant = best_v;
   h->memint_split = best_split;
+  h->memint_persistent = best_pers;
   h->sunset_variant = best_sc.first;
   h->grid_sun = best_sc.second;
   // batches: whole steps without and with the concurrent groups (second group's sunset

@@ -144,7 +144,7 @@ int sunset_max_ctas_per_sm(bool fp64, int variant, size_t smem);
 cudaError_t configure_sunset(bool fp64, size_t smem);
 cudaError_t launch_memint(bool fp64, int variant, int split, int nwhole, const RunDev *d_runs, const int *d_base,
                           int nruns, int total_ctas, int fin_nb_max, int use_maps, const int *d_t, int *d_err,
-                          int measure, size_t smem, cudaStream_t st);
+                          int measure, size_t smem, int *queue, int grid_cap, cudaStream_t st);
 constexpr int FIN_TP = 128;  // t' per CTA of the finishing kernel
 size_t memint_smem_bytes(bool fp64, int Malloc, int variant);
 cudaError_t configure_memint(bool fp64, size_t smem);

@@ -26,6 +26,7 @@
 // measurement of its orbits. No data leaves the CTA except the new row, so the
 // whole step needs no grid barrier. In split mode two CTAs share a chunk's
 // triangle and memint_finish_kernel runs the leapfrog (memint_kernel below).
+#include <algorithm>
 #include <cstdio>
 #include <type_traits>
 
@@ -553,7 +554,11 @@ __host__ __device__ inline int split_block(int J0, int Jn) {
 // releases the stage through the empty mbarrier. Once per column block both
 // groups meet at a named barrier: the row sums of that block are complete and
 // the column group runs its leapfrog.
-// SPLIT: the first nwhole CTAs take whole chunks as above; after them CTA
+// Items: with a null queue CTA v takes item v. With a queue the grid is
+// persistent (one CTA per SM): every CTA takes items from the counter until none
+// are left, keeping its TMEM allocation and its stage barriers -- whose phases
+// run on across items -- and the tadpole sum of the run it last took.
+// SPLIT: the first nwhole items are whole chunks as above; after them item
 // nwhole + 2k + h streams half h of chunk nwhole + k's triangle, keeps its row
 // sums in row buffer h and stores the column sums of its column blocks instead
 // of running the leapfrog; memint_finish_kernel completes those chunks. Split
@@ -566,9 +571,10 @@ __host__ __device__ inline int split_block(int J0, int Jn) {
 // the column group's warp q reads, and takes over that warp's columns and
 // orbits, so the arithmetic and its order are the column group's.
 template <typename TS, int T, int NST, int OPT, bool SPLIT, bool LFW = false, bool COMP = false>
-__global__ void __launch_bounds__(2 * T * (KC / OPT) + 32 + (LFW ? T * (KC / OPT) : 0))
+__global__ void __launch_bounds__(2 * T * (KC / OPT) + 32 + (LFW ? T * (KC / OPT) : 0), 1)
 memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int nruns,
-              const int *__restrict__ d_t, int *__restrict__ d_err, int measure, int nwhole, int use_maps) {
+              const int *__restrict__ d_t, int *__restrict__ d_err, int measure, int nwhole, int use_maps,
+              int nitems, int *__restrict__ queue) {
   using C = Cfg<TS, T, NST, OPT>;
   using V = Vec<TS, OPT>;
   using A = typename std::conditional<COMP, Acc<TS, OPT>, PlainAcc<TS, OPT>>::type;
@@ -577,7 +583,7 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   uint64_t *full = reinterpret_cast<uint64_t *>(smem_raw + (size_t)NST * C::STAGE_BYTES);
   uint64_t *empty = full + NST;
   // misc: [0] hartreecont, [1] M^2, [2..2+KC) acc_F(t-1) per orbit, [10] abort flag,
-  // [11] tiles issued, [12] consumer abort flag, [14] TMEM address,
+  // [11] tiles issued, [12] consumer abort flag, [13] current item, [14] TMEM address,
   // [16..16+(NG/32)*KC) diagonal partials
   double *misc = reinterpret_cast<double *>(empty + NST);  // 128 doubles
   volatile int *abort_flag = reinterpret_cast<volatile int *>(misc + 10);
@@ -594,12 +600,6 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   uint64_t *lf_empty = lf_full + 2;
   double *lf_stage = reinterpret_cast<double *>(smem_raw + smem_fixed_bytes<C>());
 
-  const bool split = SPLIT && (int)blockIdx.x >= nwhole;
-  const int item = split ? nwhole + (((int)blockIdx.x - nwhole) >> 1) : (int)blockIdx.x;
-  const int half = split ? (((int)blockIdx.x - nwhole) & 1) : 0;
-  const int r = run_at(base, nruns, item);
-  const RunDev &R = runs[r];
-  const int c = item - R.cta_base_mi;  // chunk
   const int tid = threadIdx.x;
   const bool producer = tid >= C::NT && tid < C::NT + 32;
   const bool lfwarp = LFW && tid >= C::NT + 32;  // leapfrog warps
@@ -610,36 +610,11 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   const int j0 = jq * OPT;                          // first orbit of this thread in the chunk
   const int lane = tid & 31, warp = tid >> 5;
   const int t = *d_t;
-  const int M = R.M, Ma = R.Malloc;
-  const int tmin = max(1, t - M + 1);
-  const size_t rowstride = (size_t)Ma * KC;              // one row of one chunk
-  // row sums of this chunk, [Malloc][KC]: entries (slot, j0..j0+OPT-1) are only
-  // ever written by row-group thread (slot mod T, jq), so they need no atomics.
-  // With FP32 history they live in TMEM (Malloc/T slots x OPT doubles per lane)
-  // when they fit, else in a global scratch slot; a split CTA copies them there
-  // at the end (one buffer per half) for memint_finish_kernel. The FP64 kernel,
-  // bound by FP64 arithmetic, runs 1 % faster on the global scratch.
-  double *rowacc = R.rowacc + (size_t)half * R.nchunks * rowstride + (size_t)c * rowstride;
-  const bool use_tmem = sizeof(TS) == 4 && (Ma / T) * OPT * 2 <= (int)TMEM_COLS;
-  const bool use_tmap = (use_maps & 1) && R.tmap != nullptr;
-  const bool no_tiles = (use_maps & 2) != 0;  // test hook: nothing is issued, the consumers' waits run out
-  if (use_tmem && warp == 0) tmem_alloc(const_cast<uint32_t *>(tmem_slot));
-
-  // --- tadpole mass M^2(t-1) from the per-chunk sums of F(t-1,t-1) (fixed order)
-  if (warp == 0) {
-    const double *tad = R.tad + (size_t)((t - 1) & 1) * R.nchunks;
-    double s = tad_lane_sum(tad, R.nchunks, lane);
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) {
-      misc[0] = s;                          // hartreecont = sum_k deg_k F(t-1,t-1,k)
-      misc[1] = s * R.pref_ivol + R.mass2;  // getHartreeMass2 order: (sum * (pref*ivol)) + Mass2
-    }
-  }
-  if (tid < KC) misc[2 + tid] = 0.0;
+  volatile int *item_slot = reinterpret_cast<volatile int *>(misc + 13);
+  // row sums in TMEM (FP32 history): one allocation for every item of the CTA
+  constexpr bool kTmem = sizeof(TS) == 4;
+  if (kTmem && warp == 0) tmem_alloc(const_cast<uint32_t *>(tmem_slot));
   if (tid == 0) {
-    *abort_flag = 0;
-    *issued_count = 0;
-    *cabort = 0;
     for (int q = 0; q < NST; ++q) {
       mbar_init(full + q, 1);
       mbar_init(empty + q, C::NW);  // one arrival per consumer warp
@@ -650,6 +625,58 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
         mbar_init(lf_empty + q, C::NG / 32);  // leapfrog warps
       }
     fence_proxy_async();
+  }
+  if (kTmem) tmem_fence_before();
+  __syncthreads();
+  if (kTmem) tmem_fence_after();
+  const uint32_t tbase = kTmem ? *tmem_slot : 0u;
+  const uint32_t tlane = ((uint32_t)(warp & 3) * 32u) << 16;  // this warp's TMEM lanes
+  int nb = 0;      // tiles this CTA streamed before the current item (stage barrier phases)
+  int lb = 0;      // column blocks it handed to the leapfrog warps before the current item
+  int cur_r = -1;  // run whose tadpole sum misc[0..1] holds
+  bool first = true;
+  for (;;) {
+  if (tid == 0) *item_slot = queue ? atomicAdd(queue, 1) : (first ? (int)blockIdx.x : nitems);
+  __syncthreads();
+  const int vb = *item_slot;
+  first = false;
+  if (vb >= nitems) break;
+  const bool split = SPLIT && vb >= nwhole;
+  const int item = split ? nwhole + ((vb - nwhole) >> 1) : vb;
+  const int half = split ? ((vb - nwhole) & 1) : 0;
+  const int r = run_at(base, nruns, item);
+  const RunDev &R = runs[r];
+  const int c = item - R.cta_base_mi;  // chunk
+  const int M = R.M, Ma = R.Malloc;
+  const int tmin = max(1, t - M + 1);
+  const size_t rowstride = (size_t)Ma * KC;              // one row of one chunk
+  // row sums of this chunk, [Malloc][KC]: entries (slot, j0..j0+OPT-1) are only
+  // ever written by row-group thread (slot mod T, jq), so they need no atomics.
+  // With FP32 history they live in TMEM (Malloc/T slots x OPT doubles per lane)
+  // when they fit, else in a global scratch slot; a split CTA copies them there
+  // at the end (one buffer per half) for memint_finish_kernel. The FP64 kernel,
+  // bound by FP64 arithmetic, runs 1 % faster on the global scratch.
+  double *rowacc = R.rowacc + (size_t)half * R.nchunks * rowstride + (size_t)c * rowstride;
+  const bool use_tmem = kTmem && (Ma / T) * OPT * 2 <= (int)TMEM_COLS;
+  const bool use_tmap = (use_maps & 1) && R.tmap != nullptr;
+  const bool no_tiles = (use_maps & 2) != 0;  // test hook: nothing is issued, the consumers' waits run out
+
+  // --- tadpole mass M^2(t-1) from the per-chunk sums of F(t-1,t-1) (fixed order), once per run
+  if (r != cur_r && warp == 0) {
+    const double *tad = R.tad + (size_t)((t - 1) & 1) * R.nchunks;
+    double s = tad_lane_sum(tad, R.nchunks, lane);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) {
+      misc[0] = s;                          // hartreecont = sum_k deg_k F(t-1,t-1,k)
+      misc[1] = s * R.pref_ivol + R.mass2;  // getHartreeMass2 order: (sum * (pref*ivol)) + Mass2
+    }
+  }
+  cur_r = r;
+  if (tid < KC) misc[2 + tid] = 0.0;
+  if (tid == 0) {
+    *abort_flag = 0;
+    *issued_count = 0;
+    *cabort = 0;
   }
   if (!use_tmem && rowgrp)
     for (int s = loc; s < Ma; s += T)  // the slots this thread owns
@@ -662,8 +689,6 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
     R.hcm2[0] = misc[0];
     R.hcm2[1] = misc[1];
   }
-  const uint32_t tbase = use_tmem ? *tmem_slot : 0u;
-  const uint32_t tlane = ((uint32_t)(warp & 3) * 32u) << 16;  // this warp's TMEM lanes
   // TMEM column of the row sums of slot s (s mod T is the thread's loc)
   auto tcol = [&](int s) { return tbase + tlane + (uint32_t)((s / T) * OPT * 2); };
   if (use_tmem && rowgrp) {
@@ -687,8 +712,9 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
     // ---------------- producer warp: stream every tile of its column blocks once
     TileIt it{Jlo, Jlo, Jn};
     for (int n = 0; n < ntiles; ++n, it.next()) {
-      const int stage = n % NST;
-      if (n >= NST && !mbar_wait_bounded(empty + stage, (uint32_t)(((n / NST) - 1) & 1))) {
+      const int gn = nb + n;  // the CTA's tile count picks the stage and its phase
+      const int stage = gn % NST;
+      if (gn >= NST && !mbar_wait_bounded(empty + stage, (uint32_t)(((gn / NST) - 1) & 1))) {
         if (lane == 0) {
           *abort_flag = 1;
           atomicOr(d_err, DEVERR_TIMEOUT);
@@ -710,7 +736,7 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
       for (int o = 0; o < OPT; ++o) diag[o] = emem[o] = 0.0;
       bool has_emem = false, ok = true;
       for (int J = Jlo; J <= Jhi; ++J) {
-        const int slot = (J - Jlo) & 1, use = (J - Jlo) >> 1;
+        const int slot = (lb + J - Jlo) & 1, use = (lb + J - Jlo) >> 1;
         ok = __all_sync(0xffffffffu, lf_wait(lf_full + slot, (uint32_t)(use & 1), cabort));
         if (!ok) break;
         if (use_tmem) tmem_fence_after();
@@ -768,8 +794,9 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
       for (int o = 0; o < OPT; ++o) colF[o] = colR[o] = 0.0;
 
       for (int I = lo_only ? Jn + 1 : J; I <= Jn; ++I, ++n) {
-        const int stage = n % NST;
-        bool ok = !*cabort && mbar_wait_bounded(full + stage, (uint32_t)((n / NST) & 1));
+        const int gn = nb + n;
+        const int stage = gn % NST;
+        bool ok = !*cabort && mbar_wait_bounded(full + stage, (uint32_t)((gn / NST) & 1));
         ok = __all_sync(0xffffffffu, ok);  // warp-uniform decision
         if (!ok) {
           // a wait expired here or in another consumer: leave the tile loop; all
@@ -910,7 +937,7 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
       }
       if (lf_on) {  // column sums of this block to the leapfrog warps
         if (colgrp) {
-          const int slot = (J - Jlo) & 1, use = (J - Jlo) >> 1;
+          const int slot = (lb + J - Jlo) & 1, use = (lb + J - Jlo) >> 1;
           // the buffer's previous block must have been read; a wait that runs out
           // aborts the chunk at the next tile wait of every consumer
           if (use > 0 && !mbar_wait_bounded(lf_empty + slot, (uint32_t)((use - 1) & 1))) {
@@ -953,14 +980,15 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   if (use_tmem) tmem_fence_before();
   __syncthreads();  // producer done issuing; consumers done with the triangle
   if (use_tmem) tmem_fence_after();
-  if (*abort_flag) {
+  const bool aborted_item = *abort_flag != 0;  // read by every thread between two barriers
+  if (aborted_item) {
     // drain copies still in flight into this CTA's shared memory: only the last NST
     // issued tiles can be (the producer reuses a stage after its consumers release it),
     // and for those the stage barrier's latest phase is theirs; an older tile's phase
     // parity repeats on its stage, so waiting on it would run to the bound
     if (tid == 0)
       for (int q = max(0, *issued_count - NST); q < *issued_count; ++q)
-        (void)mbar_wait_bounded(full + (q % NST), (uint32_t)((q / NST) & 1));
+        (void)mbar_wait_bounded(full + ((nb + q) % NST), (uint32_t)(((nb + q) / NST) & 1));
   } else {
     if (split && use_tmem && rowgrp)  // this half's row sums, for memint_finish_kernel
       for (int s = 0; s < Ma; s += T) {
@@ -970,15 +998,22 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
       }
     if (!split && tid < KC) memint_epilogue<TS>(R, c, t, tid, misc, C::NG / 32, M2, measure);
   }
-  if (use_tmem) {  // every path ends here: the allocating warp frees the TMEM
+  nb += ntiles;
+  if (lf_on) lb += Jhi - Jlo + 1;
+  if (use_tmem) tmem_fence_before();
+  __syncthreads();  // the item's TMEM reads and misc values are done with
+  if (use_tmem) tmem_fence_after();
+  // a wait that ran out leaves this CTA's stage barriers mid-phase: it takes no more
+  // items (the others go on taking them; the error word reports the timeout)
+  if (aborted_item) break;
+  }  // items
+  if (kTmem) {  // every path ends here: the allocating warp frees the TMEM
     tmem_fence_before();
     __syncthreads();
     if (warp == 0) {
       tmem_fence_after();
       tmem_dealloc(tbase);
     }
-  } else {
-    __syncthreads();
   }
 }
 
@@ -1610,44 +1645,53 @@ cudaError_t configure_memint(bool fp64, size_t smem) {
 }
 
 // use_maps: bit 0 tensor-map boxes (else bulk copies), bit 1 the test hook that
-// issues no tiles (memint_kernel only)
+// issues no tiles (memint_kernel only). queue: null, or a device counter that makes
+// memint_kernel persistent on at most grid_cap CTAs (zeroed here before the launch).
 cudaError_t launch_memint(bool fp64, int variant, int split, int nwhole, const RunDev *d_runs, const int *d_base,
                           int nruns, int total_ctas, int fin_nb_max, int use_maps, const int *d_t, int *d_err,
-                          int measure, size_t smem, cudaStream_t st) {
+                          int measure, size_t smem, int *queue, int grid_cap, cudaStream_t st) {
   // split: the chunks from nwhole on are streamed by two half-triangle CTAs each
   // and completed by the finishing kernel
   const int nsplit = total_ctas - nwhole;
+  const bool splitting = split && nsplit > 0;
+  const int nitems = splitting ? nwhole + 2 * nsplit : total_ctas;
+  const bool persistent = queue != nullptr && grid_cap > 0 && (fp64 || variant != 0);
+  const int grid = persistent ? std::min(nitems, grid_cap) : nitems;
+  int *q = persistent ? queue : nullptr;
+  if (persistent) {
+    const cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(int), st);
+    if (e != cudaSuccess) return e;
+  }
+  const int nw = splitting ? nwhole : total_ctas;
   constexpr int NTHR_LF = CfgF32::NT + 32 + CfgF32::NG;  // consumers, producer, leapfrog warps
   if (!fp64 && (variant == 2 || variant == 3)) {  // leapfrog warps for the whole chunks; 3: compensated sums
-    if (split && nsplit > 0) {
+    if (splitting) {
       if (variant == 3)
         memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT, true, true, true>
-            <<<nwhole + 2 * nsplit, NTHR_LF, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, nwhole, use_maps);
+            <<<grid, NTHR_LF, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, nw, use_maps, nitems, q);
       else
         memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT, true, true>
-            <<<nwhole + 2 * nsplit, NTHR_LF, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, nwhole, use_maps);
+            <<<grid, NTHR_LF, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, nw, use_maps, nitems, q);
       memint_finish_kernel<float><<<nsplit * fin_nb_max, FIN_THREADS, 0, st>>>(d_runs, d_base, nruns, fin_nb_max,
                                                                                nwhole, d_t, measure);
     } else if (variant == 3) {
       memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT, false, true, true>
-          <<<total_ctas, NTHR_LF, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, total_ctas, use_maps);
+          <<<grid, NTHR_LF, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, nw, use_maps, nitems, q);
     } else {
       memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT, false, true>
-          <<<total_ctas, NTHR_LF, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, total_ctas, use_maps);
+          <<<grid, NTHR_LF, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, nw, use_maps, nitems, q);
     }
     return cudaGetLastError();
   }
-  if (split && nsplit > 0 && (fp64 || variant == 1)) {
+  if (splitting && (fp64 || variant == 1)) {
     if (fp64) {
-      memint_kernel<double, CfgF64::T, CfgF64::NST, CfgF64::OPT, true><<<nwhole + 2 * nsplit, CfgF64::NT + 32, smem,
-                                                                         st>>>(d_runs, d_base, nruns, d_t, d_err,
-                                                                               measure, nwhole, use_maps);
+      memint_kernel<double, CfgF64::T, CfgF64::NST, CfgF64::OPT, true>
+          <<<grid, CfgF64::NT + 32, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, nw, use_maps, nitems, q);
       memint_finish_kernel<double><<<nsplit * fin_nb_max, FIN_THREADS, 0, st>>>(d_runs, d_base, nruns, fin_nb_max,
                                                                                 nwhole, d_t, measure);
     } else {
-      memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT, true><<<nwhole + 2 * nsplit, CfgF32::NT + 32, smem,
-                                                                        st>>>(d_runs, d_base, nruns, d_t, d_err,
-                                                                              measure, nwhole, use_maps);
+      memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT, true>
+          <<<grid, CfgF32::NT + 32, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, nw, use_maps, nitems, q);
       memint_finish_kernel<float><<<nsplit * fin_nb_max, FIN_THREADS, 0, st>>>(d_runs, d_base, nruns, fin_nb_max,
                                                                                nwhole, d_t, measure);
     }
@@ -1655,10 +1699,10 @@ cudaError_t launch_memint(bool fp64, int variant, int split, int nwhole, const R
   }
   if (fp64)
     memint_kernel<double, CfgF64::T, CfgF64::NST, CfgF64::OPT, false>
-        <<<total_ctas, CfgF64::NT + 32, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, total_ctas, use_maps);
+        <<<grid, CfgF64::NT + 32, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, nw, use_maps, nitems, q);
   else if (variant == 1)
     memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT, false>
-        <<<total_ctas, CfgF32::NT + 32, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, total_ctas, use_maps);
+        <<<grid, CfgF32::NT + 32, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, nw, use_maps, nitems, q);
   else
     memint_blk_kernel<CfgF32::NST><<<total_ctas, 288, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure);
   return cudaGetLastError();

@@ -54,14 +54,15 @@ class KbMeasScalars(C.Structure):
 class KbTuning(C.Structure):
     _fields_ = [("memint_variant", C.c_int32), ("sunset_grid", C.c_int32), ("batch_order", C.c_int32),
                 ("sunset_variant", C.c_int32), ("memint_split", C.c_int32), ("memint_bulk", C.c_int32),
-                ("test_no_tiles", C.c_int32), ("memint_compensated", C.c_int32), ("batch_overlap", C.c_int32)]
+                ("test_no_tiles", C.c_int32), ("memint_compensated", C.c_int32), ("batch_overlap", C.c_int32),
+                ("memint_persistent", C.c_int32)]
 
     def as_dict(self):
         return {"memint_variant": self.memint_variant, "sunset_grid": self.sunset_grid,
                 "batch_order": self.batch_order, "sunset_variant": self.sunset_variant,
                 "memint_split": self.memint_split, "memint_bulk": self.memint_bulk,
                 "test_no_tiles": self.test_no_tiles, "memint_compensated": self.memint_compensated,
-                "batch_overlap": self.batch_overlap}
+                "batch_overlap": self.batch_overlap, "memint_persistent": self.memint_persistent}
 
 
 class KbError(RuntimeError):
@@ -322,7 +323,7 @@ class Handle:
 
     def set_tuning(self, memint_variant=None, sunset_grid=None, batch_order=None, sunset_variant=None,
                    memint_split=None, memint_bulk=None, test_no_tiles=None, memint_compensated=None,
-                   batch_overlap=None):
+                   batch_overlap=None, memint_persistent=None):
         cur = KbTuning()
         self._check(self.lib.kb_get_tuning(self.h, C.byref(cur)))
         if memint_variant is not None:
@@ -343,6 +344,8 @@ class Handle:
             cur.memint_compensated = int(memint_compensated)
         if batch_overlap is not None:
             cur.batch_overlap = int(batch_overlap)
+        if memint_persistent is not None:
+            cur.memint_persistent = int(memint_persistent)
         self._check(self.lib.kb_set_tuning(self.h, C.byref(cur)))
 
     def autotune(self, trials=3):

@@ -1,7 +1,7 @@
 """The KB_DEBUG build (libkb2pi_debug.so): device-side bounds checks on ring,
 tile and Sigma indices stay clear on small lattices and windows (Ns = 4..8,
 M = 3..10, wrapping rings, both precisions, every memory-integral split mode,
-a batch of uneven runs), and the checked build computes what the release build
+the persistent memory-integral grid, a batch of uneven runs), and the checked build computes what the release build
 computes. The checked library runs in a child process (KB2PI_LIB selects it for
 that process); a failed check would surface as KB_ERR_RANGE from kb_sync.
 """
@@ -18,7 +18,7 @@ ROOT = os.path.dirname(HERE)
 DEBUG_LIB = os.path.join(ROOT, "qftdynamicsm.jl_gb300", "kb2pi", "libkb2pi_debug.so")
 
 CASES = [
-    # (runs, precision, memint_split[, sunset_variant]): each run (Ns, M, lambda, T)
+    # (runs, precision, memint_split[, sunset_variant[, memint_persistent]]): each run (Ns, M, lambda, T)
     ([(4, 3, 2.0, 1.5)], 0, 0),
     ([(8, 9, 2.0, 1.5), (6, 5, 3.0, 2.0)], 1, 0, 2),  # the tensor-core sunset
     ([(6, 5, 3.0, 2.0)], 0, 1),
@@ -27,6 +27,8 @@ CASES = [
     ([(8, 9, 1.0, 1.5)], 1, 2),
     ([(4, 3, 2.0, 1.5), (6, 10, 3.0, 1.0), (8, 6, 1.5, 2.5)], 1, 2),
     ([(6, 4, 2.0, 1.5), (8, 9, 3.0, 2.0)], 0, 2),
+    ([(4, 3, 2.0, 1.5), (6, 10, 3.0, 1.0), (8, 6, 1.5, 2.5)], 1, 2, 0, 1),  # persistent memory integrals
+    ([(6, 4, 2.0, 1.5), (8, 9, 3.0, 2.0)], 0, 1, 0, 1),
 ]
 STEPS = 24
 
@@ -48,6 +50,8 @@ def run_cases():
             h.init(r, 1.0 / (np.exp(np.sqrt(k2 + 1.0) / T) - 1.0), 1.0)
         if sv:
             h.set_tuning(sunset_variant=sv[0])
+        if len(sv) > 1:
+            h.set_tuning(memint_persistent=sv[1])
         h.steps(3, 4, 0)
         if split and prec == 1:
             h.set_tuning(memint_variant=2 if split == 2 else 1, memint_split=split)

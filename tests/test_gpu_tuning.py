@@ -309,8 +309,68 @@ def test_memint_bulk_copies_match_tensor_maps(precision):
         h.close()
 
 
-@pytest.mark.parametrize("precision,variant", [(0, None), (1, None), (1, 2)])
-def test_bounded_wait_runs_out_and_is_reported(precision, variant):
+@pytest.mark.parametrize("precision,variant,split", [(0, 0, 0), (0, 0, 1), (1, 1, 0), (1, 1, 1), (1, 2, 0), (1, 2, 2)])
+def test_persistent_memint_is_bitwise_the_grid_of_one_cta_per_item(precision, variant, split):
+    """memint_persistent 1 (one CTA per SM taking chunk items from a queue, its stage
+    barriers' phases running on across items, the tadpole sum kept per run) gives the
+    same F, rho, n and E as one CTA per item, bitwise; 222 chunks at Ns = 40, more
+    than one per SM, so CTAs take several items (and split halves with split 1, 2)."""
+    cfg = dict(Ns=40, M=20, N=4, lam=3.0, dt=0.1, pexp=1, T=1.5)
+    hs = []
+    for pers in (0, 1):
+        h = make_gpu(cfg, precision)
+        _, k2, _ = h.orbits()
+        h.init(0, occupation(cfg, k2), 1.0)
+        h.set_tuning(memint_variant=variant, memint_split=split, memint_persistent=pers)
+        assert h.tuning()["memint_persistent"] == pers
+        h.steps(3, 30, 0)
+        for t in range(33, 36):  # single steps after the graph-captured ones
+            h.step(t)
+        hs.append(h)
+    a, b = hs
+    ma, mb = a.measure(0, 35), b.measure(0, 35)
+    assert ma["E"] == mb["E"] and np.array_equal(ma["n"], mb["n"])
+    tmin, _ = a.window(0)
+    for tp in sorted({tmin, (tmin + 35) // 2, 34, 35}):
+        assert np.array_equal(a.get(0, 0, 35, tp), b.get(0, 0, 35, tp))
+        assert np.array_equal(a.get(0, 1, 35, tp), b.get(0, 1, 35, tp))
+    for h in hs:
+        h.close()
+
+
+def test_persistent_memint_batched_runs_and_errors():
+    """Uneven batched runs (several runs per CTA, tadpole sums switching between
+    runs) bitwise equal with and without the persistent grid; the register-blocked
+    kernel has no persistent form; the autotuner reports its choice."""
+    from kb2pi import capi
+
+    cfgs = [dict(Ns=24, M=30, lam=2.0, T=1.0), dict(Ns=8, M=41, lam=4.0, T=2.0), dict(Ns=16, M=37, lam=1.0, T=0.7),
+            dict(Ns=6, M=9, lam=3.0, T=1.5), dict(Ns=24, M=20, lam=1.0, T=1.0)]
+    out = []
+    for pers in (0, 1):
+        ps = [capi.KbParams(Ns=c["Ns"], sdim=3, M=c["M"], N=4, pexp=1, precision=1, device=0, flags=0, dt=0.1,
+                            lam=c["lam"], mass2=1.0, mass=1.0) for c in cfgs]
+        h = capi.Handle(ps)
+        for r, c in enumerate(cfgs):
+            _, k2, _ = h.orbits(r)
+            h.init(r, occupation(dict(c), k2), 1.0)
+        h.set_tuning(memint_variant=2, memint_split=1, batch_order=1, memint_persistent=pers)
+        h.steps(3, 50, 0)
+        out.append([(h.measure(r, 52), h.get(r, 0, 52, 48), h.get(r, 1, 52, 48)) for r in range(len(cfgs))])
+        if pers:
+            with pytest.raises(capi.KbError, match="KB_ERR_PARAM"):
+                h.set_tuning(memint_variant=0, memint_split=0, memint_persistent=1)
+            chosen = h.autotune(trials=1)
+            assert chosen["memint_persistent"] in (0, 1)
+        h.close()
+    for (ma, Fa, ra), (mb, Fb, rb) in zip(out[0], out[1]):
+        assert ma["E"] == mb["E"] and np.array_equal(ma["n"], mb["n"])
+        assert np.array_equal(Fa, Fb) and np.array_equal(ra, rb)
+
+
+@pytest.mark.parametrize("precision,variant,persistent", [(0, None, 0), (1, None, 0), (1, 2, 0), (0, None, 1),
+                                                          (1, 2, 1)])
+def test_bounded_wait_runs_out_and_is_reported(precision, variant, persistent):
     """Failure detection without a GPU fault: with the test hook the memory-
     integral producer issues no tiles, so every consumer's bounded wait runs out
     (about 2 s), the kernel sets its error bit, frees its tensor memory and
@@ -324,6 +384,8 @@ def test_bounded_wait_runs_out_and_is_reported(precision, variant):
     h.init(0, occupation(cfg, k2), 1.0)
     if variant is not None:  # the leapfrog warps leave their hand-off wait when the consumers abort
         h.set_tuning(memint_variant=variant)
+    if persistent:  # an aborted item ends its CTA's queue loop
+        h.set_tuning(memint_persistent=1)
     h.steps(3, 5, 0)
     h.sync()
     h.set_tuning(test_no_tiles=1)
