@@ -224,25 +224,28 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 }
 
 // Tensor maps of the two history rings as [tiles][T rows][T*KC] (tile-major
-// layout: every T x T x KC tile is contiguous, rows RS apart); box = one tile.
-// Returns a device copy of the two maps, or null (the kernels then use plain
-// bulk copies).
+// layout: every T x T x KC tile is contiguous, rows RS apart): maps 0, 1 (F, rho)
+// with one tile as the box, maps 2, 3 with the lower T/2 rows of a tile (diagonal
+// tiles). Returns a device copy of the four maps, or null (the kernels then use
+// plain bulk copies).
 void *make_history_maps(const Run &R) {
   auto enc = tensor_map_encoder();
   if (!enc) return nullptr;
-  alignas(64) CUtensorMap maps[2];
+  alignas(64) CUtensorMap maps[4];
   const cuuint64_t inner = (cuuint64_t)R.T * KC;
   const cuuint64_t dims[3] = {inner, (cuuint64_t)R.T,
                               (cuuint64_t)R.nchunks * (R.Malloc / R.T) * (R.Malloc / R.T)};
   const cuuint64_t strides[2] = {inner * R.esz, inner * R.T * R.esz};
-  const cuuint32_t box[3] = {(cuuint32_t)inner, (cuuint32_t)R.T, 1}, estr[3] = {1, 1, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
   const CUtensorMapDataType dt = R.esz == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
   void *bases[2] = {R.hist_F, R.hist_r};
-  for (int f = 0; f < 2; ++f)
-    if (enc(&maps[f], dt, 3, bases[f], dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+  for (int m = 0; m < 4; ++m) {
+    const cuuint32_t box[3] = {(cuuint32_t)inner, (cuuint32_t)(m < 2 ? R.T : R.T / 2), 1};
+    if (enc(&maps[m], dt, 3, bases[m & 1], dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) !=
         CUDA_SUCCESS)
       return nullptr;
+  }
   void *d = nullptr;
   if (cudaMalloc(&d, sizeof maps) != cudaSuccess) {
     cudaGetLastError();

@@ -86,7 +86,8 @@ struct RunDev {
   double *fin_prev;  // [nchunks][KC] acc_F(t-1)
   double *hcm2;      // [2] hartreecont and M^2(t-1) of the step
   // tensor maps (CUtensorMap, 64-byte aligned, device memory) of hist_F and hist_r
-  // as [tiles][T rows][T KC]: a tile is one box; null when the CUDA driver has no encoder
+  // as [tiles][T rows][T KC]: [0], [1] a tile per box, [2], [3] its lower T/2 rows;
+  // null when the CUDA driver has no encoder
   const void *tmap;
   int *err;  // the handle's device error word (timeouts; bounds checks of KB_DEBUG builds)
 };

@@ -342,6 +342,7 @@ __device__ __forceinline__ void tile_box(int I, int J, int tmin, int tlast, int 
 template <typename TS, typename C>
 __device__ __forceinline__ void issue_tile(int stage, int I, int J, const RunDev &R, int c, TS *stages,
                                            uint64_t *full, int tmin, int tlast, bool use_tmap) {
+  constexpr int T = C::T, TH = T / 2;
   const int lane = threadIdx.x & 31;
   uint64_t *bar = full + stage;
   TS *dst = stages + (size_t)stage * C::STAGE;
@@ -349,27 +350,39 @@ __device__ __forceinline__ void issue_tile(int stage, int I, int J, const RunDev
   const int sb0 = (J * C::T) % R.Malloc;
   const TS *hF = reinterpret_cast<const TS *>(R.hist_F);
   const TS *hR = reinterpret_cast<const TS *>(R.hist_r);
+  // a diagonal tile inside the window is read only on and below its diagonal (column
+  // sums take rows a >= b, row sums columns b < a): its upper-right quadrant (rows
+  // < T/2, columns >= T/2) is not loaded -- the lower half as rows, the upper-left
+  // quadrant as half rows; the stage keeps whatever that quadrant held
+  int r0, x0;
+  tile_box<C>(I, J, tmin, tlast, r0, x0);
+  const bool quad = (I == J) && r0 == 0 && x0 == 0;
+  const size_t off = hist_off(R.Malloc, T, c, sa0, sb0, 0);  // start of the tile
   if (lane == 0) {
-    constexpr int T = C::T;
     (void)KB_DCHECK(I >= J && J * T <= tlast && I * T <= tlast && (I + 1) * T - 1 >= tmin && c >= 0 &&
                         c < R.nchunks && (I - J) * T < R.M + T && R.Malloc % T == 0 && sa0 + T <= R.Malloc &&
-                        sb0 + T <= R.Malloc,
+                        sb0 + T <= R.Malloc && (!quad || (I * T >= tmin && I * T + T - 1 <= tlast)),
                     R.err, DCHK_MI_TILE);
+    constexpr uint32_t QB = 2u * TH * (TH * KC) * (uint32_t)sizeof(TS);  // upper-left quadrants of F and rho
+    constexpr uint32_t XB = 3u * C::XV * (uint32_t)sizeof(TS);           // the three x vectors
     if (use_tmap) {
-      int r0, x0;
-      tile_box<C>(I, J, tmin, tlast, r0, x0);
       const int nb = R.Malloc / T;
       const int tile = (c * nb + sa0 / T) * nb + sb0 / T;
-      mbar_expect_tx(bar, 2 * C::TILE * (uint32_t)sizeof(TS) + 3 * C::XV * (uint32_t)sizeof(TS));
       const char *tm = reinterpret_cast<const char *>(R.tmap);
-      tma_load_3d(dst, tm, x0, r0, tile, bar);
-      tma_load_3d(dst + C::TILE, tm + 128, x0, r0, tile, bar);
+      if (quad) {  // maps 2, 3: boxes of the lower T/2 rows
+        mbar_expect_tx(bar, 2u * TH * C::RS * (uint32_t)sizeof(TS) + QB + XB);
+        tma_load_3d(dst + TH * C::RS, tm + 256, 0, TH, tile, bar);
+        tma_load_3d(dst + C::TILE + TH * C::RS, tm + 384, 0, TH, tile, bar);
+      } else {
+        mbar_expect_tx(bar, 2 * C::TILE * (uint32_t)sizeof(TS) + XB);
+        tma_load_3d(dst, tm, x0, r0, tile, bar);
+        tma_load_3d(dst + C::TILE, tm + 128, x0, r0, tile, bar);
+      }
     } else {
       constexpr uint32_t ROWB = (uint32_t)(C::RS * sizeof(TS));
-      const size_t off = hist_off(R.Malloc, T, c, sa0, sb0, 0);  // start of the tile
-      const int rlo = max(0, tmin - I * T), rhi = min(T - 1, tlast - I * T);  // rows of the window
+      const int rlo = quad ? TH : max(0, tmin - I * T), rhi = min(T - 1, tlast - I * T);  // rows of the window
       const uint32_t n = (uint32_t)(rhi - rlo + 1) * ROWB;
-      mbar_expect_tx(bar, 2 * n + 3 * C::XV * (uint32_t)sizeof(TS));
+      mbar_expect_tx(bar, 2 * n + (quad ? QB : 0u) + XB);
       const size_t e = (size_t)rlo * C::RS;
       bulk_g2s(dst + e, hF + off + e, n, bar);
       bulk_g2s(dst + C::TILE + e, hR + off + e, n, bar);
@@ -379,6 +392,12 @@ __device__ __forceinline__ void issue_tile(int stage, int I, int J, const RunDev
     bulk_g2s(dst + 2 * C::TILE, sr + (size_t)sa0 * KC, C::XV * sizeof(TS), bar);
     bulk_g2s(dst + 2 * C::TILE + C::XV, sr + (size_t)sb0 * KC, C::XV * sizeof(TS), bar);
     bulk_g2s(dst + 2 * C::TILE + 2 * C::XV, sF + (size_t)sb0 * KC, C::XV * sizeof(TS), bar);
+  }
+  __syncwarp();  // the expected bytes are set before any half row lands
+  if (quad && lane < 2 * TH) {  // one half row (columns < T/2 of row rr) per lane and field
+    const int f = lane / TH, rr = lane % TH;
+    const size_t e = (size_t)rr * C::RS;
+    bulk_g2s(dst + f * C::TILE + e, (f ? hR : hF) + off + e, TH * KC * (uint32_t)sizeof(TS), bar);
   }
   __syncwarp();
 }
