@@ -703,6 +703,11 @@ def run_ours(args):
         mi_kernel, key = "memint_kernel<float,32,3,2,split> + memint_finish_kernel", "traffic_bytes_per_step_split"
     else:
         mi_kernel, key = "memint_kernel<float,32,3,2>", "traffic_bytes_per_launch"
+    if tuning.get("memint_persistent"):
+        mi_kernel += " (persistent grid, one CTA per SM)"
+    # the committed full-size capture covers the persistent tail-split form only
+    if key != "traffic_bytes_per_step_tail_lfw" or not tuning.get("memint_persistent"):
+        key = None
     traffic = read_traffic(key) if key and (CFG["Ns"], CFG["M"]) == (64, 1000) else None
     fp32_peak = fp32_fma_peak_tflops(local)
     line = {

@@ -206,10 +206,11 @@ typedef struct kb_tuning {
                            * TF32 head/tail operands, Ns <= 78); KB_PREC_FP64: 0 */
   int32_t memint_split;   /* 1: each chunk's triangle of history tiles is streamed by two CTAs (equal
                            * halves by column blocks), then a finishing kernel adds their sums and runs
-                           * the leapfrog; 2: the same for the chunks past the last whole wave of one
-                           * CTA per SM only (the others as 0); 0 (default): one CTA per chunk, the
-                           * same arithmetic whatever the handle's size. 1 and 2 need memint_variant
-                           * 1 or 2 in KB_PREC_MIXED */
+                           * the leapfrog; 2: the chunks past the last whole wave of one CTA per SM
+                           * only (the others as 0), each in 2..6 parts, as many as make the pieces
+                           * fill the SMs best; 0 (default): one CTA per chunk, the same arithmetic
+                           * whatever the handle's size. 1 and 2 need memint_variant 1 or 2 in
+                           * KB_PREC_MIXED */
   int32_t memint_bulk;    /* 1: history tiles by plain bulk copies of whole rows instead of tensor-map
                            * boxes (the path taken when the CUDA driver has no tensor-map encoder); 0 */
   int32_t test_no_tiles;  /* test hook, 0 in use: 1 makes the memory-integral producer issue no tiles,

@@ -508,7 +508,7 @@ int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out) {
         {(void **)&R.k2_d, (size_t)R.Spad * 8}, {(void **)&R.deg_d, (size_t)R.Spad * 8},
         {(void **)&R.Cm_d, (size_t)R.H * R.H * 8}, {(void **)&R.tad, (size_t)2 * R.nchunks * 8},
         {(void **)&R.meas, (size_t)5 * R.Spad * 8}, {(void **)&R.epart, (size_t)4 * R.nchunks * 8},
-        {(void **)&R.rowacc, (size_t)2 * R.nchunks * R.Malloc * KC * 8},
+        {(void **)&R.rowacc, (size_t)kb::MEMINT_MAX_PARTS * R.nchunks * R.Malloc * KC * 8},
         {(void **)&R.colacc, (size_t)2 * R.nchunks * R.Malloc * KC * 8},
         {(void **)&R.fin, (size_t)R.nchunks * sizeof(int)},
         {(void **)&R.fin_part, (size_t)R.nchunks * ((R.Malloc + kb::FIN_TP - 1) / kb::FIN_TP) * KC * 8},

@@ -16,8 +16,8 @@
 //                                              by t mod 2
 //   meas            [5][Spad]                 double: F(t-1,t-1), ddF, n, omega, c
 //   epart           [nchunks][4]              double: E_kin, E_pot, E_mem partials
-//   rowacc          [2][nchunks][Malloc][KC]  double: row sums of the memory integrals
-//                                              (the second half only in split mode)
+//   rowacc          [MEMINT_MAX_PARTS][nchunks][Malloc][KC]  double: row sums of the memory
+//                                              integrals (buffers past the first in split mode)
 //   colacc          [2][nchunks][Malloc][KC]  double: column sums (F, rho) of a split step
 //   fin, fin_part, fin_prev, hcm2             partial sums and arrival counts of the
 //                                              finishing kernel of a split step
@@ -29,6 +29,7 @@
 namespace kb {
 
 constexpr int KC = 8;  // orbits per chunk (innermost dimension)
+constexpr int MEMINT_MAX_PARTS = 6;  // parts a split chunk's triangle is streamed in (row-sum buffers)
 
 // device error bits (per handle)
 enum : int { DEVERR_TIMEOUT = 1, DEVERR_SMEM = 2, DEVERR_GEOM = 4, DEVERR_BOUNDS = 8 };
@@ -68,7 +69,7 @@ struct RunDev {
   double *tad;              // [2][nchunks]
   double *meas;             // [5][Spad]
   double *epart;            // [nchunks][4]
-  double *rowacc;           // [2][nchunks][Malloc][KC] row sums of the memory integrals (one per half when split)
+  double *rowacc;           // [MEMINT_MAX_PARTS][nchunks][Malloc][KC] row sums of the memory integrals (one per part when split)
   double *colacc;           // [2][nchunks][Malloc][KC] column sums F, rho of a split step
   int cta_base_sun, cta_base_mi;  // first item of this run in the batched grids
   int sun_rows;                   // t' rows per sunset item (taken one after the other), 1 for FP64
@@ -143,6 +144,7 @@ size_t sunset_scratch_elems(int H);
 int sunset_grid(bool fp64, int num_sms, int total_rows);
 int sunset_max_ctas_per_sm(bool fp64, int variant, size_t smem);
 cudaError_t configure_sunset(bool fp64, size_t smem);
+int memint_split_parts(int nwhole, int nsplit, int sm_slots);
 cudaError_t launch_memint(bool fp64, int variant, int split, int nwhole, const RunDev *d_runs, const int *d_base,
                           int nruns, int total_ctas, int fin_nb_max, int use_maps, const int *d_t, int *d_err,
                           int measure, size_t smem, int *queue, int grid_cap, cudaStream_t st);

@@ -549,15 +549,19 @@ __device__ bool lf_wait(uint64_t *bar, uint32_t parity, volatile int *cabort) {
 constexpr size_t LF_STAGE_BYTES = 2 * 128 * 2 * 2 * sizeof(double);
 static_assert(LF_STAGE_BYTES <= 8 * 32 * KC * sizeof(double), "the stage fits where memint_blk_kernel keeps its column buffer");
 
-// Split mode: the triangle of a chunk is cut between column blocks into two
-// halves with (nearly) equal tile counts; half 0 takes blocks [J0, Js), half 1
-// blocks [Js, Jn]. Both kernels of the split step compute Js the same way.
-__host__ __device__ inline int split_block(int J0, int Jn) {
+// Split mode: the triangle of a chunk is cut between column blocks into k parts
+// of (nearly) equal tile counts (block J of J0..Jn holds Jn - J + 1 tiles); part p
+// takes blocks [split_bound(p), split_bound(p + 1)) and may be empty when the
+// triangle has fewer blocks than parts. With k = 2 the cut is where the first
+// half reaches half the tiles.
+__host__ __device__ inline int split_bound(int J0, int Jn, int k, int p) {
+  if (p <= 0) return J0;
+  if (p >= k) return Jn + 1;
   const int nb = Jn - J0 + 1, total = nb * (nb + 1) / 2;
   int acc = 0;
   for (int J = J0; J <= Jn; ++J) {
     acc += Jn - J + 1;
-    if (2 * acc >= total) return J + 1;
+    if (k * acc >= p * total) return J + 1;
   }
   return Jn + 1;
 }
@@ -578,11 +582,12 @@ __host__ __device__ inline int split_block(int J0, int Jn) {
 // are left, keeping its TMEM allocation and its stage barriers -- whose phases
 // run on across items -- and the tadpole sum of the run it last took.
 // SPLIT: the first nwhole items are whole chunks as above; after them item
-// nwhole + 2k + h streams half h of chunk nwhole + k's triangle, keeps its row
-// sums in row buffer h and stores the column sums of its column blocks instead
-// of running the leapfrog; memint_finish_kernel completes those chunks. Split
-// chunks fill the partial last wave of a large grid (nwhole = whole waves) or
-// double the CTAs of a small one (nwhole = 0).
+// nwhole + parts i + p streams part p of chunk nwhole + i's triangle, keeps its
+// row sums in row buffer p and stores the column sums of its column blocks
+// instead of running the leapfrog; memint_finish_kernel completes those chunks.
+// Split chunks fill the partial last wave of a large grid (nwhole = whole waves,
+// parts chosen so that the pieces fill the SMs) or double the CTAs of a small one
+// (nwhole = 0, two parts).
 // LFW (FP32 history): four more warps run the leapfrog of a whole chunk's column
 // blocks. The column group hands each block's column sums over through a
 // double-buffered shared-memory stage (lf_full / lf_empty mbarriers) and goes on
@@ -593,7 +598,7 @@ template <typename TS, int T, int NST, int OPT, bool SPLIT, bool LFW = false, bo
 __global__ void __launch_bounds__(2 * T * (KC / OPT) + 32 + (LFW ? T * (KC / OPT) : 0), 1)
 memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int nruns,
               const int *__restrict__ d_t, int *__restrict__ d_err, int measure, int nwhole, int use_maps,
-              int nitems, int *__restrict__ queue) {
+              int nitems, int *__restrict__ queue, int parts) {
   using C = Cfg<TS, T, NST, OPT>;
   using V = Vec<TS, OPT>;
   using A = typename std::conditional<COMP, Acc<TS, OPT>, PlainAcc<TS, OPT>>::type;
@@ -661,8 +666,8 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   first = false;
   if (vb >= nitems) break;
   const bool split = SPLIT && vb >= nwhole;
-  const int item = split ? nwhole + ((vb - nwhole) >> 1) : vb;
-  const int half = split ? ((vb - nwhole) & 1) : 0;
+  const int item = split ? nwhole + (vb - nwhole) / parts : vb;
+  const int part = split ? (vb - nwhole) % parts : 0;
   const int r = run_at(base, nruns, item);
   const RunDev &R = runs[r];
   const int c = item - R.cta_base_mi;  // chunk
@@ -673,9 +678,9 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   // ever written by row-group thread (slot mod T, jq), so they need no atomics.
   // With FP32 history they live in TMEM (Malloc/T slots x OPT doubles per lane)
   // when they fit, else in a global scratch slot; a split CTA copies them there
-  // at the end (one buffer per half) for memint_finish_kernel. The FP64 kernel,
+  // at the end (one buffer per part) for memint_finish_kernel. The FP64 kernel,
   // bound by FP64 arithmetic, runs 1 % faster on the global scratch.
-  double *rowacc = R.rowacc + (size_t)half * R.nchunks * rowstride + (size_t)c * rowstride;
+  double *rowacc = R.rowacc + (size_t)part * R.nchunks * rowstride + (size_t)c * rowstride;
   const bool use_tmem = kTmem && (Ma / T) * OPT * 2 <= (int)TMEM_COLS;
   const bool use_tmap = (use_maps & 1) && R.tmap != nullptr;
   const bool no_tiles = (use_maps & 2) != 0;  // test hook: nothing is issued, the consumers' waits run out
@@ -704,7 +709,7 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   __syncthreads();
   if (use_tmem) tmem_fence_after();
   const double M2 = misc[1];
-  if (SPLIT && c == 0 && half == 0 && tid == 0) {  // for memint_finish_kernel
+  if (SPLIT && c == 0 && part == 0 && tid == 0) {  // for memint_finish_kernel
     R.hcm2[0] = misc[0];
     R.hcm2[1] = misc[1];
   }
@@ -719,10 +724,9 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
 
   const bool lo_only = pexp_lo(R.pexp);
   const int J0 = tmin / T, Jn = (t - 1) / T;
-  // column blocks of this CTA: all of them, or one half of the triangle
-  const int Js = split ? split_block(J0, Jn) : J0;
-  const int Jlo = (split && half == 1) ? Js : J0;
-  const int Jhi = (split && half == 0) ? Js - 1 : Jn;
+  // column blocks of this item: all of them, or one part of the triangle
+  const int Jlo = split ? split_bound(J0, Jn, parts, part) : J0;
+  const int Jhi = split ? split_bound(J0, Jn, parts, part + 1) - 1 : Jn;
   int ntiles = 0;
   if (!lo_only)
     for (int J = Jlo; J <= Jhi; ++J) ntiles += Jn - J + 1;
@@ -1009,7 +1013,7 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
       for (int q = max(0, *issued_count - NST); q < *issued_count; ++q)
         (void)mbar_wait_bounded(full + ((nb + q) % NST), (uint32_t)(((nb + q) / NST) & 1));
   } else {
-    if (split && use_tmem && rowgrp)  // this half's row sums, for memint_finish_kernel
+    if (split && use_tmem && rowgrp)  // this part's row sums, for memint_finish_kernel
       for (int s = 0; s < Ma; s += T) {
         double v[OPT];
         TmemRow<OPT>::ld(tcol(s), v);
@@ -1038,7 +1042,7 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
 
 // Second kernel of a split step: CTA (chunk, k) takes the FIN_TP t' from tmin +
 // k FIN_TP on, FIN_IT (t', orbit) items per thread with all their loads issued
-// before any arithmetic. It adds the column sums and the two halves' row sums,
+// before any arithmetic. It adds the column sums and the parts' row sums (in part order),
 // runs the leapfrog (the same arithmetic as memint_kernel's) and stores its
 // per-orbit sums of the acc_F(t) terms; the CTA of the chunk that arrives last
 // adds those in CTA order and runs the diagonal and measurement (no CTA waits
@@ -1053,7 +1057,7 @@ static_assert(FIN_IT * FIN_THREADS == FIN_TP * KC, "whole items per thread");
 template <typename TS>
 __global__ void __launch_bounds__(FIN_THREADS, sizeof(TS) == 4 ? 4 : 2)
 memint_finish_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int nruns, int nb_max,
-                     int nwhole, const int *__restrict__ d_t, int measure) {
+                     int nwhole, const int *__restrict__ d_t, int measure, int parts) {
   __shared__ double red[FIN_THREADS / 32][KC];
   __shared__ double misc[16 + KC];
   __shared__ int is_last;
@@ -1069,7 +1073,7 @@ memint_finish_kernel(const RunDev *__restrict__ runs, const int *__restrict__ ba
   const int nact = (nq + FIN_TP * KC - 1) / (FIN_TP * KC);  // CTAs of this chunk with work (<= fin_nb)
   if (blk >= nact) return;
   const size_t rowstride = (size_t)Ma * KC, st_row = (size_t)R.nchunks * rowstride, cs = (size_t)c * rowstride;
-  const size_t half2 = (size_t)R.nchunks * rowstride;
+  const size_t pbuf = (size_t)R.nchunks * rowstride;  // one row-sum buffer, and the rho column sums' offset
   const double M2 = R.hcm2[1];
   const bool lo_only = pexp_lo(R.pexp);
   const int j = tid % KC;  // FIN_THREADS is a multiple of KC: one orbit per thread
@@ -1093,8 +1097,10 @@ memint_finish_kernel(const RunDev *__restrict__ runs, const int *__restrict__ ba
     const size_t e = cs + (size_t)(b % Ma) * KC + j;
     xr[u] = lo_only ? (TS)0 : sr[e];
     xf[u] = lo_only ? (TS)0 : sf[e];
-    aF[u] = R.colacc[e] + (R.rowacc[e] + R.rowacc[half2 + e]);
-    aR[u] = R.colacc[half2 + e];
+    double rsum = R.rowacc[e] + R.rowacc[pbuf + e];
+    for (int p = 2; p < parts; ++p) rsum += R.rowacc[(size_t)p * pbuf + e];
+    aF[u] = R.colacc[e] + rsum;
+    aR[u] = R.colacc[pbuf + e];
     f1[u] = F1[e];
     f2[u] = (b <= t - 2) ? F2[e] : F1[cs + (size_t)((t - 2) % Ma) * KC + j];
     r1[u] = R1[e];
@@ -1663,17 +1669,37 @@ cudaError_t configure_memint(bool fp64, size_t smem) {
                               (int)smem);
 }
 
+// parts of a split chunk: two, or for the chunks past the whole waves of a large
+// grid (nwhole > 0) the k in [2, MEMINT_MAX_PARTS] whose nsplit k pieces fill the
+// sm_slots CTA slots in the fewest piece lengths, ceil(nsplit k / sm_slots) / k
+// (the smaller k on a tie): 59 chunks on 152 SMs take 5 parts, 0.4 of a chunk's
+// stream for the last wave instead of 0.5
+int memint_split_parts(int nwhole, int nsplit, int sm_slots) {
+  if (nwhole <= 0 || nsplit <= 0 || sm_slots <= 0) return 2;
+  int best = 2;
+  double best_len = 1e30;
+  for (int k = 2; k <= MEMINT_MAX_PARTS; ++k) {
+    const double len = (double)((nsplit * k + sm_slots - 1) / sm_slots) / k;
+    if (len < best_len - 1e-12) {
+      best_len = len;
+      best = k;
+    }
+  }
+  return best;
+}
+
 // use_maps: bit 0 tensor-map boxes (else bulk copies), bit 1 the test hook that
 // issues no tiles (memint_kernel only). queue: null, or a device counter that makes
 // memint_kernel persistent on at most grid_cap CTAs (zeroed here before the launch).
 cudaError_t launch_memint(bool fp64, int variant, int split, int nwhole, const RunDev *d_runs, const int *d_base,
                           int nruns, int total_ctas, int fin_nb_max, int use_maps, const int *d_t, int *d_err,
                           int measure, size_t smem, int *queue, int grid_cap, cudaStream_t st) {
-  // split: the chunks from nwhole on are streamed by two half-triangle CTAs each
-  // and completed by the finishing kernel
+  // split: the chunks from nwhole on are streamed in parts (memint_split_parts) and
+  // completed by the finishing kernel
   const int nsplit = total_ctas - nwhole;
   const bool splitting = split && nsplit > 0;
-  const int nitems = splitting ? nwhole + 2 * nsplit : total_ctas;
+  const int parts = splitting ? memint_split_parts(nwhole, nsplit, grid_cap) : 1;
+  const int nitems = splitting ? nwhole + parts * nsplit : total_ctas;
   const bool persistent = queue != nullptr && grid_cap > 0 && (fp64 || variant != 0);
   const int grid = persistent ? std::min(nitems, grid_cap) : nitems;
   int *q = persistent ? queue : nullptr;
@@ -1687,41 +1713,41 @@ cudaError_t launch_memint(bool fp64, int variant, int split, int nwhole, const R
     if (splitting) {
       if (variant == 3)
         memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT, true, true, true>
-            <<<grid, NTHR_LF, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, nw, use_maps, nitems, q);
+            <<<grid, NTHR_LF, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, nw, use_maps, nitems, q, parts);
       else
         memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT, true, true>
-            <<<grid, NTHR_LF, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, nw, use_maps, nitems, q);
+            <<<grid, NTHR_LF, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, nw, use_maps, nitems, q, parts);
       memint_finish_kernel<float><<<nsplit * fin_nb_max, FIN_THREADS, 0, st>>>(d_runs, d_base, nruns, fin_nb_max,
-                                                                               nwhole, d_t, measure);
+                                                                               nwhole, d_t, measure, parts);
     } else if (variant == 3) {
       memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT, false, true, true>
-          <<<grid, NTHR_LF, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, nw, use_maps, nitems, q);
+          <<<grid, NTHR_LF, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, nw, use_maps, nitems, q, parts);
     } else {
       memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT, false, true>
-          <<<grid, NTHR_LF, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, nw, use_maps, nitems, q);
+          <<<grid, NTHR_LF, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, nw, use_maps, nitems, q, parts);
     }
     return cudaGetLastError();
   }
   if (splitting && (fp64 || variant == 1)) {
     if (fp64) {
       memint_kernel<double, CfgF64::T, CfgF64::NST, CfgF64::OPT, true>
-          <<<grid, CfgF64::NT + 32, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, nw, use_maps, nitems, q);
+          <<<grid, CfgF64::NT + 32, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, nw, use_maps, nitems, q, parts);
       memint_finish_kernel<double><<<nsplit * fin_nb_max, FIN_THREADS, 0, st>>>(d_runs, d_base, nruns, fin_nb_max,
-                                                                                nwhole, d_t, measure);
+                                                                                nwhole, d_t, measure, parts);
     } else {
       memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT, true>
-          <<<grid, CfgF32::NT + 32, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, nw, use_maps, nitems, q);
+          <<<grid, CfgF32::NT + 32, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, nw, use_maps, nitems, q, parts);
       memint_finish_kernel<float><<<nsplit * fin_nb_max, FIN_THREADS, 0, st>>>(d_runs, d_base, nruns, fin_nb_max,
-                                                                               nwhole, d_t, measure);
+                                                                               nwhole, d_t, measure, parts);
     }
     return cudaGetLastError();
   }
   if (fp64)
     memint_kernel<double, CfgF64::T, CfgF64::NST, CfgF64::OPT, false>
-        <<<grid, CfgF64::NT + 32, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, nw, use_maps, nitems, q);
+        <<<grid, CfgF64::NT + 32, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, nw, use_maps, nitems, q, parts);
   else if (variant == 1)
     memint_kernel<float, CfgF32::T, CfgF32::NST, CfgF32::OPT, false>
-        <<<grid, CfgF32::NT + 32, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, nw, use_maps, nitems, q);
+        <<<grid, CfgF32::NT + 32, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, nw, use_maps, nitems, q, parts);
   else
     memint_blk_kernel<CfgF32::NST><<<total_ctas, 288, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure);
   return cudaGetLastError();

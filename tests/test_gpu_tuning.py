@@ -201,20 +201,22 @@ def test_memint_split_mixed_and_batched():
     h.close()
 
 
-@pytest.mark.parametrize("precision,tol", [(0, 1e-10), (1, 1e-6)])
-def test_memint_tail_split_matches_whole(precision, tol):
-    """memint_split 2 at Ns=40 (222 chunks): the chunks of the whole waves of one
-    CTA per SM stream whole, the rest split in two and the finishing kernel
-    completes them; F, rho, n and E agree with the whole-chunk kernel (FP64 to
-    1e-10, mixed to 1e-6) with the window wrapped."""
-    cfg = dict(Ns=40, M=20, N=4, lam=3.0, dt=0.1, pexp=1, T=1.5)
+@pytest.mark.parametrize("precision,tol,Ns,variant", [(0, 1e-10, 40, 1), (1, 1e-6, 40, 1), (0, 1e-10, 36, 1),
+                                                      (1, 1e-6, 36, 2), (1, 1e-6, 38, 2), (0, 1e-10, 38, 1)])
+def test_memint_tail_split_matches_whole(precision, tol, Ns, variant):
+    """memint_split 2 at Ns = 36, 38, 40 (167, 193, 222 chunks): the chunks of the
+    whole waves of one CTA per SM stream whole, the rest in parts (6, 3 and 2 parts
+    on 152 SMs: as many as fill the last wave best) that the finishing kernel
+    completes; F, rho, n and E agree with the whole-chunk kernel (FP64 to 1e-10,
+    mixed to 1e-6) with the window wrapped."""
+    cfg = dict(Ns=Ns, M=20, N=4, lam=3.0, dt=0.1, pexp=1, T=1.5)
     hs = []
     for split in (0, 2):
         h = make_gpu(cfg, precision)
         _, k2, _ = h.orbits()
         h.init(0, occupation(cfg, k2), 1.0)
         if precision == 1:
-            h.set_tuning(memint_variant=1, memint_split=split)
+            h.set_tuning(memint_variant=variant, memint_split=split)
         else:
             h.set_tuning(memint_split=split)
         assert h.tuning()["memint_split"] == split
