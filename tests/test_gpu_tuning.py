@@ -286,12 +286,14 @@ def test_leapfrog_warps_batched_runs():
         assert a["E"] == b["E"] and np.array_equal(a["n"], b["n"])
 
 
-@pytest.mark.parametrize("precision", [0, 1])
-def test_memint_bulk_copies_match_tensor_maps(precision):
+@pytest.mark.parametrize("precision,M", [(0, 40), (1, 40), (1, 100)])
+def test_memint_bulk_copies_match_tensor_maps(precision, M):
     """History tiles by plain bulk copies (memint_bulk 1, the path without a
     tensor-map encoder) give the same F, rho, n and E as the tensor-map boxes,
-    bitwise: both deliver the same bytes in the same stage layout."""
-    cfg = dict(Ns=12, M=40, N=4, lam=3.0, dt=0.1, pexp=1, T=1.5)
+    bitwise: both deliver the same bytes in the same stage layout. M = 100 puts
+    whole FP32 diagonal tiles inside the window, whose upper-right quadrants
+    neither path loads."""
+    cfg = dict(Ns=12, M=M, N=4, lam=3.0, dt=0.1, pexp=1, T=1.5)
     hs = []
     for bulk in (0, 1):
         h = make_gpu(cfg, precision)
