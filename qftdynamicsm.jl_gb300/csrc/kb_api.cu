@@ -81,6 +81,7 @@ struct kb_handle {
   int memint_split = 0;           // 1: two half-triangle CTAs per chunk and a finishing kernel;
                                   // 2: the same for the chunks past the last whole wave only
   int memint_persistent = 0;      // 1: one memory-integral CTA per SM taking items from a queue
+  std::vector<std::pair<int, void *>> sun_imgs;  // sunset table images by Ns (RunDev::sun_img)
   int *d_mi_queue = nullptr;      // [2] item counters of the persistent memory-integral grids (per group)
   int batch_order = 0;            // order of the runs' CTA ranges in the batched grids
   // concurrent halves of a batch (kb_tuning.batch_overlap > 0): the runs split into two
@@ -538,6 +539,24 @@ int kb_create_batch(const kb_params *p, int32_t nruns, kb_handle **out) {
     cudaMemcpyAsync(R.Cm_d, R.Cm.data(), R.Cm.size() * 8, cudaMemcpyHostToDevice, h->st);
     cudaStreamSynchronize(h->st);  // host vectors above are temporaries
     RunDev &D = R.dev;
+    // the sunset kernel's tables for this lattice size, built once and shared by the runs
+    // of the same Ns (without an image the kernel builds them itself)
+    D.sun_img = nullptr;
+    if (kb::pexp_sunset(R.p.pexp)) {
+      for (auto &im : h->sun_imgs)
+        if (im.first == R.p.Ns) D.sun_img = static_cast<const unsigned char *>(im.second);
+      if (!D.sun_img) {
+        void *img = nullptr;
+        if (cudaMalloc(&img, kb::sunset_image_bytes(h->fp64, R.H)) == cudaSuccess &&
+            kb::launch_sunset_image(h->fp64, R.H, R.Cm_d, img, h->st) == cudaSuccess) {
+          h->sun_imgs.push_back({R.p.Ns, img});
+          D.sun_img = static_cast<const unsigned char *>(img);
+        } else {
+          cudaGetLastError();
+          if (img) cudaFree(img);
+        }
+      }
+    }
     D.Ns = R.p.Ns;
     D.H = R.H;
     D.S = R.S;
@@ -672,6 +691,7 @@ void kb_destroy(kb_handle *h) {
     if (m.host) cudaFreeHost(m.host);
   }
   for (auto &R : h->runs) free_run(R);
+  for (auto &im : h->sun_imgs) cudaFree(im.second);
   void *ptrs[] = {h->d_runs, h->d_base_sun, h->d_base_mi, h->d_grp_sun[0], h->d_grp_mi[0], h->d_t, h->d_err, h->d_mi_queue,
                   h->sun_scratch};
   for (void *q : ptrs)

@@ -91,6 +91,9 @@ struct RunDev {
   // null when the CUDA driver has no encoder
   const void *tmap;
   int *err;  // the handle's device error word (timeouts; bounds checks of KB_DEBUG builds)
+  // the sunset kernel's shared-memory tables for this run's lattice size, built once per
+  // handle (shared by the runs of the same Ns); null: the kernel builds them itself
+  const unsigned char *sun_img;
 };
 
 #ifdef KB_DEBUG
@@ -133,6 +136,8 @@ cudaError_t launch_sunset(bool fp64, int variant, const RunDev *d_runs, const in
                           int total_rows, int grid, const int *d_t, void *scratch, size_t scratch_stride, size_t smem,
                           cudaStream_t st);
 size_t sunset_smem_bytes(bool fp64, int H);
+size_t sunset_image_bytes(bool fp64, int H);
+cudaError_t launch_sunset_image(bool fp64, int H, const double *Cm, void *img, cudaStream_t st);
 // tensor-core sunset of KB_PREC_MIXED (kb_sunset_tc.cu): sunset variant 2
 size_t sunset_tc_smem_bytes(int H);  // dynamic shared memory; 0 when H is beyond the kernel
 size_t sunset_tc_static_bytes();

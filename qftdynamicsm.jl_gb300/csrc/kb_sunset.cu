@@ -194,6 +194,15 @@ __device__ void sun_build_cf(const SunGeom &g, TC *CF, Cm cm) {
 // (sun_tables_bytes), the expand table at `etab` unless null, the cosine matrix
 // from cm(X, x) = C[X][x]; ends with a barrier. The regions and the orbit buffer of
 // the returned context are left to the caller.
+// the context of tables already at `base` (built there, or copied in from an image)
+template <typename TC>
+__device__ SunCtx<TC> sun_tables_ctx(const SunGeom &g, unsigned char *base, uint16_t *etab) {
+  const TC *CT = reinterpret_cast<const TC *>(base);
+  const uint16_t *pr = reinterpret_cast<const uint16_t *>(CT + g.H4 * g.H4 + g.cf);
+  const uint16_t *it2 = pr + g.P4;
+  return SunCtx<TC>{CT, pr, it2, it2 + g.n2, etab, nullptr, nullptr, nullptr, g};
+}
+
 template <typename TC, typename Cm>
 __device__ SunCtx<TC> sun_build_tables(const SunGeom &g, unsigned char *base, uint16_t *etab, Cm cm) {
   TC *CT = reinterpret_cast<TC *>(base);
@@ -244,7 +253,15 @@ __device__ SunCtx<TC> sun_build_tables(const SunGeom &g, unsigned char *base, ui
     }
   }
   __syncthreads();
-  return SunCtx<TC>{CT, pr, it2, it3, etab, nullptr, nullptr, nullptr, g};
+  return sun_tables_ctx<TC>(g, base, etab);
+}
+
+// copy of a table image (built by sun_image_kernel) into shared memory; ends with a barrier
+__device__ __forceinline__ void sun_copy_image(const unsigned char *img, unsigned char *base, size_t bytes) {
+  const uint4 *src = reinterpret_cast<const uint4 *>(img);
+  uint4 *dst = reinterpret_cast<uint4 *>(base);
+  for (size_t i = threadIdx.x; i < bytes / 16; i += blockDim.x) dst[i] = __ldg(src + i);
+  __syncthreads();
 }
 
 // unroll of the pass loops (FP64 at 2: the 4 x 4 double tile fills the registers)
@@ -443,8 +460,13 @@ sunset_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
       cur_ns = R.Ns;
       const SunGeom g(R.H);
       const SunLayout L = sun_layout(sizeof(TC) == 8, g);
-      c = sun_build_tables<TC>(g, smem_raw, L.has_etab ? reinterpret_cast<uint16_t *>(smem_raw + L.etab) : nullptr,
-                               [&](int X, int x) { return R.Cm[X * g.H + x]; });
+      uint16_t *etab = L.has_etab ? reinterpret_cast<uint16_t *>(smem_raw + L.etab) : nullptr;
+      if (R.sun_img) {  // the handle's image of these tables
+        sun_copy_image(R.sun_img, smem_raw, L.regions);
+        c = sun_tables_ctx<TC>(g, smem_raw, etab);
+      } else {
+        c = sun_build_tables<TC>(g, smem_raw, etab, [&](int X, int x) { return R.Cm[X * g.H + x]; });
+      }
       c.bufF = reinterpret_cast<TC *>(smem_raw + L.regions);
       if (SCRATCH) {
         c.R1 = scratch + (size_t)blockIdx.x * scratch_stride;
@@ -555,6 +577,39 @@ sunset_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
 }  // namespace
 
 size_t sunset_smem_bytes(bool fp64, int H) { return sun_layout(fp64, SunGeom(H)).bytes; }
+
+namespace {
+// the tables of sunset_kernel for octant size H as the image of their shared memory
+// ([0, regions) of sun_layout): one CTA builds them and writes them out
+template <typename TC>
+__global__ void __launch_bounds__(SUN_THREADS, 1) sun_image_kernel(int H, const double *__restrict__ Cm,
+                                                                  unsigned char *__restrict__ img) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const SunGeom g(H);
+  const SunLayout L = sun_layout(sizeof(TC) == 8, g);
+  (void)sun_build_tables<TC>(g, smem_raw, L.has_etab ? reinterpret_cast<uint16_t *>(smem_raw + L.etab) : nullptr,
+                             [&](int X, int x) { return Cm[X * H + x]; });
+  const uint4 *src = reinterpret_cast<const uint4 *>(smem_raw);
+  uint4 *dst = reinterpret_cast<uint4 *>(img);
+  for (size_t i = threadIdx.x; i < L.regions / 16; i += blockDim.x) dst[i] = src[i];
+}
+}  // namespace
+
+size_t sunset_image_bytes(bool fp64, int H) { return sun_layout(fp64, SunGeom(H)).regions; }
+
+cudaError_t launch_sunset_image(bool fp64, int H, const double *Cm, void *img, cudaStream_t st) {
+  const size_t bytes = sunset_image_bytes(fp64, H);
+  cudaError_t e = fp64 ? cudaFuncSetAttribute(sun_image_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)bytes)
+                       : cudaFuncSetAttribute(sun_image_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)bytes);
+  if (e != cudaSuccess) return e;
+  if (fp64)
+    sun_image_kernel<double><<<1, SUN_THREADS, bytes, st>>>(H, Cm, reinterpret_cast<unsigned char *>(img));
+  else
+    sun_image_kernel<float><<<1, SUN_THREADS, bytes, st>>>(H, Cm, reinterpret_cast<unsigned char *>(img));
+  return cudaGetLastError();
+}
 
 // t' rows per sunset item of a run (FP32): up to 8 for the small lattices whose rows
 // are short, as long as the work items of the largest pass of all the item's rows
