@@ -807,7 +807,7 @@ def main():
     ap.add_argument("--sunset-variant", type=int, default=None,
                     help="fix the FP32 sunset variant (0: 1024, 1: 512 threads, 2: tensor cores)")
     ap.add_argument("--batch-overlap", type=int, default=None,
-                    help="c3: fix the concurrent-group step (CTAs of the second group's sunset; 0 = off)")
+                    help="c3: fix the concurrent-group step (SMs of the second group's sunset; 0 = off)")
     args = ap.parse_args()
     if args.config == "c3" and args.impl == "ours":
         return run_batched(args)

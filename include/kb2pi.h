@@ -224,8 +224,9 @@ typedef struct kb_tuning {
   int32_t batch_overlap;      /* batches of two or more runs (no 1/N expansion): 0 (default) one
                                * launch per kernel for all runs; n > 0 splits the runs into two
                                * groups of about equal memory-integral work and runs the second
-                               * group's sunset on n CTAs, on a second stream, while the first
-                               * group's memory integrals stream (the same arithmetic per run) */
+                               * group's sunset on n SMs (as many CTAs as fit there), on a second
+                               * stream, while the first group's memory integrals stream (on the
+                               * other SMs with memint_persistent); the same arithmetic per run */
   int32_t memint_persistent;  /* 1: the memory-integral grid is persistent -- one CTA per SM takes
                                * chunk items (whole or split) from a device counter until none are
                                * left, keeping its TMEM, stage barriers and the run's tadpole sum

@@ -830,11 +830,14 @@ static int launch_sun(kb_handle *h, const int *base, int n, int total, int grid,
   return KB_OK;
 }
 // the memory integrals of the runs of one schedule table (group g's queue when persistent)
-static int launch_mi(kb_handle *h, const int *base, int n, int total, int measure, cudaStream_t st, int g) {
-  const int nwhole = h->memint_split == 2 ? (total / h->num_sms) * h->num_sms : 0;
+// sms: the SMs the grid may take (a persistent grid has that many CTAs; fewer than the
+// device's leaves the rest to a concurrent kernel); the whole waves are waves of sms CTAs
+static int launch_mi(kb_handle *h, const int *base, int n, int total, int measure, cudaStream_t st, int g,
+                     int sms) {
+  const int nwhole = h->memint_split == 2 ? (total / sms) * sms : 0;
   KB_CUDA(h, kb::launch_memint(h->fp64, memint_launch_variant(h), h->memint_split, nwhole, h->d_runs, base, n, total,
                                h->fin_nb_max, !h->memint_bulk + 2 * h->test_no_tiles, h->d_t, h->d_err, measure,
-                               h->smem_mi, h->memint_persistent ? h->d_mi_queue + g : nullptr, h->num_sms, st));
+                               h->smem_mi, h->memint_persistent ? h->d_mi_queue + g : nullptr, sms, st));
   return KB_OK;
 }
 
@@ -867,9 +870,14 @@ static int launch_step_overlap(kb_handle *h, int measure, cudaEvent_t e0, cudaEv
   if (e1) KB_CUDA(h, cudaEventRecord(e1, h->st));
   KB_CUDA(h, cudaEventRecord(h->ev_fork, h->st));
   KB_CUDA(h, cudaStreamWaitEvent(h->st2, h->ev_fork, 0));
-  if ((rc = launch_sun(h, h->d_grp_sun[1], h->grp_n[1], h->grp_sun[1], h->batch_overlap, h->st2))) return rc;
-  if ((rc = launch_mi(h, h->d_grp_mi[0], h->grp_n[0], h->grp_mi[0], measure, h->st, 0))) return rc;
-  if ((rc = launch_mi(h, h->d_grp_mi[1], h->grp_n[1], h->grp_mi[1], measure, h->st2, 1))) return rc;
+  // group 1's sunset on batch_overlap SMs (as many CTAs as fit there); a persistent grid
+  // for group 0's memory integrals takes the other SMs
+  const int occ = h->sunset_variant == 2 ? 1 : std::max(1, kb::sunset_max_ctas_per_sm(h->fp64, h->sunset_variant,
+                                                                                        h->smem_sun));
+  if ((rc = launch_sun(h, h->d_grp_sun[1], h->grp_n[1], h->grp_sun[1], h->batch_overlap * occ, h->st2))) return rc;
+  const int sms0 = h->memint_persistent ? std::max(1, h->num_sms - h->batch_overlap) : h->num_sms;
+  if ((rc = launch_mi(h, h->d_grp_mi[0], h->grp_n[0], h->grp_mi[0], measure, h->st, 0, sms0))) return rc;
+  if ((rc = launch_mi(h, h->d_grp_mi[1], h->grp_n[1], h->grp_mi[1], measure, h->st2, 1, h->num_sms))) return rc;
   KB_CUDA(h, cudaEventRecord(h->ev_join, h->st2));
   KB_CUDA(h, cudaStreamWaitEvent(h->st, h->ev_join, 0));
   if (e2) {
@@ -899,7 +907,7 @@ static int launch_step(kb_handle *h, int measure) {
     if (h->any_nlo || h->any_ninv) h->ev_pending.push_back({0, {e0, e1}});
   }
   {
-    const int rc = launch_mi(h, h->d_base_mi, (int)h->runs.size(), h->total_mi, measure, h->st, 0);
+    const int rc = launch_mi(h, h->d_base_mi, (int)h->runs.size(), h->total_mi, measure, h->st, 0, h->num_sms);
     if (rc) return rc;
   }
   if (h->profiling) {
@@ -1570,7 +1578,7 @@ int kb_autotune(kb_handle *h, int32_t trials, kb_tuning *chosen, double *ms_per_
       KB_CUDA(h, cudaEventRecord(e[0], h->st));
       if ((rc = launch_self_energies(h))) return rc;
       KB_CUDA(h, cudaEventRecord(e[1], h->st));
-      if ((rc = launch_mi(h, h->d_base_mi, (int)h->runs.size(), h->total_mi, 1, h->st, 0))) return rc;
+      if ((rc = launch_mi(h, h->d_base_mi, (int)h->runs.size(), h->total_mi, 1, h->st, 0, h->num_sms))) return rc;
       KB_CUDA(h, cudaEventRecord(e[2], h->st));
       KB_CUDA(h, cudaEventSynchronize(e[2]));
       float a = 0, b = 0;

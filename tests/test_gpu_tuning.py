@@ -443,12 +443,13 @@ def test_pipelined_timeout_is_reported_once(precision):
     h.close()
 
 
-@pytest.mark.parametrize("precision,split", [(0, 0), (1, 0), (1, 2)])
-def test_batch_overlap_is_bitwise_the_one_launch_step(precision, split):
+@pytest.mark.parametrize("precision,split,pers", [(0, 0, 0), (1, 0, 0), (1, 2, 0), (0, 0, 1), (1, 2, 1)])
+def test_batch_overlap_is_bitwise_the_one_launch_step(precision, split, pers):
     """Concurrent groups (batch_overlap: the second group's sunset on its own stream
-    beside the first group's memory integrals) change which launch computes a run,
-    not how: every run is bitwise the same as with one launch per kernel, through
-    kb_step and the captured graph of kb_steps alike."""
+    beside the first group's memory integrals; with the persistent grid, the first
+    group's memory integrals on the SMs the sunset leaves free) change which launch
+    computes a run, not how: every run is bitwise the same as with one launch per
+    kernel, through kb_step and the captured graph of kb_steps alike."""
     from kb2pi import capi
 
     cfgs = [dict(Ns=8, M=20, lam=2.0, T=1.0), dict(Ns=16, M=45, lam=4.0, T=2.0), dict(Ns=12, M=33, lam=1.0, T=0.7),
@@ -461,8 +462,8 @@ def test_batch_overlap_is_bitwise_the_one_launch_step(precision, split):
         for r, c in enumerate(cfgs):
             _, k2, _ = h.orbits(r)
             h.init(r, occupation(dict(c), k2), 1.0)
-        h.set_tuning(batch_overlap=ov, memint_split=split)
-        assert h.tuning()["batch_overlap"] == ov
+        h.set_tuning(batch_overlap=ov, memint_split=split, memint_persistent=pers)
+        assert h.tuning()["batch_overlap"] == ov and h.tuning()["memint_persistent"] == pers
         h.steps(3, 30, 0)
         for t in range(33, 41):
             h.step(t)
