@@ -1681,17 +1681,31 @@ int kb_autotune(kb_handle *h, int32_t trials, kb_tuning *chosen, double *ms_per_
     for (int ov : cands) {
       if (ov < 0 || (ov == 0 && best_step < 1e30f)) continue;
       if ((rc = set_overlap(h, ov, best_o))) break;
+      // the step as kb_steps runs it, one launch of a captured graph: stream priorities do
+      // not carry into a graph, so the two-stream step is timed the way it will run
+      cudaGraph_t gr = nullptr;
+      cudaGraphExec_t ge = nullptr;
+      KB_CUDA(h, cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+      rc = launch_step(h, 1);
+      const cudaError_t ec = cudaStreamEndCapture(h->st, &gr);
+      if (!rc && ec != cudaSuccess) rc = fail(h, KB_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(ec));
+      if (!rc) {
+        const cudaError_t ei = cudaGraphInstantiate(&ge, gr, 0);
+        if (ei != cudaSuccess) rc = fail(h, KB_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(ei));
+      }
+      if (gr) cudaGraphDestroy(gr);
       float best = 1e30f;
       for (int q = 0; q < trials && !rc; ++q) {
         KB_CUDA(h, kb::launch_set_t(h->d_t, t, h->st));
         KB_CUDA(h, cudaEventRecord(e[0], h->st));
-        if ((rc = launch_step(h, 1))) break;
+        KB_CUDA(h, cudaGraphLaunch(ge, h->st));
         KB_CUDA(h, cudaEventRecord(e[2], h->st));
         KB_CUDA(h, cudaEventSynchronize(e[2]));
         float a = 0;
         KB_CUDA(h, cudaEventElapsedTime(&a, e[0], e[2]));
         best = std::min(best, a);
       }
+      if (ge) cudaGraphExecDestroy(ge);
       if (rc) break;
       if (best < best_step) {
         best_step = best;
