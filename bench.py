@@ -767,7 +767,7 @@ def run_ours(args):
         "fp64_plain": fp64,
         "compensated_sums": comp,
         "speedup_mixed_vs_fp64": (value / fp64["steps_per_s"]) if fp64 else None,
-        "batched_config3": batched,
+        "batched_64_runs": batched,
     }
     if ws == 1 and not args.no_cpu:
         try:

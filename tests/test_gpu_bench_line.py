@@ -39,4 +39,4 @@ def test_our_arm_line_at_the_small_case():
     assert line["gpu_launches"] >= 3 * line["steps"]
     assert line["clocks"]["sm_max_mhz"] > 0
     assert line["tuning"]["source"] == "kb_autotune"
-    assert line.get("batched_config3") is None  # measured beside the c5 workload only
+    assert line.get("batched_64_runs") is None  # measured beside the Ns=64, M=1000 workload only
