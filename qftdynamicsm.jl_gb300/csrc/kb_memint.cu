@@ -16,16 +16,18 @@
 // the two-time triangle then feeds two rows at once:
 //   F(a,b):   acc_F(b) += x_rho(a) F      acc_F(a) += x_rho(b) F
 //   rho(a,b): acc_r(b) += x_rho(a) rho    acc_F(a) += x_F(b) rho
-// and the diagonal pair F(a,a) feeds acc_F(a) once. One CTA owns KC = 8 orbits
-// (a "chunk") and sweeps the whole triangle of its chunk exactly once, in
+// and the diagonal pair F(a,a) feeds acc_F(a) once. One CTA at a time owns KC = 8
+// orbits (a "chunk") and sweeps the whole triangle of its chunk exactly once, in
 // T x T time tiles streamed from HBM by TMA (tensor-map boxes, or bulk copies)
 // into a shared-memory ring: column sums stay in registers, row sums collect
 // in tensor memory (FP32 history) or a global scratch (FP64). When a column
 // block is complete its leapfrog runs at once, and after the last block the
 // CTA computes the diagonal F(t,t), its tadpole partial sum and the
 // measurement of its orbits. No data leaves the CTA except the new row, so the
-// whole step needs no grid barrier. In split mode two CTAs share a chunk's
-// triangle and memint_finish_kernel runs the leapfrog (memint_kernel below).
+// whole step needs no grid barrier. In split mode a chunk's triangle is
+// streamed in parts and memint_finish_kernel runs the leapfrog; the grid is
+// one CTA per item, or persistent with the items taken from a queue
+// (memint_kernel below).
 #include <algorithm>
 #include <cstdio>
 #include <type_traits>
