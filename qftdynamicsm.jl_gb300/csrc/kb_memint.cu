@@ -89,6 +89,12 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
 __device__ __forceinline__ void fence_proxy_async() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
+// L2 prefetch of one box of a 3D tensor map (no shared memory, no barrier)
+__device__ __forceinline__ void tma_prefetch_3d(const void *tmap, int x, int y, int z) {
+  asm volatile("cp.async.bulk.prefetch.tensor.3d.L2.global.tile [%0, {%1, %2, %3}];" ::"l"(tmap), "r"(x), "r"(y),
+               "r"(z)
+               : "memory");
+}
 // tiled TMA load of one box of a 3D tensor map (x innermost, in elements)
 __device__ __forceinline__ void tma_load_3d(void *dst, const void *tmap, int x, int y, int z, uint64_t *bar) {
   asm volatile(
@@ -610,6 +616,7 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   uint64_t *empty = full + NST;
   // misc: [0] hartreecont, [1] M^2, [2..2+KC) acc_F(t-1) per orbit, [10] abort flag,
   // [11] tiles issued, [12] consumer abort flag, [13] current item, [14] TMEM address,
+  // [15] the next item when the producer took it early (else -1),
   // [16..16+(NG/32)*KC) diagonal partials
   double *misc = reinterpret_cast<double *>(empty + NST);  // 128 doubles
   volatile int *abort_flag = reinterpret_cast<volatile int *>(misc + 10);
@@ -637,6 +644,7 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   const int lane = tid & 31, warp = tid >> 5;
   const int t = *d_t;
   volatile int *item_slot = reinterpret_cast<volatile int *>(misc + 13);
+  volatile int *next_slot = reinterpret_cast<volatile int *>(misc + 15);
   // row sums in TMEM (FP32 history): one allocation for every item of the CTA
   constexpr bool kTmem = sizeof(TS) == 4;
   if (kTmem && warp == 0) tmem_alloc(const_cast<uint32_t *>(tmem_slot));
@@ -650,6 +658,7 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
         mbar_init(lf_full + q, C::NG / 32);   // column-group warps
         mbar_init(lf_empty + q, C::NG / 32);  // leapfrog warps
       }
+    *next_slot = -1;
     fence_proxy_async();
   }
   if (kTmem) tmem_fence_before();
@@ -662,7 +671,11 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   int cur_r = -1;  // run whose tadpole sum misc[0..1] holds
   bool first = true;
   for (;;) {
-  if (tid == 0) *item_slot = queue ? atomicAdd(queue, 1) : (first ? (int)blockIdx.x : nitems);
+  if (tid == 0) {
+    const int pre = *next_slot;  // taken by the producer during the previous item
+    *next_slot = -1;
+    *item_slot = pre >= 0 ? pre : queue ? atomicAdd(queue, 1) : (first ? (int)blockIdx.x : nitems);
+  }
   __syncthreads();
   const int vb = *item_slot;
   first = false;
@@ -749,6 +762,32 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
       if (*abort_flag || no_tiles) break;
       issue_tile<TS, C>(stage, it.I, it.J, R, c, stages, full, tmin, t - 1, use_tmap);
       if (lane == 0) *issued_count = n + 1;
+    }
+    // with every tile of this item issued, take the next item now and fetch its first
+    // tiles into L2 while the consumers finish this one (the loop's head hands it over)
+    if (queue && lane == 0 && !*abort_flag && !no_tiles) {
+      const int nv = atomicAdd(queue, 1);
+      *next_slot = nv;
+      if (nv < nitems && (use_maps & 1)) {
+        const bool s2 = SPLIT && nv >= nwhole;
+        const int it2 = s2 ? nwhole + (nv - nwhole) / parts : nv;
+        const int p2 = s2 ? (nv - nwhole) % parts : 0;
+        const RunDev &R2 = runs[run_at(base, nruns, it2)];
+        const int c2 = it2 - R2.cta_base_mi;
+        const int tmin2 = max(1, t - R2.M + 1), J02 = tmin2 / T, Jn2 = (t - 1) / T;
+        const int Jlo2 = s2 ? split_bound(J02, Jn2, parts, p2) : J02;
+        const int Jhi2 = s2 ? split_bound(J02, Jn2, parts, p2 + 1) - 1 : Jn2;
+        if (R2.tmap && !pexp_lo(R2.pexp) && Jlo2 <= Jhi2) {
+          const int nbk = R2.Malloc / T;
+          TileIt i2{Jlo2, Jlo2, Jn2};
+          for (int q = 0; q < NST && (i2.J < Jhi2 || (i2.J == Jhi2 && i2.I <= Jn2)); ++q, i2.next()) {
+            const int tile = (c2 * nbk + ((i2.I * T) % R2.Malloc) / T) * nbk + ((i2.J * T) % R2.Malloc) / T;
+            const char *tm = reinterpret_cast<const char *>(R2.tmap);
+            tma_prefetch_3d(tm, 0, 0, tile);
+            tma_prefetch_3d(tm + 128, 0, 0, tile);
+          }
+        }
+      }
     }
     __syncwarp();
   } else if (lfwarp) {
