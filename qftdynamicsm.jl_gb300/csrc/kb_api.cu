@@ -973,6 +973,7 @@ int kb_measure(kb_handle *h, int32_t run, int32_t t, kb_meas_scalars *s, double 
   int rc = kb_sync(h);
   if (rc) return rc;
   double *outs[5] = {F, ddF, n, omega, c};
+  if (n || omega || c) KB_CUDA(h, kb::launch_meas_derive(h->d_runs, run, R.S, h->st));
   for (int q = 0; q < 5; ++q)
     if (outs[q]) KB_CUDA(h, cudaMemcpyAsync(outs[q], R.meas + (size_t)q * R.Spad, R.S * 8, cudaMemcpyDeviceToHost, h->st));
   kb_meas_scalars tmp;
@@ -1002,6 +1003,7 @@ int kb_measure_enqueue(kb_handle *h, int32_t run, int32_t t) {
     m.cap = need;
   }
   // behind step t's kernels on the handle's stream; step t+1's run after them
+  KB_CUDA(h, kb::launch_meas_derive(h->d_runs, run, R.S, h->st));
   KB_CUDA(h, cudaMemcpyAsync(m.host, R.meas, nm * 8, cudaMemcpyDeviceToHost, h->st));
   KB_CUDA(h, cudaMemcpyAsync(m.host + nm, R.epart, ne * 8, cudaMemcpyDeviceToHost, h->st));
   KB_CUDA(h, cudaMemcpyAsync(m.host + nm + ne, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->st));

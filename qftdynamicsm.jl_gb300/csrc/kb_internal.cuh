@@ -158,6 +158,8 @@ size_t memint_smem_bytes(bool fp64, int Malloc, int variant);
 cudaError_t configure_memint(bool fp64, size_t smem);
 int memint_tile(bool fp64);
 cudaError_t launch_measure_init(const RunDev *d_runs, int nruns, int t, cudaStream_t st);
+// n, omega, c of a run's measured step from its F(t-1,t-1) and ddF (before they are read)
+cudaError_t launch_meas_derive(const RunDev *d_runs, int run, int S, cudaStream_t st);
 cudaError_t launch_set_t(int *d_t, int t, cudaStream_t st);
 cudaError_t launch_record(const RunDev *d_runs, int nruns, const int *d_t, const int *d_ctl, double *rec,
                           const long long *d_off, long long block, cudaStream_t st);

@@ -305,10 +305,15 @@ struct Cfg {
   static_assert(NG % 32 == 0, "whole warps per group");
 };
 
+// two copies of a run's parameters (memint_kernel: the current item's and the next
+// one's) and two control words, after the small scratch
+constexpr size_t RUNBUF_BYTES = (2 * sizeof(RunDev) + 2 * sizeof(int) + 15) & ~(size_t)15;
+static_assert(sizeof(RunDev) % 8 == 0, "copied as 8-byte words");
+
 template <typename C>
 __host__ __device__ constexpr size_t smem_fixed_bytes() {
-  // stages + full/empty barriers + small scratch
-  return (size_t)C::NST * C::STAGE_BYTES + 2 * C::NST * 8 + 128 * 8 + 16;
+  // stages + full/empty barriers + small scratch + run parameters
+  return (size_t)C::NST * C::STAGE_BYTES + 2 * C::NST * 8 + 128 * 8 + 16 + RUNBUF_BYTES;
 }
 
 // Time tile iterator over the triangle: J = column block, I = row block >= J.
@@ -414,13 +419,35 @@ __device__ __forceinline__ void consumer_sync(int nthreads) {
   asm volatile("bar.sync 1, %0;" ::"r"(nthreads) : "memory");
 }
 
+// Per-orbit frequency, its lattice correction and particle number of the measurement
+// (createMeasurement, Measurement.jl:38-64) from F(t-1,t-1) and its second time
+// derivative ddF. Each product, quotient and root is rounded on its own (no fused
+// multiply-adds), so the kernels that derive them -- at the measured step's read,
+// in the recorded stream, at initialisation -- give the same bits.
+__device__ __forceinline__ void meas_derived(double Fmm, double ddF, double dt2, double &omg, double &cc,
+                                             double &nn) {
+  const double q = __ddiv_rn(ddF, Fmm);
+  omg = (q > 0) ? __dsqrt_rn(q) : 0.0;
+  const double w = __dmul_rn(__dmul_rn(0.25, dt2), __dmul_rn(omg, omg));
+  cc = (w < 1) ? __dsqrt_rn(__dsub_rn(1.0, w)) : 1.0;
+  const double p = __dmul_rn(ddF, Fmm);
+  nn = (p > 0) ? __dsub_rn(__dmul_rn(cc, __dsqrt_rn(p)), 0.5) : 0.0;
+}
+
 // Diagonal F(t,t) (Evolution.jl:969-974), its tadpole partial for the next
 // step and the measurement of the chunk's orbits (createMeasurement,
-// Measurement.jl:38-64); threads 0..KC-1 of the CTA, one orbit each. misc holds
+// Measurement.jl:38-64: F(t-1,t-1) and ddF here, the rest by meas_derived where the
+// measurement is read); threads 0..KC-1 of the CTA, one orbit each. misc holds
 // hartreecont, acc_F(t-1) per orbit and the nwarps x KC partial sums of acc_F(t).
+// pre (if not null): the orbits' k^2, degeneracy, F(t-1,t-1), F(t,t-1) and F(t,t-2),
+// KC values each, gathered while the item was streamed; else they are loaded here.
+// red (if not null): the orbit's tadpole and energy terms go to red[q KC + orbit]
+// for memint_epilogue_sum, and the caller may spread the orbits over warps (the
+// FP64 arithmetic then runs on several SM sub-partitions); else threads 0..KC-1 of
+// one warp sum them with shuffles.
 template <typename TS>
 __device__ void memint_epilogue(const RunDev &R, int c, int t, int tid, const double *misc, int nwarps,
-                                double M2, int measure) {
+                                double M2, int measure, const double *pre = nullptr, double *red = nullptr) {
   const double hc = misc[0];
   const int Ma = R.Malloc, T = R.T;
   const size_t rowstride = (size_t)Ma * KC;
@@ -433,25 +460,34 @@ __device__ void memint_epilogue(const RunDev &R, int c, int t, int tid, const do
   for (int w = 0; w < nwarps; ++w) accd += misc[16 + w * KC + tid];
   const int jj = tid;
   const int kd = c * KC + jj;
-  const double kd2 = (kd < R.S) ? R.k2[kd] : 0.0;
+  // every load ahead of the first store (the stores below could alias them as far as
+  // the compiler knows): one round trip instead of a chain of them
+  const bool kin = kd < R.S;
+  double kd2, dg, Ft1, Ft2, Fmm;
+  if (pre) {
+    kd2 = pre[jj];
+    dg = pre[KC + jj];
+    Fmm = pre[2 * KC + jj];
+    Ft1 = pre[3 * KC + jj];
+    Ft2 = pre[4 * KC + jj];
+  } else {
+    kd2 = kin ? R.k2[kd] : 0.0;
+    dg = kin ? R.deg[kd] : 0.0;
+    // F(t, t-1), F(t, t-2): written in this launch, possibly by another CTA of the chunk
+    Ft1 = __ldcg(FNrow + (size_t)((t - 1) % Ma) * KC + jj);
+    Ft2 = __ldcg(FNrow + (size_t)((t - 2) % Ma) * KC + jj);
+    // measurement (createMeasurement, Measurement.jl:38-64): F(t-1,t-1) from the state
+    Fmm = F1row[(size_t)((t - 1) % Ma) * KC + jj];
+  }
   const double omd = (kd2 + M2) * R.dt2;
-  // F(t, t-1), F(t, t-2): written in this launch, possibly by another CTA of the chunk
-  const double Ft1 = __ldcg(FNrow + (size_t)((t - 1) % Ma) * KC + jj);
-  const double Ft2 = __ldcg(FNrow + (size_t)((t - 2) % Ma) * KC + jj);
   const double Ftt = (2.0 - omd) * Ft1 - Ft2 - accd * R.dt3;
   FNrow[(size_t)(t % Ma) * KC + jj] = Ftt;
   RNrow[(size_t)(t % Ma) * KC + jj] = 0.0;
   reinterpret_cast<TS *>(R.hist_F)[hdo] = (TS)Ftt;
   reinterpret_cast<TS *>(R.hist_r)[hdo] = (TS)0;
-  const double dg = (kd < R.S) ? R.deg[kd] : 0.0;
   double tp = dg * Ftt;  // tadpole partial sum of this chunk for the next step
-  // measurement (createMeasurement, Measurement.jl:38-64): F(t-1,t-1) from the state
-  const double Fmm = F1row[(size_t)((t - 1) % Ma) * KC + jj];
   const double dt = R.dt, dt2 = R.dt2;
   const double ddF = (Ftt - 2 * Ft1 + Fmm) / dt2;
-  const double omg = (ddF / Fmm > 0) ? sqrt(ddF / Fmm) : 0.0;
-  const double cc = (0.25 * dt2 * (omg * omg) < 1) ? sqrt(1. - 0.25 * dt2 * (omg * omg)) : 1.0;
-  const double nn = (ddF * Fmm > 0) ? (cc * sqrt(ddF * Fmm)) - 0.5 : 0.0;
   double ek = 0.5 * ddF * dg;
   double ep = 0.5 * (R.mass2 + kd2 + 0.5 * R.pref_ivol * hc) * Fmm * dg;
   double em = 0.25 * dt * dg * misc[2 + jj];
@@ -459,9 +495,13 @@ __device__ void memint_epilogue(const RunDev &R, int c, int t, int tid, const do
     const int Sp = R.nchunks * KC;
     R.meas[0 * Sp + kd] = Fmm;
     R.meas[1 * Sp + kd] = ddF;
-    R.meas[2 * Sp + kd] = nn;
-    R.meas[3 * Sp + kd] = omg;
-    R.meas[4 * Sp + kd] = cc;
+  }
+  if (red) {
+    red[jj] = tp;
+    red[KC + jj] = ek;
+    red[2 * KC + jj] = ep;
+    red[3 * KC + jj] = em;
+    return;
   }
   // fixed-order reduction over the KC orbits (lanes 0..KC-1 of warp 0)
 #pragma unroll
@@ -482,14 +522,31 @@ __device__ void memint_epilogue(const RunDev &R, int c, int t, int tid, const do
   }
 }
 
+// sum q (0 tadpole, 1..3 kinetic, potential, memory energy) of memint_epilogue's
+// per-orbit terms in red, added in the order lane 0 of its shuffle tree adds them
+__device__ void memint_epilogue_sum(const RunDev &R, int c, int t, int q, const double *red, double M2,
+                                    int measure) {
+  static_assert(KC == 8, "the tree below is the one of eight lanes");
+  const double *v = red + q * KC;
+  const double s = ((v[0] + v[4]) + (v[2] + v[6])) + ((v[1] + v[5]) + (v[3] + v[7]));
+  if (q == 0) {
+    R.tad[(size_t)(t & 1) * R.nchunks + c] = s;
+  } else if (measure) {
+    R.epart[(size_t)c * 4 + q - 1] = s;
+    if (q == 3) R.epart[(size_t)c * 4 + 3] = M2;
+  }
+}
+
 // leapfrog of column b (t' = b) for orbits j0 .. j0+OPT-1 of chunk c
 // (evolve_r!/evolve_F!, Evolution.jl:890-915) from the column sums colF, colR
 // and the row sums rowb of row b; adds the column's acc_F(t) terms to diag and
-// keeps acc_F(t-1) in emem (b = t-1)
+// keeps acc_F(t-1) in emem (b = t-1); capt (if not null) gets F(t,t-1) at [j] and
+// F(t,t-2) at [KC + j]
 template <typename TS, int OPT>
 __device__ __forceinline__ void leapfrog_column(const RunDev &R, int c, int t, int tmin, int b, int j0, double M2,
                                                 bool lo_only, const double *colF, const double *colR,
-                                                const double *rowb, double *diag, double *emem, bool &has_emem) {
+                                                const double *rowb, double *diag, double *emem, bool &has_emem,
+                                                double *capt = nullptr) {
   const int Ma = R.Malloc;
   const size_t rowstride = (size_t)Ma * KC, st_row = (size_t)R.nchunks * rowstride;
   const double dt3 = R.dt3;
@@ -536,6 +593,7 @@ __device__ __forceinline__ void leapfrog_column(const RunDev &R, int c, int t, i
     hR[ho] = (TS)rn;
     diag[o] += xbr_d * Fn + xbF_d * rn;
     if (b == t - 1) emem[o] = accF;
+    if (capt && b >= t - 2) capt[(t - 1 - b) * KC + j] = Fn;  // F(t,t-1), F(t,t-2) for the diagonal
   }
   if (b == t - 1) has_emem = true;
 }
@@ -617,14 +675,26 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   // misc: [0] hartreecont, [1] M^2, [2..2+KC) acc_F(t-1) per orbit, [10] abort flag,
   // [11] tiles issued, [12] consumer abort flag, [13] current item, [14] TMEM address,
   // [15] the next item when the producer took it early (else -1),
-  // [16..16+(NG/32)*KC) diagonal partials
+  // [16..16+(NG/32)*KC) diagonal partials, [48..48+5*KC) the diagonal's inputs (epi),
+  // [88..88+4*KC) its per-orbit tadpole and energy terms
   double *misc = reinterpret_cast<double *>(empty + NST);  // 128 doubles
   volatile int *abort_flag = reinterpret_cast<volatile int *>(misc + 10);
   volatile int *issued_count = reinterpret_cast<volatile int *>(misc + 11);
   // consumers leave the tile loop together: the flag is only written by
   // consumers and they all meet at the named barrier after the tile loop
   volatile int *cabort = reinterpret_cast<volatile int *>(misc + 12);
-  static_assert(16 + (C::NG / 32) * KC <= 128, "misc scratch too small");
+  static_assert(16 + (C::NG / 32) * KC <= 48 && 48 + 5 * KC <= 88 && 88 + 4 * KC <= 120, "misc scratch too small");
+  // inputs of memint_epilogue for a whole chunk: k^2, degeneracy and F(t-1,t-1) of its
+  // orbits from the producer warp once it has issued the item's tiles, F(t,t-1) and
+  // F(t,t-2) from the leapfrog of those columns
+  double *epi = misc + 48;
+  // the item's run parameters in shared memory (runbuf[rb]): the loop reads them all
+  // through, and a global read that misses L1 under the stream costs a round trip to
+  // L2. The producer copies the next item's into runbuf[rb ^ 1] once it has taken it;
+  // runctl[0]: that run (-1: none), runctl[1]: the current item's run if copied so
+  RunDev *runbuf = reinterpret_cast<RunDev *>(misc + 130);
+  volatile int *runctl = reinterpret_cast<volatile int *>(runbuf + 2);
+  int rb = 0;
   static_assert(C::NG == 128, "one TMEM lane per row-group thread, column group in warps 0..3");
   volatile uint32_t *tmem_slot = reinterpret_cast<volatile uint32_t *>(misc + 14);
   // LFW: [120..122) lf_full, [122..124) lf_empty mbarriers; the hand-off stage
@@ -659,6 +729,7 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
         mbar_init(lf_empty + q, C::NG / 32);  // leapfrog warps
       }
     *next_slot = -1;
+    runctl[0] = -1;
     fence_proxy_async();
   }
   if (kTmem) tmem_fence_before();
@@ -669,11 +740,14 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   int nb = 0;      // tiles this CTA streamed before the current item (stage barrier phases)
   int lb = 0;      // column blocks it handed to the leapfrog warps before the current item
   int cur_r = -1;  // run whose tadpole sum misc[0..1] holds
+  int pre_issued = 0;  // producer warp: tiles of the coming item it issued during the last one
   bool first = true;
   for (;;) {
   if (tid == 0) {
     const int pre = *next_slot;  // taken by the producer during the previous item
     *next_slot = -1;
+    runctl[1] = pre >= 0 ? runctl[0] : -1;
+    runctl[0] = -1;
     *item_slot = pre >= 0 ? pre : queue ? atomicAdd(queue, 1) : (first ? (int)blockIdx.x : nitems);
   }
   __syncthreads();
@@ -683,8 +757,19 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   const bool split = SPLIT && vb >= nwhole;
   const int item = split ? nwhole + (vb - nwhole) / parts : vb;
   const int part = split ? (vb - nwhole) % parts : 0;
-  const int r = run_at(base, nruns, item);
-  const RunDev &R = runs[r];
+  int r = runctl[1];
+  if (r >= 0) {
+    rb ^= 1;  // copied by the producer during the previous item
+  } else {
+    r = run_at(base, nruns, item);
+    if (warp == 0) {
+      const uint64_t *src = reinterpret_cast<const uint64_t *>(runs + r);
+      uint64_t *dst = reinterpret_cast<uint64_t *>(runbuf + rb);
+      for (int w = lane; w < (int)(sizeof(RunDev) / 8); w += 32) dst[w] = src[w];
+    }
+    __syncthreads();
+  }
+  const RunDev &R = runbuf[rb];
   const int c = item - R.cta_base_mi;  // chunk
   const int M = R.M, Ma = R.Malloc;
   const int tmin = max(1, t - M + 1);
@@ -749,7 +834,11 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
   if (producer) {
     // ---------------- producer warp: stream every tile of its column blocks once
     TileIt it{Jlo, Jlo, Jn};
-    for (int n = 0; n < ntiles; ++n, it.next()) {
+    const int n0 = min(pre_issued, ntiles);  // already issued at the end of the previous item
+    for (int q = 0; q < n0; ++q) it.next();
+    pre_issued = 0;
+    if (lane == 0) *issued_count = n0;
+    for (int n = n0; n < ntiles; ++n, it.next()) {
       const int gn = nb + n;  // the CTA's tile count picks the stage and its phase
       const int stage = gn % NST;
       if (gn >= NST && !mbar_wait_bounded(empty + stage, (uint32_t)(((gn / NST) - 1) & 1))) {
@@ -763,29 +852,76 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
       issue_tile<TS, C>(stage, it.I, it.J, R, c, stages, full, tmin, t - 1, use_tmap);
       if (lane == 0) *issued_count = n + 1;
     }
-    // with every tile of this item issued, take the next item now and fetch its first
-    // tiles into L2 while the consumers finish this one (the loop's head hands it over)
-    if (queue && lane == 0 && !*abort_flag && !no_tiles) {
-      const int nv = atomicAdd(queue, 1);
-      *next_slot = nv;
-      if (nv < nitems && (use_maps & 1)) {
+    // the diagonal's inputs that are not written in this step (the loads are in flight
+    // while the tiles stream; the epilogue finds them in shared memory)
+    if (!split && lane < KC) {
+      const int kd = c * KC + lane;
+      const bool kin = kd < R.S;
+      const size_t st_row = (size_t)R.nchunks * rowstride;
+      epi[lane] = kin ? R.k2[kd] : 0.0;
+      epi[KC + lane] = kin ? R.deg[kd] : 0.0;
+      epi[2 * KC + lane] = R.st_F[(size_t)((t - 1) % 3) * st_row + (size_t)c * rowstride + (size_t)((t - 1) % Ma) * KC + lane];
+    }
+    // with every tile of this item issued, take the next item now: its first tiles
+    // go to L2 at once and into the stage ring as soon as this item's last tiles
+    // release their stages, so that they load while the consumers finish this item
+    if (queue && !no_tiles) {
+      int nv = nitems;
+      if (lane == 0 && !*abort_flag) {
+        nv = atomicAdd(queue, 1);
+        *next_slot = nv;
+      }
+      nv = __shfl_sync(0xffffffffu, nv, 0);
+      if (nv < nitems) {
         const bool s2 = SPLIT && nv >= nwhole;
         const int it2 = s2 ? nwhole + (nv - nwhole) / parts : nv;
         const int p2 = s2 ? (nv - nwhole) % parts : 0;
-        const RunDev &R2 = runs[run_at(base, nruns, it2)];
+        const int r2 = run_at(base, nruns, it2);
+        const RunDev &R2 = runs[r2];
+        {  // the next item's run parameters into the buffer the current item does not use
+          const uint64_t *src = reinterpret_cast<const uint64_t *>(runs + r2);
+          uint64_t *dst = reinterpret_cast<uint64_t *>(runbuf + (rb ^ 1));
+          for (int w = lane; w < (int)(sizeof(RunDev) / 8); w += 32) dst[w] = src[w];
+          __syncwarp();
+          if (lane == 0) runctl[0] = r2;
+        }
         const int c2 = it2 - R2.cta_base_mi;
         const int tmin2 = max(1, t - R2.M + 1), J02 = tmin2 / T, Jn2 = (t - 1) / T;
         const int Jlo2 = s2 ? split_bound(J02, Jn2, parts, p2) : J02;
         const int Jhi2 = s2 ? split_bound(J02, Jn2, parts, p2 + 1) - 1 : Jn2;
-        if (R2.tmap && !pexp_lo(R2.pexp) && Jlo2 <= Jhi2) {
+        int nt2 = 0;
+        if (!pexp_lo(R2.pexp))
+          for (int J = Jlo2; J <= Jhi2 && nt2 < NST; ++J) nt2 += Jn2 - J + 1;
+        nt2 = min(nt2, NST);
+        const bool tmap2 = (use_maps & 1) && R2.tmap != nullptr;
+        if (tmap2 && lane == 0) {
           const int nbk = R2.Malloc / T;
           TileIt i2{Jlo2, Jlo2, Jn2};
-          for (int q = 0; q < NST && (i2.J < Jhi2 || (i2.J == Jhi2 && i2.I <= Jn2)); ++q, i2.next()) {
+          for (int q = 0; q < nt2; ++q, i2.next()) {
             const int tile = (c2 * nbk + ((i2.I * T) % R2.Malloc) / T) * nbk + ((i2.J * T) % R2.Malloc) / T;
             const char *tm = reinterpret_cast<const char *>(R2.tmap);
             tma_prefetch_3d(tm, 0, 0, tile);
             tma_prefetch_3d(tm + 128, 0, 0, tile);
           }
+        }
+        // the coming item's tiles continue this CTA's tile count: tile q of it is
+        // tile ntiles + q of this item's count (the stage and phase it will be waited on)
+        TileIt i2{Jlo2, Jlo2, Jn2};
+        for (int q = 0; q < nt2; ++q, i2.next()) {
+          const int gn = nb + ntiles + q;
+          const int stage = gn % NST;
+          const bool ok = gn < NST || mbar_wait_bounded(empty + stage, (uint32_t)(((gn / NST) - 1) & 1));
+          if (!__all_sync(0xffffffffu, ok)) {
+            if (lane == 0) {
+              *abort_flag = 1;
+              atomicOr(d_err, DEVERR_TIMEOUT);
+            }
+            break;
+          }
+          if (__any_sync(0xffffffffu, *abort_flag != 0)) break;  // a consumer gave up: issue no more
+          issue_tile<TS, C>(stage, i2.I, i2.J, R2, c2, stages, full, tmin2, t - 1, tmap2);
+          pre_issued = q + 1;
+          if (lane == 0) *issued_count = ntiles + q + 1;  // drained with this item's tiles on an abort
         }
       }
     }
@@ -817,7 +953,8 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
         if (b >= tmin && b <= t - 1) {
           if (!use_tmem)
             for (int o = 0; o < OPT; ++o) rowb[o] = rowacc[(size_t)(b % Ma) * KC + lj0 + o];
-          leapfrog_column<TS, OPT>(R, c, t, tmin, b, lj0, M2, lo_only, colF, colR, rowb, diag, emem, has_emem);
+          leapfrog_column<TS, OPT>(R, c, t, tmin, b, lj0, M2, lo_only, colF, colR, rowb, diag, emem, has_emem,
+                                   epi + 3 * KC);
         }
       }
       if (ok) {
@@ -1027,7 +1164,8 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
       if (bvalid) {
         if (!use_tmem)
           for (int o = 0; o < OPT; ++o) rowb[o] = rowacc[(size_t)(b % Ma) * KC + j0 + o];
-        leapfrog_column<TS, OPT>(R, c, t, tmin, b, j0, M2, lo_only, colF, colR, rowb, diag, emem, has_emem);
+        leapfrog_column<TS, OPT>(R, c, t, tmin, b, j0, M2, lo_only, colF, colR, rowb, diag, emem, has_emem,
+                                 split ? nullptr : epi + 3 * KC);
       }
     }
     if (!split && !lf_on && !aborted && colgrp) {
@@ -1060,7 +1198,13 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
         TmemRow<OPT>::ld(tcol(s), v);
         for (int o = 0; o < OPT; ++o) rowacc[(size_t)(s + loc) * KC + j0 + o] = v[o];
       }
-    if (!split && tid < KC) memint_epilogue<TS>(R, c, t, tid, misc, C::NG / 32, M2, measure);
+    if (!split) {
+      // two orbits on each of warps 0..3, one warp per SM sub-partition
+      if (warp < KC / 2 && lane < 2)
+        memint_epilogue<TS>(R, c, t, 2 * warp + lane, misc, C::NG / 32, M2, measure, epi, misc + 88);
+      __syncthreads();
+      if (warp < 4 && lane == 0) memint_epilogue_sum(R, c, t, warp, misc + 88, M2, measure);
+    }
   }
   nb += ntiles;
   if (lf_on) lb += Jhi - Jlo + 1;
@@ -1577,9 +1721,8 @@ __global__ void measure_init_kernel(const RunDev *__restrict__ runs, int nruns, 
     const double Fmm = Fm[(size_t)((t - 1) % Ma) * KC + jj];
     const double dt2 = R.dt2;
     const double ddF = (Ftt - 2 * Fmt + Fmm) / dt2;
-    const double omg = (ddF / Fmm > 0) ? sqrt(ddF / Fmm) : 0.0;
-    const double cc = (0.25 * dt2 * (omg * omg) < 1) ? sqrt(1. - 0.25 * dt2 * (omg * omg)) : 1.0;
-    const double nn = (ddF * Fmm > 0) ? (cc * sqrt(ddF * Fmm)) - 0.5 : 0.0;
+    double omg, cc, nn;
+    meas_derived(Fmm, ddF, dt2, omg, cc, nn);
     const double dg = R.deg[kd];
     R.meas[0 * Sp + kd] = Fmm;
     R.meas[1 * Sp + kd] = ddF;
@@ -1651,9 +1794,29 @@ __global__ void record_kernel(const RunDev *__restrict__ runs, const int *__rest
     out[5] = R.epart[3];
   }
   const int Sp = R.nchunks * KC;
-  for (int i = threadIdx.x; i < 5 * R.S; i += blockDim.x) {
-    const int q = i / R.S, k = i - q * R.S;
-    out[6 + i] = R.meas[(size_t)q * Sp + k];
+  for (int k = threadIdx.x; k < R.S; k += blockDim.x) {
+    const double Fmm = R.meas[k], ddF = R.meas[(size_t)Sp + k];
+    double omg, cc, nn;
+    meas_derived(Fmm, ddF, R.dt2, omg, cc, nn);
+    out[6 + k] = Fmm;
+    out[6 + R.S + k] = ddF;
+    out[6 + 2 * R.S + k] = nn;
+    out[6 + 3 * R.S + k] = omg;
+    out[6 + 4 * R.S + k] = cc;
+  }
+}
+
+// n, omega and c of run `run`'s measured step (meas blocks 2, 3, 4) from its F(t-1,t-1)
+// and ddF (blocks 0, 1)
+__global__ void meas_derive_kernel(const RunDev *__restrict__ runs, int run) {
+  const RunDev &R = runs[run];
+  const int Sp = R.nchunks * KC;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < R.S; k += gridDim.x * blockDim.x) {
+    double omg, cc, nn;
+    meas_derived(R.meas[k], R.meas[(size_t)Sp + k], R.dt2, omg, cc, nn);
+    R.meas[(size_t)2 * Sp + k] = nn;
+    R.meas[(size_t)3 * Sp + k] = omg;
+    R.meas[(size_t)4 * Sp + k] = cc;
   }
 }
 
@@ -1791,6 +1954,11 @@ cudaError_t launch_memint(bool fp64, int variant, int split, int nwhole, const R
         <<<grid, CfgF32::NT + 32, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure, nw, use_maps, nitems, q, parts);
   else
     memint_blk_kernel<CfgF32::NST><<<total_ctas, 288, smem, st>>>(d_runs, d_base, nruns, d_t, d_err, measure);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_meas_derive(const RunDev *d_runs, int run, int S, cudaStream_t st) {
+  meas_derive_kernel<<<(S + 255) / 256, 256, 0, st>>>(d_runs, run);
   return cudaGetLastError();
 }
 
