@@ -96,6 +96,8 @@ __device__ __forceinline__ void tma_prefetch_3d(const void *tmap, int x, int y, 
                : "memory");
 }
 // tiled TMA load of one box of a 3D tensor map (x innermost, in elements)
+__device__ __forceinline__ void prefetch_l2g(const void *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
 __device__ __forceinline__ void tma_load_3d(void *dst, const void *tmap, int x, int y, int z, uint64_t *bar) {
   asm volatile(
       "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
@@ -935,7 +937,23 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
       double diag[OPT], emem[OPT];
       for (int o = 0; o < OPT; ++o) diag[o] = emem[o] = 0.0;
       bool has_emem = false, ok = true;
+      // the state and Sigma entries of this lane's column of block J go to L2 a block
+      // ahead: the step's stream has long evicted them, and the last block's leapfrog,
+      // which nothing overlaps, would otherwise wait on DRAM
+      auto lf_prefetch = [&](int J) {
+        const int b = J * T + lloc;
+        if (J > Jhi || b < tmin || b > t - 1) return;
+        const size_t str = (size_t)R.nchunks * rowstride, o = (size_t)c * rowstride + (size_t)(b % Ma) * KC + lj0;
+        prefetch_l2g(R.st_F + (size_t)((t - 1) % 3) * str + o);
+        prefetch_l2g(R.st_F + (size_t)((t - 2) % 3) * str + o);
+        prefetch_l2g(R.st_r + (size_t)((t - 1) % 3) * str + o);
+        prefetch_l2g(R.st_r + (size_t)((t - 2) % 3) * str + o);
+        prefetch_l2g(reinterpret_cast<const TS *>(R.sig_r) + o);
+        prefetch_l2g(reinterpret_cast<const TS *>(R.sig_F) + o);
+      };
+      lf_prefetch(Jlo);
       for (int J = Jlo; J <= Jhi; ++J) {
+        lf_prefetch(J + 1);
         const int slot = (lb + J - Jlo) & 1, use = (lb + J - Jlo) >> 1;
         ok = __all_sync(0xffffffffu, lf_wait(lf_full + slot, (uint32_t)(use & 1), cabort));
         if (!ok) break;
