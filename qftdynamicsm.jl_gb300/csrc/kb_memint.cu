@@ -937,9 +937,10 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
       double diag[OPT], emem[OPT];
       for (int o = 0; o < OPT; ++o) diag[o] = emem[o] = 0.0;
       bool has_emem = false, ok = true;
-      // the state and Sigma entries of this lane's column of block J go to L2 a block
-      // ahead: the step's stream has long evicted them, and the last block's leapfrog,
-      // which nothing overlaps, would otherwise wait on DRAM
+      // the state and Sigma entries of this lane's column of the last block go to L2 one
+      // block ahead: the step's stream has long evicted them, and that block's leapfrog,
+      // which nothing overlaps, would otherwise wait on DRAM (an earlier block's runs
+      // while tiles stream, and a prefetch a long column ahead would be evicted again)
       auto lf_prefetch = [&](int J) {
         const int b = J * T + lloc;
         if (J > Jhi || b < tmin || b > t - 1) return;
@@ -951,9 +952,9 @@ memint_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
         prefetch_l2g(reinterpret_cast<const TS *>(R.sig_r) + o);
         prefetch_l2g(reinterpret_cast<const TS *>(R.sig_F) + o);
       };
-      lf_prefetch(Jlo);
+      if (Jlo == Jhi) lf_prefetch(Jlo);
       for (int J = Jlo; J <= Jhi; ++J) {
-        lf_prefetch(J + 1);
+        if (J + 1 == Jhi) lf_prefetch(J + 1);
         const int slot = (lb + J - Jlo) & 1, use = (lb + J - Jlo) >> 1;
         ok = __all_sync(0xffffffffu, lf_wait(lf_full + slot, (uint32_t)(use & 1), cabort));
         if (!ok) break;
