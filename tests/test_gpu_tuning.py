@@ -372,6 +372,43 @@ def test_persistent_memint_batched_runs_and_errors():
         assert np.array_equal(Fa, Fb) and np.array_equal(ra, rb)
 
 
+@pytest.mark.parametrize("split", [0, 2])
+def test_persistent_item_boundaries_mixed_expansions(split):
+    """The persistent grid's item boundaries -- the next item's first tiles issued while
+    the current one finishes, its run parameters copied ahead -- over items of every
+    shape: LO runs with no tiles at all, windows of 3 and 5 steps with fewer tiles than
+    the stage ring holds, classical and quantum NLO runs, 427 chunk items for 152 CTAs
+    (several per CTA, the run changing between them or not). Bitwise the same as one CTA
+    per item: n, omega, c, E and rows of F and rho."""
+    from kb2pi import capi
+
+    cfgs = [dict(Ns=40, M=33, lam=2.0, T=1.0, pexp=1), dict(Ns=32, M=3, lam=3.0, T=1.5, pexp=2),
+            dict(Ns=24, M=64, lam=1.0, T=0.7, pexp=0), dict(Ns=16, M=5, lam=4.0, T=2.0, pexp=1),
+            dict(Ns=8, M=100, lam=2.0, T=1.2, pexp=1)]
+    out = []
+    for pers in (0, 1):
+        ps = [capi.KbParams(Ns=c["Ns"], sdim=3, M=c["M"], N=4, pexp=c["pexp"], precision=1, device=0, flags=0,
+                            dt=0.1, lam=c["lam"], mass2=1.0, mass=1.0) for c in cfgs]
+        h = capi.Handle(ps)
+        for r, c in enumerate(cfgs):
+            _, k2, _ = h.orbits(r)
+            h.init(r, occupation(dict(c), k2), 1.0)
+        h.set_tuning(memint_variant=2, memint_split=split, batch_order=1, memint_persistent=pers)
+        h.steps(3, 110, 0)
+        rows = []
+        for r in range(len(cfgs)):
+            tmin, _ = h.window(r)
+            rows.append((h.measure(r, 112), [(h.get(r, 0, 112, tp), h.get(r, 1, 112, tp)) for tp in (tmin, 111, 112)]))
+        out.append(rows)
+        h.close()
+    for (ma, ra), (mb, rb) in zip(out[0], out[1]):
+        assert ma["E"] == mb["E"] and ma["M2"] == mb["M2"]
+        for k in ("n", "omega", "c", "F", "ddF"):
+            assert np.array_equal(ma[k], mb[k]), k
+        for (Fa, Ra), (Fb, Rb) in zip(ra, rb):
+            assert np.array_equal(Fa, Fb) and np.array_equal(Ra, Rb)
+
+
 @pytest.mark.parametrize("precision,variant,persistent", [(0, None, 0), (1, None, 0), (1, 2, 0), (0, None, 1),
                                                           (1, 2, 1)])
 def test_bounded_wait_runs_out_and_is_reported(precision, variant, persistent):
