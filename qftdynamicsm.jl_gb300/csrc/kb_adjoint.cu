@@ -378,7 +378,7 @@ cudaError_t launch_adjoint_step(const RunDev &R, const AdjBuffers &A, int t, dou
   const bool nlo = pexp_sunset(R.pexp);
   if (nlo && !sigma_ready) {
     e = launch_sunset(true, 0, sl.runs, sl.base, sl.nruns, sl.total_rows, sl.grid, sl.d_t, sl.scratch, sl.stride,
-                      sl.smem, st);
+                      sl.smem, nullptr, st);
     if (e != cudaSuccess) return e;
   }
   adj_step_kernel<<<R.nchunks, KC * ADJ_TPB, 0, st>>>(R, t, A, emem_weight);

@@ -132,9 +132,10 @@ __device__ inline int run_at(const int *sched, int nruns, int item) {
 }
 
 // host launchers (kb_sunset.cu, kb_memint.cu)
+// queue: item counter (zeroed here before the launch) or null for a fixed item order
 cudaError_t launch_sunset(bool fp64, int variant, const RunDev *d_runs, const int *d_base, int nruns,
                           int total_rows, int grid, const int *d_t, void *scratch, size_t scratch_stride, size_t smem,
-                          cudaStream_t st);
+                          int *queue, cudaStream_t st);
 size_t sunset_smem_bytes(bool fp64, int H);
 size_t sunset_image_bytes(bool fp64, int H);
 cudaError_t launch_sunset_image(bool fp64, int H, const double *Cm, void *img, cudaStream_t st);

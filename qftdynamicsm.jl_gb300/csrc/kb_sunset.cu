@@ -99,7 +99,8 @@ __host__ __device__ inline size_t sun_tables_bytes(bool fp64, const SunGeom &g) 
 // shared memory of sunset_kernel: the tables, the expand table ([H][P4] orbit
 // indices) when everything fits in the 227 KB a CTA may use, one orbit buffer and,
 // FP32, the two pass regions (FP64 keeps them in a per-CTA global scratch slot)
-constexpr size_t SUN_SMEM_CAP = 232448;
+constexpr size_t SUN_SMEM_HEAD = 16;  // sunset_kernel's item counter ahead of the layout
+constexpr size_t SUN_SMEM_CAP = 232448 - SUN_SMEM_HEAD;
 struct SunLayout {
   size_t etab, regions, bytes;
   bool has_etab;
@@ -441,15 +442,33 @@ __device__ void sun_transform(const SunCtx<TC> &c, In in, Out out) {
 // An item of a run is R.sun_rows consecutive t' rows (several for the small
 // lattices of a batch, so that their per-item work -- finding the run, the L2
 // prefetch of the next row -- is spread over more rows), taken one after the other.
+// Items: with a queue (a counter zeroed before the launch) every CTA takes the next
+// item when it is done with one -- the items of a batch differ in cost, and runs are
+// ordered costliest first -- and takes it early, so that its rows can go to L2 while
+// the current item's inverse transforms run; without one CTA b takes b, b + grid, ...
 template <typename TC, typename TS, bool SCRATCH, int NTHR, int MINB>
 __global__ void __launch_bounds__(NTHR, MINB)
 sunset_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int nruns, int total,
-              const int *__restrict__ d_t, TC *__restrict__ scratch, size_t scratch_stride) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+              const int *__restrict__ d_t, TC *__restrict__ scratch, size_t scratch_stride, int *__restrict__ queue) {
+  extern __shared__ __align__(16) unsigned char smem_dyn[];
+  // the item counter's value in the first 16 bytes, the layout of sun_layout after them
+  // (no static shared memory: the kernel may take the device's whole per-block maximum)
+  volatile int &q_slot = *reinterpret_cast<int *>(smem_dyn);
+  unsigned char *smem_raw = smem_dyn + SUN_SMEM_HEAD;
   const int t = *d_t;  // Sigma(t-1, t') for t' in [tmin, t-1]
   int cur_ns = -1;
   SunCtx<TC> c{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, SunGeom(1)};
-  for (int w = blockIdx.x; w < total; w += gridDim.x) {
+  // the next item from the queue; every thread calls it (two barriers)
+  auto take = [&]() {
+    __syncthreads();  // the previous item number has been read by every thread
+    if (threadIdx.x == 0) q_slot = atomicAdd(queue, 1);
+    __syncthreads();
+    return q_slot;
+  };
+  int nxt = -1;  // the next item if taken early (queue)
+  for (int w = queue ? take() : (int)blockIdx.x; w < total;
+       w = queue ? (nxt >= 0 ? nxt : take()) : w + (int)gridDim.x) {
+    nxt = -1;
     const int r = run_at(base, nruns, w);
     const RunDev &R = runs[r];
     if (!pexp_sunset(R.pexp) || t < 3) continue;
@@ -533,11 +552,12 @@ sunset_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
       // the next row of this CTA goes to L2 while the inverse transforms run
       {
         int w2 = w, g2 = gi + 1;
-        if (g2 >= nrow) {
-          w2 = w + gridDim.x;
+        if (g2 >= nrow || tmin + (w - R.cta_base_sun) * nrow + g2 > t - 1) {  // the item's last row
+          if (queue && nxt < 0) nxt = take();
+          w2 = queue ? nxt : w + (int)gridDim.x;
           g2 = 0;
         }
-        if (w2 < total) {
+        if (w2 >= 0 && w2 < total) {
           const RunDev &R2n = runs[run_at(base, nruns, w2)];
           const int ng2 = SCRATCH ? 1 : R2n.sun_rows;
           const int tp2 = max(1, t - R2n.M + 1) + (w2 - R2n.cta_base_sun) * ng2 + g2;
@@ -576,7 +596,7 @@ sunset_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
 
 }  // namespace
 
-size_t sunset_smem_bytes(bool fp64, int H) { return sun_layout(fp64, SunGeom(H)).bytes; }
+size_t sunset_smem_bytes(bool fp64, int H) { return SUN_SMEM_HEAD + sun_layout(fp64, SunGeom(H)).bytes; }
 
 namespace {
 // the tables of sunset_kernel for octant size H as the image of their shared memory
@@ -664,15 +684,19 @@ cudaError_t configure_sunset(bool fp64, size_t smem) {
 
 cudaError_t launch_sunset(bool fp64, int variant, const RunDev *d_runs, const int *d_base, int nruns,
                           int total_rows, int grid, const int *d_t, void *scratch, size_t scratch_stride, size_t smem,
-                          cudaStream_t st) {
+                          int *queue, cudaStream_t st) {
   if (total_rows <= 0 || grid <= 0) return cudaSuccess;
+  if (queue) {  // a memset node in a captured step
+    const cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(int), st);
+    if (e != cudaSuccess) return e;
+  }
   if (fp64)
     KB_SUNSET_F64<<<grid, SUN_THREADS, smem, st>>>(d_runs, d_base, nruns, total_rows, d_t,
-                                                   reinterpret_cast<double *>(scratch), scratch_stride);
+                                                   reinterpret_cast<double *>(scratch), scratch_stride, queue);
   else if (variant == 1)
-    KB_SUNSET_F32_HALF<<<grid, SUN_THREADS, smem, st>>>(d_runs, d_base, nruns, total_rows, d_t, nullptr, 0);
+    KB_SUNSET_F32_HALF<<<grid, SUN_THREADS, smem, st>>>(d_runs, d_base, nruns, total_rows, d_t, nullptr, 0, queue);
   else
-    KB_SUNSET_F32<<<grid, SUN_THREADS_F32, smem, st>>>(d_runs, d_base, nruns, total_rows, d_t, nullptr, 0);
+    KB_SUNSET_F32<<<grid, SUN_THREADS_F32, smem, st>>>(d_runs, d_base, nruns, total_rows, d_t, nullptr, 0, queue);
   return cudaGetLastError();
 }
 
