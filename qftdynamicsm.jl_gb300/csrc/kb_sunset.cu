@@ -25,9 +25,9 @@
 //
 // Intermediates E/D and B live in two regions R1, R2 of about H*P values: in
 // shared memory for FP32, in a per-CTA global scratch slot for FP64 (whose
-// regions do not fit next to each other in 227 KB). The grid is persistent:
-// CTA b handles the t' rows b, b + gridDim, ... of all runs of the batch, so
-// the same launch serves every step of a CUDA graph (rows outside the window
+// regions do not fit next to each other in 227 KB). The grid is persistent: its
+// CTAs take the items (t' rows) of all runs of the batch from a device counter,
+// so the same launch serves every step of a CUDA graph (rows outside the window
 // are skipped).
 #include <algorithm>
 #include <cmath>
