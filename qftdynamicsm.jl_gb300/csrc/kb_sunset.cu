@@ -119,6 +119,14 @@ __host__ __device__ inline SunLayout sun_layout(bool fp64, const SunGeom &g) {
 }
 
 __device__ __forceinline__ void prefetch_l2(const void *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+// 16-byte asynchronous copy global -> shared (L2 only), its group commit and the wait for
+// all of this thread's groups
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 // 4-wide vector load/store for float (float4) and double (2 x double2)
 __device__ __forceinline__ void ld4(const float *p, float v[4]) {
@@ -422,16 +430,25 @@ __device__ void sun_pass3(const SunCtx<TC> &c, const TC *D, Out out) {
   }
 }
 
-template <typename TC, typename In, typename Out>
-__device__ void sun_transform(const SunCtx<TC> &c, In in, Out out) {
+// after_expand() runs once the input has been read (every thread, behind a barrier),
+// after_pass2() once R2 is free again (pass 3 reads R1 only)
+template <typename TC, typename In, typename Out, typename A, typename B>
+__device__ void sun_transform_hooked(const SunCtx<TC> &c, In in, Out out, A after_expand, B after_pass2) {
   sun_expand<TC>(c, c.R1, in);
   __syncthreads();
+  after_expand();
   sun_pass1<TC>(c, c.R1, c.R2);
   __syncthreads();
   sun_pass2<TC>(c, c.R2, c.R1);
   __syncthreads();
+  after_pass2();
   sun_pass3<TC>(c, c.R1, out);
   __syncthreads();
+}
+
+template <typename TC, typename In, typename Out>
+__device__ void sun_transform(const SunCtx<TC> &c, In in, Out out) {
+  sun_transform_hooked<TC>(c, in, out, [] {}, [] {});
 }
 
 // NTHR threads per CTA; MINB resident CTAs per SM the register budget allows.
@@ -466,9 +483,15 @@ sunset_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
     return q_slot;
   };
   int nxt = -1;  // the next item if taken early (queue)
+  // FP32 rows are staged with asynchronous copies: rho into R2 while F's pass 3 runs (R2
+  // is free from then on), the next row's F into the orbit buffer while the current
+  // row's inverse F transform runs (free once its expand has read it)
+  constexpr bool ASYNC = !SCRATCH && sizeof(TS) == 4 && sizeof(TC) == 4;
+  int pre_w = -1, pre_g = -1;  // the row whose F is on its way into the orbit buffer
   for (int w = queue ? take() : (int)blockIdx.x; w < total;
        w = queue ? (nxt >= 0 ? nxt : take()) : w + (int)gridDim.x) {
     nxt = -1;
+    if (ASYNC) cp_async_wait_all();  // nothing of this thread's lands in shared memory later
     const int r = run_at(base, nruns, w);
     const RunDev &R = runs[r];
     if (!pexp_sunset(R.pexp) || t < 3) continue;
@@ -503,6 +526,9 @@ sunset_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
     const int tid = threadIdx.x, nthr = blockDim.x;
     const int nrow = SCRATCH ? 1 : R.sun_rows;
     for (int gi = 0; gi < nrow; ++gi) {
+      const bool prestaged = ASYNC && pre_w == w && pre_g == gi;
+      if (ASYNC) cp_async_wait_all();
+      pre_w = pre_g = -1;
       const int tp = tmin + (w - R.cta_base_sun) * nrow + gi;
       if (tp > t - 1) break;  // rows of an item are consecutive: the rest are past the window too
       const int slot = tp % R.Malloc;
@@ -528,15 +554,38 @@ sunset_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
         }
         __syncthreads();
       };
+      // the same with 16-byte asynchronous copies (FP32: half a chunk's 8 orbits each, the
+      // padding orbits of the last chunk up to rup4(S) included); completes at a wait
+      auto astage = [&](const void *hist, size_t hb, TC *dst, int nch, size_t cs) {
+        const TS *h = reinterpret_cast<const TS *>(hist) + hb;
+        const int lim = rup4(S);
+        for (int q = tid; q < 2 * nch; q += nthr) {
+          const int e0 = (q >> 1) * KC + (q & 1) * 4;
+          if (e0 < lim) cp_async16(dst + e0, h + (size_t)(q >> 1) * cs + (q & 1) * 4);
+        }
+        cp_async_commit();
+      };
 
       // forward transforms of F(t-1,t') -> bufF and rho(t-1,t') -> R2 (orbit layout);
       // each row is staged in the region the transform writes last, the rho row
       // fetched into L2 meanwhile
       for (int q = tid; q < R.nchunks; q += nthr)
         prefetch_l2(reinterpret_cast<const TS *>(R.hist_r) + hbase + q * cstride);
-      stage(R.hist_F, c.bufF);
-      sun_transform<TC>(c, [&](int o) { return c.bufF[o]; }, [&](int o, TC v) { c.bufF[o] = v; });
-      stage(R.hist_r, c.R2);
+      if (prestaged)
+        __syncthreads();  // every thread's copies have landed
+      else
+        stage(R.hist_F, c.bufF);
+      sun_transform_hooked<TC>(
+          c, [&](int o) { return c.bufF[o]; }, [&](int o, TC v) { c.bufF[o] = v; }, [] {},
+          [&] {
+            if (ASYNC) astage(R.hist_r, hbase, c.R2, R.nchunks, cstride);
+          });
+      if (ASYNC) {
+        cp_async_wait_all();
+        __syncthreads();
+      } else {
+        stage(R.hist_r, c.R2);
+      }
       sun_transform<TC>(c, [&](int o) { return c.R2[o]; }, [&](int o, TC v) { c.R2[o] = v; });
 
       // pointwise sunset in position space (Evolution.jl:28-29, classical :114-115)
@@ -549,7 +598,12 @@ sunset_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
       }
       __syncthreads();
 
-      // the next row of this CTA goes to L2 while the inverse transforms run
+      // the next row of this CTA goes to L2 while the inverse transforms run; its F is
+      // staged into the orbit buffer during the inverse F transform when it has this
+      // lattice size (the same layout)
+      const void *nhF = nullptr;
+      size_t nhb = 0, ncs = 0;
+      int nw = -1, ng = -1, nnch = 0;
       {
         int w2 = w, g2 = gi + 1;
         if (g2 >= nrow || tmin + (w - R.cta_base_sun) * nrow + g2 > t - 1) {  // the item's last row
@@ -567,6 +621,14 @@ sunset_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
             for (int q = tid; q < R2n.nchunks; q += nthr) {
               prefetch_l2(reinterpret_cast<const char *>(R2n.hist_F) + b2 + q * cs2);
               prefetch_l2(reinterpret_cast<const char *>(R2n.hist_r) + b2 + q * cs2);
+            }
+            if (ASYNC && R2n.Ns == cur_ns) {
+              nhF = R2n.hist_F;
+              nhb = b2 / sizeof(TS);
+              ncs = cs2 / sizeof(TS);
+              nnch = R2n.nchunks;
+              nw = w2;
+              ng = g2;
             }
           }
         }
@@ -588,7 +650,16 @@ sunset_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
       sun_transform<TC>(c, [&](int o) { return gr[o]; }, [&](int o, TC v) { c.R2[o] = v; });
       flush(sigr, fr);
       const TC *gF = c.bufF;
-      sun_transform<TC>(c, [&](int o) { return gF[o]; }, [&](int o, TC v) { c.R2[o] = v; });
+      sun_transform_hooked<TC>(
+          c, [&](int o) { return gF[o]; }, [&](int o, TC v) { c.R2[o] = v; },
+          [&] {
+            if (ASYNC && nw >= 0) {
+              astage(nhF, nhb, c.bufF, nnch, ncs);
+              pre_w = nw;
+              pre_g = ng;
+            }
+          },
+          [] {});
       flush(sigF, fF);
     }
   }
