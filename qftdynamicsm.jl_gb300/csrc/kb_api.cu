@@ -919,6 +919,23 @@ static int launch_step(kb_handle *h, int measure) {
   return KB_OK;
 }
 
+// the graph of one step (its kernels, then t advanced on the device), captured once per
+// tuning: kb_steps launches it per step, kb_step too unless per-kernel events are on
+static int ensure_step_graph(kb_handle *h) {
+  if (h->graph) return KB_OK;
+  cudaGraph_t g;
+  KB_CUDA(h, cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+  int rc = launch_step(h, 1);
+  cudaError_t ea = (rc == 0) ? (cudaError_t)kb::launch_advance_t(h->d_t, h->st) : cudaSuccess;
+  cudaError_t ec = cudaStreamEndCapture(h->st, &g);
+  if (rc) return rc;
+  if (ea != cudaSuccess || ec != cudaSuccess) return fail(h, KB_ERR_CUDA, "graph capture failed");
+  cudaError_t ei = cudaGraphInstantiate(&h->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (ei != cudaSuccess) return fail(h, KB_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(ei));
+  return KB_OK;
+}
+
 int kb_step(kb_handle *h, int32_t t) {
   if (!h) return KB_ERR_PARAM;
   if (h->t_cur < 2) return fail(h, KB_ERR_PARAM, "kb_step before kb_init");
@@ -926,7 +943,12 @@ int kb_step(kb_handle *h, int32_t t) {
   cudaSetDevice(h->device);
   NvtxRange range("kb_step");
   KB_CUDA(h, kb::launch_set_t(h->d_t, t, h->st));
-  int rc = launch_step(h, 1);
+  int rc = 0;
+  if (h->profiling) {  // the step's own launches, between the profiling events
+    rc = launch_step(h, 1);
+  } else if (!(rc = ensure_step_graph(h))) {
+    KB_CUDA(h, cudaGraphLaunch(h->graph, h->st));
+  }
   if (rc) return rc;
   h->t_cur = t;
   h->sigma_valid = h->any_nlo || h->any_ninv;
@@ -1189,18 +1211,7 @@ int kb_steps(kb_handle *h, int32_t t0, int32_t count, int32_t measure_every, kb_
   cudaSetDevice(h->device);
   const int nr = (int)h->runs.size();
   // steps between measurements run from one captured graph
-  if (!h->graph) {
-    cudaGraph_t g;
-    KB_CUDA(h, cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
-    int rc = launch_step(h, 1);
-    cudaError_t ea = (rc == 0) ? (cudaError_t)kb::launch_advance_t(h->d_t, h->st) : cudaSuccess;
-    cudaError_t ec = cudaStreamEndCapture(h->st, &g);
-    if (rc) return rc;
-    if (ea != cudaSuccess || ec != cudaSuccess) return fail(h, KB_ERR_CUDA, "graph capture failed");
-    cudaError_t ei = cudaGraphInstantiate(&h->graph, g, 0);
-    cudaGraphDestroy(g);
-    if (ei != cudaSuccess) return fail(h, KB_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(ei));
-  }
+  if (int rc = ensure_step_graph(h)) return rc;
   KB_CUDA(h, kb::launch_set_t(h->d_t, t0, h->st));
   int nm = 0;
   for (int i = 0; i < count; ++i) {
