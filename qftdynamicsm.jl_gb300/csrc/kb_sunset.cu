@@ -663,6 +663,7 @@ sunset_kernel(const RunDev *__restrict__ runs, const int *__restrict__ base, int
       flush(sigF, fF);
     }
   }
+  if (ASYNC) cp_async_wait_all();  // no copy lands in this CTA's shared memory after it ends
 }
 
 }  // namespace
